@@ -1,0 +1,425 @@
+#!/usr/bin/env python
+"""Headline benchmark of the GB300 fuzzy-metaball renderer.
+
+Workload (one "step"): forward-render the larger synthetic scene of N = 1000 Gaussians from 16
+cameras of 640x480 (fx = fy = 600) spread on a 1.0 m sphere, float32, depth + alpha per pixel.
+Metric: ray-Gaussian evaluations per second, counted as E = sum over the (tile, Gaussian) keys of
+the pixels in the key's 8x8 tile, with the run's cut-off (peak density 1e-7) -- the algorithmic
+work of the render. Renders/s and the per-call drop-in numbers are reported beside it.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+One JSON line on stdout (rank 0). Multi-GPU runs are independent replicas (no collective on the
+data path); value is the whole-job aggregate.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "fuzzy-ellipses_gb300")
+for _p in (ROOT, PKG):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+import numpy as np  # noqa: E402
+
+METRIC = "Mray-Gaussian evals/s"
+WORKLOAD = ("N=1000 Gaussians (means U[-0.3,0.3]^3 m, scales logU[0.005,0.03] m, Haar rotations, "
+            "logw N(0,0.5^2)), 16 cameras 640x480 fx=fy=600 on a 1.0 m Fibonacci sphere, fp32, "
+            "density cut-off 1e-7 (exact k-sigma screen bounds)")
+PER_EVAL_FMA = 20   # FP32 FMA-pipe instructions per ray-Gaussian evaluation in the forward blend
+PER_EVAL_MUFU = 3   # rcp, ex2 (alpha), ex2 (softmax weight)
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile-step", action="store_true",
+                    help="build the workload, warm up, run one batched forward step and exit "
+                         "(the command the committed ncu summaries capture)")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class ClockSampler:
+    """Samples SM clocks and throttle reasons with nvidia-smi while the timed region runs."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_id):
+        self.gpu = gpu_id
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (OSError, ValueError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, power, reasons = [], [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax.append(float(parts[1]))
+                power.append(float(parts[2]))
+            except ValueError:
+                continue
+            for name, val in zip(names, parts[4:8]):
+                if val.lower().startswith("active"):
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "power_w_max": max(power) if power else None,
+                "samples": len(sm), "reasons": sorted(reasons)}
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            return json.load(f), "measured"
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+def ncu_traffic():
+    """Per-launch DRAM bytes of the blend from the committed ncu summary, if present."""
+    path = os.path.join(ROOT, "profiles", "blend_fwd_cfg1.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        return d.get("dram_bytes_per_launch_full_workload")
+    return None
+
+
+def build_workload(dev):
+    import torch
+
+    from fuzzy_ellipses import synthetic as S
+    scene, cams = S.config1(seed=0)
+    m = torch.from_numpy(scene.means).to(dev)
+    p = torch.from_numpy(scene.prec).to(dev)
+    w = torch.from_numpy(scene.logw).to(dev)
+    return scene, cams, (m, p, w)
+
+
+def count_evals(fe, cams, mpw):
+    """E = sum over 8x8-tile keys of the pixels in the key's tile, per camera."""
+    m, p, w = mpw
+    per_cam = []
+    for c in cams:
+        keys, ranges = fe.render_binning(m, p, w, c.fx, c.fy, c.cx, c.cy, c.quat, c.trans,
+                                         c.height, c.width, tile=(8, 8))
+        r = ranges.cpu().numpy()
+        gx = (c.width + 7) // 8
+        t = np.arange(r.shape[0])
+        tx, ty = t % gx, t // gx
+        pix = np.minimum(8, c.width - 8 * tx) * np.minimum(8, c.height - 8 * ty)
+        per_cam.append(int(((r[:, 1] - r[:, 0]) * pix).sum()))
+    return per_cam
+
+
+def cpu_baseline_sample(scene, cam, n_pix, seconds_cap=30.0):
+    """Time the float64 fm_render restatement (dense) on a bounded pixel sample; px/s."""
+    from oracle import fm_render_np as O
+    rng = np.random.default_rng(0)
+    pix = rng.choice(cam.height * cam.width, n_pix, replace=False)
+    rays = O.pinhole_rays(cam.height, cam.width, cam.fx, cam.fy, cam.cx, cam.cy)[pix]
+    t0 = time.perf_counter()
+    done = 0
+    for s in range(0, n_pix, 1024):
+        O.render_func_quat(scene.means, scene.prec, scene.logw, rays[s:s + 1024], cam.quat,
+                           cam.trans, 21.4, 2.66)
+        done += min(1024, n_pix - s)
+        if time.perf_counter() - t0 > seconds_cap:
+            break
+    return done / (time.perf_counter() - t0), done
+
+
+def run_reference(args):
+    """The reference arm: the CPU implementation of the path (float64 restatement of fm_render,
+    torch, all host threads), same workload and metric, bounded per-step sample."""
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    import torch
+
+    from fuzzy_ellipses import synthetic as S
+    from oracle import fm_render_torch as OT
+    torch.set_num_threads(os.cpu_count() or 1)
+    scene, cams = S.config1(seed=0)
+    per_cam_evals = None
+    evals_path = os.path.join(ROOT, "profiles", "cfg1_evals_per_camera.json")
+    if os.path.exists(evals_path):
+        with open(evals_path) as f:
+            per_cam_evals = json.load(f)["evals_per_camera"]
+    e_render = float(np.mean(per_cam_evals)) if per_cam_evals else None
+    m = torch.from_numpy(scene.means).double()
+    p = torch.from_numpy(scene.prec).double()
+    w = torch.from_numpy(scene.logw).double()
+    H, W = 480, 640
+    n_pix = 4096
+    rng = np.random.default_rng(0)
+    times = []
+    with torch.no_grad():
+        for i in range(args.warmup + args.steps):
+            c = cams[i % len(cams)]
+            rays_all = OT.pinhole_rays(H, W, c.fx, c.fy, c.cx, c.cy)
+            pix = torch.from_numpy(rng.choice(H * W, n_pix, replace=False))
+            t0 = time.perf_counter()
+            OT.render_func_quat(m, p, w, rays_all[pix], torch.from_numpy(c.quat).double(),
+                                torch.from_numpy(c.trans).double(), 21.4, 2.66)
+            if i >= args.warmup:
+                times.append(time.perf_counter() - t0)
+    px_s = n_pix / statistics.mean(times)
+    renders_s = px_s / (H * W)
+    value = renders_s * e_render / 1e6 if e_render else None
+    out = {"metric": METRIC, "value": value, "unit": "Mevals/s", "impl": "reference",
+           "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+           "ms_per_step": 1e3 * statistics.mean(times), "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+           "config": {"workload": WORKLOAD, "sample_per_step": f"{n_pix} pixels of one camera"},
+           "renders_per_s": renders_s, "dense_evals_per_s": px_s * scene.n,
+           "cpu_baseline": {"value": value, "unit": "Mevals/s", "cores": torch.get_num_threads(),
+                            "kind": "port",
+                            "sample": f"{n_pix} random pixels of one 640x480 camera per step, "
+                                      "dense over N=1000 (torch float64 restatement of fm_render)"},
+           "e2e": {"value": value, "unit": "Mevals/s", "h2d_bytes_per_step": 0,
+                   "d2h_bytes_per_step": 0}}
+    print(json.dumps(out), flush=True)
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+        return
+    import torch
+
+    import fuzzy_ellipses as fe
+
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    scene, cams, mpw = build_workload(dev)
+    m, p, w = mpw
+    H, W = cams[0].height, cams[0].width
+    npix = H * W
+    views = [dict(scene=0, height=c.height, width=c.width, fx=c.fx, fy=c.fy, cx=c.cx, cy=c.cy,
+                  quat=c.quat, trans=c.trans) for c in cams]
+    batch = fe.Batch([(0, scene.n)], views)
+    per_cam_evals = count_evals(fe, cams, mpw) if not args.profile_step else [0] * len(cams)
+    e_step = float(sum(per_cam_evals))
+    depth = torch.empty(batch.n_pixels, device=dev)
+    alpha = torch.empty(batch.n_pixels, device=dev)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+
+    for _ in range(args.warmup):
+        batch.forward(m, p, w, depth, alpha)
+    if args.profile_step:
+        batch.forward(m, p, w, depth, alpha)
+        torch.cuda.synchronize()
+        assert batch.status()["device_error"] == 0
+        return
+    st = batch.status()
+    assert st["device_error"] == 0 and st["num_keys"] == st["want_keys"], st
+
+    # ---- timed region: K batched forward steps, L2 flushed between steps --------------------
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    props = torch.cuda.get_device_properties(dev)
+    uuid = getattr(props, "uuid", None)
+    sampler = ClockSampler(f"GPU-{uuid}" if uuid is not None else str(local))
+    sampler.start()
+    time.sleep(0.3)
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    t_wall = time.perf_counter()
+    for i in range(args.steps):
+        flush.fill_(i & 0xFF)
+        starts[i].record()
+        batch.forward(m, p, w, depth, alpha)
+        ends[i].record()
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    wall = time.perf_counter() - t_wall
+    clocks = sampler.stop()
+    step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    dev_s = sum(step_ms) / 1e3
+    if world > 1:
+        t = torch.tensor([dev_s], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        dev_s = float(t.item())
+    value = world * e_step * args.steps / dev_s / 1e6
+    renders_s = world * len(cams) * args.steps / dev_s
+
+    if rank != 0:
+        return
+
+    # ---- per-stage timings (live events on the launching stream) ---------------------------
+    stage_runs = []
+    for _ in range(5):
+        flush.fill_(1)
+        _, _, ms = batch.forward_timed(m, p, w, depth, alpha)
+        stage_runs.append(ms)
+    stages = {k: statistics.median(r[k] for r in stage_runs) for k in batch.STAGES}
+    fma_ops = fe.render.bench_peak("fma")
+    ex2_ops = fe.render.bench_peak("ex2")
+    peak_evals = min(fma_ops / PER_EVAL_FMA, ex2_ops / PER_EVAL_MUFU)
+    blend_evals_per_s = e_step / (stages["blend"] * 1e-3)
+    peaks, peak_kind = measured_peaks()
+    nk = batch.status()["num_keys"]
+    passes = (max(1, int(np.ceil(np.log2(batch_tiles(cams, 16, 16))))) + 7) // 8
+    hbm = {
+        "preprocess": (52 * scene.n + len(cams) * scene.n * (96 + 8 + 4)) / (stages["preprocess"] * 1e-3) / 1e9,
+        "sort": (16 * nk * passes) / (stages["sort"] * 1e-3) / 1e9,
+        "gather": (8 * nk + 64 * nk) / (stages["gather"] * 1e-3) / 1e9,
+    }
+
+    # ---- plain per-call drop-in on device-resident inputs ----------------------------------
+    outs = [(torch.empty(H, W, device=dev), torch.empty(H, W, device=dev)) for _ in cams]
+    for _ in range(3):
+        for c, o in zip(cams, outs):
+            fe.render_forward(m, p, w, c.fx, c.fy, c.cx, c.cy, c.quat, c.trans, H, W, out=o)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    reps = max(3, args.steps // 2)
+    e0.record()
+    for _ in range(reps):
+        for c, o in zip(cams, outs):
+            fe.render_forward(m, p, w, c.fx, c.fy, c.cx, c.cy, c.quat, c.trans, H, W, out=o)
+    e1.record()
+    torch.cuda.synchronize()
+    plain_s = e0.elapsed_time(e1) / 1e3 / reps
+    plain_renders_s = len(cams) / plain_s
+
+    # ---- end to end: host buffers in, plain C-ABI calls, host buffers out -------------------
+    m_h, p_h, w_h = [x.cpu().pin_memory() for x in (m, p, w)]
+    poses_h = torch.from_numpy(np.concatenate([np.concatenate([c.quat, c.trans]) for c in cams])
+                               .astype(np.float32)).pin_memory()
+    out_h = torch.empty((len(cams), 2, H, W), dtype=torch.float32).pin_memory()
+    m_d, p_d, w_d = torch.empty_like(m), torch.empty_like(p), torch.empty_like(w)
+    poses_d = torch.empty_like(poses_h, device=dev)
+    out_d = torch.empty((len(cams), 2, H, W), device=dev)
+    h2d = sum(x.numel() * 4 for x in (m_h, p_h, w_h, poses_h))
+    d2h = out_h.numel() * 4
+
+    def e2e_step():
+        for src, dst in ((m_h, m_d), (p_h, p_d), (w_h, w_d), (poses_h, poses_d)):
+            dst.copy_(src, non_blocking=True)
+        for i in range(len(cams)):
+            c = cams[i]
+            fe.render_forward(m_d, p_d, w_d, c.fx, c.fy, c.cx, c.cy, poses_d[7 * i:7 * i + 4],
+                              poses_d[7 * i + 4:7 * i + 7], H, W, out=(out_d[i, 0], out_d[i, 1]))
+        out_h.copy_(out_d, non_blocking=True)
+        torch.cuda.current_stream().synchronize()
+
+    for _ in range(3):
+        e2e_step()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        e2e_step()
+    e2e_s = (time.perf_counter() - t0) / args.steps
+    e2e_value = e_step / e2e_s / 1e6
+
+    # ---- CPU baseline (oracle on the host cores, bounded sample) ---------------------------
+    cpu = None
+    if not args.no_cpu_baseline:
+        px_s, done = cpu_baseline_sample(scene, cams[0], 16384, seconds_cap=25.0)
+        cpu_renders_s = px_s / npix
+        cpu = {"value": cpu_renders_s * (e_step / len(cams)) / 1e6, "unit": "Mevals/s",
+               "cores": 1, "kind": "port",
+               "sample": f"{done} random pixels of camera 0 (of 16), dense over N=1000, numpy "
+                         "float64 restatement of fm_render, single thread",
+               "renders_per_s": cpu_renders_s, "dense_evals_per_s": px_s * scene.n}
+
+    blend_achieved = blend_evals_per_s / 1e9
+    out = {
+        "metric": METRIC, "value": value, "unit": "Mevals/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dev_s / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic",
+        "config": {"workload": WORKLOAD, "step": "batched forward of all 16 cameras",
+                   "tile": "16x16", "l2": "flushed between steps (256 MiB write outside the "
+                   "per-step CUDA events); step working set ~100 MB < L2",
+                   "parallelism": f"replicas x{world}"},
+        "renders_per_s": renders_s,
+        "evals_per_step": e_step,
+        "plain_per_call": {"renders_per_s": plain_renders_s, "ms_per_render": 1e3 * plain_s / len(cams),
+                           "mevals_per_s": e_step / plain_s / 1e6},
+        "e2e": {"value": e2e_value, "unit": "Mevals/s", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h, "path": "fe_render_fwd per camera, pinned host buffers",
+                "ms_per_step": 1e3 * e2e_s},
+        "roofline": {"bound": "fma+xu", "achieved": blend_achieved,
+                     "peak": peak_evals / 1e9, "unit": "Gevals/s",
+                     "frac": blend_evals_per_s / peak_evals, "traffic": ncu_traffic(),
+                     "kernel": "blend_fwd_kernel<16,16>",
+                     "per_eval": {"fma_pipe": PER_EVAL_FMA, "mufu": PER_EVAL_MUFU},
+                     "fma_ops_per_s": fma_ops, "mufu_ex2_ops_per_s": ex2_ops,
+                     "peak_source": "fe_bench_peak microbenchmarks on this GPU (FFMA and MUFU.EX2)"},
+        "stages_ms": stages,
+        "stages_hbm_gbs": hbm, "hbm_peak_gbs": peaks.get("hbm_gbs"), "hbm_peak_kind": peak_kind,
+        "num_keys": nk,
+        "evals_per_camera": per_cam_evals,
+        "cpu_baseline": cpu,
+        "clocks": clocks,
+        "gpu_launches": batch.launches_per_forward * args.steps,
+        "wall_s_timed_region": wall,
+    }
+    print(json.dumps(out), flush=True)
+
+
+def batch_tiles(cams, tw, th):
+    return sum(((c.width + tw - 1) // tw) * ((c.height + th - 1) // th) for c in cams)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,918 @@
+// api.cu -- host orchestration and the C ABI (include/fuzzy_ellipses.h).
+//
+// Replaces the reference's custom-call body RasterizeGaussiansCUDAJAX (rasterize_main.cu:29-114),
+// its host pipeline CudaRasterizer::Rasterizer::forwardJAX (rasterizer_impl.cu:174-344) and its
+// per-call GpuMemoryPool (rasterizer_impl.h:24-43, rasterizer_impl.cu:47-79). Differences by
+// design: scratch comes from a grow-only arena per (device, stream) instead of cudaMalloc/cudaFree
+// per call; every stage runs on the caller's stream; the key count stays on the device (capacity
+// is planned from the worst case N x tiles when that fits the key budget), so the steady state
+// has no host synchronisation; errors are status codes, never exit() or exceptions.
+#include <dlfcn.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <string>
+#include <utility>
+#include <vector>
+
+#include "fe_kernels.cuh"
+
+namespace fe {
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const std::string& msg) {
+  g_last_error = msg;
+  return code;
+}
+
+int cuda_fail(cudaError_t e, const char* what) {
+  return fail(FE_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define FE_CUDA(call)                                  \
+  do {                                                 \
+    cudaError_t e_ = (call);                           \
+    if (e_ != cudaSuccess) return cuda_fail(e_, #call); \
+  } while (0)
+
+constexpr size_t kAlign = 256;
+inline size_t align_up(size_t x) { return (x + kAlign - 1) / kAlign * kAlign; }
+
+// Scratch bytes the worst-case key capacity may use before the pipeline falls back to reading
+// the exact key count back (one host synchronisation, as the reference always does).
+size_t key_budget_bytes() {
+  static const size_t v = [] {
+    const char* s = std::getenv("FE_KEY_BUDGET_BYTES");
+    return s ? (size_t)std::strtoull(s, nullptr, 10) : (size_t)4 << 30;
+  }();
+  return v;
+}
+
+// Bytes of key-proportional scratch per key: two key buffers and one tile record.
+constexpr size_t kBytesPerKey = 2 * sizeof(uint64_t) + sizeof(TileRec);
+
+int bits_for(int64_t n) {
+  int b = 0;
+  while (b < 40 && (int64_t(1) << b) < n) ++b;
+  return b;
+}
+
+// A grow-only device buffer.
+struct DevBuf {
+  char* ptr = nullptr;
+  size_t cap = 0;
+  int reserve(size_t bytes, cudaStream_t st) {
+    if (bytes <= cap) return FE_OK;
+    if (ptr) {
+      // Work already enqueued may still use the old buffer.
+      FE_CUDA(cudaStreamSynchronize(st));
+      FE_CUDA(cudaFree(ptr));
+      ptr = nullptr;
+      cap = 0;
+    }
+    const size_t want = align_up(bytes + bytes / 4);
+    if (cudaMalloc(&ptr, want) != cudaSuccess) {
+      cudaGetLastError();
+      ptr = nullptr;
+      return fail(FE_ERR_OUT_OF_MEMORY, "scratch arena could not grow to " +
+                                            std::to_string(want) + " bytes");
+    }
+    cap = want;
+    return FE_OK;
+  }
+};
+
+// Sequential carving of a buffer into 256-byte aligned regions.
+struct Carver {
+  char* base;
+  size_t off = 0;
+  template <class T>
+  T* take(int64_t count) {
+    T* p = reinterpret_cast<T*>(base ? base + off : nullptr);
+    off += align_up(sizeof(T) * (size_t)(count > 0 ? count : 0));
+    return p;
+  }
+};
+
+// Per-record scratch (and the control block): sized by records, tiles and pixels.
+struct RecSpace {
+  Control* ctrl;
+  GaussRec* recs;
+  TileRect* rects;
+  uint32_t* touched;
+  uint32_t* incl;
+  unsigned long long* scan_tmp;
+  uint2* ranges;
+  float4* pix;     // backward only
+  RecGrad* rgrad;  // backward only
+};
+
+// Key-proportional scratch.
+struct KeySpace {
+  uint64_t* keys_a;
+  uint64_t* keys_b;
+  uint32_t* hist;
+  TileRec* trec;
+};
+
+template <class F>
+size_t carve_rec(char* base, int64_t n_rec, int64_t n_tiles, int64_t n_pix, bool bwd, F&& out) {
+  Carver c{base};
+  RecSpace s;
+  s.ctrl = c.take<Control>(1);
+  s.recs = c.take<GaussRec>(n_rec);
+  s.rects = c.take<TileRect>(n_rec);
+  s.touched = c.take<uint32_t>(n_rec);
+  s.incl = c.take<uint32_t>(n_rec);
+  s.scan_tmp = c.take<unsigned long long>(scan_grid(n_rec));
+  s.ranges = c.take<uint2>(n_tiles);
+  s.pix = bwd ? c.take<float4>(n_pix) : nullptr;
+  s.rgrad = bwd ? c.take<RecGrad>(n_rec) : nullptr;
+  out(s);
+  return c.off;
+}
+
+template <class F>
+size_t carve_keys(char* base, int64_t cap, F&& out) {
+  Carver c{base};
+  KeySpace s;
+  s.keys_a = c.take<uint64_t>(cap);
+  s.keys_b = c.take<uint64_t>(cap);
+  s.hist = c.take<uint32_t>(int64_t(sort_grid(cap) + 1) * 256);
+  s.trec = c.take<TileRec>(cap);
+  out(s);
+  return c.off;
+}
+
+// Scratch owned by one (device, stream) pair for the plain entry points.
+struct Arena {
+  DevBuf rec, keys;
+  unsigned long long* h_pinned = nullptr;
+  int init() {
+    if (!h_pinned) FE_CUDA(cudaMallocHost(&h_pinned, 64));
+    return FE_OK;
+  }
+};
+
+std::mutex g_arena_mu;
+std::map<std::pair<int, cudaStream_t>, Arena*> g_arenas;
+
+int arena_for(cudaStream_t st, Arena** out) {
+  int dev = 0;
+  FE_CUDA(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lk(g_arena_mu);
+  Arena*& a = g_arenas[{dev, st}];
+  if (!a) a = new Arena();
+  const int rc = a->init();
+  if (rc) return rc;
+  *out = a;
+  return FE_OK;
+}
+
+int check_desc(const fe_render_desc* d) {
+  if (!d) return fail(FE_ERR_INVALID_ARGUMENT, "descriptor is NULL");
+  if (d->magic != FE_DESC_MAGIC || d->version != FE_DESC_VERSION)
+    return fail(FE_ERR_DESCRIPTOR, "descriptor magic/version mismatch");
+  if (d->n_gaussians < 0 || d->height < 1 || d->width < 1 || d->height > 65535 * 8 ||
+      d->width > 65535 * 8)
+    return fail(FE_ERR_INVALID_ARGUMENT, "image size or Gaussian count out of range");
+  if (!(d->fx != 0.f) || !(d->fy != 0.f) || !std::isfinite(d->fx) || !std::isfinite(d->fy))
+    return fail(FE_ERR_INVALID_ARGUMENT, "focal lengths must be finite and non-zero");
+  if (d->cull_mode != FE_CULL_EPS && d->cull_mode != FE_CULL_NSTD)
+    return fail(FE_ERR_INVALID_ARGUMENT, "unknown cull mode");
+  const bool tile_ok = (d->tile_w == 0 && d->tile_h == 0) || (d->tile_w == 8 && d->tile_h == 8) ||
+                       (d->tile_w == 16 && d->tile_h == 16) || (d->tile_w == 32 && d->tile_h == 8);
+  if (!tile_ok) return fail(FE_ERR_INVALID_ARGUMENT, "tile shape must be 8x8, 16x16 or 32x8");
+  return FE_OK;
+}
+
+inline void tile_shape(const fe_render_desc* d, int& tw, int& th) {
+  tw = d->tile_w ? d->tile_w : 16;
+  th = d->tile_h ? d->tile_h : 16;
+}
+
+// Shared binning + blend pipeline over a views table. Sizes are host-known; the key count
+// lives on the device. When `sync_count` is set the key count is read back after the scan and
+// the key scratch sized exactly (used when the worst case exceeds the key budget).
+struct Pipeline {
+  ViewsArg va;
+  int64_t n_rec, n_tiles, n_pix;
+  int tile_w, tile_h;
+  int cull_mode;
+  float cull_param;
+  float beta2, beta3;
+  const float *means, *prec, *logw, *quat, *trans;
+};
+
+int run_binning(const Pipeline& p, int64_t worst, DevBuf& recbuf, DevBuf& keybuf,
+                unsigned long long* h_pinned, bool bwd, cudaStream_t st, RecSpace& rs,
+                KeySpace& ks, int64_t& cap, uint64_t*& sorted) {
+  size_t rec_bytes = carve_rec(nullptr, p.n_rec, p.n_tiles, p.n_pix, bwd, [](const RecSpace&) {});
+  int rc = recbuf.reserve(rec_bytes, st);
+  if (rc) return rc;
+  carve_rec(recbuf.ptr, p.n_rec, p.n_tiles, p.n_pix, bwd, [&](const RecSpace& s) { rs = s; });
+
+  // `worst`: every record touching every tile of its view.
+  const bool exact = worst > 0 && (size_t)worst * kBytesPerKey <= key_budget_bytes();
+
+  FE_CUDA(cudaMemsetAsync(rs.ctrl, 0, sizeof(Control), st));
+  FE_CUDA(cudaMemsetAsync(rs.ranges, 0, sizeof(uint2) * (size_t)p.n_tiles, st));
+  launch_preprocess(p.va, p.n_rec, p.means, p.prec, p.logw, p.quat, nullptr, p.trans, p.cull_mode,
+                    p.cull_param, p.tile_w, p.tile_h, rs.recs, rs.rects, rs.touched, st);
+  if (exact) {
+    cap = worst;
+  } else {
+    // Scan with an unbounded capacity first, read the count back, then size the keys.
+    launch_scan(rs.touched, rs.incl, p.n_rec, INT64_C(0xffffffff), rs.scan_tmp, rs.ctrl, st);
+    FE_CUDA(cudaMemcpyAsync(h_pinned, &rs.ctrl->want_keys, sizeof(unsigned long long),
+                            cudaMemcpyDeviceToHost, st));
+    FE_CUDA(cudaStreamSynchronize(st));
+    cap = (int64_t)*h_pinned;
+    if (cap < 1) cap = 1;
+  }
+  const size_t key_bytes = carve_keys(nullptr, cap, [](const KeySpace&) {});
+  rc = keybuf.reserve(key_bytes, st);
+  if (rc) return rc;
+  carve_keys(keybuf.ptr, cap, [&](const KeySpace& s) { ks = s; });
+  if (exact) launch_scan(rs.touched, rs.incl, p.n_rec, cap, rs.scan_tmp, rs.ctrl, st);
+  launch_emit_keys(p.va, rs.incl, rs.rects, p.n_rec, rs.ctrl, ks.keys_a, cap, st);
+  sorted = launch_sort(ks.keys_a, ks.keys_b, bits_for(p.n_tiles), rs.ctrl, cap, ks.hist, st);
+  launch_ranges_gather(p.va, sorted, rs.ctrl, cap, rs.recs, p.tile_w, p.tile_h, rs.ranges,
+                       ks.trec, st);
+  return FE_OK;
+}
+
+Pipeline single_view_pipeline(const fe_render_desc* d, const float* means, const float* prec,
+                              const float* logw, const float* quat, const float* trans) {
+  Pipeline p{};
+  int tw, th;
+  tile_shape(d, tw, th);
+  ViewDev v{};
+  v.fx = d->fx; v.fy = d->fy; v.cx = d->cx; v.cy = d->cy;
+  v.H = d->height; v.W = d->width;
+  v.gx = (d->width + tw - 1) / tw;
+  v.gy = (d->height + th - 1) / th;
+  v.n = d->n_gaussians;
+  p.va.table = nullptr;
+  p.va.count = 1;
+  p.va.one = v;
+  p.n_rec = d->n_gaussians;
+  p.n_tiles = (int64_t)v.gx * v.gy;
+  p.n_pix = (int64_t)d->height * d->width;
+  p.tile_w = tw;
+  p.tile_h = th;
+  p.cull_mode = d->cull_mode;
+  p.cull_param = d->cull_param;
+  p.beta2 = d->beta2;
+  p.beta3 = d->beta3;
+  p.means = means; p.prec = prec; p.logw = logw; p.quat = quat; p.trans = trans;
+  return p;
+}
+
+}  // namespace
+}  // namespace fe
+
+using namespace fe;
+
+extern "C" {
+
+const char* fe_version(void) { return "fuzzy_ellipses_gb300 0.1.0 (sm_103a)"; }
+
+const char* fe_last_error_message(void) { return g_last_error.c_str(); }
+
+const char* fe_status_string(int s) {
+  switch (s) {
+    case FE_OK: return "ok";
+    case FE_ERR_INVALID_ARGUMENT: return "invalid argument";
+    case FE_ERR_DESCRIPTOR: return "bad descriptor";
+    case FE_ERR_CUDA: return "CUDA error";
+    case FE_ERR_OUT_OF_MEMORY: return "out of device memory";
+    case FE_ERR_CAPACITY: return "key capacity exceeded";
+    case FE_ERR_DEVICE_TIMEOUT: return "device wait timed out";
+    case FE_ERR_UNSUPPORTED: return "unsupported";
+    case FE_ERR_SCRATCH_LIMIT: return "request exceeds the fixed scratch size";
+    default: return "unknown status";
+  }
+}
+
+void fe_render_desc_init(fe_render_desc* d, int32_t n, int32_t h, int32_t w, float fx, float fy,
+                         float cx, float cy) {
+  std::memset(d, 0, sizeof(*d));
+  d->magic = FE_DESC_MAGIC;
+  d->version = FE_DESC_VERSION;
+  d->n_gaussians = n;
+  d->height = h;
+  d->width = w;
+  d->fx = fx; d->fy = fy; d->cx = cx; d->cy = cy;
+  d->beta2 = 21.4f;
+  d->beta3 = 2.66f;
+  d->cull_mode = FE_CULL_EPS;
+  d->cull_param = kDefaultCullEps;
+  d->tile_w = 16;
+  d->tile_h = 16;
+}
+
+int fe_render_fwd(const fe_render_desc* d, const float* means, const float* prec,
+                  const float* logw, const float* quat, const float* trans, float* depth,
+                  float* alpha, float* stats, fe_stream_t stream_) {
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream_);
+  int rc = check_desc(d);
+  if (rc) return rc;
+  if (!depth || !alpha || !quat || !trans)
+    return fail(FE_ERR_INVALID_ARGUMENT, "NULL output or pose pointer");
+  const int64_t npix = (int64_t)d->height * d->width;
+  if (d->n_gaussians == 0) {
+    FE_CUDA(cudaMemsetAsync(depth, 0, sizeof(float) * npix, st));
+    FE_CUDA(cudaMemsetAsync(alpha, 0, sizeof(float) * npix, st));
+    if (stats) FE_CUDA(cudaMemsetAsync(stats, 0, sizeof(float) * 3 * npix, st));
+    return FE_OK;
+  }
+  if (!means || !prec || !logw) return fail(FE_ERR_INVALID_ARGUMENT, "NULL Gaussian pointer");
+  Arena* a = nullptr;
+  rc = arena_for(st, &a);
+  if (rc) return rc;
+  Pipeline p = single_view_pipeline(d, means, prec, logw, quat, trans);
+  RecSpace rs;
+  KeySpace ks;
+  int64_t cap = 0;
+  uint64_t* sorted = nullptr;
+  rc = run_binning(p, p.n_rec * p.n_tiles, a->rec, a->keys, a->h_pinned, false, st, rs, ks, cap,
+                   sorted);
+  if (rc) return rc;
+  launch_blend_fwd(p.va, p.tile_w, p.tile_h, p.n_tiles, ks.trec, rs.ranges, p.beta2, p.beta3,
+                   depth, alpha, stats, npix, rs.ctrl, st);
+  FE_CUDA(cudaGetLastError());
+  return FE_OK;
+}
+
+int fe_render_bwd(const fe_render_desc* d, const float* means, const float* prec,
+                  const float* logw, const float* quat, const float* trans, const float* depth,
+                  const float* alpha, const float* stats, const float* gdepth,
+                  const float* galpha, float* gmeans, float* gprec, float* glogw,
+                  fe_stream_t stream_) {
+  (void)alpha;
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream_);
+  int rc = check_desc(d);
+  if (rc) return rc;
+  const int64_t n = d->n_gaussians;
+  if (n == 0) return FE_OK;
+  if (!means || !prec || !logw || !quat || !trans || !depth || !stats || !gmeans || !gprec ||
+      !glogw)
+    return fail(FE_ERR_INVALID_ARGUMENT, "NULL pointer");
+  FE_CUDA(cudaMemsetAsync(gmeans, 0, sizeof(float) * 3 * n, st));
+  FE_CUDA(cudaMemsetAsync(gprec, 0, sizeof(float) * 9 * n, st));
+  FE_CUDA(cudaMemsetAsync(glogw, 0, sizeof(float) * n, st));
+  Arena* a = nullptr;
+  rc = arena_for(st, &a);
+  if (rc) return rc;
+  Pipeline p = single_view_pipeline(d, means, prec, logw, quat, trans);
+  RecSpace rs;
+  KeySpace ks;
+  int64_t cap = 0;
+  uint64_t* sorted = nullptr;
+  rc = run_binning(p, p.n_rec * p.n_tiles, a->rec, a->keys, a->h_pinned, true, st, rs, ks, cap,
+                   sorted);
+  if (rc) return rc;
+  FE_CUDA(cudaMemsetAsync(rs.rgrad, 0, sizeof(RecGrad) * (size_t)p.n_rec, st));
+  launch_pixel_prep(p.va, p.n_pix, depth, stats, p.n_pix, gdepth, galpha, rs.pix, st);
+  launch_blend_bwd(p.va, p.tile_w, p.tile_h, sorted, rs.ctrl, cap, ks.trec, rs.recs, rs.pix,
+                   p.beta2, p.beta3, rs.rgrad, st);
+  launch_record_vjp(p.va, p.n_rec, means, prec, quat, trans, rs.recs, rs.rgrad, gmeans, gprec,
+                    glogw, st);
+  FE_CUDA(cudaGetLastError());
+  return FE_OK;
+}
+
+int fe_render_binning(const fe_render_desc* d, const float* means, const float* prec,
+                      const float* logw, const float* quat, const float* trans, uint64_t* keys,
+                      int64_t key_capacity, uint32_t* ranges, int64_t* h_num_keys,
+                      fe_stream_t stream_) {
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream_);
+  int rc = check_desc(d);
+  if (rc) return rc;
+  if (!h_num_keys || !ranges || !quat || !trans || key_capacity < 0)
+    return fail(FE_ERR_INVALID_ARGUMENT, "NULL pointer or negative capacity");
+  *h_num_keys = 0;
+  Pipeline p = single_view_pipeline(d, means, prec, logw, quat, trans);
+  FE_CUDA(cudaMemsetAsync(ranges, 0, sizeof(uint2) * (size_t)p.n_tiles, st));
+  if (p.n_rec == 0) return FE_OK;
+  if (!means || !prec || !logw) return fail(FE_ERR_INVALID_ARGUMENT, "NULL Gaussian pointer");
+  Arena* a = nullptr;
+  rc = arena_for(st, &a);
+  if (rc) return rc;
+  RecSpace rs;
+  KeySpace ks;
+  int64_t cap = 0;
+  uint64_t* sorted = nullptr;
+  rc = run_binning(p, p.n_rec * p.n_tiles, a->rec, a->keys, a->h_pinned, false, st, rs, ks, cap,
+                   sorted);
+  if (rc) return rc;
+  FE_CUDA(cudaMemcpyAsync(a->h_pinned, &rs.ctrl->num_keys, sizeof(unsigned long long),
+                          cudaMemcpyDeviceToHost, st));
+  FE_CUDA(cudaStreamSynchronize(st));
+  const int64_t K = (int64_t)*a->h_pinned;
+  *h_num_keys = K;
+  if (K > key_capacity) return fail(FE_ERR_CAPACITY, "key capacity too small");
+  if (K > 0 && keys)
+    FE_CUDA(cudaMemcpyAsync(keys, sorted, sizeof(uint64_t) * (size_t)K, cudaMemcpyDeviceToDevice, st));
+  FE_CUDA(cudaMemcpyAsync(ranges, rs.ranges, sizeof(uint2) * (size_t)p.n_tiles,
+                          cudaMemcpyDeviceToDevice, st));
+  FE_CUDA(cudaGetLastError());
+  return FE_OK;
+}
+
+int fe_check_device_status(fe_stream_t stream_, uint32_t* device_error) {
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream_);
+  Arena* a = nullptr;
+  int rc = arena_for(st, &a);
+  if (rc) return rc;
+  FE_CUDA(cudaStreamSynchronize(st));
+  uint32_t err = 0;
+  if (a->rec.ptr) {
+    Control* ctrl = reinterpret_cast<Control*>(a->rec.ptr);
+    FE_CUDA(cudaMemcpy(&err, &ctrl->error, sizeof(uint32_t), cudaMemcpyDeviceToHost));
+    FE_CUDA(cudaMemset(&ctrl->error, 0, sizeof(uint32_t)));
+  }
+  if (device_error) *device_error = err;
+  return FE_OK;
+}
+
+
+// ---------------------------------------------------------------------------------------------
+// Reference-compatible binning and the legacy interface
+// ---------------------------------------------------------------------------------------------
+
+int fe_reference_binning(int32_t P, int32_t height, int32_t width, float n_std,
+                         const float* means, const float* scales, const float* rots,
+                         const float* view, const float* proj, float tan_fovx, float tan_fovy,
+                         int32_t* radii, float* means2d, uint32_t* tiles_touched, uint64_t* keys,
+                         int64_t key_capacity, uint32_t* ranges, int64_t* h_num_keys,
+                         fe_stream_t stream_) {
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream_);
+  if (P < 0 || height < 1 || width < 1 || !h_num_keys || key_capacity < 0 ||
+      key_capacity > INT64_C(0xffffffff))
+    return fail(FE_ERR_INVALID_ARGUMENT, "bad size or capacity");
+  const int gx = (width + 7) / 8, gy = (height + 7) / 8;
+  const int64_t T = (int64_t)gx * gy;
+  *h_num_keys = 0;
+  if (ranges) FE_CUDA(cudaMemsetAsync(ranges, 0, sizeof(uint2) * (size_t)T, st));
+  if (P == 0) return FE_OK;
+  if (!means || !scales || !rots || !view || !proj || !radii || !means2d || !tiles_touched ||
+      !keys || !ranges)
+    return fail(FE_ERR_INVALID_ARGUMENT, "NULL pointer");
+  Arena* a = nullptr;
+  int rc = arena_for(st, &a);
+  if (rc) return rc;
+  RecSpace rs;
+  const size_t rb = carve_rec(nullptr, P, T, 0, false, [](const RecSpace&) {});
+  rc = a->rec.reserve(rb, st);
+  if (rc) return rc;
+  carve_rec(a->rec.ptr, P, T, 0, false, [&](const RecSpace& s_) { rs = s_; });
+  FE_CUDA(cudaMemsetAsync(rs.ctrl, 0, sizeof(Control), st));
+  launch_preprocess_reference(P, n_std, means, scales, rots, view, proj, width, height, tan_fovx,
+                              tan_fovy, gx, gy, radii, means2d, rs.rects, rs.touched, st);
+  launch_scan(rs.touched, tiles_touched, P, key_capacity, rs.scan_tmp, rs.ctrl, st);
+  FE_CUDA(cudaMemcpyAsync(a->h_pinned, &rs.ctrl->want_keys, sizeof(unsigned long long),
+                          cudaMemcpyDeviceToHost, st));
+  FE_CUDA(cudaStreamSynchronize(st));
+  const int64_t K = (int64_t)*a->h_pinned;
+  *h_num_keys = K;
+  if (K > key_capacity) return fail(FE_ERR_CAPACITY, "key capacity too small");
+  if (K == 0) return FE_OK;
+  KeySpace ks;
+  const size_t kb = carve_keys(nullptr, K, [](const KeySpace&) {});
+  rc = a->keys.reserve(kb, st);
+  if (rc) return rc;
+  carve_keys(a->keys.ptr, K, [&](const KeySpace& s_) { ks = s_; });
+  ViewsArg va{};
+  va.count = 1;
+  va.one.H = height; va.one.W = width; va.one.gx = gx; va.one.gy = gy; va.one.n = P;
+  launch_emit_keys(va, tiles_touched, rs.rects, P, rs.ctrl, keys, K, st);
+  uint64_t* sorted = launch_sort(keys, ks.keys_b, bits_for(T), rs.ctrl, K, ks.hist, st);
+  if (sorted != keys)
+    FE_CUDA(cudaMemcpyAsync(keys, sorted, sizeof(uint64_t) * (size_t)K, cudaMemcpyDeviceToDevice, st));
+  launch_ranges(keys, rs.ctrl, K, reinterpret_cast<uint2*>(ranges), st);
+  FE_CUDA(cudaGetLastError());
+  return FE_OK;
+}
+
+// rasterizer_impl.cu:154-172: the reference's choice of n_std from the Gaussian count.
+static float reference_num_stds(int n) {
+  if (n <= 1000) return 3.0f;
+  if (n <= 5000) return 0.75f;
+  if (n <= 100000) return 0.50f;
+  return 0.10f;
+}
+
+int fe_rasterize_legacy(const fe_legacy_desc* d, const float* means, const float* weights,
+                        const float* scales, const float* rots, const float* rays,
+                        const float* rot, const float* trans, const float* view,
+                        const float* proj, float* out_z, float* out_alpha, fe_stream_t stream_) {
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream_);
+  if (!d || d->P < 0 || d->image_height < 1 || d->image_width < 1)
+    return fail(FE_ERR_INVALID_ARGUMENT, "bad legacy descriptor");
+  const int P = d->P, H = d->image_height, W = d->image_width;
+  const int gx = (W + 7) / 8, gy = (H + 7) / 8;
+  const int64_t T = (int64_t)gx * gy, npix = (int64_t)H * W;
+  if (!out_z || !out_alpha) return fail(FE_ERR_INVALID_ARGUMENT, "NULL output");
+  if (P == 0) {
+    FE_CUDA(cudaMemsetAsync(out_z, 0, sizeof(float) * npix, st));
+    FE_CUDA(cudaMemsetAsync(out_alpha, 0, sizeof(float) * npix, st));
+    return FE_OK;
+  }
+  if (!means || !weights || !scales || !rots || !rays || !rot || !trans || !view || !proj)
+    return fail(FE_ERR_INVALID_ARGUMENT, "NULL input");
+  Arena* a = nullptr;
+  int rc = arena_for(st, &a);
+  if (rc) return rc;
+  // Per-record space plus the reference's radii/means2d outputs.
+  RecSpace rs;
+  Carver extra{nullptr};
+  const size_t rb = carve_rec(nullptr, P, T, 0, false, [](const RecSpace&) {});
+  extra.off = rb;
+  extra.take<int32_t>(P);
+  extra.take<float>(2 * (int64_t)P);
+  rc = a->rec.reserve(extra.off, st);
+  if (rc) return rc;
+  carve_rec(a->rec.ptr, P, T, 0, false, [&](const RecSpace& s_) { rs = s_; });
+  Carver ex2{a->rec.ptr};
+  ex2.off = rb;
+  int32_t* radii = ex2.take<int32_t>(P);
+  float* means2d = ex2.take<float>(2 * (int64_t)P);
+
+  ViewsArg va{};
+  va.count = 1;
+  va.one.H = H; va.one.W = W; va.one.gx = gx; va.one.gy = gy; va.one.n = P;
+  va.one.fx = 1.f; va.one.fy = 1.f;
+  FE_CUDA(cudaMemsetAsync(rs.ctrl, 0, sizeof(Control), st));
+  FE_CUDA(cudaMemsetAsync(rs.ranges, 0, sizeof(uint2) * (size_t)T, st));
+  launch_preprocess_reference(P, reference_num_stds(P), means, scales, rots, view, proj, W, H,
+                              d->tan_fovx, d->tan_fovy, gx, gy, radii, means2d, rs.rects,
+                              rs.touched, st);
+  launch_legacy_records(va, P, means, scales, rots, weights, rot, trans, rays, rs.recs, st);
+  const int64_t worst = (int64_t)P * T;
+  int64_t cap;
+  if ((size_t)worst * kBytesPerKey <= key_budget_bytes()) {
+    cap = worst;
+    launch_scan(rs.touched, rs.incl, P, cap, rs.scan_tmp, rs.ctrl, st);
+  } else {
+    launch_scan(rs.touched, rs.incl, P, INT64_C(0xffffffff), rs.scan_tmp, rs.ctrl, st);
+    FE_CUDA(cudaMemcpyAsync(a->h_pinned, &rs.ctrl->want_keys, sizeof(unsigned long long),
+                            cudaMemcpyDeviceToHost, st));
+    FE_CUDA(cudaStreamSynchronize(st));
+    cap = (int64_t)*a->h_pinned;
+    if (cap < 1) cap = 1;
+  }
+  KeySpace ks;
+  const size_t kb = carve_keys(nullptr, cap, [](const KeySpace&) {});
+  rc = a->keys.reserve(kb, st);
+  if (rc) return rc;
+  carve_keys(a->keys.ptr, cap, [&](const KeySpace& s_) { ks = s_; });
+  launch_emit_keys(va, rs.incl, rs.rects, P, rs.ctrl, ks.keys_a, cap, st);
+  uint64_t* sorted = launch_sort(ks.keys_a, ks.keys_b, bits_for(T), rs.ctrl, cap, ks.hist, st);
+  launch_ranges_gather(va, sorted, rs.ctrl, cap, rs.recs, 8, 8, rs.ranges, ks.trec, st);
+  launch_blend_fwd(va, 8, 8, T, ks.trec, rs.ranges, 21.4f, 2.66f, out_z, out_alpha, nullptr, 0,
+                   rs.ctrl, st);
+  FE_CUDA(cudaGetLastError());
+  return FE_OK;
+}
+
+// ---------------------------------------------------------------------------------------------
+// XLA custom-call targets (api_version 2)
+// ---------------------------------------------------------------------------------------------
+
+static void xla_report(XlaCustomCallStatus* status, int rc) {
+  if (rc == FE_OK || !status) return;
+  using SetFailure = void (*)(XlaCustomCallStatus*, const char*, size_t);
+  static SetFailure fn = reinterpret_cast<SetFailure>(dlsym(RTLD_DEFAULT, "XlaCustomCallStatusSetFailure"));
+  std::string msg = std::string("fuzzy_ellipses: ") + fe_status_string(rc) + ": " + g_last_error;
+  if (fn) fn(status, msg.c_str(), msg.size());
+  else std::fprintf(stderr, "%s\n", msg.c_str());
+}
+
+void fe_render_fwd_xla(fe_stream_t stream, void** buffers, const char* opaque, size_t opaque_len,
+                       XlaCustomCallStatus* status) {
+  fe_render_desc d;
+  if (opaque_len != sizeof(fe_render_desc)) {
+    xla_report(status, fail(FE_ERR_DESCRIPTOR, "opaque has the wrong size"));
+    return;
+  }
+  std::memcpy(&d, opaque, sizeof d);
+  float** b = reinterpret_cast<float**>(buffers);
+  xla_report(status, fe_render_fwd(&d, b[0], b[1], b[2], b[3], b[4], b[5], b[6], b[7], stream));
+}
+
+void fe_render_bwd_xla(fe_stream_t stream, void** buffers, const char* opaque, size_t opaque_len,
+                       XlaCustomCallStatus* status) {
+  fe_render_desc d;
+  if (opaque_len != sizeof(fe_render_desc)) {
+    xla_report(status, fail(FE_ERR_DESCRIPTOR, "opaque has the wrong size"));
+    return;
+  }
+  std::memcpy(&d, opaque, sizeof d);
+  float** b = reinterpret_cast<float**>(buffers);
+  xla_report(status, fe_render_bwd(&d, b[0], b[1], b[2], b[3], b[4], b[5], b[6], b[7], b[8], b[9],
+                                   b[10], b[11], b[12], stream));
+}
+
+void fe_rasterize_legacy_xla(fe_stream_t stream, void** buffers, const char* opaque,
+                             size_t opaque_len, XlaCustomCallStatus* status) {
+  if (opaque_len != sizeof(fe_legacy_desc)) {
+    xla_report(status, fail(FE_ERR_DESCRIPTOR, "opaque has the wrong size"));
+    return;
+  }
+  fe_legacy_desc d;
+  std::memcpy(&d, opaque, sizeof d);
+  float** b = reinterpret_cast<float**>(buffers);
+  xla_report(status, fe_rasterize_legacy(&d, b[0], b[1], b[2], b[3], b[4], b[5], b[6], b[7], b[8],
+                                         b[9], b[10], stream));
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------------------------
+// Batches
+// ---------------------------------------------------------------------------------------------
+
+struct fe_batch {
+  int device = 0;
+  fe_render_desc desc{};
+  int tile_w = 16, tile_h = 16;
+  int32_t n_views = 0;
+  ViewDev* views_d = nullptr;
+  float* quat_d = nullptr;
+  float* trans_d = nullptr;
+  int64_t n_rec = 0, n_tiles = 0, n_pix = 0, cap = 0;
+  int64_t n_gauss = 0;  // extent of the concatenated Gaussian arrays the scenes reference
+  DevBuf rec, keys;
+  RecSpace rs{};
+  KeySpace ks{};
+  uint64_t* sorted = nullptr;
+  unsigned long long* h_pinned = nullptr;
+};
+
+extern "C" {
+
+int fe_batch_create(const fe_render_desc* desc, const fe_scene* scenes, int32_t n_scenes,
+                    const fe_view* views, int32_t n_views, fe_batch** out) {
+  if (!out) return fail(FE_ERR_INVALID_ARGUMENT, "out is NULL");
+  *out = nullptr;
+  if (!desc || desc->magic != FE_DESC_MAGIC || desc->version != FE_DESC_VERSION)
+    return fail(FE_ERR_DESCRIPTOR, "descriptor magic/version mismatch");
+  if (n_scenes < 0 || n_views < 1 || !views || (n_scenes > 0 && !scenes))
+    return fail(FE_ERR_INVALID_ARGUMENT, "empty batch");
+  fe_render_desc probe = *desc;
+  probe.height = 1; probe.width = 1; probe.n_gaussians = 0; probe.fx = 1.f; probe.fy = 1.f;
+  int rc = check_desc(&probe);
+  if (rc) return rc;
+  for (int i = 0; i < n_views; ++i) {
+    const fe_view& v = views[i];
+    if (v.scene < 0 || v.scene >= n_scenes || v.height < 1 || v.width < 1 || v.pixel_offset < 0 ||
+        !(v.fx != 0.f) || !(v.fy != 0.f) || scenes[v.scene].n < 0 || scenes[v.scene].gauss_offset < 0)
+      return fail(FE_ERR_INVALID_ARGUMENT, "bad view " + std::to_string(i));
+  }
+  fe_batch* b = new fe_batch();
+  b->desc = *desc;
+  tile_shape(desc, b->tile_w, b->tile_h);
+  if (cudaGetDevice(&b->device) != cudaSuccess) {
+    delete b;
+    return fail(FE_ERR_CUDA, "cudaGetDevice failed");
+  }
+  std::vector<ViewDev> vt(n_views);
+  std::vector<float> q(4 * (size_t)n_views), t(3 * (size_t)n_views);
+  int64_t rec = 0, tiles = 0, pix_end = 0, worst = 0;
+  for (int i = 0; i < n_views; ++i) {
+    const fe_view& v = views[i];
+    ViewDev& d = vt[i];
+    d.fx = v.fx; d.fy = v.fy; d.cx = v.cx; d.cy = v.cy;
+    d.H = v.height; d.W = v.width;
+    d.gx = (v.width + b->tile_w - 1) / b->tile_w;
+    d.gy = (v.height + b->tile_h - 1) / b->tile_h;
+    d.n = scenes[v.scene].n;
+    d.pose = i;
+    d.gauss_base = scenes[v.scene].gauss_offset;
+    d.rec_base = rec;
+    d.tile_base = tiles;
+    d.pix_base = v.pixel_offset;
+    rec += d.n;
+    tiles += (int64_t)d.gx * d.gy;
+    worst += (int64_t)d.n * d.gx * d.gy;
+    pix_end = std::max<int64_t>(pix_end, v.pixel_offset + (int64_t)v.height * v.width);
+    for (int k = 0; k < 4; ++k) q[4 * i + k] = v.quat[k];
+    for (int k = 0; k < 3; ++k) t[3 * i + k] = v.trans[k];
+  }
+  for (int s_ = 0; s_ < n_scenes; ++s_)
+    b->n_gauss = std::max<int64_t>(b->n_gauss, scenes[s_].gauss_offset + scenes[s_].n);
+  if (tiles > INT64_C(0xffffffff)) {
+    delete b;
+    return fail(FE_ERR_INVALID_ARGUMENT, "too many tiles in one batch");
+  }
+  b->n_views = n_views;
+  b->n_rec = rec;
+  b->n_tiles = tiles;
+  b->n_pix = pix_end;
+  const int64_t budget_keys = (int64_t)(key_budget_bytes() / kBytesPerKey);
+  b->cap = std::max<int64_t>(1, std::min<int64_t>({worst, budget_keys, INT64_C(0xffffffff)}));
+  auto cleanup = [&](int code) {
+    fe_batch_destroy(b);
+    return code;
+  };
+  if (cudaMalloc(&b->views_d, sizeof(ViewDev) * n_views) != cudaSuccess ||
+      cudaMalloc(&b->quat_d, sizeof(float) * q.size()) != cudaSuccess ||
+      cudaMalloc(&b->trans_d, sizeof(float) * t.size()) != cudaSuccess) {
+    cudaGetLastError();
+    return cleanup(fail(FE_ERR_OUT_OF_MEMORY, "batch tables"));
+  }
+  if (cudaMemcpy(b->views_d, vt.data(), sizeof(ViewDev) * n_views, cudaMemcpyHostToDevice) ||
+      cudaMemcpy(b->quat_d, q.data(), sizeof(float) * q.size(), cudaMemcpyHostToDevice) ||
+      cudaMemcpy(b->trans_d, t.data(), sizeof(float) * t.size(), cudaMemcpyHostToDevice))
+    return cleanup(fail(FE_ERR_CUDA, "batch table upload"));
+  const size_t rb = carve_rec(nullptr, b->n_rec, b->n_tiles, b->n_pix, true, [](const RecSpace&) {});
+  const size_t kb = carve_keys(nullptr, b->cap, [](const KeySpace&) {});
+  rc = b->rec.reserve(rb, nullptr);
+  if (!rc) rc = b->keys.reserve(kb, nullptr);
+  if (rc) return cleanup(rc);
+  carve_rec(b->rec.ptr, b->n_rec, b->n_tiles, b->n_pix, true, [&](const RecSpace& s_) { b->rs = s_; });
+  carve_keys(b->keys.ptr, b->cap, [&](const KeySpace& s_) { b->ks = s_; });
+  if (cudaMallocHost(&b->h_pinned, 64) != cudaSuccess) {
+    cudaGetLastError();
+    b->h_pinned = nullptr;
+    return cleanup(fail(FE_ERR_OUT_OF_MEMORY, "pinned staging"));
+  }
+  *out = b;
+  return FE_OK;
+}
+
+void fe_batch_destroy(fe_batch* b) {
+  if (!b) return;
+  cudaFree(b->views_d);
+  cudaFree(b->quat_d);
+  cudaFree(b->trans_d);
+  cudaFree(b->rec.ptr);
+  cudaFree(b->keys.ptr);
+  if (b->h_pinned) cudaFreeHost(b->h_pinned);
+  delete b;
+}
+
+int64_t fe_batch_pixels(const fe_batch* b) { return b ? b->n_pix : 0; }
+
+int64_t fe_batch_scratch_bytes(const fe_batch* b) {
+  return b ? (int64_t)(b->rec.cap + b->keys.cap) : 0;
+}
+
+static Pipeline batch_pipeline(fe_batch* b, const float* means, const float* prec,
+                               const float* logw) {
+  Pipeline p{};
+  p.va.table = b->views_d;
+  p.va.count = b->n_views;
+  p.n_rec = b->n_rec;
+  p.n_tiles = b->n_tiles;
+  p.n_pix = b->n_pix;
+  p.tile_w = b->tile_w;
+  p.tile_h = b->tile_h;
+  p.cull_mode = b->desc.cull_mode;
+  p.cull_param = b->desc.cull_param;
+  p.beta2 = b->desc.beta2;
+  p.beta3 = b->desc.beta3;
+  p.means = means; p.prec = prec; p.logw = logw; p.quat = b->quat_d; p.trans = b->trans_d;
+  return p;
+}
+
+static int batch_binning(fe_batch* b, const Pipeline& p, cudaStream_t st) {
+  const RecSpace& rs = b->rs;
+  const KeySpace& ks = b->ks;
+  FE_CUDA(cudaMemsetAsync(rs.ctrl, 0, sizeof(Control), st));
+  FE_CUDA(cudaMemsetAsync(rs.ranges, 0, sizeof(uint2) * (size_t)p.n_tiles, st));
+  launch_preprocess(p.va, p.n_rec, p.means, p.prec, p.logw, p.quat, nullptr, p.trans, p.cull_mode,
+                    p.cull_param, p.tile_w, p.tile_h, rs.recs, rs.rects, rs.touched, st);
+  launch_scan(rs.touched, rs.incl, p.n_rec, b->cap, rs.scan_tmp, rs.ctrl, st);
+  launch_emit_keys(p.va, rs.incl, rs.rects, p.n_rec, rs.ctrl, ks.keys_a, b->cap, st);
+  b->sorted = launch_sort(ks.keys_a, ks.keys_b, bits_for(p.n_tiles), rs.ctrl, b->cap, ks.hist, st);
+  launch_ranges_gather(p.va, b->sorted, rs.ctrl, b->cap, rs.recs, p.tile_w, p.tile_h, rs.ranges,
+                       ks.trec, st);
+  return FE_OK;
+}
+
+int fe_batch_fwd(fe_batch* b, const float* means, const float* prec, const float* logw,
+                 float* depth, float* alpha, float* stats, fe_stream_t stream_) {
+  if (!b || !depth || !alpha) return fail(FE_ERR_INVALID_ARGUMENT, "NULL argument");
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream_);
+  Pipeline p = batch_pipeline(b, means, prec, logw);
+  if (p.n_rec > 0 && (!means || !prec || !logw))
+    return fail(FE_ERR_INVALID_ARGUMENT, "NULL Gaussian pointer");
+  int rc = batch_binning(b, p, st);
+  if (rc) return rc;
+  launch_blend_fwd(p.va, p.tile_w, p.tile_h, p.n_tiles, b->ks.trec, b->rs.ranges, p.beta2, p.beta3,
+                   depth, alpha, stats, p.n_pix, b->rs.ctrl, st);
+  FE_CUDA(cudaGetLastError());
+  return FE_OK;
+}
+
+int fe_batch_bwd(fe_batch* b, const float* means, const float* prec, const float* logw,
+                 const float* depth, const float* alpha, const float* stats, const float* gdepth,
+                 const float* galpha, float* gmeans, float* gprec, float* glogw,
+                 fe_stream_t stream_) {
+  (void)alpha;
+  if (!b || !depth || !stats || !gmeans || !gprec || !glogw)
+    return fail(FE_ERR_INVALID_ARGUMENT, "NULL argument");
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream_);
+  Pipeline p = batch_pipeline(b, means, prec, logw);
+  FE_CUDA(cudaMemsetAsync(gmeans, 0, sizeof(float) * 3 * (size_t)b->n_gauss, st));
+  FE_CUDA(cudaMemsetAsync(gprec, 0, sizeof(float) * 9 * (size_t)b->n_gauss, st));
+  FE_CUDA(cudaMemsetAsync(glogw, 0, sizeof(float) * (size_t)b->n_gauss, st));
+  int rc = batch_binning(b, p, st);
+  if (rc) return rc;
+  FE_CUDA(cudaMemsetAsync(b->rs.rgrad, 0, sizeof(RecGrad) * (size_t)p.n_rec, st));
+  launch_pixel_prep(p.va, p.n_pix, depth, stats, p.n_pix, gdepth, galpha, b->rs.pix, st);
+  launch_blend_bwd(p.va, p.tile_w, p.tile_h, b->sorted, b->rs.ctrl, b->cap, b->ks.trec,
+                   b->rs.recs, b->rs.pix, p.beta2, p.beta3, b->rs.rgrad, st);
+  launch_record_vjp(p.va, p.n_rec, means, prec, p.quat, p.trans, b->rs.recs, b->rs.rgrad, gmeans,
+                    gprec, glogw, st);
+  FE_CUDA(cudaGetLastError());
+  return FE_OK;
+}
+
+int fe_batch_status(fe_batch* b, fe_stream_t stream_, int64_t* num_keys, int64_t* want_keys,
+                    uint32_t* device_error) {
+  if (!b) return fail(FE_ERR_INVALID_ARGUMENT, "NULL batch");
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream_);
+  Control c;
+  FE_CUDA(cudaMemcpyAsync(b->h_pinned, b->rs.ctrl, sizeof(unsigned long long) * 3,
+                          cudaMemcpyDeviceToHost, st));
+  FE_CUDA(cudaStreamSynchronize(st));
+  std::memcpy(&c, b->h_pinned, sizeof(unsigned long long) * 3);
+  if (num_keys) *num_keys = (int64_t)c.num_keys;
+  if (want_keys) *want_keys = (int64_t)c.want_keys;
+  if (device_error) *device_error = c.error;
+  return FE_OK;
+}
+
+}  // extern "C"
+
+namespace fe {
+double run_peak(int kind, int iters, float* scratch, cudaStream_t st);
+}
+
+extern "C" {
+
+int fe_batch_fwd_timed(fe_batch* b, const float* means, const float* prec, const float* logw,
+                       float* depth, float* alpha, float* stats, float* stage_ms,
+                       fe_stream_t stream_) {
+  if (!b || !depth || !alpha || !stage_ms) return fail(FE_ERR_INVALID_ARGUMENT, "NULL argument");
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream_);
+  Pipeline p = batch_pipeline(b, means, prec, logw);
+  const RecSpace& rs = b->rs;
+  const KeySpace& ks = b->ks;
+  cudaEvent_t ev[7];
+  for (auto& e : ev) FE_CUDA(cudaEventCreate(&e));
+  FE_CUDA(cudaMemsetAsync(rs.ctrl, 0, sizeof(Control), st));
+  FE_CUDA(cudaMemsetAsync(rs.ranges, 0, sizeof(uint2) * (size_t)p.n_tiles, st));
+  FE_CUDA(cudaEventRecord(ev[0], st));
+  launch_preprocess(p.va, p.n_rec, p.means, p.prec, p.logw, p.quat, nullptr, p.trans, p.cull_mode,
+                    p.cull_param, p.tile_w, p.tile_h, rs.recs, rs.rects, rs.touched, st);
+  FE_CUDA(cudaEventRecord(ev[1], st));
+  launch_scan(rs.touched, rs.incl, p.n_rec, b->cap, rs.scan_tmp, rs.ctrl, st);
+  FE_CUDA(cudaEventRecord(ev[2], st));
+  launch_emit_keys(p.va, rs.incl, rs.rects, p.n_rec, rs.ctrl, ks.keys_a, b->cap, st);
+  FE_CUDA(cudaEventRecord(ev[3], st));
+  b->sorted = launch_sort(ks.keys_a, ks.keys_b, bits_for(p.n_tiles), rs.ctrl, b->cap, ks.hist, st);
+  FE_CUDA(cudaEventRecord(ev[4], st));
+  launch_ranges_gather(p.va, b->sorted, rs.ctrl, b->cap, rs.recs, p.tile_w, p.tile_h, rs.ranges,
+                       ks.trec, st);
+  FE_CUDA(cudaEventRecord(ev[5], st));
+  launch_blend_fwd(p.va, p.tile_w, p.tile_h, p.n_tiles, ks.trec, rs.ranges, p.beta2, p.beta3,
+                   depth, alpha, stats, p.n_pix, rs.ctrl, st);
+  FE_CUDA(cudaEventRecord(ev[6], st));
+  FE_CUDA(cudaEventSynchronize(ev[6]));
+  for (int i = 0; i < 6; ++i) FE_CUDA(cudaEventElapsedTime(&stage_ms[i], ev[i], ev[i + 1]));
+  for (auto& e : ev) cudaEventDestroy(e);
+  FE_CUDA(cudaGetLastError());
+  return FE_OK;
+}
+
+int fe_batch_launch_count(const fe_batch* b) {
+  if (!b) return 0;
+  const int passes = (bits_for(b->n_tiles) + 7) / 8;
+  return 1 + 3 + 1 + 3 * passes + 1 + 1;
+}
+
+int fe_bench_peak(int kind, int iters, double* ops_per_second, fe_stream_t stream_) {
+  if (!ops_per_second || kind < 0 || kind > 1 || iters < 1)
+    return fail(FE_ERR_INVALID_ARGUMENT, "bad peak benchmark request");
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream_);
+  float* scratch = nullptr;
+  FE_CUDA(cudaMalloc(&scratch, 1 << 20));
+  *ops_per_second = run_peak(kind, iters, scratch, st);
+  cudaFree(scratch);
+  FE_CUDA(cudaGetLastError());
+  return FE_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,350 @@
+// binning.cu -- from per-record footprints to per-tile Gaussian lists.
+//
+//  scan      inclusive prefix sum of tiles_touched (reference: thrust::inclusive_scan,
+//            cuda_rasterizer/rasterizer_impl.cu:244), total key count kept on the device
+//  emit      one thread per key writes (global_tile << 32 | gaussian) in Gaussian-major,
+//            row-then-column order (reference: getGaussianTileKeys, rasterizer_impl.cu:82-124)
+//  sort      the project's own stable LSD radix sort on the tile bits only: emission order is
+//            already ascending in Gaussian id, so a stable sort by tile yields (tile, Gaussian)
+//            order, identical to the reference's full 64-bit thrust::sort of unique keys
+//            (rasterizer_impl.cu:287)
+//  ranges    [first, last+1) of every non-empty tile; empty tiles keep {0,0}
+//            (reference: getPerTileRanges, rasterizer_impl.cu:127-152)
+//  gather    re-expands each key's record around its tile centre into the contiguous tile-record
+//            stream the blend reads with TMA bulk copies
+//
+// Every kernel reads the key count from device memory and uses a fixed grid, so the sequence
+// needs no host synchronisation and can be captured in a CUDA graph.
+#include "fe_kernels.cuh"
+
+namespace fe {
+
+namespace {
+
+constexpr int kScanThreads = 256;
+constexpr int kSortThreads = 256;
+constexpr int kSortWarps = kSortThreads / 32;
+
+__device__ __forceinline__ int64_t chunk_of(int64_t n, int nblocks, int granule) {
+  int64_t c = (n + nblocks - 1) / nblocks;
+  return (c + granule - 1) / granule * granule;
+}
+
+// Block-wide exclusive scan of one value per thread (kScanThreads threads); returns the block total.
+template <typename T>
+__device__ __forceinline__ T block_exclusive_scan(T v, T& excl, T* warp_sums) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  T x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    T y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) warp_sums[warp] = x;
+  __syncthreads();
+  if (warp == 0) {
+    T s = lane < kScanThreads / 32 ? warp_sums[lane] : T(0);
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      T y = __shfl_up_sync(0xffffffffu, s, o);
+      if (lane >= o) s += y;
+    }
+    if (lane < kScanThreads / 32) warp_sums[lane] = s;
+  }
+  __syncthreads();
+  const T warp_prefix = warp ? warp_sums[warp - 1] : T(0);
+  const T total = warp_sums[kScanThreads / 32 - 1];
+  excl = warp_prefix + x - v;
+  __syncthreads();
+  return total;
+}
+
+__global__ void scan_reduce_kernel(const uint32_t* __restrict__ in, int64_t n,
+                                   unsigned long long* __restrict__ bsum) {
+  const int64_t chunk = chunk_of(n, gridDim.x, kScanThreads);
+  const int64_t s = blockIdx.x * chunk, e = min(n, s + chunk);
+  unsigned long long acc = 0;
+  for (int64_t i = s + threadIdx.x; i < e; i += kScanThreads) acc += in[i];
+  __shared__ unsigned long long red[kScanThreads / 32];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    unsigned long long t = 0;
+    for (int w = 0; w < kScanThreads / 32; ++w) t += red[w];
+    bsum[blockIdx.x] = t;
+  }
+}
+
+// One block: exclusive scan of the per-block sums; records the total key count.
+__global__ void scan_spine_kernel(unsigned long long* __restrict__ bsum, int nb, int64_t capacity,
+                                  Control* __restrict__ ctrl) {
+  __shared__ unsigned long long ws[kScanThreads / 32];
+  unsigned long long carry = 0;
+  for (int base = 0; base < nb; base += kScanThreads) {
+    const int i = base + threadIdx.x;
+    const unsigned long long v = i < nb ? bsum[i] : 0ull;
+    unsigned long long ex;
+    const unsigned long long tot = block_exclusive_scan<unsigned long long>(v, ex, ws);
+    if (i < nb) bsum[i] = carry + ex;
+    carry += tot;
+  }
+  if (threadIdx.x == 0) {
+    ctrl->want_keys = carry;
+    const unsigned long long cap = (unsigned long long)capacity;
+    ctrl->num_keys = carry < cap ? carry : cap;
+    if (carry > cap) atomicOr(&ctrl->error, FE_DEVERR_CAPACITY);
+  }
+}
+
+__global__ void scan_down_kernel(const uint32_t* __restrict__ in, uint32_t* __restrict__ out,
+                                 int64_t n, const unsigned long long* __restrict__ boff) {
+  __shared__ unsigned long long ws[kScanThreads / 32];
+  const int64_t chunk = chunk_of(n, gridDim.x, kScanThreads);
+  const int64_t s = blockIdx.x * chunk, e = min(n, s + chunk);
+  unsigned long long carry = boff[blockIdx.x];
+  for (int64_t base = s; base < e; base += kScanThreads) {
+    const int64_t i = base + threadIdx.x;
+    const unsigned long long v = i < e ? in[i] : 0u;
+    unsigned long long ex;
+    const unsigned long long tot = block_exclusive_scan<unsigned long long>(v, ex, ws);
+    if (i < e) {
+      const unsigned long long incl = carry + ex + v;
+      out[i] = incl > 0xffffffffull ? 0xffffffffu : (uint32_t)incl;
+    }
+    carry += tot;
+  }
+}
+
+__global__ void emit_keys_kernel(ViewsArg va, const uint32_t* __restrict__ incl,
+                                 const TileRect* __restrict__ rects, int64_t n,
+                                 const Control* __restrict__ ctrl, uint64_t* __restrict__ keys) {
+  const int64_t K = (int64_t)ctrl->num_keys;
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < K;
+       k += (int64_t)gridDim.x * blockDim.x) {
+    // First record whose inclusive prefix exceeds k.
+    int64_t lo = 0, hi = n - 1;
+    while (lo < hi) {
+      const int64_t mid = (lo + hi) >> 1;
+      if ((int64_t)incl[mid] > k) hi = mid; else lo = mid + 1;
+    }
+    const int64_t i = lo;
+    const int64_t excl = i ? (int64_t)incl[i - 1] : 0;
+    const int64_t j = k - excl;
+    const TileRect r = rects[i];
+    const int w = r.x1 - r.x0;
+    const int x = r.x0 + (int)(j % w), y = r.y0 + (int)(j / w);
+    const int vi = find_view<&ViewDev::rec_base>(va, i);
+    const ViewDev& V = view_at(va, vi);
+    const uint64_t tile = (uint64_t)(V.tile_base + (int64_t)y * V.gx + x);
+    const uint64_t gid = (uint64_t)(i - V.rec_base);
+    keys[k] = (tile << 32) | gid;
+  }
+}
+
+// Number of sort blocks that receive keys: at least 2048 keys per block, at most the grid.
+__device__ __forceinline__ int sort_blocks_used(int64_t K, int grid) {
+  const int64_t b = (K + 2047) / 2048;
+  return (int)(b < 1 ? 1 : (b > grid ? grid : b));
+}
+
+// Per-block digit histograms, block-major: hist[b * 256 + digit].
+__global__ void sort_hist_kernel(const uint64_t* __restrict__ keys, const Control* __restrict__ ctrl,
+                                 int shift, uint32_t* __restrict__ hist) {
+  __shared__ uint32_t cnt[256];
+  const int64_t K = (int64_t)ctrl->num_keys;
+  const int nb = sort_blocks_used(K, gridDim.x);
+  if ((int)blockIdx.x >= nb) return;
+  const int64_t chunk = chunk_of(K, nb, kSortThreads);
+  const int64_t s = blockIdx.x * chunk, e = min(K, s + chunk);
+  cnt[threadIdx.x] = 0;
+  __syncthreads();
+  for (int64_t i = s + threadIdx.x; i < e; i += kSortThreads)
+    atomicAdd(&cnt[(uint32_t)(keys[i] >> shift) & 255u], 1u);
+  __syncthreads();
+  hist[blockIdx.x * 256 + threadIdx.x] = cnt[threadIdx.x];
+}
+
+// One block of 256 threads, thread d owns digit d: per-digit exclusive scan over the used blocks
+// (coalesced across digits), then the exclusive scan of digit totals into row `grid` of hist.
+__global__ void sort_scan_kernel(uint32_t* __restrict__ hist, const Control* __restrict__ ctrl,
+                                 int grid) {
+  __shared__ uint32_t ws[kScanThreads / 32];
+  const int nb = sort_blocks_used((int64_t)ctrl->num_keys, grid);
+  const int d = threadIdx.x;
+  uint32_t run = 0;
+  int b = 0;
+  for (; b + 4 <= nb; b += 4) {
+    const uint32_t c0 = hist[(b + 0) * 256 + d], c1 = hist[(b + 1) * 256 + d];
+    const uint32_t c2 = hist[(b + 2) * 256 + d], c3 = hist[(b + 3) * 256 + d];
+    hist[(b + 0) * 256 + d] = run; run += c0;
+    hist[(b + 1) * 256 + d] = run; run += c1;
+    hist[(b + 2) * 256 + d] = run; run += c2;
+    hist[(b + 3) * 256 + d] = run; run += c3;
+  }
+  for (; b < nb; ++b) {
+    const uint32_t c = hist[b * 256 + d];
+    hist[b * 256 + d] = run;
+    run += c;
+  }
+  uint32_t ex;
+  block_exclusive_scan<uint32_t>(run, ex, ws);
+  hist[grid * 256 + d] = ex;
+}
+
+// Stable scatter: keys are taken in order 256 at a time; ranks within a 256-key slice come from
+// warp match-any groups plus per-warp digit counts scanned across warps in warp order.
+__global__ void sort_scatter_kernel(const uint64_t* __restrict__ in, uint64_t* __restrict__ out,
+                                    const Control* __restrict__ ctrl, int shift,
+                                    const uint32_t* __restrict__ hist) {
+  __shared__ uint32_t off[256];
+  __shared__ uint32_t tot[256];
+  __shared__ uint32_t wc[kSortWarps][256];
+  const int64_t K = (int64_t)ctrl->num_keys;
+  const int nb = sort_blocks_used(K, gridDim.x);
+  if ((int)blockIdx.x >= nb) return;
+  const int64_t chunk = chunk_of(K, nb, kSortThreads);
+  const int64_t s = blockIdx.x * chunk, e = min(K, s + chunk);
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  off[tid] = hist[blockIdx.x * 256 + tid] + hist[gridDim.x * 256 + tid];
+  const uint32_t lt_mask = (1u << lane) - 1u;
+  for (int64_t base = s; base < e; base += kSortThreads) {
+#pragma unroll
+    for (int w = 0; w < kSortWarps; ++w) wc[w][tid] = 0;
+    const int64_t i = base + tid;
+    const bool valid = i < e;
+    const uint64_t key = valid ? in[i] : 0ull;
+    const uint32_t d = valid ? ((uint32_t)(key >> shift) & 255u) : 256u;
+    const uint32_t peers = __match_any_sync(0xffffffffu, d);
+    const uint32_t rank = __popc(peers & lt_mask);
+    __syncthreads();
+    if (valid && rank == 0) wc[warp][d] = __popc(peers);
+    __syncthreads();
+    {
+      uint32_t run = 0;
+#pragma unroll
+      for (int w = 0; w < kSortWarps; ++w) {
+        const uint32_t c = wc[w][tid];
+        wc[w][tid] = run;
+        run += c;
+      }
+      tot[tid] = run;
+    }
+    __syncthreads();
+    if (valid) out[off[d] + wc[warp][d] + rank] = key;
+    __syncthreads();
+    off[tid] += tot[tid];
+  }
+}
+
+__device__ __forceinline__ void tile_record(const GaussRec& g, float du, float dv, TileRec& t) {
+  float a0[3], y0[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    a0[k] = fmaf(dv, g.a2[k], fmaf(du, g.a1[k], g.a0[k]));
+    y0[k] = fmaf(dv, g.y2[k], fmaf(du, g.y1[k], g.y0[k]));
+  }
+  auto d3 = [](const float* a, const float* b) { return fmaf(a[2], b[2], fmaf(a[1], b[1], a[0] * b[0])); };
+  t.V[0] = d3(a0, a0);
+  t.V[1] = 2.f * d3(a0, g.a1);
+  t.V[2] = 2.f * d3(a0, g.a2);
+  t.V[3] = d3(g.a1, g.a1);
+  t.V[4] = 2.f * d3(g.a1, g.a2);
+  t.V[5] = d3(g.a2, g.a2);
+  t.P[0] = d3(a0, g.b);
+  t.P[1] = d3(g.a1, g.b);
+  t.P[2] = d3(g.a2, g.b);
+  const float kn = -0.5f * kLog2e;
+  t.N[0] = kn * d3(y0, y0);
+  t.N[1] = 2.f * kn * d3(y0, g.y1);
+  t.N[2] = 2.f * kn * d3(y0, g.y2);
+  t.N[3] = kn * d3(g.y1, g.y1);
+  t.N[4] = 2.f * kn * d3(g.y1, g.y2);
+  t.N[5] = kn * d3(g.y2, g.y2);
+  t.C = g.c2;
+}
+
+__global__ void ranges_gather_kernel(ViewsArg va, const uint64_t* __restrict__ keys,
+                                     const Control* __restrict__ ctrl,
+                                     const GaussRec* __restrict__ recs, int tile_w, int tile_h,
+                                     uint2* __restrict__ ranges, TileRec* __restrict__ trec) {
+  const int64_t K = (int64_t)ctrl->num_keys;
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < K;
+       k += (int64_t)gridDim.x * blockDim.x) {
+    const uint64_t key = keys[k];
+    const uint32_t tile = (uint32_t)(key >> 32);
+    const uint32_t gid = (uint32_t)key;
+    if (k == 0 || (uint32_t)(keys[k - 1] >> 32) != tile) ranges[tile].x = (uint32_t)k;
+    if (k == K - 1 || (uint32_t)(keys[k + 1] >> 32) != tile) ranges[tile].y = (uint32_t)(k + 1);
+    if (trec) {
+      const int vi = find_view<&ViewDev::tile_base>(va, tile);
+      const ViewDev& V = view_at(va, vi);
+      const int lt = (int)(tile - V.tile_base);
+      const int tx = lt % V.gx, ty = lt / V.gx;
+      const float tcx = tx * tile_w + 0.5f * (tile_w - 1);
+      const float tcy = ty * tile_h + 0.5f * (tile_h - 1);
+      const GaussRec g = recs[V.rec_base + gid];
+      TileRec t;
+      tile_record(g, tcx - g.uc, tcy - g.vc, t);
+      trec[k] = t;
+    }
+  }
+}
+
+inline int grid_for(int64_t work, int threads, int cap) {
+  const int64_t b = (work + threads - 1) / threads;
+  return (int)(b < 1 ? 1 : (b > cap ? cap : b));
+}
+
+}  // namespace
+
+int scan_grid(int64_t n) { return grid_for(n, 4 * kScanThreads, 1024); }
+int sort_grid(int64_t key_capacity) { return grid_for(key_capacity, 2048, 2 * 152); }
+
+void launch_scan(const uint32_t* touched, uint32_t* incl, int64_t n, int64_t capacity,
+                 unsigned long long* scratch, Control* ctrl, cudaStream_t st) {
+  const int nb = scan_grid(n);
+  scan_reduce_kernel<<<nb, kScanThreads, 0, st>>>(touched, n, scratch);
+  scan_spine_kernel<<<1, kScanThreads, 0, st>>>(scratch, nb, capacity, ctrl);
+  scan_down_kernel<<<nb, kScanThreads, 0, st>>>(touched, incl, n, scratch);
+}
+
+void launch_emit_keys(const ViewsArg& va, const uint32_t* incl, const TileRect* rects, int64_t n,
+                      const Control* ctrl, uint64_t* keys, int64_t capacity, cudaStream_t st) {
+  emit_keys_kernel<<<grid_for(capacity, 256, 4 * 152 * 8), 256, 0, st>>>(va, incl, rects, n, ctrl,
+                                                                         keys);
+}
+
+uint64_t* launch_sort(uint64_t* a, uint64_t* b, int key_bits, const Control* ctrl,
+                      int64_t capacity, uint32_t* hist, cudaStream_t st) {
+  const int nb = sort_grid(capacity);
+  uint64_t* src = a;
+  uint64_t* dst = b;
+  for (int lo = 0; lo < key_bits; lo += 8) {
+    const int shift = 32 + lo;
+    sort_hist_kernel<<<nb, kSortThreads, 0, st>>>(src, ctrl, shift, hist);
+    sort_scan_kernel<<<1, kScanThreads, 0, st>>>(hist, ctrl, nb);
+    sort_scatter_kernel<<<nb, kSortThreads, 0, st>>>(src, dst, ctrl, shift, hist);
+    uint64_t* t = src;
+    src = dst;
+    dst = t;
+  }
+  return src;
+}
+
+void launch_ranges_gather(const ViewsArg& va, const uint64_t* keys, const Control* ctrl,
+                          int64_t capacity, const GaussRec* recs, int tile_w, int tile_h,
+                          uint2* ranges, TileRec* trec, cudaStream_t st) {
+  ranges_gather_kernel<<<grid_for(capacity, 256, 4 * 152 * 8), 256, 0, st>>>(
+      va, keys, ctrl, recs, tile_w, tile_h, ranges, trec);
+}
+
+void launch_ranges(const uint64_t* keys, const Control* ctrl, int64_t capacity, uint2* ranges,
+                   cudaStream_t st) {
+  ViewsArg va{};
+  ranges_gather_kernel<<<grid_for(capacity, 256, 4 * 152 * 8), 256, 0, st>>>(
+      va, keys, ctrl, nullptr, 8, 8, ranges, nullptr);
+}
+
+}  // namespace fe

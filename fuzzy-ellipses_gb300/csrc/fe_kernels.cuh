@@ -1,0 +1,67 @@
+// fe_kernels.cuh -- launcher declarations for the renderer's kernels.
+#pragma once
+
+#include "fe_common.cuh"
+
+namespace fe {
+
+// preprocess.cu
+void launch_preprocess(const ViewsArg& va, int64_t n_rec, const float* means, const float* prec,
+                       const float* logw, const float* quat, const float* rotm,
+                       const float* trans, int cull_mode, float cull_param, int tile_w,
+                       int tile_h, GaussRec* recs, TileRect* rects, uint32_t* touched,
+                       cudaStream_t st);
+void launch_preprocess_reference(int P, float n_std, const float* means, const float* scales,
+                                 const float* rots, const float* viewmatrix,
+                                 const float* projmatrix, int W, int H, float tan_fovx,
+                                 float tan_fovy, int gx, int gy, int32_t* radii, float* means2d,
+                                 TileRect* rects, uint32_t* touched, cudaStream_t st);
+void launch_legacy_records(const ViewsArg& va, int P, const float* means, const float* scales,
+                           const float* rots, const float* logw, const float* rotm,
+                           const float* trans, const float* rays, GaussRec* recs,
+                           cudaStream_t st);
+
+// binning.cu
+// Blocks used by the fixed-grid scan / sort kernels.
+int scan_grid(int64_t n);
+int sort_grid(int64_t key_capacity);
+// Inclusive prefix sum of touched[0..n) into incl; total clamped to capacity in ctrl->num_keys,
+// the unclamped total in ctrl->want_keys, FE_DEVERR_CAPACITY set on overflow.
+// scratch: scan_grid(n) * 8 bytes.
+void launch_scan(const uint32_t* touched, uint32_t* incl, int64_t n, int64_t capacity,
+                 unsigned long long* scratch, Control* ctrl, cudaStream_t st);
+void launch_emit_keys(const ViewsArg& va, const uint32_t* incl, const TileRect* rects, int64_t n,
+                      const Control* ctrl, uint64_t* keys, int64_t capacity, cudaStream_t st);
+// Stable LSD radix sort of keys on bits [32, 32+key_bits); returns the buffer holding the
+// result (a or b). hist: 256 * (sort_grid(capacity) + 1) uint32.
+uint64_t* launch_sort(uint64_t* a, uint64_t* b, int key_bits, const Control* ctrl,
+                      int64_t capacity, uint32_t* hist, cudaStream_t st);
+// Tile ranges (ranges must be zeroed beforehand) and the tile-local record stream.
+void launch_ranges_gather(const ViewsArg& va, const uint64_t* keys, const Control* ctrl,
+                          int64_t capacity, const GaussRec* recs, int tile_w, int tile_h,
+                          uint2* ranges, TileRec* trec, cudaStream_t st);
+// Ranges only (reference-compatible binning).
+void launch_ranges(const uint64_t* keys, const Control* ctrl, int64_t capacity, uint2* ranges,
+                   cudaStream_t st);
+
+// blend_fwd.cu
+void launch_blend_fwd(const ViewsArg& va, int tile_w, int tile_h, int64_t n_tiles,
+                      const TileRec* trec, const uint2* ranges, float beta2, float beta3,
+                      float* depth, float* alpha, float* stats, int64_t stats_stride,
+                      Control* ctrl, cudaStream_t st);
+
+// blend_bwd.cu
+void launch_pixel_prep(const ViewsArg& va, int64_t n_pix, const float* depth, const float* stats,
+                       int64_t stats_stride, const float* grad_depth, const float* grad_alpha,
+                       float4* pix, cudaStream_t st);
+void launch_blend_bwd(const ViewsArg& va, int tile_w, int tile_h, const uint64_t* keys,
+                      const Control* ctrl, int64_t capacity, const TileRec* trec,
+                      const GaussRec* recs, const float4* pix, float beta2, float beta3,
+                      RecGrad* rgrad, cudaStream_t st);
+// Gradients are accumulated (atomically) into gmeans/gprec/glogw, which must be zeroed first.
+void launch_record_vjp(const ViewsArg& va, int64_t n_rec, const float* means, const float* prec,
+                       const float* quat, const float* trans, const GaussRec* recs,
+                       const RecGrad* rgrad, float* gmeans, float* gprec, float* glogw,
+                       cudaStream_t st);
+
+}  // namespace fe

@@ -1,0 +1,156 @@
+"""ctypes binding of the native library ``_lib/libfuzzy_ellipses.so`` (C ABI: include/fuzzy_ellipses.h).
+
+The library is built in-tree by ``fuzzy-ellipses_gb300/build.py``. There is no fallback: if the
+library is missing, every render entry point raises ``NativeLibraryMissing``.
+"""
+
+from __future__ import annotations
+
+import ctypes
+import os
+import threading
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_lib", "libfuzzy_ellipses.so")
+
+FE_DESC_MAGIC = 0x31644546
+FE_DESC_VERSION = 1
+FE_CULL_EPS = 0
+FE_CULL_NSTD = 1
+FE_DEVERR_CAPACITY = 1
+FE_DEVERR_TIMEOUT = 2
+
+STATUS_NAMES = {
+    0: "FE_OK", 1: "FE_ERR_INVALID_ARGUMENT", 2: "FE_ERR_DESCRIPTOR", 3: "FE_ERR_CUDA",
+    4: "FE_ERR_OUT_OF_MEMORY", 5: "FE_ERR_CAPACITY", 6: "FE_ERR_DEVICE_TIMEOUT",
+    7: "FE_ERR_UNSUPPORTED", 8: "FE_ERR_SCRATCH_LIMIT",
+}
+
+
+class NativeLibraryMissing(ImportError):
+    pass
+
+
+class FEError(RuntimeError):
+    def __init__(self, status, message):
+        super().__init__(f"{STATUS_NAMES.get(status, status)}: {message}")
+        self.status = status
+
+
+class RenderDesc(ctypes.Structure):
+    """Mirror of ``fe_render_desc``."""
+    _fields_ = [
+        ("magic", ctypes.c_uint32), ("version", ctypes.c_uint32),
+        ("n_gaussians", ctypes.c_int32), ("height", ctypes.c_int32), ("width", ctypes.c_int32),
+        ("fx", ctypes.c_float), ("fy", ctypes.c_float), ("cx", ctypes.c_float), ("cy", ctypes.c_float),
+        ("beta2", ctypes.c_float), ("beta3", ctypes.c_float),
+        ("cull_mode", ctypes.c_int32), ("cull_param", ctypes.c_float),
+        ("tile_w", ctypes.c_int32), ("tile_h", ctypes.c_int32),
+        ("flags", ctypes.c_uint32), ("reserved", ctypes.c_uint32),
+    ]
+
+
+class LegacyDesc(ctypes.Structure):
+    """Mirror of ``fe_legacy_desc`` (byte-compatible with the reference's RasterizeDescriptor,
+    rasterize_main.h:14-20)."""
+    _fields_ = [("image_height", ctypes.c_int32), ("image_width", ctypes.c_int32),
+                ("P", ctypes.c_int32), ("tan_fovx", ctypes.c_float), ("tan_fovy", ctypes.c_float)]
+
+
+class View(ctypes.Structure):
+    """Mirror of ``fe_view``."""
+    _fields_ = [("scene", ctypes.c_int32), ("height", ctypes.c_int32), ("width", ctypes.c_int32),
+                ("fx", ctypes.c_float), ("fy", ctypes.c_float), ("cx", ctypes.c_float),
+                ("cy", ctypes.c_float), ("quat", ctypes.c_float * 4), ("trans", ctypes.c_float * 3),
+                ("pixel_offset", ctypes.c_int64)]
+
+
+class SceneEntry(ctypes.Structure):
+    """Mirror of ``fe_scene``."""
+    _fields_ = [("gauss_offset", ctypes.c_int64), ("n", ctypes.c_int32), ("reserved", ctypes.c_int32)]
+
+
+P = ctypes.c_void_p
+I32 = ctypes.c_int32
+I64 = ctypes.c_int64
+F32 = ctypes.c_float
+
+# name -> (restype, argtypes); every symbol the public header declares.
+PROTOTYPES = {
+    "fe_version": (ctypes.c_char_p, []),
+    "fe_last_error_message": (ctypes.c_char_p, []),
+    "fe_status_string": (ctypes.c_char_p, [ctypes.c_int]),
+    "fe_render_desc_init": (None, [ctypes.POINTER(RenderDesc), I32, I32, I32, F32, F32, F32, F32]),
+    "fe_render_fwd": (ctypes.c_int, [ctypes.POINTER(RenderDesc)] + [P] * 8 + [P]),
+    "fe_render_bwd": (ctypes.c_int, [ctypes.POINTER(RenderDesc)] + [P] * 13 + [P]),
+    "fe_render_binning": (ctypes.c_int, [ctypes.POINTER(RenderDesc)] + [P] * 6 + [I64, P,
+                                                                                ctypes.POINTER(I64), P]),
+    "fe_render_fwd_xla": (None, [P, P, P, ctypes.c_size_t, P]),
+    "fe_render_bwd_xla": (None, [P, P, P, ctypes.c_size_t, P]),
+    "fe_rasterize_legacy_xla": (None, [P, P, P, ctypes.c_size_t, P]),
+    "fe_rasterize_legacy": (ctypes.c_int, [ctypes.POINTER(LegacyDesc)] + [P] * 11 + [P]),
+    "fe_reference_binning": (ctypes.c_int, [I32, I32, I32, F32, P, P, P, P, P, F32, F32,
+                                            P, P, P, P, I64, P, ctypes.POINTER(I64), P]),
+    "fe_batch_create": (ctypes.c_int, [ctypes.POINTER(RenderDesc), ctypes.POINTER(SceneEntry), I32,
+                                       ctypes.POINTER(View), I32, ctypes.POINTER(P)]),
+    "fe_batch_destroy": (None, [P]),
+    "fe_batch_pixels": (I64, [P]),
+    "fe_batch_scratch_bytes": (I64, [P]),
+    "fe_batch_fwd": (ctypes.c_int, [P] + [P] * 6 + [P]),
+    "fe_batch_bwd": (ctypes.c_int, [P] + [P] * 11 + [P]),
+    "fe_batch_status": (ctypes.c_int, [P, P, ctypes.POINTER(I64), ctypes.POINTER(I64),
+                                       ctypes.POINTER(ctypes.c_uint32)]),
+    "fe_check_device_status": (ctypes.c_int, [P, ctypes.POINTER(ctypes.c_uint32)]),
+    "fe_batch_fwd_timed": (ctypes.c_int, [P] + [P] * 6 + [ctypes.POINTER(ctypes.c_float), P]),
+    "fe_batch_launch_count": (ctypes.c_int, [P]),
+    "fe_bench_peak": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_double), P]),
+}
+
+_lib = None
+_lock = threading.Lock()
+
+
+def load(path: str | None = None):
+    """Load (once) and return the native library; raises NativeLibraryMissing if absent."""
+    global _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        p = path or LIB_PATH
+        if not os.path.exists(p):
+            raise NativeLibraryMissing(
+                f"{p} is missing: build it with `python fuzzy-ellipses_gb300/build.py` "
+                "(or __graft_entry__.build()); there is no non-CUDA fallback")
+        lib = ctypes.CDLL(p)
+        for name, (res, args) in PROTOTYPES.items():
+            fn = getattr(lib, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = lib
+        return lib
+
+
+def check(status: int):
+    if status != 0:
+        msg = load().fe_last_error_message().decode(errors="replace")
+        raise FEError(status, msg)
+
+
+def make_desc(n, height, width, fx, fy, cx, cy, beta2=21.4, beta3=2.66, cull="eps",
+              cull_param=None, tile=(16, 16), flags=0) -> RenderDesc:
+    d = RenderDesc()
+    load().fe_render_desc_init(ctypes.byref(d), int(n), int(height), int(width), float(fx),
+                               float(fy), float(cx), float(cy))
+    d.beta2 = float(beta2)
+    d.beta3 = float(beta3)
+    if cull == "eps":
+        d.cull_mode = FE_CULL_EPS
+        d.cull_param = 1e-7 if cull_param is None else float(cull_param)
+    elif cull == "nstd":
+        d.cull_mode = FE_CULL_NSTD
+        d.cull_param = 3.0 if cull_param is None else float(cull_param)
+    else:
+        raise ValueError("cull must be 'eps' or 'nstd'")
+    d.tile_w, d.tile_h = int(tile[0]), int(tile[1])
+    d.flags = int(flags)
+    return d

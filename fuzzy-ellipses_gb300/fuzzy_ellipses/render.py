@@ -1,0 +1,379 @@
+"""torch-facing render API over the native C ABI.
+
+``render`` is the drop-in for the reference's render entry point, re-specified as in
+``baseline/fm_render.py:113-126`` (``render_func_quat``): precision factor in fm_render's
+``prec_full`` convention, camera given by pinhole intrinsics and a (quaternion, translation) pose.
+It is differentiable with respect to means, precisions and log-weights through a
+``torch.autograd.Function`` whose backward is the native recompute-based backward kernel.
+
+``rasterize`` mirrors the reference's legacy ``fuzzy_ellipses.rasterize``
+(``fuzzy_ellipses/__init__.py:189-236``): same arguments, same conventions (full-angle
+``tan_fov``, identity view matrix, ``getNumStds`` cut-off, 8x8 tiles), same
+``nan_to_num`` post-processing.
+
+All work is enqueued on torch's current CUDA stream; there is no CPU path.
+"""
+
+from __future__ import annotations
+
+import ctypes
+import math
+
+import numpy as np
+import torch
+
+from . import _native as N
+
+__all__ = ["render", "render_forward", "render_binning", "rasterize", "reference_binning", "Batch",
+           "projection_matrix", "reference_num_stds", "device_status"]
+
+
+def _stream():
+    return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+def _ptr(t):
+    return ctypes.c_void_p(t.data_ptr()) if t is not None else ctypes.c_void_p(0)
+
+
+def _as_dev(x, device, shape=None, name="tensor"):
+    if not torch.is_tensor(x):
+        x = torch.as_tensor(np.asarray(x, dtype=np.float32))
+    x = x.to(device=device, dtype=torch.float32).contiguous()
+    if shape is not None and tuple(x.shape) != tuple(shape):
+        x = x.reshape(shape)
+    return x
+
+
+def _check_inputs(means, prec, logw):
+    if not (torch.is_tensor(means) and means.is_cuda):
+        raise TypeError("means must be a CUDA tensor (the renderer has no CPU path)")
+    n = means.shape[0]
+    if means.shape != (n, 3) or prec.shape != (n, 3, 3) or logw.shape != (n,):
+        raise ValueError(f"expected means (N,3), prec (N,3,3), logw (N,); got {tuple(means.shape)}, "
+                         f"{tuple(prec.shape)}, {tuple(logw.shape)}")
+    return n
+
+
+class _RenderFn(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, means, prec, logw, quat, trans, desc):
+        lib = N.load()
+        dev = means.device
+        means = means.detach().contiguous().float()
+        prec = prec.detach().contiguous().float()
+        logw = logw.detach().contiguous().float()
+        H, W = desc.height, desc.width
+        depth = torch.empty((H, W), device=dev, dtype=torch.float32)
+        alpha = torch.empty((H, W), device=dev, dtype=torch.float32)
+        need = any(ctx.needs_input_grad[:3])
+        stats = torch.empty((3, H, W), device=dev, dtype=torch.float32) if need else None
+        N.check(lib.fe_render_fwd(ctypes.byref(desc), _ptr(means), _ptr(prec), _ptr(logw),
+                                  _ptr(quat), _ptr(trans), _ptr(depth), _ptr(alpha), _ptr(stats),
+                                  _stream()))
+        ctx.desc = desc
+        if need:
+            ctx.save_for_backward(means, prec, logw, quat, trans, depth, alpha, stats)
+        return depth, alpha
+
+    @staticmethod
+    def backward(ctx, gdepth, galpha):
+        lib = N.load()
+        means, prec, logw, quat, trans, depth, alpha, stats = ctx.saved_tensors
+        gm = torch.empty_like(means)
+        gp = torch.empty_like(prec)
+        gw = torch.empty_like(logw)
+        gd = gdepth.contiguous().float() if gdepth is not None else None
+        ga = galpha.contiguous().float() if galpha is not None else None
+        N.check(lib.fe_render_bwd(ctypes.byref(ctx.desc), _ptr(means), _ptr(prec), _ptr(logw),
+                                  _ptr(quat), _ptr(trans), _ptr(depth), _ptr(alpha), _ptr(stats),
+                                  _ptr(gd), _ptr(ga), _ptr(gm), _ptr(gp), _ptr(gw), _stream()))
+        return gm, gp, gw, None, None, None
+
+
+def render(means, prec, logw, fx, fy, cx, cy, quat, t, height, width, beta2=21.4, beta3=2.66, *,
+           cull="eps", cull_param=None, tile=(16, 16)):
+    """Render depth and alpha (H, W) of one pinhole camera; differentiable in means/prec/logw.
+
+    means (N,3), prec (N,3,3) (upper triangle read, precision U U^T), logw (N,): CUDA float32.
+    quat (4,) scalar-first and t (3,): camera rotation (rays_world = rays_cam @ quat_to_rot(quat))
+    and centre. ``cull='eps'`` drops a Gaussian where its peak density along a ray is below
+    ``cull_param`` (default 1e-7); ``cull='nstd'`` uses a fixed ``cull_param`` sigma radius.
+    """
+    n = _check_inputs(means, prec, logw)
+    dev = means.device
+    q = _as_dev(quat, dev, (4,))
+    tt = _as_dev(t, dev, (3,))
+    desc = N.make_desc(n, height, width, fx, fy, cx, cy, beta2, beta3, cull, cull_param, tile)
+    return _RenderFn.apply(means, prec, logw, q, tt, desc)
+
+
+def render_forward(means, prec, logw, fx, fy, cx, cy, quat, t, height, width, beta2=21.4,
+                   beta3=2.66, *, cull="eps", cull_param=None, tile=(16, 16), out=None,
+                   stats=None):
+    """Non-differentiable forward into optional preallocated ``out=(depth, alpha)``."""
+    lib = N.load()
+    n = _check_inputs(means, prec, logw)
+    dev = means.device
+    q = _as_dev(quat, dev, (4,))
+    tt = _as_dev(t, dev, (3,))
+    desc = N.make_desc(n, height, width, fx, fy, cx, cy, beta2, beta3, cull, cull_param, tile)
+    if out is None:
+        out = (torch.empty((height, width), device=dev), torch.empty((height, width), device=dev))
+    N.check(lib.fe_render_fwd(ctypes.byref(desc), _ptr(means), _ptr(prec), _ptr(logw), _ptr(q),
+                              _ptr(tt), _ptr(out[0]), _ptr(out[1]), _ptr(stats), _stream()))
+    return out
+
+
+def render_binning(means, prec, logw, fx, fy, cx, cy, quat, t, height, width, *, cull="eps",
+                   cull_param=None, tile=(16, 16), key_capacity=None):
+    """The tile binning ``render`` uses: returns (keys (K,) int64 holding (tile << 32 | gaussian),
+    ranges (T, 2) int64). Synchronises once."""
+    lib = N.load()
+    n = _check_inputs(means, prec, logw)
+    dev = means.device
+    q = _as_dev(quat, dev, (4,))
+    tt = _as_dev(t, dev, (3,))
+    desc = N.make_desc(n, height, width, fx, fy, cx, cy, 21.4, 2.66, cull, cull_param, tile)
+    gx = (width + tile[0] - 1) // tile[0]
+    gy = (height + tile[1] - 1) // tile[1]
+    cap = int(key_capacity) if key_capacity is not None else max(1, n * gx * gy)
+    keys = torch.empty(cap, dtype=torch.int64, device=dev)
+    ranges = torch.empty((gx * gy, 2), dtype=torch.int32, device=dev)
+    nk = ctypes.c_int64(0)
+    N.check(lib.fe_render_binning(ctypes.byref(desc), _ptr(means), _ptr(prec), _ptr(logw), _ptr(q),
+                                  _ptr(tt), _ptr(keys), cap, _ptr(ranges), ctypes.byref(nk),
+                                  _stream()))
+    return keys[:nk.value], ranges.to(torch.int64) & 0xFFFFFFFF
+
+
+def bench_peak(kind):
+    """Measured pipe throughput (operations/s): 'fma' (FP32 FMA) or 'ex2' (MUFU ex2)."""
+    lib = N.load()
+    out = ctypes.c_double(0.0)
+    N.check(lib.fe_bench_peak({"fma": 0, "ex2": 1}[kind], 4096, ctypes.byref(out), _stream()))
+    return float(out.value)
+
+
+def device_status():
+    """Synchronise the current stream and return (and clear) its device error word."""
+    lib = N.load()
+    err = ctypes.c_uint32(0)
+    N.check(lib.fe_check_device_status(_stream(), ctypes.byref(err)))
+    return int(err.value)
+
+
+# ---------------------------------------------------------------------------------------------
+# Legacy interface (fuzzy_ellipses/__init__.py:36-76,189-239 of the reference)
+# ---------------------------------------------------------------------------------------------
+
+def projection_matrix(width, height, fx, fy, cx, cy, znear, zfar):
+    """``getProjectionMatrixJax`` (reference ``fuzzy_ellipses/__init__.py:36-76``): the transposed
+    OpenGL-style projection; cx, cy are ignored as in the reference. float64 math, float32 result."""
+    fov_x = math.atan(width / 2 / fx) * 2.0
+    fov_y = math.atan(height / 2 / fy) * 2.0
+    top = math.tan(fov_y / 2) * znear
+    bottom = -top
+    right = math.tan(fov_x / 2) * znear
+    left = -right
+    m = np.array([
+        [2.0 * znear / (right - left), 0.0, (right + left) / (right - left), 0.0],
+        [0.0, 2.0 * znear / (top - bottom), (top + bottom) / (top - bottom), 0.0],
+        [0.0, 0.0, zfar / (zfar - znear), -(zfar * znear) / (zfar - znear)],
+        [0.0, 0.0, 1.0, 0.0],
+    ])
+    return m.T.astype(np.float32)
+
+
+def reference_num_stds(n):
+    """``getNumStds`` (reference ``cuda_rasterizer/rasterizer_impl.cu:154-172``)."""
+    if n <= 1000:
+        return 3.0
+    if n <= 5000:
+        return 0.75
+    if n <= 100000:
+        return 0.5
+    return 0.1
+
+
+def _legacy_scalars(image_height, image_width, fx, fy, cx, cy, near, far):
+    # fuzzy_ellipses/__init__.py:206-216: tan of the *full* field-of-view angle, identity view.
+    tan_fovx = math.tan(math.atan(image_width / 2 / fx) * 2.0)
+    tan_fovy = math.tan(math.atan(image_height / 2 / fy) * 2.0)
+    view = np.eye(4, dtype=np.float32)
+    proj = (view.astype(np.float64) @ projection_matrix(image_width, image_height, fx, fy, cx, cy,
+                                                        near, far).astype(np.float64)).astype(np.float32)
+    return np.float32(tan_fovx), np.float32(tan_fovy), view, proj
+
+
+def rasterize(means3D, scales, rotations, weights, camera_rays, camera_rot, camera_trans,
+              image_height, image_width, fx, fy, cx, cy, near, far):
+    """Reference-signature forward render returning ``(z, alpha)`` of shape (H, W).
+
+    Binning follows the reference exactly (tile keys bit-exact with its CUDA rasterizer); depth
+    and alpha come from this library's blend over those tiles, with the precision implied by
+    (scales, rotations) and the pinhole rays in ``camera_rays`` rotated by ``camera_rot`` from
+    origin ``camera_trans``.
+    """
+    lib = N.load()
+    dev = means3D.device if torch.is_tensor(means3D) and means3D.is_cuda else torch.device("cuda")
+    means = _as_dev(means3D, dev)
+    P = means.shape[0]
+    H, W = int(image_height), int(image_width)
+    tfx, tfy, view, proj = _legacy_scalars(H, W, fx, fy, cx, cy, near, far)
+    d = N.LegacyDesc(H, W, P, float(tfx), float(tfy))
+    bufs = [means, _as_dev(weights, dev), _as_dev(scales, dev), _as_dev(rotations, dev),
+            _as_dev(camera_rays, dev), _as_dev(camera_rot, dev), _as_dev(camera_trans, dev),
+            _as_dev(view, dev), _as_dev(proj, dev)]
+    z = torch.empty((H, W), device=dev)
+    alpha = torch.empty((H, W), device=dev)
+    N.check(lib.fe_rasterize_legacy(ctypes.byref(d), *[_ptr(b) for b in bufs], _ptr(z), _ptr(alpha),
+                                    _stream()))
+    z = torch.nan_to_num(z, posinf=10.0, neginf=0.0)        # __init__.py:233
+    alpha = torch.nan_to_num(alpha, posinf=1.0, neginf=0.0)  # __init__.py:234
+    return z, alpha
+
+
+def reference_binning(means, scales, rotations, viewmatrix, projmatrix, height, width, tan_fovx,
+                      tan_fovy, n_std=None, key_capacity=None):
+    """Reference-compatible binning on the GPU. Returns a dict of CUDA tensors:
+    radii (P,) int32, means2d (P,2), tiles_touched (P,) uint32-as-int64 inclusive prefix sum,
+    keys (K,) uint64-as-int64 sorted, ranges (T,2) int64."""
+    lib = N.load()
+    dev = means.device if torch.is_tensor(means) and means.is_cuda else torch.device("cuda")
+    m = _as_dev(means, dev)
+    P = m.shape[0]
+    if n_std is None:
+        n_std = reference_num_stds(P)
+    gx, gy = (width + 7) // 8, (height + 7) // 8
+    T = gx * gy
+    cap = int(key_capacity) if key_capacity is not None else max(1, P * T)
+    radii = torch.zeros(P, dtype=torch.int32, device=dev)
+    means2d = torch.zeros((P, 2), dtype=torch.float32, device=dev)
+    touched = torch.zeros(P, dtype=torch.int32, device=dev)
+    keys = torch.zeros(max(cap, 1), dtype=torch.int64, device=dev)
+    ranges = torch.zeros((T, 2), dtype=torch.int32, device=dev)
+    nk = ctypes.c_int64(0)
+    # Keep every uploaded input referenced until the call has been enqueued: a temporary dropped
+    # earlier could hand its memory to the next upload before the kernels read it.
+    s_d, r_d = _as_dev(scales, dev), _as_dev(rotations, dev)
+    v_d, p_d = _as_dev(viewmatrix, dev), _as_dev(projmatrix, dev)
+    N.check(lib.fe_reference_binning(P, int(height), int(width), float(n_std), _ptr(m),
+                                     _ptr(s_d), _ptr(r_d), _ptr(v_d), _ptr(p_d),
+                                     float(tan_fovx), float(tan_fovy), _ptr(radii), _ptr(means2d),
+                                     _ptr(touched), _ptr(keys), cap, _ptr(ranges), ctypes.byref(nk),
+                                     _stream()))
+    k = int(nk.value)
+    return {"radii": radii, "means2d": means2d,
+            "tiles_touched": touched.to(torch.int64) & 0xFFFFFFFF,
+            "keys": keys[:k], "ranges": ranges.to(torch.int64) & 0xFFFFFFFF, "num_keys": k}
+
+
+# ---------------------------------------------------------------------------------------------
+# Batches
+# ---------------------------------------------------------------------------------------------
+
+class Batch:
+    """Many renders (scenes x cameras) planned once and launched together.
+
+    ``scenes``: list of (gauss_offset, n) into concatenated Gaussian arrays.
+    ``views``: list of dicts with keys scene, height, width, fx, fy, cx, cy, quat, trans and
+    optionally pixel_offset (default: packed in order).
+    The plan reserves scratch for the worst-case key count, so ``forward`` performs no host
+    synchronisation and can be captured in a CUDA graph.
+    """
+
+    def __init__(self, scenes, views, beta2=21.4, beta3=2.66, *, cull="eps", cull_param=None,
+                 tile=(16, 16)):
+        lib = N.load()
+        desc = N.make_desc(0, 1, 1, 1.0, 1.0, 0.0, 0.0, beta2, beta3, cull, cull_param, tile)
+        sc = (N.SceneEntry * max(1, len(scenes)))()
+        for i, (off, n) in enumerate(scenes):
+            sc[i].gauss_offset = int(off)
+            sc[i].n = int(n)
+        vs = (N.View * len(views))()
+        off = 0
+        self.pixel_offsets = []
+        self.shapes = []
+        for i, v in enumerate(views):
+            vs[i].scene = int(v["scene"])
+            vs[i].height = int(v["height"])
+            vs[i].width = int(v["width"])
+            vs[i].fx, vs[i].fy, vs[i].cx, vs[i].cy = (float(v["fx"]), float(v["fy"]),
+                                                      float(v["cx"]), float(v["cy"]))
+            for k in range(4):
+                vs[i].quat[k] = float(v["quat"][k])
+            for k in range(3):
+                vs[i].trans[k] = float(v["trans"][k])
+            po = int(v.get("pixel_offset", off))
+            vs[i].pixel_offset = po
+            self.pixel_offsets.append(po)
+            self.shapes.append((int(v["height"]), int(v["width"])))
+            off = max(off, po + int(v["height"]) * int(v["width"]))
+        h = ctypes.c_void_p()
+        N.check(lib.fe_batch_create(ctypes.byref(desc), sc, len(scenes), vs, len(views),
+                                    ctypes.byref(h)))
+        self._h = h
+        self.n_pixels = int(lib.fe_batch_pixels(h))
+        self.scratch_bytes = int(lib.fe_batch_scratch_bytes(h))
+
+    def close(self):
+        if getattr(self, "_h", None) and self._h.value:
+            N.load().fe_batch_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def forward(self, means, prec, logw, depth=None, alpha=None, stats=None):
+        lib = N.load()
+        dev = means.device
+        if depth is None:
+            depth = torch.empty(self.n_pixels, device=dev)
+        if alpha is None:
+            alpha = torch.empty(self.n_pixels, device=dev)
+        N.check(lib.fe_batch_fwd(self._h, _ptr(means), _ptr(prec), _ptr(logw), _ptr(depth),
+                                 _ptr(alpha), _ptr(stats), _stream()))
+        return depth, alpha
+
+    def backward(self, means, prec, logw, depth, alpha, stats, gdepth, galpha):
+        lib = N.load()
+        gm, gp, gw = torch.empty_like(means), torch.empty_like(prec), torch.empty_like(logw)
+        N.check(lib.fe_batch_bwd(self._h, _ptr(means), _ptr(prec), _ptr(logw), _ptr(depth),
+                                 _ptr(alpha), _ptr(stats), _ptr(gdepth), _ptr(galpha), _ptr(gm),
+                                 _ptr(gp), _ptr(gw), _stream()))
+        return gm, gp, gw
+
+    STAGES = ("preprocess", "scan", "emit", "sort", "gather", "blend")
+
+    def forward_timed(self, means, prec, logw, depth=None, alpha=None, stats=None):
+        """forward() with per-stage CUDA-event timings (ms); synchronises."""
+        lib = N.load()
+        dev = means.device
+        if depth is None:
+            depth = torch.empty(self.n_pixels, device=dev)
+        if alpha is None:
+            alpha = torch.empty(self.n_pixels, device=dev)
+        ms = (ctypes.c_float * 6)()
+        N.check(lib.fe_batch_fwd_timed(self._h, _ptr(means), _ptr(prec), _ptr(logw), _ptr(depth),
+                                       _ptr(alpha), _ptr(stats), ms, _stream()))
+        return depth, alpha, dict(zip(self.STAGES, [float(x) for x in ms]))
+
+    @property
+    def launches_per_forward(self):
+        return int(N.load().fe_batch_launch_count(self._h))
+
+    def status(self):
+        lib = N.load()
+        nk, wk, err = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_uint32()
+        N.check(lib.fe_batch_status(self._h, _stream(), ctypes.byref(nk), ctypes.byref(wk),
+                                    ctypes.byref(err)))
+        return {"num_keys": nk.value, "want_keys": wk.value, "device_error": err.value}
+
+    def view_image(self, flat, i):
+        h, w = self.shapes[i]
+        o = self.pixel_offsets[i]
+        return flat[o:o + h * w].view(h, w)

@@ -1,0 +1,258 @@
+/*
+ * fuzzy_ellipses.h -- C ABI of the GB300-native fuzzy-metaball renderer.
+ *
+ * Every entry point takes plain pointers, sizes and a CUDA stream, returns an fe_status code
+ * (never throws, exits or traps) and enqueues all of its work on the caller's stream.
+ * Pointers named "d_*" are device pointers; everything else is host memory.
+ *
+ * The renderer computes, per pixel of a pinhole camera, the fuzzy-metaball depth (softmax of the
+ * ray-Gaussian peak depths) and alpha (1 - exp(-sum of peak densities)) defined by the reference's
+ * baseline/fm_render.py:11-126, restricted per screen tile to the Gaussians whose cut-off
+ * ellipsoid the tile's rays can reach.
+ *
+ * Gaussian parameters (per scene of N Gaussians, float32, row-major):
+ *   means (N,3); prec (N,3,3) in fm_render's prec_full convention -- only the upper triangle U
+ *   is read and the precision is U U^T (baseline/fm_render.py:14,26); logw (N,).
+ * Camera pose (fm_render.render_func_quat, baseline/fm_render.py:113-126): world rays are
+ *   rays_cam @ quat_to_rot(quat), quat = (w,x,y,z) scalar first, ray origin = trans.
+ * Camera rays: rays_cam(u,v) = ((u-cx)/fx, (v-cy)/fy, 1) for integer pixel (u,v), pixel index
+ *   v*W + u (baseline/ycb_fmb_rotscale.py:182-189).
+ */
+#ifndef FUZZY_ELLIPSES_H_
+#define FUZZY_ELLIPSES_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Same type as cudaStream_t; NULL is the legacy default stream. */
+typedef struct CUstream_st *fe_stream_t;
+
+/* XLA's opaque status object for api_version 2 custom calls. */
+typedef struct XlaCustomCallStatus_ XlaCustomCallStatus;
+
+typedef enum fe_status {
+  FE_OK = 0,
+  FE_ERR_INVALID_ARGUMENT = 1, /* a size, pointer or enum value is out of range */
+  FE_ERR_DESCRIPTOR = 2,       /* descriptor has the wrong magic, version or length */
+  FE_ERR_CUDA = 3,             /* a CUDA runtime call failed; see fe_last_error_message() */
+  FE_ERR_OUT_OF_MEMORY = 4,    /* the scratch arena could not grow */
+  FE_ERR_CAPACITY = 5,         /* device-side key count exceeded the planned capacity */
+  FE_ERR_DEVICE_TIMEOUT = 6,   /* a bounded device-side wait gave up */
+  FE_ERR_UNSUPPORTED = 7,
+  FE_ERR_SCRATCH_LIMIT = 8     /* request larger than the fixed scratch of the no-alloc entry */
+} fe_status;
+
+/* How far a Gaussian's screen footprint reaches (the binning cut-off). */
+typedef enum fe_cull_mode {
+  /* Cull where the Gaussian's peak density exp(logw - d^2/2) along a pixel ray is below
+   * cull_param (default 1e-7): Mahalanobis radius k = sqrt(2*(logw - ln eps)). */
+  FE_CULL_EPS = 0,
+  /* Fixed radius k = cull_param standard deviations (the reference binning uses 3.0). */
+  FE_CULL_NSTD = 1
+} fe_cull_mode;
+
+#define FE_DESC_MAGIC 0x31644546u /* "FEd1" */
+#define FE_DESC_VERSION 1
+
+/* Flags for fe_render_desc.flags */
+#define FE_FLAG_SAVE_STATS 1u /* write per-pixel softmax statistics needed by the backward */
+
+/* Render descriptor: everything a render needs besides the Gaussian and pose buffers. It is also
+ * the opaque payload of the XLA custom call targets (bit-copied; the size and magic are checked).
+ * Replaces RasterizeDescriptor{H,W,P,tan_fovx,tan_fovy} of the reference (rasterize_main.h:14-20,
+ * packed by bindings.h:20-29). */
+typedef struct fe_render_desc {
+  uint32_t magic;      /* FE_DESC_MAGIC */
+  uint32_t version;    /* FE_DESC_VERSION */
+  int32_t n_gaussians; /* N >= 0 */
+  int32_t height;      /* H >= 1 */
+  int32_t width;       /* W >= 1 */
+  float fx, fy, cx, cy;
+  float beta2, beta3;  /* softmax temperature terms (reference default 21.4, 2.66) */
+  int32_t cull_mode;   /* fe_cull_mode */
+  float cull_param;    /* eps for FE_CULL_EPS, k for FE_CULL_NSTD; <= 0 selects the default */
+  int32_t tile_w;      /* screen tile width/height in pixels: 8x8, 16x16 or 32x8; 0 = 16x16 */
+  int32_t tile_h;
+  uint32_t flags;      /* FE_FLAG_* */
+  uint32_t reserved;
+} fe_render_desc;
+
+/* Fill d with defaults for an HxW image of n Gaussians. */
+void fe_render_desc_init(fe_render_desc *d, int32_t n_gaussians, int32_t height, int32_t width,
+                         float fx, float fy, float cx, float cy);
+
+/* Forward render of one camera. Replaces the reference's XLA target body
+ * RasterizeGaussiansCUDAJAX (rasterize_main.cu:29-114) and its host orchestration
+ * CudaRasterizer::Rasterizer::forwardJAX (cuda_rasterizer/rasterizer_impl.cu:174-344).
+ *   d_means (N,3), d_prec (N,3,3), d_logw (N), d_quat (4), d_trans (3): inputs;
+ *   d_depth (H,W), d_alpha (H,W): outputs;
+ *   d_stats (3,H,W) or NULL: per-pixel (max logit, softmax normaliser, density sum), required
+ *     by fe_render_bwd; written when non-NULL.
+ * Scratch comes from a per-(device, stream) arena that grows only; the steady state performs no
+ * allocation and no host synchronisation. */
+int fe_render_fwd(const fe_render_desc *desc, const float *d_means, const float *d_prec,
+                  const float *d_logw, const float *d_quat, const float *d_trans, float *d_depth,
+                  float *d_alpha, float *d_stats, fe_stream_t stream);
+
+/* Backward of fe_render_fwd: given dL/ddepth and dL/dalpha (H,W) and the forward's outputs and
+ * stats, writes dL/dmeans (N,3), dL/dprec (N,3,3; strictly-lower entries are 0, as jax.grad
+ * through triu gives) and dL/dlogw (N). No reference counterpart: the reference differentiates
+ * baseline/fm_render.py with jax.grad (notebook cell 12). */
+int fe_render_bwd(const fe_render_desc *desc, const float *d_means, const float *d_prec,
+                  const float *d_logw, const float *d_quat, const float *d_trans,
+                  const float *d_depth, const float *d_alpha, const float *d_stats,
+                  const float *d_grad_depth, const float *d_grad_alpha, float *d_grad_means,
+                  float *d_grad_prec, float *d_grad_logw, fe_stream_t stream);
+
+/* The binning fe_render_fwd performs, exposed for tests and tools: the sorted keys
+ * ((tile << 32) | gaussian index, tiles of desc->tile_w x desc->tile_h in row-major order), the
+ * per-tile [first, last+1) ranges (T,2; empty tiles {0,0}) and the key count. Synchronises the
+ * stream once to return *h_num_keys. Its counterpart in the reference is the key list that
+ * forwardJAX builds internally (cuda_rasterizer/rasterizer_impl.cu:269-302). */
+int fe_render_binning(const fe_render_desc *desc, const float *d_means, const float *d_prec,
+                      const float *d_logw, const float *d_quat, const float *d_trans,
+                      uint64_t *d_keys, int64_t key_capacity, uint32_t *d_ranges,
+                      int64_t *h_num_keys, fe_stream_t stream);
+
+/* XLA custom-call targets (api_version 2: status-returning), registered under the names
+ * "fe_render_fwd" and "fe_render_bwd". opaque = an fe_render_desc.
+ * fwd buffers: [means, prec, logw, quat, trans, depth, alpha, stats]
+ * bwd buffers: [means, prec, logw, quat, trans, depth, alpha, stats, grad_depth, grad_alpha,
+ *               grad_means, grad_prec, grad_logw]
+ * Replaces RasterizeGaussiansCUDAJAX (rasterize_main.h:26-30, registered by ext.cpp:23-33). */
+void fe_render_fwd_xla(fe_stream_t stream, void **buffers, const char *opaque, size_t opaque_len,
+                       XlaCustomCallStatus *status);
+void fe_render_bwd_xla(fe_stream_t stream, void **buffers, const char *opaque, size_t opaque_len,
+                       XlaCustomCallStatus *status);
+
+/* ---------------------------------------------------------------------------------------------
+ * Legacy interface: the reference's own custom-call signature and descriptor.
+ * --------------------------------------------------------------------------------------------- */
+
+/* Byte-compatible with the reference's RasterizeDescriptor (rasterize_main.h:14-20). */
+typedef struct fe_legacy_desc {
+  int32_t image_height;
+  int32_t image_width;
+  int32_t P;
+  float tan_fovx;
+  float tan_fovy;
+} fe_legacy_desc;
+
+/* Reference-compatible binning (tile keys, sort order, tile ranges bit-exact with the reference
+ * CUDA rasterizer's preprocessCUDA + getGaussianTileKeys + thrust sort + getPerTileRanges,
+ * cuda_rasterizer/forward.cu:126-203 and rasterizer_impl.cu:82-152,244-302). Inputs are the
+ * reference's: means (P,3) in camera frame, scales (P,3), rotations (P,4), viewmatrix and
+ * projmatrix (16 floats each, column-major as the reference uses them), tan_fovx/tan_fovy,
+ * n_std (rasterizer_impl.cu:154-172 picks it from P). Outputs (device): radii (P), means2d (P,2),
+ * tiles_touched (P, inclusive prefix sum as the reference leaves it), keys (capacity entries;
+ * the first *h_num_keys are valid and sorted), ranges (T,2) with empty tiles {0,0}.
+ * The call synchronises the stream once to return *h_num_keys (as the reference does at
+ * rasterizer_impl.cu:248). 8x8 tiles, as the reference's config.h:8-9. */
+int fe_reference_binning(int32_t P, int32_t height, int32_t width, float n_std,
+                         const float *d_means, const float *d_scales, const float *d_rotations,
+                         const float *d_viewmatrix, const float *d_projmatrix, float tan_fovx,
+                         float tan_fovy, int32_t *d_radii, float *d_means2d,
+                         uint32_t *d_tiles_touched, uint64_t *d_keys, int64_t key_capacity,
+                         uint32_t *d_ranges, int64_t *h_num_keys, fe_stream_t stream);
+
+/* The reference's XLA target signature, same buffer order (rasterize_main.cu:54-68):
+ * [means3D, weights, scales, rotations, camera_rays, camera_rot, camera_trans, viewmatrix,
+ *  projmatrix, out_z, out_alpha], opaque = fe_legacy_desc. Binning follows the reference
+ * (fe_reference_binning); depth/alpha are computed with this library's blend from the same keys,
+ * using the precision implied by (scales, rotations) and pinhole rays recovered from
+ * camera_rays (rays must be of the form ((u-cx)/fx, (v-cy)/fy, 1), as every reference caller
+ * passes). api_version 2. */
+void fe_rasterize_legacy_xla(fe_stream_t stream, void **buffers, const char *opaque,
+                             size_t opaque_len, XlaCustomCallStatus *status);
+/* The same as fe_rasterize_legacy_xla with named pointers, for ctypes / torch callers. */
+int fe_rasterize_legacy(const fe_legacy_desc *desc, const float *d_means, const float *d_weights,
+                        const float *d_scales, const float *d_rotations, const float *d_camera_rays,
+                        const float *d_camera_rot, const float *d_camera_trans,
+                        const float *d_viewmatrix, const float *d_projmatrix, float *d_out_z,
+                        float *d_out_alpha, fe_stream_t stream);
+
+/* ---------------------------------------------------------------------------------------------
+ * Batched renders: many scenes and cameras in one launch sequence.
+ * --------------------------------------------------------------------------------------------- */
+
+/* One render of a batch: a scene (a slice of the concatenated Gaussian arrays) seen by a camera. */
+typedef struct fe_view {
+  int32_t scene;          /* index into the scene table */
+  int32_t height, width;
+  float fx, fy, cx, cy;
+  float quat[4];          /* scalar first */
+  float trans[3];
+  int64_t pixel_offset;   /* first pixel of this render in the batch output buffers */
+} fe_view;
+
+typedef struct fe_scene {
+  int64_t gauss_offset;   /* first Gaussian of the scene in the concatenated arrays */
+  int32_t n;              /* Gaussians in the scene */
+  int32_t reserved;
+} fe_scene;
+
+typedef struct fe_batch fe_batch;
+
+/* Plan a batch on the current device: uploads the view/scene tables and reserves scratch for the
+ * worst-case key count (so the batch runs with no host synchronisation and can be captured in a
+ * CUDA graph). desc supplies beta2/beta3, cull mode/param and tile shape; its size/intrinsics
+ * fields are ignored. */
+int fe_batch_create(const fe_render_desc *desc, const fe_scene *scenes, int32_t n_scenes,
+                    const fe_view *views, int32_t n_views, fe_batch **out);
+void fe_batch_destroy(fe_batch *b);
+/* Total output pixels of the batch (sum of H*W). */
+int64_t fe_batch_pixels(const fe_batch *b);
+/* Scratch bytes reserved by the batch. */
+int64_t fe_batch_scratch_bytes(const fe_batch *b);
+/* Forward render of every view. Outputs are indexed by fe_view.pixel_offset. d_stats (3, pixels)
+ * or NULL. */
+int fe_batch_fwd(fe_batch *b, const float *d_means, const float *d_prec, const float *d_logw,
+                 float *d_depth, float *d_alpha, float *d_stats, fe_stream_t stream);
+/* Backward of fe_batch_fwd; gradients are accumulated over all views of a scene. */
+int fe_batch_bwd(fe_batch *b, const float *d_means, const float *d_prec, const float *d_logw,
+                 const float *d_depth, const float *d_alpha, const float *d_stats,
+                 const float *d_grad_depth, const float *d_grad_alpha, float *d_grad_means,
+                 float *d_grad_prec, float *d_grad_logw, fe_stream_t stream);
+/* Synchronise `stream` and report the last run's key count (clamped to the planned capacity),
+ * the count it needed, and its device error word (FE_DEVERR_*). */
+int fe_batch_status(fe_batch *b, fe_stream_t stream, int64_t *num_keys, int64_t *want_keys,
+                    uint32_t *device_error);
+
+/* ---------------------------------------------------------------------------------------------
+ * Diagnostics and measurement
+ * --------------------------------------------------------------------------------------------- */
+
+/* fe_batch_fwd with a CUDA event recorded between stages on `stream`; synchronises and writes the
+ * six stage durations in milliseconds to stage_ms: preprocess, scan, key emission, sort,
+ * ranges+tile-record gather, blend. The reference times only its blend, with events
+ * (cuda_rasterizer/rasterizer_impl.cu:314-341). */
+int fe_batch_fwd_timed(fe_batch *b, const float *d_means, const float *d_prec, const float *d_logw,
+                       float *d_depth, float *d_alpha, float *d_stats, float *stage_ms,
+                       fe_stream_t stream);
+/* Number of kernels one fe_batch_fwd launches. */
+int fe_batch_launch_count(const fe_batch *b);
+/* Pipe-throughput microbenchmark: kind 0 = FP32 FMA, kind 1 = MUFU ex2; operations per second.
+ * Allocates (and frees) 1 MiB of scratch. No reference counterpart. */
+int fe_bench_peak(int kind, int iters, double *ops_per_second, fe_stream_t stream);
+
+/* Synchronise `stream` and return the device-side error word of the arena used by calls on that
+ * stream (0 = no error; see FE_DEVERR_*), clearing it. */
+int fe_check_device_status(fe_stream_t stream, uint32_t *device_error);
+
+#define FE_DEVERR_CAPACITY 1u /* more keys than planned */
+#define FE_DEVERR_TIMEOUT 2u  /* a bounded mbarrier wait gave up */
+
+/* Message for the most recent error on the calling thread. */
+const char *fe_last_error_message(void);
+const char *fe_status_string(int status);
+/* Library version string. */
+const char *fe_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FUZZY_ELLIPSES_H_ */

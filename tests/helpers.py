@@ -1,0 +1,50 @@
+"""Shared helpers for the GPU parity tests."""
+
+import numpy as np
+import torch
+
+from oracle import fm_render_np as O
+
+# Stated tolerances (the benchmark spec): absolute alpha, relative depth on pixels where the oracle's
+# alpha exceeds DEPTH_MASK_ALPHA (fm_render's depth on near-empty pixels is a softmax over far
+# Gaussians that any tile-culled renderer omits by construction).
+TOL_ALPHA = 1e-5
+TOL_DEPTH_REL = 1e-4
+DEPTH_MASK_ALPHA = 1e-3
+
+
+def to_dev(x, dev):
+    return torch.from_numpy(np.ascontiguousarray(x)).to(dev)
+
+
+def scene_to_dev(scene, dev):
+    return to_dev(scene.means, dev), to_dev(scene.prec, dev), to_dev(scene.logw, dev)
+
+
+def oracle_pixels(scene, cam, pix):
+    """Dense float64 oracle on a subset of pixel indices (v*W+u) of a camera."""
+    rays = O.pinhole_rays(cam.height, cam.width, cam.fx, cam.fy, cam.cx, cam.cy)[pix]
+    d, a, _, _ = O.render_func_quat(scene.means, scene.prec, scene.logw, rays, cam.quat,
+                                    cam.trans, 21.4, 2.66)
+    return d, a
+
+
+def parity_errors(depth, alpha, d_ref, a_ref, mask_alpha=DEPTH_MASK_ALPHA):
+    depth = np.asarray(depth, np.float64).ravel()
+    alpha = np.asarray(alpha, np.float64).ravel()
+    d_ref = np.asarray(d_ref).ravel()
+    a_ref = np.asarray(a_ref).ravel()
+    ea = float(np.abs(alpha - a_ref).max()) if alpha.size else 0.0
+    m = a_ref > mask_alpha
+    ed = float((np.abs(depth - d_ref)[m] / np.abs(d_ref[m])).max()) if m.any() else 0.0
+    return ea, ed
+
+
+def tile_lists_from_keys(keys, n_tiles):
+    keys = keys.cpu().numpy().view(np.uint64)
+    tiles = (keys >> np.uint64(32)).astype(np.int64)
+    gids = (keys & np.uint64(0xFFFFFFFF)).astype(np.int64)
+    lists = [[] for _ in range(n_tiles)]
+    for t, g in zip(tiles, gids):
+        lists[t].append(g)
+    return [np.array(x, np.int64) for x in lists]

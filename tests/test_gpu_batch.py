@@ -1,0 +1,91 @@
+"""Batched renders of uneven scenes and cameras equal the plain per-call renders; the batch runs
+without host synchronisation and replays from a CUDA graph."""
+
+import numpy as np
+import pytest
+import torch
+
+import fuzzy_ellipses as fe
+from fuzzy_ellipses import synthetic as S
+from tests.helpers import scene_to_dev
+
+pytestmark = pytest.mark.gpu
+
+
+def make_batch(dev, n_scenes=6, seed=0, tile=(16, 16)):
+    items = S.config3(seed=seed, n_scenes=n_scenes)
+    means, prec, logw, scenes, views = [], [], [], [], []
+    off = 0
+    for si, (sc, cams) in enumerate(items):
+        means.append(sc.means); prec.append(sc.prec); logw.append(sc.logw)
+        scenes.append((off, sc.n))
+        off += sc.n
+        for c in cams:
+            views.append(dict(scene=si, height=c.height, width=c.width, fx=c.fx, fy=c.fy, cx=c.cx,
+                              cy=c.cy, quat=c.quat, trans=c.trans))
+    b = fe.Batch(scenes, views, tile=tile)
+    tens = [torch.from_numpy(np.concatenate(x)).to(dev) for x in (means, prec, logw)]
+    return b, items, views, tens
+
+
+@pytest.mark.parametrize("tile", [(8, 8), (16, 16), (32, 8)])
+def test_batch_equals_single_renders(cuda_device, tile):
+    dev = cuda_device
+    b, items, views, (m, p, w) = make_batch(dev, tile=tile)
+    depth, alpha = b.forward(m, p, w)
+    st = b.status()
+    assert st["device_error"] == 0 and st["num_keys"] == st["want_keys"]
+    vi = 0
+    for si, (sc, cams) in enumerate(items):
+        ms, ps, ws = scene_to_dev(sc, dev)
+        for c in cams:
+            d1, a1 = fe.render_forward(ms, ps, ws, c.fx, c.fy, c.cx, c.cy, c.quat, c.trans,
+                                       c.height, c.width, tile=tile)
+            assert torch.equal(b.view_image(depth, vi), d1)
+            assert torch.equal(b.view_image(alpha, vi), a1)
+            vi += 1
+
+
+def test_batch_backward_equals_sum_of_single(cuda_device):
+    dev = cuda_device
+    b, items, views, (m, p, w) = make_batch(dev, n_scenes=4, seed=1)
+    stats = torch.empty(3 * b.n_pixels, device=dev)
+    depth, alpha = b.forward(m, p, w, stats=stats)
+    gen = torch.Generator(device=dev).manual_seed(0)
+    ga = torch.randn(b.n_pixels, device=dev, generator=gen)
+    gd = torch.zeros(b.n_pixels, device=dev)
+    gm, gp, gw = b.backward(m, p, w, depth, alpha, stats, gd, ga)
+    rm, rp, rw = torch.zeros_like(m), torch.zeros_like(p), torch.zeros_like(w)
+    off, vi = 0, 0
+    for sc, cams in items:
+        sl = slice(off, off + sc.n)
+        for c in cams:
+            mm, pp, ww = [t[sl].clone().requires_grad_() for t in (m, p, w)]
+            _, a = fe.render(mm, pp, ww, c.fx, c.fy, c.cx, c.cy, c.quat, c.trans, c.height, c.width)
+            (a * b.view_image(ga, vi)).sum().backward()
+            rm[sl] += mm.grad; rp[sl] += pp.grad; rw[sl] += ww.grad
+            vi += 1
+        off += sc.n
+    for x, y in ((gm, rm), (gp, rp), (gw, rw)):
+        assert float((x - y).norm() / y.norm()) < 1e-4
+
+
+def test_batch_replays_from_cuda_graph(cuda_device):
+    dev = cuda_device
+    b, items, views, (m, p, w) = make_batch(dev, n_scenes=5, seed=2)
+    depth = torch.empty(b.n_pixels, device=dev)
+    alpha = torch.empty(b.n_pixels, device=dev)
+    ref_d, ref_a = b.forward(m, p, w)
+    torch.cuda.synchronize()
+    s = torch.cuda.Stream()
+    s.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(s):
+        b.forward(m, p, w, depth, alpha)  # warm-up on the capture stream
+    torch.cuda.current_stream().wait_stream(s)
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g):
+        b.forward(m, p, w, depth, alpha)
+    depth.zero_(); alpha.zero_()
+    g.replay()
+    torch.cuda.synchronize()
+    assert torch.equal(depth, ref_d) and torch.equal(alpha, ref_a)

@@ -1,0 +1,98 @@
+"""Tile keys, sort order and tile ranges of the reference-compatible binning are bit-exact with
+the reference CUDA rasterizer (golden fixtures from its own kernels) and with the C oracle."""
+
+import os
+
+import numpy as np
+import pytest
+import torch
+
+import fuzzy_ellipses as fe
+from fuzzy_ellipses import synthetic as S
+from oracle import fm_render_np as O
+from oracle.ref_binning import ref_binning
+from tests.golden.binning_cases import binning_cases, num_stds, projection, tan_full_fov
+from tests.helpers import TOL_ALPHA, TOL_DEPTH_REL, parity_errors
+
+pytestmark = pytest.mark.gpu
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden", "ref_binning_golden.npz")
+CASES = {c["name"]: c for c in binning_cases()}
+
+
+def gpu_binning(case):
+    return fe.reference_binning(case["means"], case["scales"], case["rots"], case["view"],
+                                case["proj"], case["H"], case["W"], case["tan_fovx"],
+                                case["tan_fovy"], case["n_std"])
+
+
+@pytest.mark.parametrize("name", sorted(CASES))
+def test_reference_binning_bit_exact(cuda_device, name):
+    golden = np.load(GOLDEN)
+    g = gpu_binning(CASES[name])
+    torch.cuda.synchronize()
+    pre = f"{name}/nofma_"
+    assert np.array_equal(g["radii"].cpu().numpy(), golden[pre + "radii"])
+    assert np.array_equal(g["means2d"].cpu().numpy().view(np.uint32),
+                          golden[pre + "means2d"].view(np.uint32))
+    assert np.array_equal(g["tiles_touched"].cpu().numpy().astype(np.uint32),
+                          golden[pre + "tiles_touched"])
+    assert np.array_equal(g["keys"].cpu().numpy().view(np.uint64), golden[pre + "keys"])
+    assert np.array_equal(g["ranges"].cpu().numpy().astype(np.uint32), golden[pre + "ranges"])
+
+
+@pytest.mark.parametrize("seed", range(4))
+def test_reference_binning_matches_c_oracle_random(cuda_device, seed):
+    rng = np.random.default_rng(100 + seed)
+    n = int(rng.integers(1, 3000))
+    H, W = int(rng.integers(8, 500)), int(rng.integers(8, 700))
+    f = float(rng.uniform(0.5, 1.5) * W)
+    z = rng.uniform(0.1, 3.0, n)
+    means = np.stack([rng.uniform(-0.8, 0.8, n) * z, rng.uniform(-0.8, 0.8, n) * z, z], 1).astype(np.float32)
+    scales = np.exp(rng.uniform(np.log(1e-3), np.log(0.2), (n, 3))).astype(np.float32)
+    q = rng.standard_normal((n, 4)).astype(np.float32)
+    case = {"means": means, "scales": scales, "rots": q, "view": np.eye(4, dtype=np.float32),
+            "proj": projection(W, H, f, f), "H": H, "W": W, "n_std": num_stds(n),
+            "tan_fovx": tan_full_fov(W, f), "tan_fovy": tan_full_fov(H, f)}
+    r = ref_binning(case["means"], case["scales"], case["rots"], case["view"], case["proj"], H, W,
+                    case["tan_fovx"], case["tan_fovy"], case["n_std"])
+    g = gpu_binning(case)
+    assert g["num_keys"] == r["num_keys"]
+    assert np.array_equal(g["keys"].cpu().numpy().view(np.uint64), r["keys"])
+    assert np.array_equal(g["ranges"].cpu().numpy().astype(np.uint32), r["ranges"])
+    assert np.array_equal(g["radii"].cpu().numpy(), r["radii"])
+
+
+def test_legacy_rasterize_matches_culled_oracle(cuda_device):
+    """The reference-signature entry point: reference binning, then this library's blend."""
+    case = CASES["cfg0_like"]
+    H, W, f = case["H"], case["W"], 200.0
+    cx, cy = W / 2, H / 2
+    n = case["means"].shape[0]
+    logw = np.random.default_rng(7).normal(0, 0.5, n).astype(np.float32)
+    rays = O.pinhole_rays(H, W, f, f, cx, cy).astype(np.float32)
+    rot, trans = np.eye(3, dtype=np.float32), np.zeros(3, np.float32)
+    z, a = fe.rasterize(case["means"], case["scales"], case["rots"], logw, rays, rot, trans, H, W,
+                        f, f, cx, cy, 0.01, 4.5)
+    torch.cuda.synchronize()
+    # The binning the legacy entry used is the reference's (same floats as the wrapper builds).
+    tfx, tfy, view, proj = fe.render._legacy_scalars(H, W, f, f, cx, cy, 0.01, 4.5)
+    rb = ref_binning(case["means"], case["scales"], case["rots"], view, proj, H, W, tfx, tfy,
+                     fe.reference_num_stds(n))
+    keys = rb["keys"]
+    lists = [[] for _ in range(rb["ranges"].shape[0])]
+    for k in keys:
+        lists[int(k >> np.uint64(32))].append(int(k & np.uint64(0xFFFFFFFF)))
+    # Precision implied by (scales, rotations): Sigma = R diag(s^2) R^T, U = inv(chol(Sigma))^T.
+    prec = []
+    for s, qq in zip(case["scales"].astype(np.float64), case["rots"].astype(np.float64)):
+        r, x, y, zq = qq
+        R = np.array([[1 - 2 * (y * y + zq * zq), 2 * (x * y - r * zq), 2 * (x * zq + r * y)],
+                      [2 * (x * y + r * zq), 1 - 2 * (x * x + zq * zq), 2 * (y * zq - r * x)],
+                      [2 * (x * zq - r * y), 2 * (y * zq + r * x), 1 - 2 * (x * x + y * y)]])
+        sig = R @ np.diag(s * s) @ R.T
+        prec.append(np.linalg.inv(np.linalg.cholesky(sig)).T)
+    prec = np.array(prec)
+    dc, ac = O.render_culled(case["means"], prec, logw, H, W, f, f, cx, cy, [1, 0, 0, 0],
+                             [0, 0, 0], [np.array(l, np.int64) for l in lists], 8, 8)
+    ea, ed = parity_errors(z.cpu().numpy(), a.cpu().numpy(), dc, ac)
+    assert ea <= 2 * TOL_ALPHA and ed <= TOL_DEPTH_REL, (ea, ed)

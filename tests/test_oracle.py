@@ -1,0 +1,111 @@
+"""The float64 oracle (restatement of baseline/fm_render.py) against analytic known answers and
+against its torch restatement. No GPU."""
+
+import math
+
+import numpy as np
+import pytest
+import torch
+
+from oracle import fm_render_np as O
+from oracle import fm_render_torch as OT
+
+
+def iso_prec(sigma):
+    return np.eye(3)[None] / sigma  # U = I/sigma, precision U U^T = I/sigma^2
+
+
+def test_quat_to_rot_matches_reference_formula():
+    q = np.array([0.3, -0.5, 0.7, 0.1])
+    r = O.quat_to_rot(q)
+    assert np.allclose(r @ r.T, np.eye(3), atol=1e-12)
+    assert np.isclose(np.linalg.det(r), 1.0)
+    assert np.allclose(O.quat_to_rot([1, 0, 0, 0]), np.eye(3))
+    assert np.allclose(O.quat_to_rot([0, 0, 0, 0]), np.eye(3))  # |q|^2 <= 1e-12 -> identity
+
+
+def test_single_gaussian_on_axis_known_answer():
+    # Camera at the origin looking down +z, one isotropic Gaussian at depth d.
+    d, sigma, w = 0.5, 0.01, 0.3
+    means = np.array([[0.0, 0.0, d]])
+    rays = np.array([[0.0, 0.0, 1.0], [0.02, 0.0, 1.0], [0.0, -0.05, 1.0]])
+    csr = np.stack([rays, np.zeros_like(rays)], 1)
+    depth, alpha, _, _ = O.render_func_rays(csr, means, iso_prec(sigma), np.array([w]), 21.4, 2.66)
+    for i, (x, y, _) in enumerate(rays):
+        r2 = x * x + y * y
+        z = d / (1.0 + r2)                               # peak of the ray parameter
+        d0 = r2 * d * d / (sigma * sigma * (1.0 + r2))    # squared Mahalanobis distance at the peak
+        assert math.isclose(depth[i], z, rel_tol=1e-12)
+        assert math.isclose(alpha[i], 1.0 - math.exp(-math.exp(w - 0.5 * d0)), rel_tol=1e-12)
+
+
+def test_two_gaussians_depth_softmax_known_answer():
+    z1, z2, s, w1, w2, b2, b3 = 0.4, 0.6, 0.02, 0.1, -0.2, 21.4, 2.66
+    means = np.array([[0.0, 0.0, z1], [0.0, 0.0, z2]])
+    csr = np.stack([np.array([[0.0, 0.0, 1.0]]), np.zeros((1, 3))], 1)
+    depth, alpha, _, w = O.render_func_rays(csr, means, np.concatenate([iso_prec(s)] * 2),
+                                            np.array([w1, w2]), b2, b3, return_weights=True)
+    l1, l2 = -b2 * z1 + b3 * w1, -b2 * z2 + b3 * w2
+    e1, e2 = 1.0, math.exp(l2 - l1)
+    assert math.isclose(depth[0], (e1 * z1 + e2 * z2) / (e1 + e2), rel_tol=1e-12)
+    assert math.isclose(alpha[0], 1 - math.exp(-(math.exp(w1) + math.exp(w2))), rel_tol=1e-12)
+    assert np.allclose(w[:, 0].sum(), 1.0)
+
+
+def test_behind_camera_counts_for_alpha_not_depth():
+    # fm_render.py:89-96: the z>0 mask applies to the depth weights only.
+    means = np.array([[0.0, 0.0, -0.5], [0.0, 0.0, 0.5]])
+    csr = np.stack([np.array([[0.0, 0.0, 1.0]]), np.zeros((1, 3))], 1)
+    depth, alpha, _, _ = O.render_func_rays(csr, means, np.concatenate([iso_prec(0.05)] * 2),
+                                            np.array([0.0, -30.0]), 21.4, 2.66)
+    assert math.isclose(alpha[0], 1 - math.exp(-(1.0 + math.exp(-30.0))), rel_tol=1e-12)
+    # The softmax max runs over every Gaussian before the mask (fm_render.py:93-96): the behind
+    # Gaussian's logit (-beta2 * -0.5) is the max, the front weight exp(-101) falls under the
+    # +1e-20 floor, and depth becomes the floor-weighted mean of all z: (-0.5 + 0.5) / 2 = 0.
+    assert abs(depth[0]) < 1e-12
+    # With a front log-weight of 0 its relative weight exp(-21.4) clears the floor by far.
+    depth2, _, _, _ = O.render_func_rays(csr, means, np.concatenate([iso_prec(0.05)] * 2),
+                                         np.array([0.0, 0.0]), 21.4, 2.66)
+    assert math.isclose(depth2[0], 0.5, rel_tol=1e-9)
+
+
+def test_triu_ignores_lower_entries():
+    rng = np.random.default_rng(0)
+    means = rng.uniform(-0.05, 0.05, (3, 3)) + [0, 0, 0.5]
+    prec = np.triu(rng.uniform(50, 100, (3, 3, 3)))
+    rays = O.pinhole_rays(6, 5, 20.0, 20.0, 2.5, 3.0)
+    csr = np.stack([rays, np.zeros_like(rays)], 1)
+    a = O.render_func_rays(csr, means, prec, np.zeros(3), 21.4, 2.66)
+    noisy = prec + np.tril(rng.uniform(-9, 9, (3, 3, 3)), -1)
+    b = O.render_func_rays(csr, means, noisy, np.zeros(3), 21.4, 2.66)
+    assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
+
+
+def test_numpy_and_torch_restatements_agree_and_grad_of_lower_is_zero():
+    from fuzzy_ellipses import synthetic as S
+    sc, cams = S.config0()
+    c = cams[0]
+    d1, a1 = O.render_pinhole(sc.means, sc.prec, sc.logw, 24, 20, 24.0, 24.0, 10.0, 12.0, c.quat, c.trans)
+    m = torch.from_numpy(sc.means).double().requires_grad_()
+    p = torch.from_numpy(sc.prec).double().requires_grad_()
+    w = torch.from_numpy(sc.logw).double()
+    d2, a2 = OT.render_pinhole(m, p, w, 24, 20, 24.0, 24.0, 10.0, 12.0,
+                               torch.from_numpy(c.quat).double(), torch.from_numpy(c.trans).double())
+    assert np.allclose(d1, d2.detach().numpy(), atol=1e-13)
+    assert np.allclose(a1, a2.detach().numpy(), atol=1e-13)
+    (a2.sum() + d2.sum()).backward()
+    assert torch.all(torch.tril(p.grad, -1) == 0)
+
+
+def test_culled_equals_dense_with_full_lists():
+    from fuzzy_ellipses import synthetic as S
+    sc, cams = S.config0()
+    c = cams[0]
+    H, W, f = 16, 24, 24.0
+    d_ref, a_ref = O.render_pinhole(sc.means, sc.prec, sc.logw, H, W, f, f, W / 2, H / 2, c.quat, c.trans)
+    lists = [np.arange(sc.n)] * (((W + 7) // 8) * ((H + 7) // 8))
+    d, a = O.render_culled(sc.means, sc.prec, sc.logw, H, W, f, f, W / 2, H / 2, c.quat, c.trans,
+                           lists, 8, 8)
+    assert np.allclose(a, a_ref, atol=1e-14)
+    mask = a_ref > 1e-6
+    assert np.allclose(d[mask], d_ref[mask], rtol=1e-12)
