@@ -311,8 +311,8 @@ def main():
         _, _, ms = batch.forward_timed(m, p, w, depth, alpha)
         stage_runs.append(ms)
     stages = {k: statistics.median(r[k] for r in stage_runs) for k in batch.STAGES}
-    fma_ops = fe.render.bench_peak("fma")
-    ex2_ops = fe.render.bench_peak("ex2")
+    fma_ops = fe.bench_peak("fma")
+    ex2_ops = fe.bench_peak("ex2")
     peak_evals = min(fma_ops / PER_EVAL_FMA, ex2_ops / PER_EVAL_MUFU)
     blend_evals_per_s = e_step / (stages["blend"] * 1e-3)
     peaks, peak_kind = measured_peaks()

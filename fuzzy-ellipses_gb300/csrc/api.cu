@@ -190,6 +190,9 @@ int check_desc(const fe_render_desc* d) {
   const bool tile_ok = (d->tile_w == 0 && d->tile_h == 0) || (d->tile_w == 8 && d->tile_h == 8) ||
                        (d->tile_w == 16 && d->tile_h == 16) || (d->tile_w == 32 && d->tile_h == 8);
   if (!tile_ok) return fail(FE_ERR_INVALID_ARGUMENT, "tile shape must be 8x8, 16x16 or 32x8");
+  if (d->px_per_thread != 0 && d->px_per_thread != 1 && d->px_per_thread != 2 &&
+      d->px_per_thread != 4)
+    return fail(FE_ERR_INVALID_ARGUMENT, "px_per_thread must be 0, 1, 2 or 4");
   return FE_OK;
 }
 
@@ -205,6 +208,7 @@ struct Pipeline {
   ViewsArg va;
   int64_t n_rec, n_tiles, n_pix;
   int tile_w, tile_h;
+  int px;  // pixels per thread in the blend (0 = default)
   int cull_mode;
   float cull_param;
   float beta2, beta3;
@@ -268,6 +272,7 @@ Pipeline single_view_pipeline(const fe_render_desc* d, const float* means, const
   p.n_pix = (int64_t)d->height * d->width;
   p.tile_w = tw;
   p.tile_h = th;
+  p.px = (int)d->px_per_thread;
   p.cull_mode = d->cull_mode;
   p.cull_param = d->cull_param;
   p.beta2 = d->beta2;
@@ -346,7 +351,7 @@ int fe_render_fwd(const fe_render_desc* d, const float* means, const float* prec
   rc = run_binning(p, p.n_rec * p.n_tiles, a->rec, a->keys, a->h_pinned, false, st, rs, ks, cap,
                    sorted);
   if (rc) return rc;
-  launch_blend_fwd(p.va, p.tile_w, p.tile_h, p.n_tiles, ks.trec, rs.ranges, p.beta2, p.beta3,
+  launch_blend_fwd(p.va, p.tile_w, p.tile_h, p.px, p.n_tiles, ks.trec, rs.ranges, p.beta2, p.beta3,
                    depth, alpha, stats, npix, rs.ctrl, st);
   FE_CUDA(cudaGetLastError());
   return FE_OK;
@@ -578,7 +583,7 @@ int fe_rasterize_legacy(const fe_legacy_desc* d, const float* means, const float
   launch_emit_keys(va, rs.incl, rs.rects, P, rs.ctrl, ks.keys_a, cap, st);
   uint64_t* sorted = launch_sort(ks.keys_a, ks.keys_b, bits_for(T), rs.ctrl, cap, ks.hist, st);
   launch_ranges_gather(va, sorted, rs.ctrl, cap, rs.recs, 8, 8, rs.ranges, ks.trec, st);
-  launch_blend_fwd(va, 8, 8, T, ks.trec, rs.ranges, 21.4f, 2.66f, out_z, out_alpha, nullptr, 0,
+  launch_blend_fwd(va, 8, 8, 0, T, ks.trec, rs.ranges, 21.4f, 2.66f, out_z, out_alpha, nullptr, 0,
                    rs.ctrl, st);
   FE_CUDA(cudaGetLastError());
   return FE_OK;
@@ -777,6 +782,7 @@ static Pipeline batch_pipeline(fe_batch* b, const float* means, const float* pre
   p.n_pix = b->n_pix;
   p.tile_w = b->tile_w;
   p.tile_h = b->tile_h;
+  p.px = (int)b->desc.px_per_thread;
   p.cull_mode = b->desc.cull_mode;
   p.cull_param = b->desc.cull_param;
   p.beta2 = b->desc.beta2;
@@ -809,7 +815,7 @@ int fe_batch_fwd(fe_batch* b, const float* means, const float* prec, const float
     return fail(FE_ERR_INVALID_ARGUMENT, "NULL Gaussian pointer");
   int rc = batch_binning(b, p, st);
   if (rc) return rc;
-  launch_blend_fwd(p.va, p.tile_w, p.tile_h, p.n_tiles, b->ks.trec, b->rs.ranges, p.beta2, p.beta3,
+  launch_blend_fwd(p.va, p.tile_w, p.tile_h, p.px, p.n_tiles, b->ks.trec, b->rs.ranges, p.beta2, p.beta3,
                    depth, alpha, stats, p.n_pix, b->rs.ctrl, st);
   FE_CUDA(cudaGetLastError());
   return FE_OK;
@@ -887,7 +893,7 @@ int fe_batch_fwd_timed(fe_batch* b, const float* means, const float* prec, const
   launch_ranges_gather(p.va, b->sorted, rs.ctrl, b->cap, rs.recs, p.tile_w, p.tile_h, rs.ranges,
                        ks.trec, st);
   FE_CUDA(cudaEventRecord(ev[5], st));
-  launch_blend_fwd(p.va, p.tile_w, p.tile_h, p.n_tiles, ks.trec, rs.ranges, p.beta2, p.beta3,
+  launch_blend_fwd(p.va, p.tile_w, p.tile_h, p.px, p.n_tiles, ks.trec, rs.ranges, p.beta2, p.beta3,
                    depth, alpha, stats, p.n_pix, rs.ctrl, st);
   FE_CUDA(cudaEventRecord(ev[6], st));
   FE_CUDA(cudaEventSynchronize(ev[6]));
@@ -900,7 +906,8 @@ int fe_batch_fwd_timed(fe_batch* b, const float* means, const float* prec, const
 int fe_batch_launch_count(const fe_batch* b) {
   if (!b) return 0;
   const int passes = (bits_for(b->n_tiles) + 7) / 8;
-  return 1 + 3 + 1 + 3 * passes + 1 + 1;
+  const int scan = b->n_rec <= 65536 ? 1 : 3;
+  return 1 + scan + 1 + 3 * passes + 1 + 1;
 }
 
 int fe_bench_peak(int kind, int iters, double* ops_per_second, fe_stream_t stream_) {

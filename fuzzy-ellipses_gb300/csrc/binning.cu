@@ -22,6 +22,7 @@ namespace fe {
 namespace {
 
 constexpr int kScanThreads = 256;
+constexpr int64_t kSmallScan = 65536;  // inputs up to this size use the single-CTA scan
 constexpr int kSortThreads = 256;
 constexpr int kSortWarps = kSortThreads / 32;
 
@@ -117,29 +118,79 @@ __global__ void scan_down_kernel(const uint32_t* __restrict__ in, uint32_t* __re
   }
 }
 
+// One warp per record: the lanes write the record's rectangle of keys, row by row, at its scan
+// offset (coalesced), skipping anything beyond the device-side key count.
 __global__ void emit_keys_kernel(ViewsArg va, const uint32_t* __restrict__ incl,
                                  const TileRect* __restrict__ rects, int64_t n,
                                  const Control* __restrict__ ctrl, uint64_t* __restrict__ keys) {
   const int64_t K = (int64_t)ctrl->num_keys;
-  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < K;
-       k += (int64_t)gridDim.x * blockDim.x) {
-    // First record whose inclusive prefix exceeds k.
-    int64_t lo = 0, hi = n - 1;
-    while (lo < hi) {
-      const int64_t mid = (lo + hi) >> 1;
-      if ((int64_t)incl[mid] > k) hi = mid; else lo = mid + 1;
-    }
-    const int64_t i = lo;
-    const int64_t excl = i ? (int64_t)incl[i - 1] : 0;
-    const int64_t j = k - excl;
+  const int lane = threadIdx.x & 31;
+  const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+  for (int64_t i = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; i < n; i += warps) {
+    const int64_t end = (int64_t)incl[i];
+    const int64_t off = i ? (int64_t)incl[i - 1] : 0;
+    if (end == off || off >= K) continue;
     const TileRect r = rects[i];
     const int w = r.x1 - r.x0;
-    const int x = r.x0 + (int)(j % w), y = r.y0 + (int)(j / w);
     const int vi = find_view<&ViewDev::rec_base>(va, i);
     const ViewDev& V = view_at(va, vi);
-    const uint64_t tile = (uint64_t)(V.tile_base + (int64_t)y * V.gx + x);
     const uint64_t gid = (uint64_t)(i - V.rec_base);
-    keys[k] = (tile << 32) | gid;
+    const int64_t cnt = min(end, K) - off;
+    for (int64_t j = lane; j < cnt; j += 32) {
+      const int x = r.x0 + (int)(j % w), y = r.y0 + (int)(j / w);
+      const uint64_t tile = (uint64_t)(V.tile_base + (int64_t)y * V.gx + x);
+      keys[off + j] = (tile << 32) | gid;
+    }
+  }
+}
+
+// Single-CTA inclusive scan for small inputs: 1024 threads x 4 consecutive values per pass.
+__global__ void __launch_bounds__(1024) scan_small_kernel(const uint32_t* __restrict__ in,
+                                                          uint32_t* __restrict__ out, int64_t n,
+                                                          int64_t capacity,
+                                                          Control* __restrict__ ctrl) {
+  __shared__ unsigned long long ws[32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  unsigned long long carry = 0;
+  for (int64_t base = 0; base < n; base += 4096) {
+    const int64_t i0 = base + 4 * threadIdx.x;
+    uint32_t v[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) v[k] = i0 + k < n ? in[i0 + k] : 0u;
+    unsigned long long t = (unsigned long long)v[0] + v[1] + v[2] + v[3];
+    unsigned long long x = t;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      unsigned long long y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += y;
+    }
+    if (lane == 31) ws[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+      unsigned long long s2 = ws[lane];
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        unsigned long long y = __shfl_up_sync(0xffffffffu, s2, o);
+        if (lane >= o) s2 += y;
+      }
+      ws[lane] = s2;
+    }
+    __syncthreads();
+    unsigned long long run = carry + (warp ? ws[warp - 1] : 0ull) + x - t;
+    const unsigned long long total = ws[31];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      run += v[k];
+      if (i0 + k < n) out[i0 + k] = run > 0xffffffffull ? 0xffffffffu : (uint32_t)run;
+    }
+    carry += total;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    ctrl->want_keys = carry;
+    const unsigned long long cap = (unsigned long long)capacity;
+    ctrl->num_keys = carry < cap ? carry : cap;
+    if (carry > cap) atomicOr(&ctrl->error, FE_DEVERR_CAPACITY);
   }
 }
 
@@ -166,31 +217,26 @@ __global__ void sort_hist_kernel(const uint64_t* __restrict__ keys, const Contro
   hist[blockIdx.x * 256 + threadIdx.x] = cnt[threadIdx.x];
 }
 
-// One block of 256 threads, thread d owns digit d: per-digit exclusive scan over the used blocks
-// (coalesced across digits), then the exclusive scan of digit totals into row `grid` of hist.
+// One block per digit: exclusive scan of that digit's per-block counts (in block order), written
+// back in place; the digit total goes to row `grid` of hist. Each thread owns a contiguous run
+// of blocks so the scan keeps block order.
 __global__ void sort_scan_kernel(uint32_t* __restrict__ hist, const Control* __restrict__ ctrl,
                                  int grid) {
   __shared__ uint32_t ws[kScanThreads / 32];
   const int nb = sort_blocks_used((int64_t)ctrl->num_keys, grid);
-  const int d = threadIdx.x;
+  const int d = blockIdx.x;
+  const int per = (nb + kScanThreads - 1) / kScanThreads;
+  const int b0 = threadIdx.x * per, b1 = min(nb, b0 + per);
   uint32_t run = 0;
-  int b = 0;
-  for (; b + 4 <= nb; b += 4) {
-    const uint32_t c0 = hist[(b + 0) * 256 + d], c1 = hist[(b + 1) * 256 + d];
-    const uint32_t c2 = hist[(b + 2) * 256 + d], c3 = hist[(b + 3) * 256 + d];
-    hist[(b + 0) * 256 + d] = run; run += c0;
-    hist[(b + 1) * 256 + d] = run; run += c1;
-    hist[(b + 2) * 256 + d] = run; run += c2;
-    hist[(b + 3) * 256 + d] = run; run += c3;
-  }
-  for (; b < nb; ++b) {
-    const uint32_t c = hist[b * 256 + d];
-    hist[b * 256 + d] = run;
-    run += c;
-  }
+  for (int b = b0; b < b1; ++b) run += hist[b * 256 + d];
   uint32_t ex;
-  block_exclusive_scan<uint32_t>(run, ex, ws);
-  hist[grid * 256 + d] = ex;
+  const uint32_t total = block_exclusive_scan<uint32_t>(run, ex, ws);
+  for (int b = b0; b < b1; ++b) {
+    const uint32_t c = hist[b * 256 + d];
+    hist[b * 256 + d] = ex;
+    ex += c;
+  }
+  if (threadIdx.x == 0) hist[grid * 256 + d] = total;
 }
 
 // Stable scatter: keys are taken in order 256 at a time; ranks within a 256-key slice come from
@@ -201,13 +247,19 @@ __global__ void sort_scatter_kernel(const uint64_t* __restrict__ in, uint64_t* _
   __shared__ uint32_t off[256];
   __shared__ uint32_t tot[256];
   __shared__ uint32_t wc[kSortWarps][256];
+  __shared__ uint32_t ws[kScanThreads / 32];
   const int64_t K = (int64_t)ctrl->num_keys;
   const int nb = sort_blocks_used(K, gridDim.x);
   if ((int)blockIdx.x >= nb) return;
   const int64_t chunk = chunk_of(K, nb, kSortThreads);
   const int64_t s = blockIdx.x * chunk, e = min(K, s + chunk);
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  off[tid] = hist[blockIdx.x * 256 + tid] + hist[gridDim.x * 256 + tid];
+  {
+    // Digit bases: exclusive scan of the 256 digit totals.
+    uint32_t base;
+    block_exclusive_scan<uint32_t>(hist[gridDim.x * 256 + tid], base, ws);
+    off[tid] = base + hist[blockIdx.x * 256 + tid];
+  }
   const uint32_t lt_mask = (1u << lane) - 1u;
   for (int64_t base = s; base < e; base += kSortThreads) {
 #pragma unroll
@@ -238,12 +290,17 @@ __global__ void sort_scatter_kernel(const uint64_t* __restrict__ in, uint64_t* _
   }
 }
 
+// (du, dv): offset of the tile centre from the record's centre (uc, vc), in pixels. The
+// Mahalanobis polynomial is expanded at the record's centre when that lies within kNearCentre
+// pixels of the tile centre (there it vanishes, up to the rounding of the centre), otherwise at
+// the tile centre (where it is large across the whole tile).
 __device__ __forceinline__ void tile_record(const GaussRec& g, float du, float dv, TileRec& t) {
   float a0[3], y0[3];
+  const bool near = fabsf(du) <= kNearCentre && fabsf(dv) <= kNearCentre;
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
     a0[k] = fmaf(dv, g.a2[k], fmaf(du, g.a1[k], g.a0[k]));
-    y0[k] = fmaf(dv, g.y2[k], fmaf(du, g.y1[k], g.y0[k]));
+    y0[k] = near ? g.y0[k] : fmaf(dv, g.y2[k], fmaf(du, g.y1[k], g.y0[k]));
   }
   auto d3 = [](const float* a, const float* b) { return fmaf(a[2], b[2], fmaf(a[1], b[1], a[0] * b[0])); };
   t.V[0] = d3(a0, a0);
@@ -263,6 +320,10 @@ __device__ __forceinline__ void tile_record(const GaussRec& g, float du, float d
   t.N[4] = 2.f * kn * d3(g.y1, g.y2);
   t.N[5] = kn * d3(g.y2, g.y2);
   t.C = g.c2;
+  t.cu = near ? -du : 0.f;
+  t.cv = near ? -dv : 0.f;
+  t.pad[0] = 0.f;
+  t.pad[1] = 0.f;
 }
 
 __global__ void ranges_gather_kernel(ViewsArg va, const uint64_t* __restrict__ keys,
@@ -304,6 +365,10 @@ int sort_grid(int64_t key_capacity) { return grid_for(key_capacity, 2048, 2 * 15
 
 void launch_scan(const uint32_t* touched, uint32_t* incl, int64_t n, int64_t capacity,
                  unsigned long long* scratch, Control* ctrl, cudaStream_t st) {
+  if (n <= kSmallScan) {
+    scan_small_kernel<<<1, 1024, 0, st>>>(touched, incl, n, capacity, ctrl);
+    return;
+  }
   const int nb = scan_grid(n);
   scan_reduce_kernel<<<nb, kScanThreads, 0, st>>>(touched, n, scratch);
   scan_spine_kernel<<<1, kScanThreads, 0, st>>>(scratch, nb, capacity, ctrl);
@@ -312,8 +377,8 @@ void launch_scan(const uint32_t* touched, uint32_t* incl, int64_t n, int64_t cap
 
 void launch_emit_keys(const ViewsArg& va, const uint32_t* incl, const TileRect* rects, int64_t n,
                       const Control* ctrl, uint64_t* keys, int64_t capacity, cudaStream_t st) {
-  emit_keys_kernel<<<grid_for(capacity, 256, 4 * 152 * 8), 256, 0, st>>>(va, incl, rects, n, ctrl,
-                                                                         keys);
+  (void)capacity;
+  emit_keys_kernel<<<grid_for(n * 32, 256, 152 * 16), 256, 0, st>>>(va, incl, rects, n, ctrl, keys);
 }
 
 uint64_t* launch_sort(uint64_t* a, uint64_t* b, int key_bits, const Control* ctrl,
@@ -324,7 +389,7 @@ uint64_t* launch_sort(uint64_t* a, uint64_t* b, int key_bits, const Control* ctr
   for (int lo = 0; lo < key_bits; lo += 8) {
     const int shift = 32 + lo;
     sort_hist_kernel<<<nb, kSortThreads, 0, st>>>(src, ctrl, shift, hist);
-    sort_scan_kernel<<<1, kScanThreads, 0, st>>>(hist, ctrl, nb);
+    sort_scan_kernel<<<256, kScanThreads, 0, st>>>(hist, ctrl, nb);
     sort_scatter_kernel<<<nb, kSortThreads, 0, st>>>(src, dst, ctrl, shift, hist);
     uint64_t* t = src;
     src = dst;

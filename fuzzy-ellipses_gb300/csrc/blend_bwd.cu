@@ -56,22 +56,25 @@ __global__ void __launch_bounds__(128) blend_bwd_kernel(
     const int lt = (int)(tile - V.tile_base);
     const int tx = lt % V.gx, ty = lt / V.gx;
     const float4* t4 = reinterpret_cast<const float4*>(trec + k);
-    const float4 x0 = t4[0], x1 = t4[1], x2 = t4[2], x3 = t4[3];
+    const float4 x0 = t4[0], x1 = t4[1], x2 = t4[2], x3 = t4[3], x4 = t4[4];
     const float V0 = x0.x, V1 = x0.y, V2 = x0.z, V3 = x0.w, V4 = x1.x, V5 = x1.y;
     const float P0 = x1.z, P1 = x1.w, P2 = x2.x;
     const float N0 = x2.y, N1 = x2.z, N2 = x2.w, N3 = x3.x, N4 = x3.y, N5 = x3.z, C = x3.w;
+    const float cu = x4.x, cvv = x4.y;
 
     float gV[6] = {0, 0, 0, 0, 0, 0}, gP[3] = {0, 0, 0}, gN[6] = {0, 0, 0, 0, 0, 0}, gC = 0.f;
     const int xs = min(TW, V.W - tx * TW), ys = min(TH, V.H - ty * TH);
     for (int ly = 0; ly < ys; ++ly) {
       const float dv = ly - 0.5f * (TH - 1), dv2 = dv * dv;
+      const float ev = dv - cvv, ev2 = ev * ev;
       const float4* prow = pix + V.pix_base + (int64_t)(ty * TH + ly) * V.W + tx * TW;
       for (int lx = 0; lx < xs; ++lx) {
         const float du = lx - 0.5f * (TW - 1), du2 = du * du, dudv = du * dv;
+        const float eu = du - cu, eu2 = eu * eu, euev = eu * ev;
         const float4 px = prow[lx];  // depth, m, gD/W, gA(1-alpha)
         const float vsv = fmaf(V5, dv2, fmaf(V4, dudv, fmaf(V3, du2, fmaf(V2, dv, fmaf(V1, du, V0)))));
         const float psv = fmaf(P2, dv, fmaf(P1, du, P0));
-        const float nq = fmaf(N5, dv2, fmaf(N4, dudv, fmaf(N3, du2, fmaf(N2, dv, fmaf(N1, du, N0)))));
+        const float nq = fmaf(N5, ev2, fmaf(N4, euev, fmaf(N3, eu2, fmaf(N2, ev, fmaf(N1, eu, N0)))));
         const float qi = rcp_approx(vsv);
         const float z = psv * qi;
         const float s2 = fmaf(nq, qi, C);
@@ -91,8 +94,8 @@ __global__ void __launch_bounds__(128) blend_bwd_kernel(
         gV[0] += gvsv; gV[1] = fmaf(gvsv, du, gV[1]); gV[2] = fmaf(gvsv, dv, gV[2]);
         gV[3] = fmaf(gvsv, du2, gV[3]); gV[4] = fmaf(gvsv, dudv, gV[4]); gV[5] = fmaf(gvsv, dv2, gV[5]);
         gP[0] += gpsv; gP[1] = fmaf(gpsv, du, gP[1]); gP[2] = fmaf(gpsv, dv, gP[2]);
-        gN[0] += gnq; gN[1] = fmaf(gnq, du, gN[1]); gN[2] = fmaf(gnq, dv, gN[2]);
-        gN[3] = fmaf(gnq, du2, gN[3]); gN[4] = fmaf(gnq, dudv, gN[4]); gN[5] = fmaf(gnq, dv2, gN[5]);
+        gN[0] += gnq; gN[1] = fmaf(gnq, eu, gN[1]); gN[2] = fmaf(gnq, ev, gN[2]);
+        gN[3] = fmaf(gnq, eu2, gN[3]); gN[4] = fmaf(gnq, euev, gN[4]); gN[5] = fmaf(gnq, ev2, gN[5]);
       }
     }
 
@@ -100,12 +103,14 @@ __global__ void __launch_bounds__(128) blend_bwd_kernel(
     const GaussRec g = recs[V.rec_base + gid];
     const float tcx = tx * TW + 0.5f * (TW - 1), tcy = ty * TH + 0.5f * (TH - 1);
     const float du = tcx - g.uc, dv = tcy - g.vc;
+    // Same choice of expansion centre as the gather (binning.cu tile_record).
+    const bool near = fabsf(du) <= kNearCentre && fabsf(dv) <= kNearCentre;
     const float kn = -0.5f * kLog2e;
     float a0[3], y0[3];
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
       a0[c] = fmaf(dv, g.a2[c], fmaf(du, g.a1[c], g.a0[c]));
-      y0[c] = fmaf(dv, g.y2[c], fmaf(du, g.y1[c], g.y0[c]));
+      y0[c] = near ? g.y0[c] : fmaf(dv, g.y2[c], fmaf(du, g.y1[c], g.y0[c]));
     }
     float ga0[3], ga1[3], ga2[3], gb[3], gy0[3], gy1[3], gy2[3];
 #pragma unroll
@@ -119,8 +124,10 @@ __global__ void __launch_bounds__(128) blend_bwd_kernel(
       gy2[c] = 2.f * kn * (gN[2] * y0[c] + gN[4] * g.y1[c] + gN[5] * g.y2[c]);
       ga1[c] = fmaf(du, ga0[c], ga1[c]);
       ga2[c] = fmaf(dv, ga0[c], ga2[c]);
-      gy1[c] = fmaf(du, gy0[c], gy1[c]);
-      gy2[c] = fmaf(dv, gy0[c], gy2[c]);
+      if (!near) {
+        gy1[c] = fmaf(du, gy0[c], gy1[c]);
+        gy2[c] = fmaf(dv, gy0[c], gy2[c]);
+      }
     }
     float* dst = reinterpret_cast<float*>(rgrad + (V.rec_base + gid));
     red_add_v4(dst + 0, ga0[0], ga0[1], ga0[2], ga1[0]);

@@ -54,18 +54,27 @@ struct __align__(16) GaussRec {
 static_assert(sizeof(GaussRec) == 96, "GaussRec layout");
 
 // Tile-local polynomial form of a record (what the blend streams with TMA bulk copies).
-// With (du,dv) the pixel offset from the tile centre:
+// With (du,dv) the pixel offset from the tile centre and (eu,ev) = (du-cu, dv-cv) the offset from
+// the expansion centre (cu,cv) of the Mahalanobis term:
 //   vsv = V0 + V1 du + V2 dv + V3 du^2 + V4 du dv + V5 dv^2
 //   psv = P0 + P1 du + P2 dv
-//   nq  = N0 + ... (same monomials), already scaled by -log2(e)/2
+//   nq  = N0 + N1 eu + N2 ev + N3 eu^2 + N4 eu ev + N5 ev^2, scaled by -log2(e)/2
 //   s2  = C + nq/vsv  (log2 of the peak density),  z = psv/vsv
+// nq vanishes at the Gaussian's projected centre; expanding it there (whenever that centre is
+// near the tile) keeps float32 evaluation free of cancellation for Gaussians of sub-pixel size.
 struct __align__(16) TileRec {
   float V[6];
   float P[3];
   float N[6];
   float C;
+  float cu, cv;
+  float pad[2];
 };
-static_assert(sizeof(TileRec) == 64, "TileRec layout");
+static_assert(sizeof(TileRec) == 80, "TileRec layout");
+
+// The Mahalanobis polynomial of a tile record is expanded at the record's centre when that lies
+// within this many pixels of the tile centre (in both directions), else at the tile centre.
+constexpr float kNearCentre = 64.f;
 
 // Record-space gradient accumulator of one (Gaussian, view) pair: d/d{a0,a1,a2,b,y0,y1,y2,logw}.
 struct __align__(16) RecGrad {

@@ -45,7 +45,8 @@ void launch_ranges(const uint64_t* keys, const Control* ctrl, int64_t capacity, 
                    cudaStream_t st);
 
 // blend_fwd.cu
-void launch_blend_fwd(const ViewsArg& va, int tile_w, int tile_h, int64_t n_tiles,
+// px: pixels per thread (1, 2 or 4; 0 = default for the tile shape).
+void launch_blend_fwd(const ViewsArg& va, int tile_w, int tile_h, int px, int64_t n_tiles,
                       const TileRec* trec, const uint2* ranges, float beta2, float beta3,
                       float* depth, float* alpha, float* stats, int64_t stats_stride,
                       Control* ctrl, cudaStream_t st);

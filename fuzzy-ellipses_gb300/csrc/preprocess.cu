@@ -4,7 +4,8 @@
 //  * preprocess_kernel: the footprint is the exact screen bounding box of the Gaussian's
 //    k-sigma ellipsoid as seen through the pinhole (every pixel whose ray line passes within
 //    Mahalanobis distance k of the mean), from the dual conic of the ellipsoid. k comes from a
-//    density cut-off (FE_CULL_EPS) or is fixed (FE_CULL_NSTD).
+//    density cut-off (FE_CULL_EPS) or is fixed (FE_CULL_NSTD). Float32 throughout, with the
+//    conic's discriminant and the record terms in forms free of cancellation.
 //  * preprocess_reference_kernel: the reference's binning (cuda_rasterizer/forward.cu:126-203 with
 //    computeCov3D :65-122, computeCov2D :21-60 and auxiliary.h:46-61,144-169), restated with
 //    explicitly rounded float operations so the compiler cannot contract them, which makes its
@@ -14,7 +15,7 @@
 namespace fe {
 
 // ------------------------------------------------------------------------------------------
-// Record builder (double precision; one call per (Gaussian, view)).
+// Record builder, double precision (the legacy-interface records).
 // ------------------------------------------------------------------------------------------
 
 // U: upper-triangular precision factor (row-major 3x3, lower entries ignored), precision U U^T.
@@ -91,6 +92,11 @@ __device__ __forceinline__ void load_pose(const float* quat, const float* rotm, 
 }
 
 // Clamp a floating tile coordinate into [lo, hi] before converting to int.
+__device__ __forceinline__ int clamp_tile(float x, int lo, int hi) {
+  if (!(x > (float)lo)) return lo;   // also catches NaN
+  if (x > (float)hi) return hi;
+  return (int)x;
+}
 __device__ __forceinline__ int clamp_tile(double x, int lo, int hi) {
   if (!(x > lo)) return lo;   // also catches NaN
   if (x > hi) return hi;
@@ -98,80 +104,146 @@ __device__ __forceinline__ int clamp_tile(double x, int lo, int hi) {
 }
 
 // ------------------------------------------------------------------------------------------
-// Exact-projection binning
+// Exact-projection binning (float32, cancellation-free forms)
 // ------------------------------------------------------------------------------------------
 
-__global__ void preprocess_kernel(ViewsArg va, int64_t n_rec, const float* __restrict__ means,
-                                  const float* __restrict__ prec, const float* __restrict__ logw,
-                                  const float* __restrict__ quat, const float* __restrict__ rotm,
-                                  const float* __restrict__ trans, int cull_mode, float cull_param,
-                                  int tile_w, int tile_h, GaussRec* __restrict__ recs,
-                                  TileRect* __restrict__ rects, uint32_t* __restrict__ touched) {
+// Record and footprint of one (Gaussian, view) pair in float32.
+//   M = U^T R^T (a = M rays_cam), Y = cof(M), det M = U00 U11 U22 (R is a rotation).
+//   Camera-frame covariance: Sc = Yh^T Yh with Yh = Y / det M = M^-T (entries of order sigma).
+//   The k-sigma ellipsoid's outline is the conic whose dual is C = k2 Sc - p p^T (p: camera-frame
+//   mean, k2 = k^2). Its vertical tangents x = (c02 +- sqrt(D)) / c22 use
+//     D = c02^2 - c00 c22 = k2 (|pz Yh0 - px Yh2|^2 - k2 |Yh0 x Yh2|^2)
+//   (Yh0, Yh2: columns of Yh), where the p^4 terms cancel analytically; likewise for y.
+__device__ __forceinline__ void footprint_and_record(
+    const float* mean, const float* prec, float logw, const float* R, const float* t,
+    const ViewDev& V, int cull_mode, float cull_param, int tile_w, int tile_h, GaussRec& rec,
+    int& tx0, int& ty0, int& tx1, int& ty1) {
+  const float U00 = prec[0], U01 = prec[1], U02 = prec[2], U11 = prec[4], U12 = prec[5],
+              U22 = prec[8];
+  const V3<float> p = v3(mean[0] - t[0], mean[1] - t[1], mean[2] - t[2]);
+  const V3<float> pc = matvec(R, p);
+  // M[i][j] = sum_{k<=i} U[k][i] R[j][k]
+  float M[9];
+#pragma unroll
+  for (int j = 0; j < 3; ++j) {
+    M[0 * 3 + j] = U00 * R[j * 3 + 0];
+    M[1 * 3 + j] = U01 * R[j * 3 + 0] + U11 * R[j * 3 + 1];
+    M[2 * 3 + j] = U02 * R[j * 3 + 0] + U12 * R[j * 3 + 1] + U22 * R[j * 3 + 2];
+  }
+  float Y[9];
+  cofactor3(M, Y);
+  const float detM = U00 * U11 * U22;
+
+  // Cut-off radius.
+  float k2;
+  if (cull_mode == FE_CULL_EPS) {
+    const float eps = cull_param > 0.f ? cull_param : kDefaultCullEps;
+    k2 = 2.f * (logw - logf(eps));
+  } else {
+    const float k = cull_param > 0.f ? cull_param : 3.f;
+    k2 = k * k;
+  }
+  tx0 = ty0 = tx1 = ty1 = 0;
+  if (k2 > 0.f) {
+    bool full = !(detM != 0.f) || !isfinite(detM);
+    if (!full) {
+      const float inv = 1.f / detM;
+      float Yh[9];
+#pragma unroll
+      for (int q = 0; q < 9; ++q) Yh[q] = Y[q] * inv;
+      // Columns c of Yh: Yh[0*3+c], Yh[1*3+c], Yh[2*3+c].
+      auto col = [&](int c) { return v3(Yh[c], Yh[3 + c], Yh[6 + c]); };
+      const V3<float> y0 = col(0), y1 = col(1), y2 = col(2);
+      const float s02 = dot(y0, y2), s12 = dot(y1, y2), s22 = dot(y2, y2);
+      const float c22 = k2 * s22 - pc.z * pc.z;
+      full = !(c22 < 0.f);
+      if (!full) {
+        const V3<float> ex = pc.z * y0 - pc.x * y2, ey = pc.z * y1 - pc.y * y2;
+        const V3<float> xx = cross(y0, y2), xy = cross(y1, y2);
+        const float dx = fmaxf(k2 * (dot(ex, ex) - k2 * dot(xx, xx)), 0.f);
+        const float dy = fmaxf(k2 * (dot(ey, ey) - k2 * dot(xy, xy)), 0.f);
+        const float c02 = k2 * s02 - pc.x * pc.z, c12 = k2 * s12 - pc.y * pc.z;
+        const float sx = sqrtf(dx), sy = sqrtf(dy);
+        const float xa = (c02 + sx) / c22, xb = (c02 - sx) / c22;
+        const float ya = (c12 + sy) / c22, yb = (c12 - sy) / c22;
+        const float ulo = fmaf(V.fx, fminf(xa, xb), V.cx), uhi = fmaf(V.fx, fmaxf(xa, xb), V.cx);
+        const float vlo = fmaf(V.fy, fminf(ya, yb), V.cy), vhi = fmaf(V.fy, fmaxf(ya, yb), V.cy);
+        // Conservative margin covers the float32 rounding of the bounds (of order 1e-5 px).
+        const float margin = 0.02f;
+        full = !(isfinite(ulo) && isfinite(uhi) && isfinite(vlo) && isfinite(vhi));
+        if (!full) {
+          tx0 = clamp_tile(floorf((ulo - margin) / tile_w), 0, V.gx);
+          tx1 = clamp_tile(floorf((uhi + margin) / tile_w) + 1.f, 0, V.gx);
+          ty0 = clamp_tile(floorf((vlo - margin) / tile_h), 0, V.gy);
+          ty1 = clamp_tile(floorf((vhi + margin) / tile_h) + 1.f, 0, V.gy);
+        }
+      }
+    }
+    if (full) {
+      tx0 = 0; ty0 = 0; tx1 = V.gx; ty1 = V.gy;
+    }
+  }
+  if (tx1 <= tx0 || ty1 <= ty0) tx0 = ty0 = tx1 = ty1 = 0;
+
+  // Record around the projected mean (image centre when the projection is unbounded).
+  float uc = 0.5f * V.W, vc = 0.5f * V.H;
+  if (fabsf(pc.z) > 1e-6f * sqrtf(dot(pc, pc))) {
+    const float u0 = fmaf(V.fx, pc.x / pc.z, V.cx), v0 = fmaf(V.fy, pc.y / pc.z, V.cy);
+    if (isfinite(u0) && isfinite(v0)) {
+      uc = fminf(fmaxf(u0, -1.f * V.W), 2.f * V.W);
+      vc = fminf(fmaxf(v0, -1.f * V.H), 2.f * V.H);
+    }
+  }
+  const float ifx = 1.f / V.fx, ify = 1.f / V.fy;
+  const V3<float> r0 = v3((uc - V.cx) * ifx, (vc - V.cy) * ify, 1.f);
+  const V3<float> a0 = matvec(M, r0), b = matvec(M, pc);
+  const V3<float> c0 = cross(r0, pc);
+  const V3<float> y0 = matvec(Y, c0);
+  const V3<float> y1 = matvec(Y, v3(0.f, -pc.z * ifx, pc.y * ifx));
+  const V3<float> y2 = matvec(Y, v3(pc.z * ify, 0.f, -pc.x * ify));
+  rec.a0[0] = a0.x; rec.a0[1] = a0.y; rec.a0[2] = a0.z;
+  rec.a1[0] = M[0] * ifx; rec.a1[1] = M[3] * ifx; rec.a1[2] = M[6] * ifx;
+  rec.a2[0] = M[1] * ify; rec.a2[1] = M[4] * ify; rec.a2[2] = M[7] * ify;
+  rec.b[0] = b.x; rec.b[1] = b.y; rec.b[2] = b.z;
+  rec.y0[0] = y0.x; rec.y0[1] = y0.y; rec.y0[2] = y0.z;
+  rec.y1[0] = y1.x; rec.y1[1] = y1.y; rec.y1[2] = y1.z;
+  rec.y2[0] = y2.x; rec.y2[1] = y2.y; rec.y2[2] = y2.z;
+  rec.uc = uc;
+  rec.vc = vc;
+  rec.c2 = logw * kLog2e;
+}
+
+__global__ void __launch_bounds__(64) preprocess_kernel(
+    ViewsArg va, int64_t n_rec, const float* __restrict__ means, const float* __restrict__ prec,
+    const float* __restrict__ logw, const float* __restrict__ quat, const float* __restrict__ rotm,
+    const float* __restrict__ trans, int cull_mode, float cull_param, int tile_w, int tile_h,
+    GaussRec* __restrict__ recs, TileRect* __restrict__ rects, uint32_t* __restrict__ touched) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n_rec;
        i += (int64_t)gridDim.x * blockDim.x) {
     const int vi = find_view<&ViewDev::rec_base>(va, i);
     const ViewDev& V = view_at(va, vi);
     const int64_t gi = V.gauss_base + (i - V.rec_base);
-
-    RecordInputs in;
-    for (int k = 0; k < 3; ++k) in.m[k] = means[3 * gi + k];
-    for (int k = 0; k < 9; ++k) in.U[k] = (k == 3 || k == 6 || k == 7) ? 0.0 : prec[9 * gi + k];
-    in.w = logw[gi];
-    load_pose(quat, rotm, trans, V.pose, in.R, in.t);
-
-    double M[9], Y[9];
-    V3<double> pc;
-    build_camera_terms(in, M, Y, pc);
-
-    // Squared Mahalanobis cut-off radius.
-    double k2;
-    if (cull_mode == FE_CULL_EPS) {
-      const double eps = cull_param > 0.f ? (double)cull_param : (double)kDefaultCullEps;
-      k2 = 2.0 * (in.w - log(eps));
+    float R[9], t[3], m[3], pr[9];
+    if (rotm) {
+#pragma unroll
+      for (int k = 0; k < 9; ++k) R[k] = rotm[9 * V.pose + k];
     } else {
-      const double k = cull_param > 0.f ? (double)cull_param : 3.0;
-      k2 = k * k;
+      quat_to_rot<float>(quat + 4 * V.pose, R);
     }
-
-    int tx0 = 0, ty0 = 0, tx1 = 0, ty1 = 0;
-    if (k2 > 0.0) {
-      // Camera-frame covariance up to the positive factor det(M)^2: adj(M^T M) = Y^T Y.
-      double A[9];
-      for (int r = 0; r < 3; ++r)
-        for (int c = 0; c < 3; ++c)
-          A[r * 3 + c] = Y[r] * Y[c] + Y[3 + r] * Y[3 + c] + Y[6 + r] * Y[6 + c];
-      const double det = M[0] * Y[0] + M[1] * Y[1] + M[2] * Y[2];
-      const double d2 = det * det;
-      // Dual conic of the k-sigma ellipsoid, scaled by det^2: C = k2 adj(G) - det^2 pc pc^T.
-      const double c00 = k2 * A[0] - d2 * pc.x * pc.x;
-      const double c02 = k2 * A[2] - d2 * pc.x * pc.z;
-      const double c11 = k2 * A[4] - d2 * pc.y * pc.y;
-      const double c12 = k2 * A[5] - d2 * pc.y * pc.z;
-      const double c22 = k2 * A[8] - d2 * pc.z * pc.z;
-      bool full = !(d2 > 0.0) || !(c22 < 0.0) || !isfinite(c22);
-      if (!full) {
-        // Tangent lines x = x0 satisfy c00 - 2 x0 c02 + x0^2 c22 = 0 (and likewise for y).
-        const double sx = sqrt(fmax(c02 * c02 - c00 * c22, 0.0));
-        const double sy = sqrt(fmax(c12 * c12 - c11 * c22, 0.0));
-        const double xa = (c02 + sx) / c22, xb = (c02 - sx) / c22;
-        const double ya = (c12 + sy) / c22, yb = (c12 - sy) / c22;
-        const double ulo = V.fx * fmin(xa, xb) + V.cx, uhi = V.fx * fmax(xa, xb) + V.cx;
-        const double vlo = V.fy * fmin(ya, yb) + V.cy, vhi = V.fy * fmax(ya, yb) + V.cy;
-        const double margin = 1e-3;
-        tx0 = clamp_tile(floor((ulo - margin) / tile_w), 0, V.gx);
-        tx1 = clamp_tile(floor((uhi + margin) / tile_w) + 1.0, 0, V.gx);
-        ty0 = clamp_tile(floor((vlo - margin) / tile_h), 0, V.gy);
-        ty1 = clamp_tile(floor((vhi + margin) / tile_h) + 1.0, 0, V.gy);
-        full = !(isfinite(ulo) && isfinite(uhi) && isfinite(vlo) && isfinite(vhi));
-      }
-      if (full) {
-        tx0 = 0; ty0 = 0; tx1 = V.gx; ty1 = V.gy;
-      }
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      t[k] = trans[3 * V.pose + k];
+      m[k] = means[3 * gi + k];
     }
-    if (tx1 <= tx0 || ty1 <= ty0) { tx0 = ty0 = tx1 = ty1 = 0; }
+#pragma unroll
+    for (int k = 0; k < 9; ++k) pr[k] = prec[9 * gi + k];
+    GaussRec rec;
+    int tx0, ty0, tx1, ty1;
+    footprint_and_record(m, pr, logw[gi], R, t, V, cull_mode, cull_param, tile_w, tile_h, rec, tx0,
+                         ty0, tx1, ty1);
+    recs[i] = rec;
     rects[i] = TileRect{(uint16_t)tx0, (uint16_t)ty0, (uint16_t)tx1, (uint16_t)ty1};
     touched[i] = (uint32_t)((tx1 - tx0) * (ty1 - ty0));
-    write_record(in, M, Y, pc, V.fx, V.fy, V.cx, V.cy, V.H, V.W, &recs[i]);
   }
 }
 
@@ -384,7 +456,7 @@ void launch_preprocess(const ViewsArg& va, int64_t n_rec, const float* means, co
                        int tile_h, GaussRec* recs, TileRect* rects, uint32_t* touched,
                        cudaStream_t st) {
   if (n_rec <= 0) return;
-  const int threads = 128;
+  const int threads = 64;
   const int64_t want = (n_rec + threads - 1) / threads;
   const int blocks = (int)(want < 65535 ? want : 65535);
   preprocess_kernel<<<blocks, threads, 0, st>>>(va, n_rec, means, prec, logw, quat, rotm, trans,

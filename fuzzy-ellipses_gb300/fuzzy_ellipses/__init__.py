@@ -8,7 +8,7 @@ Gaussian precision factor and a (quaternion, translation) pose like ``baseline/f
 """
 
 from ._native import FEError, NativeLibraryMissing, load as load_native  # noqa: F401
-from .render import (Batch, device_status, projection_matrix, rasterize, reference_binning,  # noqa: F401
+from .api import (Batch, bench_peak, device_status, projection_matrix, rasterize, reference_binning,  # noqa: F401
                      reference_num_stds, render, render_binning, render_forward)
 
 __version__ = "0.1.0"

@@ -46,7 +46,7 @@ class RenderDesc(ctypes.Structure):
         ("beta2", ctypes.c_float), ("beta3", ctypes.c_float),
         ("cull_mode", ctypes.c_int32), ("cull_param", ctypes.c_float),
         ("tile_w", ctypes.c_int32), ("tile_h", ctypes.c_int32),
-        ("flags", ctypes.c_uint32), ("reserved", ctypes.c_uint32),
+        ("flags", ctypes.c_uint32), ("px_per_thread", ctypes.c_int32),
     ]
 
 
@@ -137,7 +137,7 @@ def check(status: int):
 
 
 def make_desc(n, height, width, fx, fy, cx, cy, beta2=21.4, beta3=2.66, cull="eps",
-              cull_param=None, tile=(16, 16), flags=0) -> RenderDesc:
+              cull_param=None, tile=(16, 16), flags=0, px=0) -> RenderDesc:
     d = RenderDesc()
     load().fe_render_desc_init(ctypes.byref(d), int(n), int(height), int(width), float(fx),
                                float(fy), float(cx), float(cy))
@@ -153,4 +153,5 @@ def make_desc(n, height, width, fx, fy, cx, cy, beta2=21.4, beta3=2.66, cull="ep
         raise ValueError("cull must be 'eps' or 'nstd'")
     d.tile_w, d.tile_h = int(tile[0]), int(tile[1])
     d.flags = int(flags)
+    d.px_per_thread = int(px)
     return d

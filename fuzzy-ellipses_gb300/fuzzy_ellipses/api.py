@@ -24,7 +24,7 @@ import torch
 
 from . import _native as N
 
-__all__ = ["render", "render_forward", "render_binning", "rasterize", "reference_binning", "Batch",
+__all__ = ["render", "render_forward", "render_binning", "rasterize", "reference_binning", "Batch", "bench_peak",
            "projection_matrix", "reference_num_stds", "device_status"]
 
 

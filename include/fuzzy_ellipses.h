@@ -78,7 +78,7 @@ typedef struct fe_render_desc {
   int32_t tile_w;      /* screen tile width/height in pixels: 8x8, 16x16 or 32x8; 0 = 16x16 */
   int32_t tile_h;
   uint32_t flags;      /* FE_FLAG_* */
-  uint32_t reserved;
+  int32_t px_per_thread; /* blend pixels per thread: 1, 2 or 4 (8x8 tiles: 1 or 2); 0 = default */
 } fe_render_desc;
 
 /* Fill d with defaults for an HxW image of n Gaussians. */

@@ -29,13 +29,30 @@ def oracle_pixels(scene, cam, pix):
     return d, a
 
 
-def parity_errors(depth, alpha, d_ref, a_ref, mask_alpha=DEPTH_MASK_ALPHA):
+def floor_dominated(scene, cam, beta2=21.4, beta3=2.66):
+    """Pixels where fm_render's depth is set by its +1e-20 weight floor (fm_render.py:93-99).
+
+    fm_render subtracts the max logit over *all* Gaussians, including those behind the camera
+    (z <= 0, whose logit -beta2*z is large), before masking them out; where the front Gaussians'
+    share of that max falls below the floor, its depth becomes the floor-weighted mean of every z.
+    A tile-culled renderer normalises over the front Gaussians instead. Returns a bool (H*W,)."""
+    rays = O.pinhole_rays(cam.height, cam.width, cam.fx, cam.fy, cam.cx, cam.cy) @ O.quat_to_rot(cam.quat)
+    zs, stds = O.ray_gaussian_terms(rays, np.tile(np.asarray(cam.trans, np.float64), (rays.shape[0], 1)),
+                                    scene.means, scene.prec, scene.logw)
+    logit = -beta2 * zs + beta3 * stds
+    mass = np.where(zs > 0, np.exp(logit - logit.max(0)), 0.0).sum(0)
+    return mass < 1e-12
+
+
+def parity_errors(depth, alpha, d_ref, a_ref, mask_alpha=DEPTH_MASK_ALPHA, exclude=None):
     depth = np.asarray(depth, np.float64).ravel()
     alpha = np.asarray(alpha, np.float64).ravel()
     d_ref = np.asarray(d_ref).ravel()
     a_ref = np.asarray(a_ref).ravel()
     ea = float(np.abs(alpha - a_ref).max()) if alpha.size else 0.0
     m = a_ref > mask_alpha
+    if exclude is not None:
+        m &= ~np.asarray(exclude).ravel()
     ed = float((np.abs(depth - d_ref)[m] / np.abs(d_ref[m])).max()) if m.any() else 0.0
     return ea, ed
 

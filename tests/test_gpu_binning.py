@@ -75,7 +75,7 @@ def test_legacy_rasterize_matches_culled_oracle(cuda_device):
                         f, f, cx, cy, 0.01, 4.5)
     torch.cuda.synchronize()
     # The binning the legacy entry used is the reference's (same floats as the wrapper builds).
-    tfx, tfy, view, proj = fe.render._legacy_scalars(H, W, f, f, cx, cy, 0.01, 4.5)
+    tfx, tfy, view, proj = fe.api._legacy_scalars(H, W, f, f, cx, cy, 0.01, 4.5)
     rb = ref_binning(case["means"], case["scales"], case["rots"], view, proj, H, W, tfx, tfy,
                      fe.reference_num_stds(n))
     keys = rb["keys"]

@@ -7,8 +7,8 @@ import torch
 import fuzzy_ellipses as fe
 from fuzzy_ellipses import synthetic as S
 from oracle import fm_render_np as O
-from tests.helpers import (TOL_ALPHA, TOL_DEPTH_REL, oracle_pixels, parity_errors, scene_to_dev,
-                           tile_lists_from_keys, to_dev)
+from tests.helpers import (TOL_ALPHA, TOL_DEPTH_REL, floor_dominated, oracle_pixels, parity_errors,
+                           scene_to_dev, tile_lists_from_keys, to_dev)
 
 pytestmark = pytest.mark.gpu
 TILES = [(8, 8), (16, 16), (32, 8)]
@@ -134,7 +134,7 @@ def test_empty_scene_and_tiny_images(cuda_device):
     scene, cams = S.config0(seed=4)
     cam = cams[0]
     for (H, W) in [(1, 1), (3, 17), (37, 23), (64, 1)]:
-        f = 200.0 * W / 200.0 + 1.0
+        f = float(max(H, W)) + 1.0
         cam2 = S.Camera(H, W, f, f, W / 2, H / 2, cam.quat, cam.trans)
         d_ref, a_ref = O.render_pinhole(scene.means, scene.prec, scene.logw, H, W, f, f, W / 2,
                                         H / 2, cam.quat, cam.trans)
@@ -156,10 +156,21 @@ def test_single_gaussian_and_behind_camera(cuda_device):
     sc = S.Scene(means, prec, logw)
     cam = S.Camera(H, W, f, f, W / 2, H / 2, quat, trans)
     d_ref, a_ref = O.render_pinhole(means, prec, logw, H, W, f, f, W / 2, H / 2, quat, trans)
+    floor = floor_dominated(sc, cam)
+    assert floor.any()  # the scene does exercise fm_render's weight floor
+    n_tiles = ((W + 7) // 8) * ((H + 7) // 8)
+    d_front, _ = O.render_culled(means, prec, logw, H, W, f, f, W / 2, H / 2, quat, trans,
+                                 [np.arange(2)] * n_tiles, 8, 8)
     for tile in TILES:
         d, a = render_np(dev, sc, cam, tile=tile)
-        ea, ed = parity_errors(d, a, d_ref, a_ref)
+        ea, ed = parity_errors(d, a, d_ref, a_ref, exclude=floor)
         assert ea <= TOL_ALPHA and ed <= TOL_DEPTH_REL, (tile, ea, ed)
+        # Where the floor governs fm_render, the renderer keeps the front-only softmax depth (the
+        # culled oracle's definition), or 0 where the front Gaussian is culled from the tile.
+        df = d.ravel()[floor]
+        dc = d_front.ravel()[floor]
+        listed = df != 0
+        assert np.all(np.abs(df[listed] - dc[listed]) <= TOL_DEPTH_REL * dc[listed])
 
 
 def test_gaussian_straddling_camera_plane_covers_image(cuda_device):
@@ -173,7 +184,7 @@ def test_gaussian_straddling_camera_plane_covers_image(cuda_device):
     cam = S.Camera(H, W, f, f, W / 2, H / 2, quat, trans)
     d_ref, a_ref = O.render_pinhole(means, prec, logw, H, W, f, f, W / 2, H / 2, quat, trans)
     d, a = render_np(dev, sc, cam)
-    ea, ed = parity_errors(d, a, d_ref, a_ref)
+    ea, ed = parity_errors(d, a, d_ref, a_ref, exclude=floor_dominated(sc, cam))
     assert ea <= TOL_ALPHA and ed <= TOL_DEPTH_REL, (ea, ed)
 
 
@@ -190,3 +201,18 @@ def test_stream_ordering_and_repeatability(cuda_device):
     s.synchronize()
     for d, a in outs[1:]:
         assert torch.equal(d, outs[0][0]) and torch.equal(a, outs[0][1])
+
+
+@pytest.mark.parametrize("tile", TILES)
+def test_subpixel_gaussians(cuda_device, tile):
+    """Gaussians a quarter of a pixel wide: the Mahalanobis polynomial is evaluated around each
+    Gaussian's own projected centre, so float32 keeps the stated tolerance."""
+    rng = np.random.default_rng(11)
+    scene = S.random_gaussians(80, 0.1, rng, scale_lo=0.002, scale_hi=0.006)
+    q, t = S.look_at(0.5 * S.random_unit_vectors(1, rng)[0])
+    cam = S.Camera(64, 64, 64.0, 64.0, 32.0, 32.0, q, t)
+    d_ref, a_ref = O.render_pinhole(scene.means, scene.prec, scene.logw, 64, 64, 64.0, 64.0, 32.0,
+                                    32.0, q, t)
+    d, a = render_np(cuda_device, scene, cam, tile=tile)
+    ea, ed = parity_errors(d, a, d_ref, a_ref)
+    assert ea <= TOL_ALPHA and ed <= TOL_DEPTH_REL, (ea, ed)
