@@ -36,8 +36,11 @@ METRIC = "Mray-Gaussian evals/s"
 WORKLOAD = ("N=1000 Gaussians (means U[-0.3,0.3]^3 m, scales logU[0.005,0.03] m, Haar rotations, "
             "logw N(0,0.5^2)), 16 cameras 640x480 fx=fy=600 on a 1.0 m Fibonacci sphere, fp32, "
             "density cut-off 1e-7 (exact k-sigma screen bounds)")
-PER_EVAL_FMA = 20   # FP32 FMA-pipe instructions per ray-Gaussian evaluation in the forward blend
-PER_EVAL_MUFU = 3   # rcp, ex2 (alpha), ex2 (softmax weight)
+# Algorithmic cost of one ray-Gaussian evaluation used for the blend roofline: 22 FP32 FMA-pipe
+# operations (three 3x3 mat-vec products reduced to quadratic forms, the peak, the log-density,
+# the logit and the three accumulations) and 3 MUFU operations (rcp and two ex2).
+PER_EVAL_FMA = 22
+PER_EVAL_MUFU = 3
 
 
 def parse():
@@ -47,6 +50,7 @@ def parse():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--profile-step", action="store_true",
                     help="build the workload, warm up, run one batched forward step and exit "
                          "(the command the committed ncu summaries capture)")
@@ -253,7 +257,14 @@ def main():
     npix = H * W
     views = [dict(scene=0, height=c.height, width=c.width, fx=c.fx, fy=c.fy, cx=c.cx, cy=c.cy,
                   quat=c.quat, trans=c.trans) for c in cams]
-    batch = fe.Batch([(0, scene.n)], views)
+    tuned = None
+    if args.profile_step:
+        cfg = dict(fe.autotune.DEFAULT)
+    else:
+        tuner = fe.autotune.Autotuner(persist=False)
+        tuned = tuner.tune([(0, scene.n)], views, m, p, w, reps=3)
+        cfg = {k: tuned[k] for k in ("tile", "px", "chunk")}
+    batch = fe.Batch([(0, scene.n)], views, tile=cfg["tile"], px=cfg["px"], chunk=cfg["chunk"])
     per_cam_evals = count_evals(fe, cams, mpw) if not args.profile_step else [0] * len(cams)
     e_step = float(sum(per_cam_evals))
     depth = torch.empty(batch.n_pixels, device=dev)
@@ -317,7 +328,7 @@ def main():
     blend_evals_per_s = e_step / (stages["blend"] * 1e-3)
     peaks, peak_kind = measured_peaks()
     nk = batch.status()["num_keys"]
-    passes = (max(1, int(np.ceil(np.log2(batch_tiles(cams, 16, 16))))) + 7) // 8
+    passes = (max(1, int(np.ceil(np.log2(batch_tiles(cams, *cfg["tile"]))))) + 7) // 8
     hbm = {
         "preprocess": (52 * scene.n + len(cams) * scene.n * (96 + 8 + 4)) / (stages["preprocess"] * 1e-3) / 1e9,
         "sort": (16 * nk * passes) / (stages["sort"] * 1e-3) / 1e9,
@@ -370,6 +381,9 @@ def main():
     e2e_s = (time.perf_counter() - t0) / args.steps
     e2e_value = e_step / e2e_s / 1e6
 
+    # ---- served mixed requests vs the plain per-call drop-in ------------------------------
+    served = None if args.no_serve else serve_bench(fe, dev)
+
     # ---- CPU baseline (oracle on the host cores, bounded sample) ---------------------------
     cpu = None
     if not args.no_cpu_baseline:
@@ -388,8 +402,10 @@ def main():
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic",
         "config": {"workload": WORKLOAD, "step": "batched forward of all 16 cameras",
-                   "tile": "16x16", "l2": "flushed between steps (256 MiB write outside the "
-                   "per-step CUDA events); step working set ~100 MB < L2",
+                   "tile": f"{cfg['tile'][0]}x{cfg['tile'][1]}", "px_per_thread": cfg["px"],
+                   "chunk_pairs": cfg["chunk"], "autotuned": tuned is not None,
+                   "l2": "flushed between steps (256 MiB write outside the per-step CUDA "
+                   "events); step working set ~100 MB < L2",
                    "parallelism": f"replicas x{world}"},
         "renders_per_s": renders_s,
         "evals_per_step": e_step,
@@ -401,7 +417,7 @@ def main():
         "roofline": {"bound": "fma+xu", "achieved": blend_achieved,
                      "peak": peak_evals / 1e9, "unit": "Gevals/s",
                      "frac": blend_evals_per_s / peak_evals, "traffic": ncu_traffic(),
-                     "kernel": "blend_fwd_kernel<16,16>",
+                     "kernel": f"blend_fwd_kernel<{cfg['tile'][0]},{cfg['tile'][1]},{cfg['px'] or 4},{cfg['chunk'] or 16}>",
                      "per_eval": {"fma_pipe": PER_EVAL_FMA, "mufu": PER_EVAL_MUFU},
                      "fma_ops_per_s": fma_ops, "mufu_ex2_ops_per_s": ex2_ops,
                      "peak_source": "fe_bench_peak microbenchmarks on this GPU (FFMA and MUFU.EX2)"},
@@ -410,11 +426,99 @@ def main():
         "num_keys": nk,
         "evals_per_camera": per_cam_evals,
         "cpu_baseline": cpu,
+        "served": served,
+        "autotune": tuned and {"bucket": tuned["bucket"],
+                               "candidates_ms": {f"{c['tile'][0]}x{c['tile'][1]}/px{c['px']}/ch{c['chunk']}": round(c["ms"], 4)
+                                                 for c in tuned["candidates"]}},
         "clocks": clocks,
         "gpu_launches": batch.launches_per_forward * args.steps,
         "wall_s_timed_region": wall,
     }
     print(json.dumps(out), flush=True)
+
+
+def _silhouette(h, w):
+    """Target silhouette for the backward requests: a centred disk."""
+    v, u = np.mgrid[0:h, 0:w]
+    return (((u - w / 2) ** 2 + (v - h / 2) ** 2) < (0.3 * min(h, w)) ** 2).astype(np.float32)
+
+
+def serve_bench(fe, dev, n_requests=200, plain_requests=60, seed=0):
+    """Served mixed requests (N log-uniform in [20, 2000], 1-32 poses, sides 96-480, 30% with a
+    silhouette-BCE backward): saturating arrivals for throughput, Poisson arrivals at half that
+    rate for latency; the plain per-call drop-in (one fe_render_fwd / autograd render per camera,
+    synchronised per request) on the same requests for comparison."""
+    import threading
+
+    import torch
+
+    from fuzzy_ellipses import serve, synthetic as S
+    stream = S.config4_request_stream(n_requests, rate_hz=1.0, seed=seed)
+    reqs = []
+    for r in stream:
+        sc = r["scene"]
+        tg = [_silhouette(c.height, c.width) for c in r["cameras"]] if r["backward"] else None
+        reqs.append(serve.RenderRequest(sc.means, sc.prec, sc.logw, r["cameras"], tg))
+    renders = sum(len(r.cameras) for r in reqs)
+
+    def run(arrival_gaps):
+        with serve.RenderServer(device=dev, lanes=3) as srv:
+            for r in reqs[:6]:
+                srv.submit(r).result()
+            t0 = time.perf_counter()
+            futs = []
+            for r, gap in zip(reqs, arrival_gaps):
+                if gap > 0:
+                    time.sleep(gap)
+                futs.append(srv.submit(r))
+            res = [f.result() for f in futs]
+            wall = time.perf_counter() - t0
+            batches = srv.stats()["batches"]
+        lat = sorted(x.latency for x in res)
+        return {"renders_per_s": renders / wall, "requests_per_s": len(reqs) / wall,
+                "p50_ms": 1e3 * lat[len(lat) // 2], "p99_ms": 1e3 * lat[min(len(lat) - 1, int(0.99 * len(lat)))],
+                "batches": batches, "wall_s": wall}
+
+    sat = run([0.0] * len(reqs))
+    rate = 0.5 * sat["requests_per_s"]
+    rng = np.random.default_rng(seed + 1)
+    poisson = run(list(rng.exponential(1.0 / rate, size=len(reqs))))
+    poisson["arrival_rate_hz"] = rate
+
+    # plain per-call drop-in on a prefix of the same requests
+    def plain(req):
+        m, p, w = [torch.from_numpy(x).to(dev) for x in (req.means, req.prec, req.logw)]
+        if req.targets is None:
+            for c in req.cameras:
+                d, a = fe.render_forward(m, p, w, c.fx, c.fy, c.cx, c.cy, c.quat, c.trans, c.height, c.width)
+                d.cpu(), a.cpu()
+            return
+        m.requires_grad_(); p.requires_grad_(); w.requires_grad_()
+        loss, cnt = 0.0, 0
+        for c, t in zip(req.cameras, req.targets):
+            d, a = fe.render(m, p, w, c.fx, c.fy, c.cx, c.cy, c.quat, c.trans, c.height, c.width)
+            ac = a.double().clamp(3e-8, 1 - 3e-8)
+            tt = torch.from_numpy(t).to(dev).double()
+            loss = loss - (tt * torch.log(ac) + (1 - tt) * torch.log(1 - ac)).sum()
+            cnt += a.numel()
+            a.detach().cpu()
+        (loss / cnt).backward()
+        m.grad.cpu(), p.grad.cpu(), w.grad.cpu()
+
+    for r in reqs[:3]:
+        plain(r)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for r in reqs[:plain_requests]:
+        plain(r)
+    torch.cuda.synchronize()
+    pw = time.perf_counter() - t0
+    plain_rs = sum(len(r.cameras) for r in reqs[:plain_requests]) / pw
+    return {"workload": f"{n_requests} requests: N logU[20,2000], 1-32 poses at 0.5 m, side U[96,480], "
+                        "30% forward+backward (silhouette BCE), fp32",
+            "saturating": sat, "poisson_half_load": poisson,
+            "plain_per_call_renders_per_s": plain_rs,
+            "served_over_plain": sat["renders_per_s"] / plain_rs}
 
 
 def batch_tiles(cams, tw, th):

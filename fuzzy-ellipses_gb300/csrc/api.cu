@@ -56,7 +56,7 @@ size_t key_budget_bytes() {
 }
 
 // Bytes of key-proportional scratch per key: two key buffers and one tile record.
-constexpr size_t kBytesPerKey = 2 * sizeof(uint64_t) + sizeof(TileRec);
+constexpr size_t kBytesPerKey = 2 * sizeof(uint64_t) + sizeof(TilePair) / 2;
 
 int bits_for(int64_t n) {
   int b = 0;
@@ -119,7 +119,7 @@ struct KeySpace {
   uint64_t* keys_a;
   uint64_t* keys_b;
   uint32_t* hist;
-  TileRec* trec;
+  TilePair* trec;  // key k at trec[k/2], slot k%2
 };
 
 template <class F>
@@ -146,7 +146,7 @@ size_t carve_keys(char* base, int64_t cap, F&& out) {
   s.keys_a = c.take<uint64_t>(cap);
   s.keys_b = c.take<uint64_t>(cap);
   s.hist = c.take<uint32_t>(int64_t(sort_grid(cap) + 1) * 256);
-  s.trec = c.take<TileRec>(cap);
+  s.trec = c.take<TilePair>((cap + 1) / 2);
   out(s);
   return c.off;
 }
@@ -193,6 +193,9 @@ int check_desc(const fe_render_desc* d) {
   if (d->px_per_thread != 0 && d->px_per_thread != 1 && d->px_per_thread != 2 &&
       d->px_per_thread != 4)
     return fail(FE_ERR_INVALID_ARGUMENT, "px_per_thread must be 0, 1, 2 or 4");
+  const uint32_t chunk = (d->flags >> 8) & 0xff;
+  if (chunk != 0 && chunk != 8 && chunk != 16 && chunk != 32)
+    return fail(FE_ERR_INVALID_ARGUMENT, "blend chunk must be 0, 8, 16 or 32 record pairs");
   return FE_OK;
 }
 
@@ -208,7 +211,8 @@ struct Pipeline {
   ViewsArg va;
   int64_t n_rec, n_tiles, n_pix;
   int tile_w, tile_h;
-  int px;  // pixels per thread in the blend (0 = default)
+  int px;     // pixels per thread in the blend (0 = default)
+  int chunk;  // record pairs per shared-memory stage in the blend (0 = default)
   int cull_mode;
   float cull_param;
   float beta2, beta3;
@@ -273,6 +277,7 @@ Pipeline single_view_pipeline(const fe_render_desc* d, const float* means, const
   p.tile_w = tw;
   p.tile_h = th;
   p.px = (int)d->px_per_thread;
+  p.chunk = (int)(d->flags >> 8) & 0xff;
   p.cull_mode = d->cull_mode;
   p.cull_param = d->cull_param;
   p.beta2 = d->beta2;
@@ -351,7 +356,7 @@ int fe_render_fwd(const fe_render_desc* d, const float* means, const float* prec
   rc = run_binning(p, p.n_rec * p.n_tiles, a->rec, a->keys, a->h_pinned, false, st, rs, ks, cap,
                    sorted);
   if (rc) return rc;
-  launch_blend_fwd(p.va, p.tile_w, p.tile_h, p.px, p.n_tiles, ks.trec, rs.ranges, p.beta2, p.beta3,
+  launch_blend_fwd(p.va, p.tile_w, p.tile_h, p.px, p.chunk, p.n_tiles, ks.trec, rs.ranges, p.beta2, p.beta3,
                    depth, alpha, stats, npix, rs.ctrl, st);
   FE_CUDA(cudaGetLastError());
   return FE_OK;
@@ -583,7 +588,7 @@ int fe_rasterize_legacy(const fe_legacy_desc* d, const float* means, const float
   launch_emit_keys(va, rs.incl, rs.rects, P, rs.ctrl, ks.keys_a, cap, st);
   uint64_t* sorted = launch_sort(ks.keys_a, ks.keys_b, bits_for(T), rs.ctrl, cap, ks.hist, st);
   launch_ranges_gather(va, sorted, rs.ctrl, cap, rs.recs, 8, 8, rs.ranges, ks.trec, st);
-  launch_blend_fwd(va, 8, 8, 0, T, ks.trec, rs.ranges, 21.4f, 2.66f, out_z, out_alpha, nullptr, 0,
+  launch_blend_fwd(va, 8, 8, 0, 0, T, ks.trec, rs.ranges, 21.4f, 2.66f, out_z, out_alpha, nullptr, 0,
                    rs.ctrl, st);
   FE_CUDA(cudaGetLastError());
   return FE_OK;
@@ -650,11 +655,15 @@ struct fe_batch {
   int device = 0;
   fe_render_desc desc{};
   int tile_w = 16, tile_h = 16;
+  bool exact = false;  // size key scratch from the device-side count (one readback per run)
   int32_t n_views = 0;
+  DevBuf tables;  // ViewDev[n_views] | quat[4 n_views] | trans[3 n_views]
   ViewDev* views_d = nullptr;
   float* quat_d = nullptr;
   float* trans_d = nullptr;
-  int64_t n_rec = 0, n_tiles = 0, n_pix = 0, cap = 0;
+  std::vector<ViewDev> views_h;
+  std::vector<float> quat_h, trans_h;
+  int64_t n_rec = 0, n_tiles = 0, n_pix = 0, cap = 0, worst = 0;
   int64_t n_gauss = 0;  // extent of the concatenated Gaussian arrays the scenes reference
   DevBuf rec, keys;
   RecSpace rs{};
@@ -662,6 +671,92 @@ struct fe_batch {
   uint64_t* sorted = nullptr;
   unsigned long long* h_pinned = nullptr;
 };
+
+namespace {
+
+// Fill the host-side plan of a batch (tables, sizes) from scenes and views.
+int plan_batch(fe_batch* b, const fe_scene* scenes, int32_t n_scenes, const fe_view* views,
+               int32_t n_views) {
+  if (n_scenes < 0 || n_views < 1 || !views || (n_scenes > 0 && !scenes))
+    return fail(FE_ERR_INVALID_ARGUMENT, "empty batch");
+  for (int i = 0; i < n_views; ++i) {
+    const fe_view& v = views[i];
+    if (v.scene < 0 || v.scene >= n_scenes || v.height < 1 || v.width < 1 || v.pixel_offset < 0 ||
+        !(v.fx != 0.f) || !(v.fy != 0.f) || scenes[v.scene].n < 0 || scenes[v.scene].gauss_offset < 0)
+      return fail(FE_ERR_INVALID_ARGUMENT, "bad view " + std::to_string(i));
+  }
+  b->views_h.assign(n_views, ViewDev{});
+  b->quat_h.assign(4 * (size_t)n_views, 0.f);
+  b->trans_h.assign(3 * (size_t)n_views, 0.f);
+  int64_t rec = 0, tiles = 0, pix_end = 0, worst = 0;
+  for (int i = 0; i < n_views; ++i) {
+    const fe_view& v = views[i];
+    ViewDev& d = b->views_h[i];
+    d.fx = v.fx; d.fy = v.fy; d.cx = v.cx; d.cy = v.cy;
+    d.H = v.height; d.W = v.width;
+    d.gx = (v.width + b->tile_w - 1) / b->tile_w;
+    d.gy = (v.height + b->tile_h - 1) / b->tile_h;
+    d.n = scenes[v.scene].n;
+    d.pose = i;
+    d.flags = v.flags;
+    d.gauss_base = scenes[v.scene].gauss_offset;
+    d.rec_base = rec;
+    d.tile_base = tiles;
+    d.pix_base = v.pixel_offset;
+    rec += d.n;
+    tiles += (int64_t)d.gx * d.gy;
+    worst += (int64_t)d.n * d.gx * d.gy;
+    pix_end = std::max<int64_t>(pix_end, v.pixel_offset + (int64_t)v.height * v.width);
+    for (int k = 0; k < 4; ++k) b->quat_h[4 * i + k] = v.quat[k];
+    for (int k = 0; k < 3; ++k) b->trans_h[3 * i + k] = v.trans[k];
+  }
+  if (tiles > INT64_C(0xffffffff)) return fail(FE_ERR_INVALID_ARGUMENT, "too many tiles in one batch");
+  b->n_gauss = 0;
+  for (int s_ = 0; s_ < n_scenes; ++s_)
+    b->n_gauss = std::max<int64_t>(b->n_gauss, scenes[s_].gauss_offset + scenes[s_].n);
+  b->n_views = n_views;
+  b->n_rec = rec;
+  b->n_tiles = tiles;
+  b->n_pix = pix_end;
+  b->worst = worst;
+  return FE_OK;
+}
+
+// Upload the tables and size the scratch (grow-only). Ordered on `st` and synchronised.
+int commit_batch(fe_batch* b, cudaStream_t st) {
+  Carver c{nullptr};
+  c.take<ViewDev>(b->n_views);
+  c.take<float>(4 * (int64_t)b->n_views);
+  c.take<float>(3 * (int64_t)b->n_views);
+  int rc = b->tables.reserve(c.off, st);
+  if (rc) return rc;
+  Carver t{b->tables.ptr};
+  b->views_d = t.take<ViewDev>(b->n_views);
+  b->quat_d = t.take<float>(4 * (int64_t)b->n_views);
+  b->trans_d = t.take<float>(3 * (int64_t)b->n_views);
+  FE_CUDA(cudaMemcpyAsync(b->views_d, b->views_h.data(), sizeof(ViewDev) * b->n_views,
+                          cudaMemcpyHostToDevice, st));
+  FE_CUDA(cudaMemcpyAsync(b->quat_d, b->quat_h.data(), sizeof(float) * b->quat_h.size(),
+                          cudaMemcpyHostToDevice, st));
+  FE_CUDA(cudaMemcpyAsync(b->trans_d, b->trans_h.data(), sizeof(float) * b->trans_h.size(),
+                          cudaMemcpyHostToDevice, st));
+  const size_t rb = carve_rec(nullptr, b->n_rec, b->n_tiles, b->n_pix, true, [](const RecSpace&) {});
+  rc = b->rec.reserve(rb, st);
+  if (rc) return rc;
+  carve_rec(b->rec.ptr, b->n_rec, b->n_tiles, b->n_pix, true, [&](const RecSpace& s_) { b->rs = s_; });
+  if (!b->exact) {
+    const int64_t budget_keys = (int64_t)(key_budget_bytes() / kBytesPerKey);
+    b->cap = std::max<int64_t>(1, std::min<int64_t>({b->worst, budget_keys, INT64_C(0xffffffff)}));
+    const size_t kb = carve_keys(nullptr, b->cap, [](const KeySpace&) {});
+    rc = b->keys.reserve(kb, st);
+    if (rc) return rc;
+    carve_keys(b->keys.ptr, b->cap, [&](const KeySpace& s_) { b->ks = s_; });
+  }
+  FE_CUDA(cudaStreamSynchronize(st));  // host tables may be rewritten by the next reset
+  return FE_OK;
+}
+
+}  // namespace
 
 extern "C" {
 
@@ -671,95 +766,47 @@ int fe_batch_create(const fe_render_desc* desc, const fe_scene* scenes, int32_t 
   *out = nullptr;
   if (!desc || desc->magic != FE_DESC_MAGIC || desc->version != FE_DESC_VERSION)
     return fail(FE_ERR_DESCRIPTOR, "descriptor magic/version mismatch");
-  if (n_scenes < 0 || n_views < 1 || !views || (n_scenes > 0 && !scenes))
-    return fail(FE_ERR_INVALID_ARGUMENT, "empty batch");
   fe_render_desc probe = *desc;
   probe.height = 1; probe.width = 1; probe.n_gaussians = 0; probe.fx = 1.f; probe.fy = 1.f;
   int rc = check_desc(&probe);
   if (rc) return rc;
-  for (int i = 0; i < n_views; ++i) {
-    const fe_view& v = views[i];
-    if (v.scene < 0 || v.scene >= n_scenes || v.height < 1 || v.width < 1 || v.pixel_offset < 0 ||
-        !(v.fx != 0.f) || !(v.fy != 0.f) || scenes[v.scene].n < 0 || scenes[v.scene].gauss_offset < 0)
-      return fail(FE_ERR_INVALID_ARGUMENT, "bad view " + std::to_string(i));
-  }
   fe_batch* b = new fe_batch();
   b->desc = *desc;
+  b->exact = (desc->flags & FE_FLAG_EXACT_KEYS) != 0;
   tile_shape(desc, b->tile_w, b->tile_h);
-  if (cudaGetDevice(&b->device) != cudaSuccess) {
+  rc = plan_batch(b, scenes, n_scenes, views, n_views);
+  if (rc) {
     delete b;
-    return fail(FE_ERR_CUDA, "cudaGetDevice failed");
+    return rc;
   }
-  std::vector<ViewDev> vt(n_views);
-  std::vector<float> q(4 * (size_t)n_views), t(3 * (size_t)n_views);
-  int64_t rec = 0, tiles = 0, pix_end = 0, worst = 0;
-  for (int i = 0; i < n_views; ++i) {
-    const fe_view& v = views[i];
-    ViewDev& d = vt[i];
-    d.fx = v.fx; d.fy = v.fy; d.cx = v.cx; d.cy = v.cy;
-    d.H = v.height; d.W = v.width;
-    d.gx = (v.width + b->tile_w - 1) / b->tile_w;
-    d.gy = (v.height + b->tile_h - 1) / b->tile_h;
-    d.n = scenes[v.scene].n;
-    d.pose = i;
-    d.gauss_base = scenes[v.scene].gauss_offset;
-    d.rec_base = rec;
-    d.tile_base = tiles;
-    d.pix_base = v.pixel_offset;
-    rec += d.n;
-    tiles += (int64_t)d.gx * d.gy;
-    worst += (int64_t)d.n * d.gx * d.gy;
-    pix_end = std::max<int64_t>(pix_end, v.pixel_offset + (int64_t)v.height * v.width);
-    for (int k = 0; k < 4; ++k) q[4 * i + k] = v.quat[k];
-    for (int k = 0; k < 3; ++k) t[3 * i + k] = v.trans[k];
-  }
-  for (int s_ = 0; s_ < n_scenes; ++s_)
-    b->n_gauss = std::max<int64_t>(b->n_gauss, scenes[s_].gauss_offset + scenes[s_].n);
-  if (tiles > INT64_C(0xffffffff)) {
-    delete b;
-    return fail(FE_ERR_INVALID_ARGUMENT, "too many tiles in one batch");
-  }
-  b->n_views = n_views;
-  b->n_rec = rec;
-  b->n_tiles = tiles;
-  b->n_pix = pix_end;
-  const int64_t budget_keys = (int64_t)(key_budget_bytes() / kBytesPerKey);
-  b->cap = std::max<int64_t>(1, std::min<int64_t>({worst, budget_keys, INT64_C(0xffffffff)}));
-  auto cleanup = [&](int code) {
-    fe_batch_destroy(b);
-    return code;
-  };
-  if (cudaMalloc(&b->views_d, sizeof(ViewDev) * n_views) != cudaSuccess ||
-      cudaMalloc(&b->quat_d, sizeof(float) * q.size()) != cudaSuccess ||
-      cudaMalloc(&b->trans_d, sizeof(float) * t.size()) != cudaSuccess) {
-    cudaGetLastError();
-    return cleanup(fail(FE_ERR_OUT_OF_MEMORY, "batch tables"));
-  }
-  if (cudaMemcpy(b->views_d, vt.data(), sizeof(ViewDev) * n_views, cudaMemcpyHostToDevice) ||
-      cudaMemcpy(b->quat_d, q.data(), sizeof(float) * q.size(), cudaMemcpyHostToDevice) ||
-      cudaMemcpy(b->trans_d, t.data(), sizeof(float) * t.size(), cudaMemcpyHostToDevice))
-    return cleanup(fail(FE_ERR_CUDA, "batch table upload"));
-  const size_t rb = carve_rec(nullptr, b->n_rec, b->n_tiles, b->n_pix, true, [](const RecSpace&) {});
-  const size_t kb = carve_keys(nullptr, b->cap, [](const KeySpace&) {});
-  rc = b->rec.reserve(rb, nullptr);
-  if (!rc) rc = b->keys.reserve(kb, nullptr);
-  if (rc) return cleanup(rc);
-  carve_rec(b->rec.ptr, b->n_rec, b->n_tiles, b->n_pix, true, [&](const RecSpace& s_) { b->rs = s_; });
-  carve_keys(b->keys.ptr, b->cap, [&](const KeySpace& s_) { b->ks = s_; });
-  if (cudaMallocHost(&b->h_pinned, 64) != cudaSuccess) {
+  if (cudaGetDevice(&b->device) != cudaSuccess || cudaMallocHost(&b->h_pinned, 64) != cudaSuccess) {
     cudaGetLastError();
     b->h_pinned = nullptr;
-    return cleanup(fail(FE_ERR_OUT_OF_MEMORY, "pinned staging"));
+    fe_batch_destroy(b);
+    return fail(FE_ERR_CUDA, "batch set-up failed");
+  }
+  rc = commit_batch(b, nullptr);
+  if (rc) {
+    fe_batch_destroy(b);
+    return rc;
   }
   *out = b;
   return FE_OK;
 }
 
+int fe_batch_reset(fe_batch* b, const fe_scene* scenes, int32_t n_scenes, const fe_view* views,
+                   int32_t n_views, fe_stream_t stream_) {
+  if (!b) return fail(FE_ERR_INVALID_ARGUMENT, "NULL batch");
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream_);
+  FE_CUDA(cudaStreamSynchronize(st));  // the previous run may still read the tables
+  int rc = plan_batch(b, scenes, n_scenes, views, n_views);
+  if (rc) return rc;
+  return commit_batch(b, st);
+}
+
 void fe_batch_destroy(fe_batch* b) {
   if (!b) return;
-  cudaFree(b->views_d);
-  cudaFree(b->quat_d);
-  cudaFree(b->trans_d);
+  cudaFree(b->tables.ptr);
   cudaFree(b->rec.ptr);
   cudaFree(b->keys.ptr);
   if (b->h_pinned) cudaFreeHost(b->h_pinned);
@@ -769,8 +816,10 @@ void fe_batch_destroy(fe_batch* b) {
 int64_t fe_batch_pixels(const fe_batch* b) { return b ? b->n_pix : 0; }
 
 int64_t fe_batch_scratch_bytes(const fe_batch* b) {
-  return b ? (int64_t)(b->rec.cap + b->keys.cap) : 0;
+  return b ? (int64_t)(b->tables.cap + b->rec.cap + b->keys.cap) : 0;
 }
+
+}  // extern "C"
 
 static Pipeline batch_pipeline(fe_batch* b, const float* means, const float* prec,
                                const float* logw) {
@@ -783,6 +832,7 @@ static Pipeline batch_pipeline(fe_batch* b, const float* means, const float* pre
   p.tile_w = b->tile_w;
   p.tile_h = b->tile_h;
   p.px = (int)b->desc.px_per_thread;
+  p.chunk = (int)(b->desc.flags >> 8) & 0xff;
   p.cull_mode = b->desc.cull_mode;
   p.cull_param = b->desc.cull_param;
   p.beta2 = b->desc.beta2;
@@ -791,20 +841,45 @@ static Pipeline batch_pipeline(fe_batch* b, const float* means, const float* pre
   return p;
 }
 
-static int batch_binning(fe_batch* b, const Pipeline& p, cudaStream_t st) {
+// Binning of a batch. With exact key sizing the key count is read back after the scan (one
+// 8-byte copy and a stream synchronisation) and the key scratch grows to fit it.
+static int batch_binning(fe_batch* b, const Pipeline& p, cudaStream_t st, cudaEvent_t* ev) {
   const RecSpace& rs = b->rs;
-  const KeySpace& ks = b->ks;
   FE_CUDA(cudaMemsetAsync(rs.ctrl, 0, sizeof(Control), st));
   FE_CUDA(cudaMemsetAsync(rs.ranges, 0, sizeof(uint2) * (size_t)p.n_tiles, st));
+  if (ev) FE_CUDA(cudaEventRecord(ev[0], st));
   launch_preprocess(p.va, p.n_rec, p.means, p.prec, p.logw, p.quat, nullptr, p.trans, p.cull_mode,
                     p.cull_param, p.tile_w, p.tile_h, rs.recs, rs.rects, rs.touched, st);
-  launch_scan(rs.touched, rs.incl, p.n_rec, b->cap, rs.scan_tmp, rs.ctrl, st);
+  if (ev) FE_CUDA(cudaEventRecord(ev[1], st));
+  if (b->exact) {
+    launch_scan(rs.touched, rs.incl, p.n_rec, INT64_C(0xffffffff), rs.scan_tmp, rs.ctrl, st);
+    FE_CUDA(cudaMemcpyAsync(b->h_pinned, &rs.ctrl->want_keys, sizeof(unsigned long long),
+                            cudaMemcpyDeviceToHost, st));
+    FE_CUDA(cudaStreamSynchronize(st));
+    const int64_t K = std::max<int64_t>(1, (int64_t)*b->h_pinned);
+    if (K > b->cap) {
+      const size_t kb = carve_keys(nullptr, K + K / 4, [](const KeySpace&) {});
+      int rc = b->keys.reserve(kb, st);
+      if (rc) return rc;
+      b->cap = K + K / 4;
+      carve_keys(b->keys.ptr, b->cap, [&](const KeySpace& s_) { b->ks = s_; });
+    }
+  } else {
+    launch_scan(rs.touched, rs.incl, p.n_rec, b->cap, rs.scan_tmp, rs.ctrl, st);
+  }
+  if (ev) FE_CUDA(cudaEventRecord(ev[2], st));
+  const KeySpace& ks = b->ks;
   launch_emit_keys(p.va, rs.incl, rs.rects, p.n_rec, rs.ctrl, ks.keys_a, b->cap, st);
+  if (ev) FE_CUDA(cudaEventRecord(ev[3], st));
   b->sorted = launch_sort(ks.keys_a, ks.keys_b, bits_for(p.n_tiles), rs.ctrl, b->cap, ks.hist, st);
+  if (ev) FE_CUDA(cudaEventRecord(ev[4], st));
   launch_ranges_gather(p.va, b->sorted, rs.ctrl, b->cap, rs.recs, p.tile_w, p.tile_h, rs.ranges,
                        ks.trec, st);
+  if (ev) FE_CUDA(cudaEventRecord(ev[5], st));
   return FE_OK;
 }
+
+extern "C" {
 
 int fe_batch_fwd(fe_batch* b, const float* means, const float* prec, const float* logw,
                  float* depth, float* alpha, float* stats, fe_stream_t stream_) {
@@ -813,10 +888,10 @@ int fe_batch_fwd(fe_batch* b, const float* means, const float* prec, const float
   Pipeline p = batch_pipeline(b, means, prec, logw);
   if (p.n_rec > 0 && (!means || !prec || !logw))
     return fail(FE_ERR_INVALID_ARGUMENT, "NULL Gaussian pointer");
-  int rc = batch_binning(b, p, st);
+  int rc = batch_binning(b, p, st, nullptr);
   if (rc) return rc;
-  launch_blend_fwd(p.va, p.tile_w, p.tile_h, p.px, p.n_tiles, b->ks.trec, b->rs.ranges, p.beta2, p.beta3,
-                   depth, alpha, stats, p.n_pix, b->rs.ctrl, st);
+  launch_blend_fwd(p.va, p.tile_w, p.tile_h, p.px, p.chunk, p.n_tiles, b->ks.trec, b->rs.ranges,
+                   p.beta2, p.beta3, depth, alpha, stats, p.n_pix, b->rs.ctrl, st);
   FE_CUDA(cudaGetLastError());
   return FE_OK;
 }
@@ -833,7 +908,7 @@ int fe_batch_bwd(fe_batch* b, const float* means, const float* prec, const float
   FE_CUDA(cudaMemsetAsync(gmeans, 0, sizeof(float) * 3 * (size_t)b->n_gauss, st));
   FE_CUDA(cudaMemsetAsync(gprec, 0, sizeof(float) * 9 * (size_t)b->n_gauss, st));
   FE_CUDA(cudaMemsetAsync(glogw, 0, sizeof(float) * (size_t)b->n_gauss, st));
-  int rc = batch_binning(b, p, st);
+  int rc = batch_binning(b, p, st, nullptr);
   if (rc) return rc;
   FE_CUDA(cudaMemsetAsync(b->rs.rgrad, 0, sizeof(RecGrad) * (size_t)p.n_rec, st));
   launch_pixel_prep(p.va, p.n_pix, depth, stats, p.n_pix, gdepth, galpha, b->rs.pix, st);
@@ -874,27 +949,15 @@ int fe_batch_fwd_timed(fe_batch* b, const float* means, const float* prec, const
   if (!b || !depth || !alpha || !stage_ms) return fail(FE_ERR_INVALID_ARGUMENT, "NULL argument");
   cudaStream_t st = reinterpret_cast<cudaStream_t>(stream_);
   Pipeline p = batch_pipeline(b, means, prec, logw);
-  const RecSpace& rs = b->rs;
-  const KeySpace& ks = b->ks;
   cudaEvent_t ev[7];
   for (auto& e : ev) FE_CUDA(cudaEventCreate(&e));
-  FE_CUDA(cudaMemsetAsync(rs.ctrl, 0, sizeof(Control), st));
-  FE_CUDA(cudaMemsetAsync(rs.ranges, 0, sizeof(uint2) * (size_t)p.n_tiles, st));
-  FE_CUDA(cudaEventRecord(ev[0], st));
-  launch_preprocess(p.va, p.n_rec, p.means, p.prec, p.logw, p.quat, nullptr, p.trans, p.cull_mode,
-                    p.cull_param, p.tile_w, p.tile_h, rs.recs, rs.rects, rs.touched, st);
-  FE_CUDA(cudaEventRecord(ev[1], st));
-  launch_scan(rs.touched, rs.incl, p.n_rec, b->cap, rs.scan_tmp, rs.ctrl, st);
-  FE_CUDA(cudaEventRecord(ev[2], st));
-  launch_emit_keys(p.va, rs.incl, rs.rects, p.n_rec, rs.ctrl, ks.keys_a, b->cap, st);
-  FE_CUDA(cudaEventRecord(ev[3], st));
-  b->sorted = launch_sort(ks.keys_a, ks.keys_b, bits_for(p.n_tiles), rs.ctrl, b->cap, ks.hist, st);
-  FE_CUDA(cudaEventRecord(ev[4], st));
-  launch_ranges_gather(p.va, b->sorted, rs.ctrl, b->cap, rs.recs, p.tile_w, p.tile_h, rs.ranges,
-                       ks.trec, st);
-  FE_CUDA(cudaEventRecord(ev[5], st));
-  launch_blend_fwd(p.va, p.tile_w, p.tile_h, p.px, p.n_tiles, ks.trec, rs.ranges, p.beta2, p.beta3,
-                   depth, alpha, stats, p.n_pix, rs.ctrl, st);
+  int rc = batch_binning(b, p, st, ev);
+  if (rc) {
+    for (auto& e : ev) cudaEventDestroy(e);
+    return rc;
+  }
+  launch_blend_fwd(p.va, p.tile_w, p.tile_h, p.px, p.chunk, p.n_tiles, b->ks.trec, b->rs.ranges,
+                   p.beta2, p.beta3, depth, alpha, stats, p.n_pix, b->rs.ctrl, st);
   FE_CUDA(cudaEventRecord(ev[6], st));
   FE_CUDA(cudaEventSynchronize(ev[6]));
   for (int i = 0; i < 6; ++i) FE_CUDA(cudaEventElapsedTime(&stage_ms[i], ev[i], ev[i + 1]));
@@ -911,7 +974,7 @@ int fe_batch_launch_count(const fe_batch* b) {
 }
 
 int fe_bench_peak(int kind, int iters, double* ops_per_second, fe_stream_t stream_) {
-  if (!ops_per_second || kind < 0 || kind > 1 || iters < 1)
+  if (!ops_per_second || kind < 0 || kind > 2 || iters < 1)
     return fail(FE_ERR_INVALID_ARGUMENT, "bad peak benchmark request");
   cudaStream_t st = reinterpret_cast<cudaStream_t>(stream_);
   float* scratch = nullptr;

@@ -10,8 +10,8 @@
 //            (rasterizer_impl.cu:287)
 //  ranges    [first, last+1) of every non-empty tile; empty tiles keep {0,0}
 //            (reference: getPerTileRanges, rasterizer_impl.cu:127-152)
-//  gather    re-expands each key's record around its tile centre into the contiguous tile-record
-//            stream the blend reads with TMA bulk copies
+//  gather    re-expands each key's record around its tile into the contiguous, pair-interleaved
+//            tile-record stream the blend reads with TMA bulk copies
 //
 // Every kernel reads the key count from device memory and uses a fixed grid, so the sequence
 // needs no host synchronisation and can be captured in a CUDA graph.
@@ -294,7 +294,8 @@ __global__ void sort_scatter_kernel(const uint64_t* __restrict__ in, uint64_t* _
 // Mahalanobis polynomial is expanded at the record's centre when that lies within kNearCentre
 // pixels of the tile centre (there it vanishes, up to the rounding of the centre), otherwise at
 // the tile centre (where it is large across the whole tile).
-__device__ __forceinline__ void tile_record(const GaussRec& g, float du, float dv, TileRec& t) {
+__device__ __forceinline__ void tile_record(const GaussRec& g, float du, float dv, float half_w,
+                                            float half_h, TileRec& t) {
   float a0[3], y0[3];
   const bool near = fabsf(du) <= kNearCentre && fabsf(dv) <= kNearCentre;
 #pragma unroll
@@ -322,33 +323,62 @@ __device__ __forceinline__ void tile_record(const GaussRec& g, float du, float d
   t.C = g.c2;
   t.cu = near ? -du : 0.f;
   t.cv = near ? -dv : 0.f;
-  t.pad[0] = 0.f;
-  t.pad[1] = 0.f;
+  // psv is affine in the pixel offset: its minimum over the tile is at a corner. Require a
+  // relative margin so float32 evaluation cannot flip the sign at any pixel.
+  const float span = fabsf(t.P[1]) * half_w + fabsf(t.P[2]) * half_h;
+  t.front = (t.P[0] - span > 1e-5f * (fabsf(t.P[0]) + span)) ? 1.f : 0.f;
+  t.pad = 0.f;
 }
 
+__device__ __forceinline__ void null_tile_record(TileRec& t) {
+  float* f = reinterpret_cast<float*>(&t);
+#pragma unroll
+  for (int i = 0; i < kRecFields; ++i) f[i] = 0.f;
+  t.V[0] = 1.f;
+  t.C = -INFINITY;
+  t.front = 1.f;
+}
+
+// One thread per pair of sorted keys: tile ranges, and the two tile records written as one
+// pair-interleaved TilePair (ten 16-byte stores).
 __global__ void ranges_gather_kernel(ViewsArg va, const uint64_t* __restrict__ keys,
                                      const Control* __restrict__ ctrl,
                                      const GaussRec* __restrict__ recs, int tile_w, int tile_h,
-                                     uint2* __restrict__ ranges, TileRec* __restrict__ trec) {
+                                     uint2* __restrict__ ranges, TilePair* __restrict__ trec) {
   const int64_t K = (int64_t)ctrl->num_keys;
-  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < K;
-       k += (int64_t)gridDim.x * blockDim.x) {
-    const uint64_t key = keys[k];
-    const uint32_t tile = (uint32_t)(key >> 32);
-    const uint32_t gid = (uint32_t)key;
-    if (k == 0 || (uint32_t)(keys[k - 1] >> 32) != tile) ranges[tile].x = (uint32_t)k;
-    if (k == K - 1 || (uint32_t)(keys[k + 1] >> 32) != tile) ranges[tile].y = (uint32_t)(k + 1);
+  const int64_t npairs = (K + 1) >> 1;
+  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < npairs;
+       p += (int64_t)gridDim.x * blockDim.x) {
+    TileRec t[2];
+#pragma unroll
+    for (int sl = 0; sl < 2; ++sl) {
+      const int64_t k = 2 * p + sl;
+      if (k >= K) {
+        null_tile_record(t[sl]);
+        continue;
+      }
+      const uint64_t key = keys[k];
+      const uint32_t tile = (uint32_t)(key >> 32);
+      const uint32_t gid = (uint32_t)key;
+      if (k == 0 || (uint32_t)(keys[k - 1] >> 32) != tile) ranges[tile].x = (uint32_t)k;
+      if (k == K - 1 || (uint32_t)(keys[k + 1] >> 32) != tile) ranges[tile].y = (uint32_t)(k + 1);
+      if (trec) {
+        const int vi = find_view<&ViewDev::tile_base>(va, tile);
+        const ViewDev& V = view_at(va, vi);
+        const int lt = (int)(tile - V.tile_base);
+        const int tx = lt % V.gx, ty = lt / V.gx;
+        const float hw = 0.5f * (tile_w - 1), hh = 0.5f * (tile_h - 1);
+        const GaussRec g = recs[V.rec_base + gid];
+        tile_record(g, tx * tile_w + hw - g.uc, ty * tile_h + hh - g.vc, hw, hh, t[sl]);
+      }
+    }
     if (trec) {
-      const int vi = find_view<&ViewDev::tile_base>(va, tile);
-      const ViewDev& V = view_at(va, vi);
-      const int lt = (int)(tile - V.tile_base);
-      const int tx = lt % V.gx, ty = lt / V.gx;
-      const float tcx = tx * tile_w + 0.5f * (tile_w - 1);
-      const float tcy = ty * tile_h + 0.5f * (tile_h - 1);
-      const GaussRec g = recs[V.rec_base + gid];
-      TileRec t;
-      tile_record(g, tcx - g.uc, tcy - g.vc, t);
-      trec[k] = t;
+      const float* a = reinterpret_cast<const float*>(&t[0]);
+      const float* b = reinterpret_cast<const float*>(&t[1]);
+      float4* dst = reinterpret_cast<float4*>(trec + p);
+#pragma unroll
+      for (int j = 0; j < kRecFields / 2; ++j)
+        dst[j] = make_float4(a[2 * j], b[2 * j], a[2 * j + 1], b[2 * j + 1]);
     }
   }
 }
@@ -400,15 +430,15 @@ uint64_t* launch_sort(uint64_t* a, uint64_t* b, int key_bits, const Control* ctr
 
 void launch_ranges_gather(const ViewsArg& va, const uint64_t* keys, const Control* ctrl,
                           int64_t capacity, const GaussRec* recs, int tile_w, int tile_h,
-                          uint2* ranges, TileRec* trec, cudaStream_t st) {
-  ranges_gather_kernel<<<grid_for(capacity, 256, 4 * 152 * 8), 256, 0, st>>>(
+                          uint2* ranges, TilePair* trec, cudaStream_t st) {
+  ranges_gather_kernel<<<grid_for((capacity + 1) / 2, 256, 4 * 152 * 8), 256, 0, st>>>(
       va, keys, ctrl, recs, tile_w, tile_h, ranges, trec);
 }
 
 void launch_ranges(const uint64_t* keys, const Control* ctrl, int64_t capacity, uint2* ranges,
                    cudaStream_t st) {
   ViewsArg va{};
-  ranges_gather_kernel<<<grid_for(capacity, 256, 4 * 152 * 8), 256, 0, st>>>(
+  ranges_gather_kernel<<<grid_for((capacity + 1) / 2, 256, 4 * 152 * 8), 256, 0, st>>>(
       va, keys, ctrl, nullptr, 8, 8, ranges, nullptr);
 }
 

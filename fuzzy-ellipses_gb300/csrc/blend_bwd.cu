@@ -43,7 +43,7 @@ __device__ __forceinline__ void red_add_v4(float* addr, float a, float b, float 
 template <int TW, int TH>
 __global__ void __launch_bounds__(128) blend_bwd_kernel(
     ViewsArg va, const uint64_t* __restrict__ keys, const Control* __restrict__ ctrl,
-    const TileRec* __restrict__ trec, const GaussRec* __restrict__ recs,
+    const TilePair* __restrict__ trec, const GaussRec* __restrict__ recs,
     const float4* __restrict__ pix, float nb2, float beta3, float beta2, RecGrad* __restrict__ rgrad) {
   const int64_t K = (int64_t)ctrl->num_keys;
   for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < K;
@@ -53,14 +53,15 @@ __global__ void __launch_bounds__(128) blend_bwd_kernel(
     const uint32_t gid = (uint32_t)key;
     const int vi = find_view<&ViewDev::tile_base>(va, tile);
     const ViewDev& V = view_at(va, vi);
+    if (V.flags & FE_VIEW_NO_GRAD) continue;
     const int lt = (int)(tile - V.tile_base);
     const int tx = lt % V.gx, ty = lt / V.gx;
-    const float4* t4 = reinterpret_cast<const float4*>(trec + k);
-    const float4 x0 = t4[0], x1 = t4[1], x2 = t4[2], x3 = t4[3], x4 = t4[4];
-    const float V0 = x0.x, V1 = x0.y, V2 = x0.z, V3 = x0.w, V4 = x1.x, V5 = x1.y;
-    const float P0 = x1.z, P1 = x1.w, P2 = x2.x;
-    const float N0 = x2.y, N1 = x2.z, N2 = x2.w, N3 = x3.x, N4 = x3.y, N5 = x3.z, C = x3.w;
-    const float cu = x4.x, cvv = x4.y;
+    // Record k lives in slot k%2 of pair k/2 (field i at float offset 2*i + slot).
+    const float* tf = reinterpret_cast<const float*>(trec + (k >> 1)) + (k & 1);
+    const float V0 = tf[0], V1 = tf[2], V2 = tf[4], V3 = tf[6], V4 = tf[8], V5 = tf[10];
+    const float P0 = tf[12], P1 = tf[14], P2 = tf[16];
+    const float N0 = tf[18], N1 = tf[20], N2 = tf[22], N3 = tf[24], N4 = tf[26], N5 = tf[28];
+    const float C = tf[30], cu = tf[32], cvv = tf[34];
 
     float gV[6] = {0, 0, 0, 0, 0, 0}, gP[3] = {0, 0, 0}, gN[6] = {0, 0, 0, 0, 0, 0}, gC = 0.f;
     const int xs = min(TW, V.W - tx * TW), ys = min(TH, V.H - ty * TH);
@@ -80,7 +81,7 @@ __global__ void __launch_bounds__(128) blend_bwd_kernel(
         const float s2 = fmaf(nq, qi, C);
         const float eA = ex2_approx(s2);
         const float l = fmaf(beta3, s2, nb2 * z);
-        const float e = (z > 0.f && px.y > -INFINITY) ? ex2_approx(l - px.y) : 0.f;
+        const float e = z > 0.f ? ex2_approx(l - px.y) : 0.f;
         const float we = px.z * e;                 // dL/ddepth * softmax weight
         const float zd = z - px.x;
         const float gs = fmaf(px.w, eA, beta3 * we * zd);       // dL/ds (natural)
@@ -149,6 +150,7 @@ __global__ void record_vjp_kernel(ViewsArg va, int64_t n_rec, const float* __res
        i += (int64_t)gridDim.x * blockDim.x) {
     const int vi = find_view<&ViewDev::rec_base>(va, i);
     const ViewDev& V = view_at(va, vi);
+    if (V.flags & FE_VIEW_NO_GRAD) continue;
     const int64_t gi = V.gauss_base + (i - V.rec_base);
     const RecGrad rg = rgrad[i];
 
@@ -237,7 +239,7 @@ __global__ void record_vjp_kernel(ViewsArg va, int64_t n_rec, const float* __res
 
 template <int TW, int TH>
 void launch_bwd_tiles(const ViewsArg& va, const uint64_t* keys, const Control* ctrl,
-                      int64_t capacity, const TileRec* trec, const GaussRec* recs,
+                      int64_t capacity, const TilePair* trec, const GaussRec* recs,
                       const float4* pix, float beta2, float beta3, RecGrad* rgrad,
                       cudaStream_t st) {
   const int64_t want = (capacity + 127) / 128;
@@ -259,7 +261,7 @@ void launch_pixel_prep(const ViewsArg& va, int64_t n_pix, const float* depth, co
 }
 
 void launch_blend_bwd(const ViewsArg& va, int tile_w, int tile_h, const uint64_t* keys,
-                      const Control* ctrl, int64_t capacity, const TileRec* trec,
+                      const Control* ctrl, int64_t capacity, const TilePair* trec,
                       const GaussRec* recs, const float4* pix, float beta2, float beta3,
                       RecGrad* rgrad, cudaStream_t st) {
   if (tile_w == 8 && tile_h == 8)

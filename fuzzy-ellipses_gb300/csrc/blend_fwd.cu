@@ -1,225 +1,325 @@
 // blend_fwd.cu -- per-tile forward blend: depth softmax and alpha in one pass.
 //
-// One CTA per screen tile, PX pixels of one row per thread. The tile's records (TileRec, 80 B, stored
-// contiguously in key order by the gather step) are streamed through a two-stage shared-memory
-// ring with 1-D TMA bulk copies (cp.async.bulk ... mbarrier::complete_tx). Per (pixel, Gaussian)
-// evaluation, from the tile-local polynomials:
-//     vsv = V(du,dv)   psv = P(du,dv)   nq = N(du-cu,dv-cv)    (polynomials; the row-constant
-//                                                               parts are shared by the PX
-//                                                               pixels a thread owns)
-//     q = rcp(vsv); z = psv q; s2 = C + nq q                   (z: peak ray parameter,
-//                                                               s2: log2 peak density)
-//     A += 2^s2                                                (alpha accumulator, all Gaussians)
-//     l = beta3 s2 - beta2 log2(e) z, masked to z > 0          (log2 softmax logit)
-// and an online max / rescaled sum over groups of G Gaussians keeps the softmax in one pass:
+// Persistent CTAs take screen tiles from a device-side work counter (one launch covers any number
+// of uneven renders); each thread owns PX pixels of one tile row. A tile's records
+// (pair-interleaved TilePairs, 160 B per two records, contiguous in key order) stream through a
+// two-stage shared-memory ring of CH pairs per stage filled by 1-D TMA bulk copies (cp.async.bulk ...
+// mbarrier::complete_tx; every wait bounded). Two records are evaluated together with packed
+// f32x2 arithmetic, so each 16-byte shared load yields two ready operands and every polynomial,
+// logit and accumulation step is one instruction for two evaluations. Per (pixel, Gaussian):
+//     vsv = V(du,dv)   psv = P(du,dv)   nq = N(du-cu, dv-cv)    (row-constant parts shared by
+//                                                                the thread's PX pixels)
+//     q = rcp(vsv); z = psv q; s2 = C + nq q                    (z: peak ray parameter,
+//                                                                s2: log2 peak density)
+//     A += 2^s2                                                 (alpha, all Gaussians)
+//     l = beta3 s2 - beta2 log2(e) z, masked to z > 0            (log2 softmax logit; the mask is
+//                                                                skipped for pairs whose psv is
+//                                                                positive over the whole tile)
+// and an online max (updated once per group of records) keeps the softmax in one pass:
 //     W = sum 2^(l-m), Z = sum 2^(l-m) z, depth = Z/W, alpha = 1 - exp(-A).
 // This is baseline/fm_render.py:11-109 (and the reference kernel gaussianRayRasterizeCUDA,
 // cuda_rasterizer/forward.cu:206-423) restricted to the tile's Gaussians.
+#include <algorithm>
+
 #include "fe_kernels.cuh"
 
 namespace fe {
 
 namespace {
 
-constexpr int kChunk = 32;   // records per pipeline stage
 constexpr int kStages = 2;
 
+template <int CH>
 struct BlendSmem {
-  TileRec buf[kStages][kChunk];
+  TilePair buf[kStages][CH];
   uint64_t full[kStages];
+  uint32_t tile;
 };
 
-__device__ __forceinline__ void null_record(TileRec& r) {
-  r.V[0] = 1.f;
+// Make slot `sl` (0 = .x, 1 = .y) of a pair contribute nothing: vsv = 1, psv = 0 (z = 0, masked),
+// C = -inf (density 0).
+__device__ __forceinline__ void null_slot(TilePair& p, int sl) {
 #pragma unroll
-  for (int k = 1; k < 6; ++k) r.V[k] = 0.f;
-#pragma unroll
-  for (int k = 0; k < 3; ++k) r.P[k] = 0.f;
-#pragma unroll
-  for (int k = 0; k < 6; ++k) r.N[k] = 0.f;
-  r.C = -INFINITY;
-  r.cu = 0.f;
-  r.cv = 0.f;
+  for (int i = 0; i < kRecFields; ++i) {
+    float v = 0.f;
+    if (i == 0) v = 1.f;
+    if (i == 15) v = -INFINITY;
+    if (sl == 0) p.f[i].x = v; else p.f[i].y = v;
+  }
 }
 
-__device__ __forceinline__ void issue_chunk(BlendSmem& sm, int stage, const TileRec* src,
+template <int CH>
+__device__ __forceinline__ void issue_chunk(BlendSmem<CH>& sm, int stage, const TilePair* src,
                                             int count) {
-  const uint32_t bytes = (uint32_t)count * (uint32_t)sizeof(TileRec);
+  const uint32_t bytes = (uint32_t)count * (uint32_t)sizeof(TilePair);
   mbar_arrive_expect_tx(&sm.full[stage], bytes);
   tma_bulk_g2s(&sm.buf[stage][0], src, bytes, &sm.full[stage]);
 }
 
 // Threads per CTA for a tile of TW x TH pixels with PX pixels per thread (PX pixels of one row,
-// CW = TW/PX apart), and the number of records per online-softmax group.
-template <int TW, int TH, int PX>
+// CW = TW/PX apart); GP record pairs per online-softmax group (one max update per group).
+template <int TW, int TH, int PX, int CH>
 struct BlendShape {
   static constexpr int NT = TW * TH / PX;
   static constexpr int CW = TW / PX;
-  static constexpr int G = PX >= 4 ? 4 : 8;
+  static constexpr int GP = PX >= 4 ? 2 : 4;
   static_assert(TW % PX == 0, "PX must divide the tile width");
+  static_assert(CH % GP == 0, "groups must tile a chunk");
+  static_assert(NT >= GP, "enough threads to pad a chunk");
 };
 
-template <int TW, int TH, int PX>
-__global__ void __launch_bounds__(BlendShape<TW, TH, PX>::NT) blend_fwd_kernel(
-    ViewsArg va, const TileRec* __restrict__ trec, const uint2* __restrict__ ranges, float nb2,
-    float beta3, float* __restrict__ depth, float* __restrict__ alpha, float* __restrict__ stats,
-    int64_t stats_stride, Control* __restrict__ ctrl) {
-  using Sh = BlendShape<TW, TH, PX>;
-  constexpr int G = Sh::G;
-  __shared__ __align__(128) BlendSmem sm;
+// Initial running max: finite, far below any logit, so logit - max is never inf - inf.
+constexpr float kNoLogit = -1e30f;
 
-  const int64_t tile = blockIdx.x;
-  const int vi = find_view<&ViewDev::tile_base>(va, tile);
-  const ViewDev& V = view_at(va, vi);
-  const int lt = (int)(tile - V.tile_base);
-  const int tx = lt % V.gx, ty = lt / V.gx;
+template <int TW, int TH, int PX, int CH>
+__global__ void __launch_bounds__(BlendShape<TW, TH, PX, CH>::NT) blend_fwd_kernel(
+    ViewsArg va, uint32_t n_tiles, const TilePair* __restrict__ trec,
+    const uint2* __restrict__ ranges, float nb2, float beta3, float* __restrict__ depth,
+    float* __restrict__ alpha, float* __restrict__ stats, int64_t stats_stride,
+    Control* __restrict__ ctrl) {
+  using Sh = BlendShape<TW, TH, PX, CH>;
+  constexpr int GP = Sh::GP;
+  __shared__ __align__(128) BlendSmem<CH> sm;
+
   const int tid = threadIdx.x;
   const int ly = tid / Sh::CW, cx = tid % Sh::CW;
-  const float dv = ly - 0.5f * (TH - 1), dv2 = dv * dv;
-  float du[PX];
+  const float dv = ly - 0.5f * (TH - 1);
+  const f2_t DV = f2_pack(dv, dv), DVSQ = f2_pack(dv * dv, dv * dv);
+  const f2_t B3 = f2_pack(beta3, beta3), NB2 = f2_pack(nb2, nb2);
+  f2_t DU[PX];
 #pragma unroll
-  for (int k = 0; k < PX; ++k) du[k] = (cx + k * Sh::CW) - 0.5f * (TW - 1);
+  for (int k = 0; k < PX; ++k) {
+    const float du = (cx + k * Sh::CW) - 0.5f * (TW - 1);
+    DU[k] = f2_pack(du, du);
+  }
+  const f2_t ZERO2 = f2_pack(0.f, 0.f);
 
-  const uint2 rg = ranges[tile];
-  const int n = (int)(rg.y - rg.x);
-  float A[PX], Wsum[PX], Zsum[PX], m[PX];
+  if (tid == 0) {
 #pragma unroll
-  for (int k = 0; k < PX; ++k) { A[k] = 0.f; Wsum[k] = 0.f; Zsum[k] = 0.f; m[k] = -INFINITY; }
+    for (int s = 0; s < kStages; ++s) mbar_init(&sm.full[s], 1);
+    fence_mbar_init();
+  }
+  uint32_t phase = 0;  // bit s: parity of the next completion to wait for on stage s
 
-  if (n > 0) {
-    const int nchunks = (n + kChunk - 1) / kChunk;
-    const TileRec* src = trec + rg.x;
-    if (tid == 0) {
-#pragma unroll
-      for (int s = 0; s < kStages; ++s) mbar_init(&sm.full[s], 1);
-      fence_mbar_init();
-    }
+  while (true) {
+    if (tid == 0) sm.tile = atomicAdd(&ctrl->next_tile, 1u);
     __syncthreads();
-    if (tid == 0) {
-      for (int c = 0; c < kStages && c < nchunks; ++c)
-        issue_chunk(sm, c, src + c * kChunk, min(kChunk, n - c * kChunk));
+    const uint32_t tile = sm.tile;
+    if (tile >= n_tiles) break;
+    const int vi = find_view<&ViewDev::tile_base>(va, tile);
+    const int gx = view_at(va, vi).gx;
+    const int lt = (int)(tile - view_at(va, vi).tile_base);
+    const int tx = lt % gx, ty = lt / gx;
+
+    const uint2 rg = ranges[tile];
+    // m starts finite (kNoLogit) so that logit - m is never (-inf) - (-inf); masked logits are
+    // -inf and give weight 0.
+    f2_t A2[PX], W2[PX], Z2[PX];
+    float m[PX];
+#pragma unroll
+    for (int k = 0; k < PX; ++k) {
+      A2[k] = ZERO2; W2[k] = ZERO2; Z2[k] = ZERO2;
+      m[k] = kNoLogit;
     }
-    for (int c = 0; c < nchunks; ++c) {
-      const int stage = c % kStages;
-      const uint32_t parity = (uint32_t)((c / kStages) & 1);
-      const int cnt = min(kChunk, n - c * kChunk);
-      const int padded = (cnt + G - 1) / G * G;
-      // Pad the chunk to whole groups with records that contribute nothing; these slots are
-      // disjoint from the bytes the bulk copy writes.
-      if (tid < padded - cnt) null_record(sm.buf[stage][cnt + tid]);
-      const bool ok = mbar_wait_bounded(&sm.full[stage], parity);
-      if (__syncthreads_or(!ok)) {
-        // A copy did not land in time: flag it, let every outstanding copy finish (bounded),
-        // and leave this tile's outputs at zero.
-        if (tid == 0) {
-          atomicOr(&ctrl->error, FE_DEVERR_TIMEOUT);
-          for (int cc = c; cc < nchunks && cc < c + kStages; ++cc)
-            (void)mbar_wait_bounded(&sm.full[cc % kStages], (uint32_t)((cc / kStages) & 1));
-        }
-        __syncthreads();
-#pragma unroll
-        for (int k = 0; k < PX; ++k) { A[k] = 0.f; Wsum[k] = 0.f; Zsum[k] = 0.f; m[k] = -INFINITY; }
-        break;
+    bool failed = false;
+
+    if (rg.y > rg.x) {
+      const uint32_t p0 = rg.x >> 1, p1 = (rg.y + 1) >> 1;
+      const int np = (int)(p1 - p0);
+      const bool first_odd = (rg.x & 1u) != 0, last_odd = (rg.y & 1u) != 0;
+      const int nchunks = (np + CH - 1) / CH;
+      const TilePair* src = trec + p0;
+      if (tid == 0) {
+        for (int c = 0; c < kStages && c < nchunks; ++c)
+          issue_chunk(sm, c, src + c * CH, min(CH, np - c * CH));
       }
-      const float4* rec4 = reinterpret_cast<const float4*>(sm.buf[stage]);
-      constexpr int R4 = sizeof(TileRec) / 16;
-      for (int j = 0; j < padded; j += G) {
-        float lg[G][PX], zg[G][PX];
-        float cmax[PX];
+      for (int c = 0; c < nchunks; ++c) {
+        const int stage = c % kStages;
+        const uint32_t parity = (phase >> stage) & 1u;
+        phase ^= 1u << stage;
+        const int cnt = min(CH, np - c * CH);
+        const int padded = (cnt + GP - 1) / GP * GP;
+        // Pad to whole groups with pairs that contribute nothing (disjoint from the copy's bytes).
+        if (tid < padded - cnt) {
+          null_slot(sm.buf[stage][cnt + tid], 0);
+          null_slot(sm.buf[stage][cnt + tid], 1);
+        }
+        const bool ok = mbar_wait_bounded(&sm.full[stage], parity);
+        // The first and last pairs may carry a neighbouring tile's record in one slot.
+        if (ok && tid == 0) {
+          if (c == 0 && first_odd) null_slot(sm.buf[stage][0], 0);
+          if (c == nchunks - 1 && last_odd) null_slot(sm.buf[stage][cnt - 1], 1);
+        }
+        if (__syncthreads_or(!ok)) {
+          // A copy did not land in time: flag it, let every outstanding copy finish (bounded)
+          // and stop this CTA; the tile's outputs are left unwritten.
+          if (tid == 0) {
+            atomicOr(&ctrl->error, FE_DEVERR_TIMEOUT);
+            for (int cc = c; cc < nchunks && cc < c + kStages; ++cc)
+              (void)mbar_wait_bounded(&sm.full[cc % kStages],
+                                      cc == c ? parity : (phase >> (cc % kStages)) & 1u);
+          }
+          failed = true;
+          break;
+        }
+        for (int j = 0; j < padded; j += GP) {
+          float la[GP][PX], lb[GP][PX];
+          f2_t zz[GP][PX];
+          float cmax[PX];
 #pragma unroll
-        for (int k = 0; k < PX; ++k) cmax[k] = -INFINITY;
+          for (int k = 0; k < PX; ++k) cmax[k] = -INFINITY;
 #pragma unroll
-        for (int q = 0; q < G; ++q) {
-          const float4 r0 = rec4[R4 * (j + q) + 0], r1 = rec4[R4 * (j + q) + 1];
-          const float4 r2 = rec4[R4 * (j + q) + 2], r3 = rec4[R4 * (j + q) + 3];
-          const float4 r4 = rec4[R4 * (j + q) + 4];
-          // V0..V5 = r0.xyzw r1.xy; P0..P2 = r1.zw r2.x; N0..N5 = r2.yzw r3.xyz; C = r3.w;
-          // (cu, cv) = r4.xy. Row-constant parts, shared by the thread's PX pixels of row dv.
-          const float bv = fmaf(r1.y, dv2, fmaf(r0.z, dv, r0.x));
-          const float cv = fmaf(r1.x, dv, r0.y);
-          const float bp = fmaf(r2.x, dv, r1.z);
-          const float ev = dv - r4.y;
-          const float bn = fmaf(r3.z * ev, ev, fmaf(r2.w, ev, r2.y));
-          const float cn = fmaf(r3.y, ev, r2.z);
+          for (int q = 0; q < GP; ++q) {
+            const ulonglong2* rp = reinterpret_cast<const ulonglong2*>(&sm.buf[stage][j + q]);
+            const ulonglong2 r0 = rp[0], r1 = rp[1], r2 = rp[2], r3 = rp[3], r4 = rp[4];
+            const ulonglong2 r5 = rp[5], r6 = rp[6], r7 = rp[7], r8 = rp[8], r9 = rp[9];
+            // V0..V5 = r0.x r0.y r1.x r1.y r2.x r2.y; P0..P2 = r3.x r3.y r4.x;
+            // N0..N5 = r4.y r5.x r5.y r6.x r6.y r7.x; C = r7.y; cu = r8.x; cv = r8.y;
+            // front = r9.x. Row-constant parts first, shared by the thread's PX pixels.
+            const f2_t bv = fma2(r2.y, DVSQ, fma2(r1.x, DV, r0.x));
+            const f2_t cv = fma2(r2.x, DV, r0.y);
+            const f2_t bp = fma2(r4.x, DV, r3.x);
+            const f2_t ev = sub2(DV, r8.y);
+            const f2_t bn = fma2(mul2(r7.x, ev), ev, fma2(r5.y, ev, r4.y));
+            const f2_t cn = fma2(r6.y, ev, r5.x);
+            float fa, fb;
+            f2_unpack(r9.x, fa, fb);
+            const bool masked = !(fa != 0.f && fb != 0.f);
+#pragma unroll
+            for (int k = 0; k < PX; ++k) {
+              const f2_t vsv = fma2(fma2(r1.y, DU[k], cv), DU[k], bv);
+              const f2_t psv = fma2(r3.y, DU[k], bp);
+              const f2_t eu = sub2(DU[k], r8.x);
+              const f2_t nq = fma2(fma2(r6.x, eu, cn), eu, bn);
+              float va, vb;
+              f2_unpack(vsv, va, vb);
+              const f2_t qi = f2_pack(rcp_approx(va), rcp_approx(vb));
+              const f2_t z = mul2(psv, qi);
+              const f2_t s2 = fma2(nq, qi, r7.y);
+              float sa, sb;
+              f2_unpack(s2, sa, sb);
+              A2[k] = add2(A2[k], f2_pack(ex2_approx(sa), ex2_approx(sb)));
+              const f2_t l = fma2(B3, s2, mul2(NB2, z));
+              float l0, l1;
+              f2_unpack(l, l0, l1);
+              if (masked) {
+                float z0, z1;
+                f2_unpack(z, z0, z1);
+                l0 = z0 > 0.f ? l0 : -INFINITY;
+                l1 = z1 > 0.f ? l1 : -INFINITY;
+              }
+              la[q][k] = l0;
+              lb[q][k] = l1;
+              zz[q][k] = z;
+              cmax[k] = fmaxf(cmax[k], fmaxf(l0, l1));
+            }
+          }
 #pragma unroll
           for (int k = 0; k < PX; ++k) {
-            const float vsv = fmaf(fmaf(r0.w, du[k], cv), du[k], bv);
-            const float psv = fmaf(r1.w, du[k], bp);
-            const float eu = du[k] - r4.x;
-            const float nq = fmaf(fmaf(r3.x, eu, cn), eu, bn);
-            const float qi = rcp_approx(vsv);
-            const float z = psv * qi;
-            const float s2 = fmaf(nq, qi, r3.w);
-            A[k] += ex2_approx(s2);
-            const float l = fmaf(beta3, s2, nb2 * z);
-            lg[q][k] = z > 0.f ? l : -INFINITY;
-            zg[q][k] = z;
-            cmax[k] = fmaxf(cmax[k], lg[q][k]);
-          }
-        }
+            if (cmax[k] > m[k]) {
+              const float sc = ex2_approx(m[k] - cmax[k]);
+              const f2_t S = f2_pack(sc, sc);
+              W2[k] = mul2(W2[k], S);
+              Z2[k] = mul2(Z2[k], S);
+              m[k] = cmax[k];
+            }
+            const f2_t M = f2_pack(m[k], m[k]);
 #pragma unroll
-        for (int k = 0; k < PX; ++k) {
-          if (cmax[k] > m[k]) {
-            const float sc = ex2_approx(m[k] - cmax[k]);
-            Wsum[k] *= sc;
-            Zsum[k] *= sc;
-            m[k] = cmax[k];
-          }
-          if (m[k] > -INFINITY) {
-#pragma unroll
-            for (int q = 0; q < G; ++q) {
-              const float e = ex2_approx(lg[q][k] - m[k]);
-              Wsum[k] += e;
-              Zsum[k] = fmaf(e, zg[q][k], Zsum[k]);
+            for (int q = 0; q < GP; ++q) {
+              float d0, d1;
+              f2_unpack(sub2(f2_pack(la[q][k], lb[q][k]), M), d0, d1);
+              const f2_t e = f2_pack(ex2_approx(d0), ex2_approx(d1));
+              W2[k] = add2(W2[k], e);
+              Z2[k] = fma2(e, zz[q][k], Z2[k]);
             }
           }
         }
+        fence_proxy_async_smem();
+        __syncthreads();
+        if (tid == 0 && c + kStages < nchunks)
+          issue_chunk(sm, stage, src + (c + kStages) * CH, min(CH, np - (c + kStages) * CH));
       }
-      fence_proxy_async_smem();
-      __syncthreads();
-      if (tid == 0 && c + kStages < nchunks)
-        issue_chunk(sm, stage, src + (c + kStages) * kChunk,
-                    min(kChunk, n - (c + kStages) * kChunk));
     }
-  }
+    if (failed) break;
 
-  const int v = ty * TH + ly;
+    const ViewDev& V = view_at(va, vi);
+    const int v = ty * TH + ly;
 #pragma unroll
-  for (int k = 0; k < PX; ++k) {
-    const int u = tx * TW + cx + k * Sh::CW;
-    if (u < V.W && v < V.H) {
-      const int64_t pix = V.pix_base + (int64_t)v * V.W + u;
-      depth[pix] = Wsum[k] > 0.f ? Zsum[k] / Wsum[k] : 0.f;
-      alpha[pix] = -expm1f(-A[k]);
-      if (stats) {
-        stats[pix] = m[k];
-        stats[stats_stride + pix] = Wsum[k];
-        stats[2 * stats_stride + pix] = A[k];
+    for (int k = 0; k < PX; ++k) {
+      const int u = tx * TW + cx + k * Sh::CW;
+      if (u < V.W && v < V.H) {
+        float a0, a1, w0, w1, z0, z1;
+        f2_unpack(A2[k], a0, a1);
+        f2_unpack(W2[k], w0, w1);
+        f2_unpack(Z2[k], z0, z1);
+        const float A = a0 + a1, W = w0 + w1, Z = z0 + z1;
+        const int64_t pix = V.pix_base + (int64_t)v * V.W + u;
+        depth[pix] = W > 0.f ? Z / W : 0.f;
+        alpha[pix] = -expm1f(-A);
+        if (stats) {
+          stats[pix] = m[k];
+          stats[stats_stride + pix] = W;
+          stats[2 * stats_stride + pix] = A;
+        }
       }
     }
+    __syncthreads();  // sm.tile is rewritten next iteration
   }
 }
 
-template <int TW, int TH, int PX>
-void launch_tiles(const ViewsArg& va, int64_t n_tiles, const TileRec* trec, const uint2* ranges,
+// Resident CTAs of one kernel instance on the current device (queried once per instance).
+template <class K>
+int resident_ctas(K kernel, int threads) {
+  static int cached = 0;
+  if (cached == 0) {
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, 0);
+    cached = sms * (per_sm > 0 ? per_sm : 1);
+  }
+  return cached;
+}
+
+template <int TW, int TH, int PX, int CH>
+void launch_tiles(const ViewsArg& va, int64_t n_tiles, const TilePair* trec, const uint2* ranges,
                   float nb2, float beta3, float* depth, float* alpha, float* stats,
                   int64_t stats_stride, Control* ctrl, cudaStream_t st) {
-  blend_fwd_kernel<TW, TH, PX><<<(unsigned)n_tiles, BlendShape<TW, TH, PX>::NT, 0, st>>>(
-      va, trec, ranges, nb2, beta3, depth, alpha, stats, stats_stride, ctrl);
+  constexpr int NT = BlendShape<TW, TH, PX, CH>::NT;
+  auto kern = blend_fwd_kernel<TW, TH, PX, CH>;
+  const int64_t grid = std::min<int64_t>(n_tiles, resident_ctas(kern, NT));
+  kern<<<(unsigned)grid, NT, 0, st>>>(va, (uint32_t)n_tiles, trec, ranges, nb2, beta3, depth,
+                                      alpha, stats, stats_stride, ctrl);
+}
+
+template <int TW, int TH, int PX>
+void launch_chunk(int chunk, const ViewsArg& va, int64_t n_tiles, const TilePair* trec,
+                  const uint2* ranges, float nb2, float beta3, float* depth, float* alpha,
+                  float* stats, int64_t stats_stride, Control* ctrl, cudaStream_t st) {
+  if (chunk == 8)
+    launch_tiles<TW, TH, PX, 8>(va, n_tiles, trec, ranges, nb2, beta3, depth, alpha, stats,
+                                stats_stride, ctrl, st);
+  else if (chunk == 32)
+    launch_tiles<TW, TH, PX, 32>(va, n_tiles, trec, ranges, nb2, beta3, depth, alpha, stats,
+                                 stats_stride, ctrl, st);
+  else
+    launch_tiles<TW, TH, PX, 16>(va, n_tiles, trec, ranges, nb2, beta3, depth, alpha, stats,
+                                 stats_stride, ctrl, st);
 }
 
 }  // namespace
 
-// Pixels per thread: px in {1, 2, 4}; 0 selects the default for the tile shape.
-void launch_blend_fwd(const ViewsArg& va, int tile_w, int tile_h, int px, int64_t n_tiles,
-                      const TileRec* trec, const uint2* ranges, float beta2, float beta3,
-                      float* depth, float* alpha, float* stats, int64_t stats_stride,
-                      Control* ctrl, cudaStream_t st) {
+// Pixels per thread: px in {1, 2, 4} (8x8 tiles: 1, 2); 0 selects the default for the tile.
+// Chunk: record pairs per shared-memory stage, 8, 16 or 32; 0 selects 16.
+void launch_blend_fwd(const ViewsArg& va, int tile_w, int tile_h, int px, int chunk,
+                      int64_t n_tiles, const TilePair* trec, const uint2* ranges, float beta2,
+                      float beta3, float* depth, float* alpha, float* stats,
+                      int64_t stats_stride, Control* ctrl, cudaStream_t st) {
   if (n_tiles <= 0) return;
   const float nb2 = -beta2 * kLog2e;
 #define FE_BLEND(TW_, TH_, PX_)                                                                 \
-  launch_tiles<TW_, TH_, PX_>(va, n_tiles, trec, ranges, nb2, beta3, depth, alpha, stats,     \
-                              stats_stride, ctrl, st)
+  launch_chunk<TW_, TH_, PX_>(chunk, va, n_tiles, trec, ranges, nb2, beta3, depth, alpha,     \
+                              stats, stats_stride, ctrl, st)
   if (tile_w == 8 && tile_h == 8) {
     if (px == 1) FE_BLEND(8, 8, 1); else FE_BLEND(8, 8, 2);
   } else if (tile_w == 32 && tile_h == 8) {

@@ -33,6 +33,8 @@ struct ViewDev {
   int32_t gx, gy;         // tiles per row / column
   int32_t n;              // Gaussians of the scene
   int32_t pose;           // index into the pose arrays (quat[4*pose], trans[3*pose])
+  uint32_t flags;         // FE_VIEW_* bits
+  uint32_t pad;
   int64_t gauss_base;     // first Gaussian of the scene in the input arrays
   int64_t rec_base;       // first record of this view
   int64_t tile_base;      // first global tile id of this view
@@ -53,7 +55,8 @@ struct __align__(16) GaussRec {
 };
 static_assert(sizeof(GaussRec) == 96, "GaussRec layout");
 
-// Tile-local polynomial form of a record (what the blend streams with TMA bulk copies).
+// Tile-local polynomial form of a record (what the blend streams with TMA bulk copies, stored
+// pair-interleaved: see TilePair).
 // With (du,dv) the pixel offset from the tile centre and (eu,ev) = (du-cu, dv-cv) the offset from
 // the expansion centre (cu,cv) of the Mahalanobis term:
 //   vsv = V0 + V1 du + V2 dv + V3 du^2 + V4 du dv + V5 dv^2
@@ -68,9 +71,19 @@ struct __align__(16) TileRec {
   float N[6];
   float C;
   float cu, cv;
-  float pad[2];
+  float front;  // 1 when psv > 0 over the whole tile (no z <= 0 masking needed), else 0
+  float pad;
 };
 static_assert(sizeof(TileRec) == 80, "TileRec layout");
+
+// Keys 2p and 2p+1 of the sorted key list share one TilePair: field i of record 2p is f[i].x and
+// of record 2p+1 is f[i].y, so one 16-byte shared-memory load yields two packed f32x2 operands.
+// Field order: V0..V5, P0..P2, N0..N5, C, cu, cv, front, pad.
+constexpr int kRecFields = 20;
+struct __align__(16) TilePair {
+  float2 f[kRecFields];
+};
+static_assert(sizeof(TilePair) == 160, "TilePair layout");
 
 // The Mahalanobis polynomial of a tile record is expanded at the record's centre when that lies
 // within this many pixels of the tile centre (in both directions), else at the tile centre.
@@ -95,7 +108,8 @@ struct Control {
   unsigned long long num_keys;  // keys produced by the last run (clamped to capacity)
   unsigned long long want_keys; // keys the run needed
   uint32_t error;               // FE_DEVERR_* bits
-  uint32_t pad[11];
+  uint32_t next_tile;           // work counter of the persistent blend
+  uint32_t pad[10];
 };
 
 // View lookup: the plain single-render path passes its one view by value (so it needs no
@@ -203,6 +217,38 @@ __device__ __forceinline__ void tma_bulk_g2s(void* smem_dst, const void* gmem_sr
           "r"(smem_addr(smem_dst)),
       "l"(gmem_src), "r"(bytes), "r"(smem_addr(bar))
       : "memory");
+}
+
+// Packed float32 pairs (Blackwell add/sub/mul/fma .f32x2): one instruction for two lanes of work.
+typedef unsigned long long f2_t;
+
+__device__ __forceinline__ f2_t f2_pack(float lo, float hi) {
+  f2_t r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
+  return r;
+}
+__device__ __forceinline__ void f2_unpack(f2_t v, float& lo, float& hi) {
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
+}
+__device__ __forceinline__ f2_t fma2(f2_t a, f2_t b, f2_t c) {
+  f2_t d;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+  return d;
+}
+__device__ __forceinline__ f2_t add2(f2_t a, f2_t b) {
+  f2_t d;
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+__device__ __forceinline__ f2_t sub2(f2_t a, f2_t b) {
+  f2_t d;
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+__device__ __forceinline__ f2_t mul2(f2_t a, f2_t b) {
+  f2_t d;
+  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
 }
 
 // ------------------------------------------------------------------------------------------

@@ -36,18 +36,20 @@ void launch_emit_keys(const ViewsArg& va, const uint32_t* incl, const TileRect* 
 // result (a or b). hist: 256 * (sort_grid(capacity) + 1) uint32.
 uint64_t* launch_sort(uint64_t* a, uint64_t* b, int key_bits, const Control* ctrl,
                       int64_t capacity, uint32_t* hist, cudaStream_t st);
-// Tile ranges (ranges must be zeroed beforehand) and the tile-local record stream.
+// Tile ranges (ranges must be zeroed beforehand) and the tile-local record stream, key k at
+// trec[k/2] slot k%2 (capacity/2 rounded up pairs).
 void launch_ranges_gather(const ViewsArg& va, const uint64_t* keys, const Control* ctrl,
                           int64_t capacity, const GaussRec* recs, int tile_w, int tile_h,
-                          uint2* ranges, TileRec* trec, cudaStream_t st);
+                          uint2* ranges, TilePair* trec, cudaStream_t st);
 // Ranges only (reference-compatible binning).
 void launch_ranges(const uint64_t* keys, const Control* ctrl, int64_t capacity, uint2* ranges,
                    cudaStream_t st);
 
 // blend_fwd.cu
-// px: pixels per thread (1, 2 or 4; 0 = default for the tile shape).
-void launch_blend_fwd(const ViewsArg& va, int tile_w, int tile_h, int px, int64_t n_tiles,
-                      const TileRec* trec, const uint2* ranges, float beta2, float beta3,
+// px: pixels per thread (1, 2 or 4; 0 = default for the tile shape); chunk: record pairs per
+// shared-memory stage (8, 16 or 32; 0 = 16). Persistent: ctrl->next_tile must be zero.
+void launch_blend_fwd(const ViewsArg& va, int tile_w, int tile_h, int px, int chunk, int64_t n_tiles,
+                      const TilePair* trec, const uint2* ranges, float beta2, float beta3,
                       float* depth, float* alpha, float* stats, int64_t stats_stride,
                       Control* ctrl, cudaStream_t st);
 
@@ -56,7 +58,7 @@ void launch_pixel_prep(const ViewsArg& va, int64_t n_pix, const float* depth, co
                        int64_t stats_stride, const float* grad_depth, const float* grad_alpha,
                        float4* pix, cudaStream_t st);
 void launch_blend_bwd(const ViewsArg& va, int tile_w, int tile_h, const uint64_t* keys,
-                      const Control* ctrl, int64_t capacity, const TileRec* trec,
+                      const Control* ctrl, int64_t capacity, const TilePair* trec,
                       const GaussRec* recs, const float4* pix, float beta2, float beta3,
                       RecGrad* rgrad, cudaStream_t st);
 // Gradients are accumulated (atomically) into gmeans/gprec/glogw, which must be zeroed first.

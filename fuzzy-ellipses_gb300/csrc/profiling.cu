@@ -38,10 +38,31 @@ __global__ void __launch_bounds__(256) peak_ex2_kernel(float* out, int iters) {
   if (s == 12345.678f) out[blockIdx.x] = s;
 }
 
+// Eight independent chains of packed fma.rn.f32x2 per thread (two FMAs per instruction).
+__global__ void __launch_bounds__(256) peak_fma2_kernel(float* out, int iters, float a, float b) {
+  f2_t x[kChains];
+  const f2_t A = f2_pack(a, a), B = f2_pack(b, b);
+#pragma unroll
+  for (int c = 0; c < kChains; ++c) x[c] = f2_pack(threadIdx.x * 1e-3f + c, c * 0.5f);
+  for (int i = 0; i < iters; ++i) {
+#pragma unroll
+    for (int c = 0; c < kChains; ++c) x[c] = fma2(x[c], A, B);
+  }
+  float s = 0.f;
+#pragma unroll
+  for (int c = 0; c < kChains; ++c) {
+    float lo, hi;
+    f2_unpack(x[c], lo, hi);
+    s += lo + hi;
+  }
+  if (s == 12345.678f) out[blockIdx.x] = s;
+}
+
 }  // namespace
 
 // Returns pipe operations per second: kind 0 = FFMA (one FMA per op), kind 1 = MUFU.EX2
-// (the ex2 kernel also issues one FADD per op, on the FMA pipe).
+// (the ex2 kernel also issues one FADD per op, on the FMA pipe), kind 2 = packed f32x2 FMA
+// (counted as two FMAs per instruction).
 double run_peak(int kind, int iters, float* scratch, cudaStream_t st) {
   int dev = 0, sms = 0;
   cudaGetDevice(&dev);
@@ -52,7 +73,8 @@ double run_peak(int kind, int iters, float* scratch, cudaStream_t st) {
   cudaEventCreate(&e1);
   auto launch = [&]() {
     if (kind == 0) peak_fma_kernel<<<blocks, threads, 0, st>>>(scratch, iters, 0.999f, 1e-4f);
-    else peak_ex2_kernel<<<blocks, threads, 0, st>>>(scratch, iters);
+    else if (kind == 1) peak_ex2_kernel<<<blocks, threads, 0, st>>>(scratch, iters);
+    else peak_fma2_kernel<<<blocks, threads, 0, st>>>(scratch, iters, 0.999f, 1e-4f);
   };
   launch();  // warm-up
   cudaEventRecord(e0, st);
@@ -63,7 +85,7 @@ double run_peak(int kind, int iters, float* scratch, cudaStream_t st) {
   cudaEventElapsedTime(&ms, e0, e1);
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
-  const double ops = 5.0 * blocks * threads * (double)iters * kChains;
+  const double ops = 5.0 * blocks * threads * (double)iters * kChains * (kind == 2 ? 2.0 : 1.0);
   return ms > 0.f ? ops / (ms * 1e-3) : 0.0;
 }
 

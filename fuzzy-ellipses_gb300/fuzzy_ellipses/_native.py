@@ -19,6 +19,12 @@ FE_CULL_EPS = 0
 FE_CULL_NSTD = 1
 FE_DEVERR_CAPACITY = 1
 FE_DEVERR_TIMEOUT = 2
+FE_FLAG_EXACT_KEYS = 2
+FE_VIEW_NO_GRAD = 1
+
+
+def flag_chunk(pairs):
+    return (int(pairs) & 0xFF) << 8
 
 STATUS_NAMES = {
     0: "FE_OK", 1: "FE_ERR_INVALID_ARGUMENT", 2: "FE_ERR_DESCRIPTOR", 3: "FE_ERR_CUDA",
@@ -62,7 +68,7 @@ class View(ctypes.Structure):
     _fields_ = [("scene", ctypes.c_int32), ("height", ctypes.c_int32), ("width", ctypes.c_int32),
                 ("fx", ctypes.c_float), ("fy", ctypes.c_float), ("cx", ctypes.c_float),
                 ("cy", ctypes.c_float), ("quat", ctypes.c_float * 4), ("trans", ctypes.c_float * 3),
-                ("pixel_offset", ctypes.c_int64)]
+                ("flags", ctypes.c_uint32), ("pixel_offset", ctypes.c_int64)]
 
 
 class SceneEntry(ctypes.Structure):
@@ -94,6 +100,7 @@ PROTOTYPES = {
     "fe_batch_create": (ctypes.c_int, [ctypes.POINTER(RenderDesc), ctypes.POINTER(SceneEntry), I32,
                                        ctypes.POINTER(View), I32, ctypes.POINTER(P)]),
     "fe_batch_destroy": (None, [P]),
+    "fe_batch_reset": (ctypes.c_int, [P, ctypes.POINTER(SceneEntry), I32, ctypes.POINTER(View), I32, P]),
     "fe_batch_pixels": (I64, [P]),
     "fe_batch_scratch_bytes": (I64, [P]),
     "fe_batch_fwd": (ctypes.c_int, [P] + [P] * 6 + [P]),

@@ -148,10 +148,11 @@ def render_binning(means, prec, logw, fx, fy, cx, cy, quat, t, height, width, *,
 
 
 def bench_peak(kind):
-    """Measured pipe throughput (operations/s): 'fma' (FP32 FMA) or 'ex2' (MUFU ex2)."""
+    """Measured pipe throughput (operations/s): 'fma' (FP32 FMA), 'ex2' (MUFU ex2) or 'fma2'
+    (packed f32x2 FMA, two FMAs per instruction)."""
     lib = N.load()
     out = ctypes.c_double(0.0)
-    N.check(lib.fe_bench_peak({"fma": 0, "ex2": 1}[kind], 4096, ctypes.byref(out), _stream()))
+    N.check(lib.fe_bench_peak({"fma": 0, "ex2": 1, "fma2": 2}[kind], 4096, ctypes.byref(out), _stream()))
     return float(out.value)
 
 
@@ -278,20 +279,33 @@ class Batch:
 
     ``scenes``: list of (gauss_offset, n) into concatenated Gaussian arrays.
     ``views``: list of dicts with keys scene, height, width, fx, fy, cx, cy, quat, trans and
-    optionally pixel_offset (default: packed in order).
-    The plan reserves scratch for the worst-case key count, so ``forward`` performs no host
-    synchronisation and can be captured in a CUDA graph.
+    optionally pixel_offset (default: packed in order) and no_grad (skip in the backward).
+    By default the plan reserves scratch for the worst-case key count, so ``forward`` performs no
+    host synchronisation and can be captured in a CUDA graph; ``exact_keys=True`` sizes the key
+    scratch from the device-side count instead (one 8-byte readback per run).
+    ``tile``, ``px`` (pixels per thread) and ``chunk`` (record pairs per shared-memory stage)
+    select the blend configuration.
     """
 
     def __init__(self, scenes, views, beta2=21.4, beta3=2.66, *, cull="eps", cull_param=None,
-                 tile=(16, 16)):
+                 tile=(16, 16), px=0, chunk=0, exact_keys=False):
         lib = N.load()
-        desc = N.make_desc(0, 1, 1, 1.0, 1.0, 0.0, 0.0, beta2, beta3, cull, cull_param, tile)
+        flags = N.flag_chunk(chunk) | (N.FE_FLAG_EXACT_KEYS if exact_keys else 0)
+        desc = N.make_desc(0, 1, 1, 1.0, 1.0, 0.0, 0.0, beta2, beta3, cull, cull_param, tile,
+                           flags=flags, px=px)
+        sc, nsc, vs, nvs = self._tables(scenes, views)
+        h = ctypes.c_void_p()
+        N.check(lib.fe_batch_create(ctypes.byref(desc), sc, nsc, vs, nvs, ctypes.byref(h)))
+        self._h = h
+        self.tile = tuple(tile)
+        self._sizes()
+
+    def _tables(self, scenes, views):
         sc = (N.SceneEntry * max(1, len(scenes)))()
         for i, (off, n) in enumerate(scenes):
             sc[i].gauss_offset = int(off)
             sc[i].n = int(n)
-        vs = (N.View * len(views))()
+        vs = (N.View * max(1, len(views)))()
         off = 0
         self.pixel_offsets = []
         self.shapes = []
@@ -305,17 +319,24 @@ class Batch:
                 vs[i].quat[k] = float(v["quat"][k])
             for k in range(3):
                 vs[i].trans[k] = float(v["trans"][k])
+            vs[i].flags = N.FE_VIEW_NO_GRAD if v.get("no_grad") else 0
             po = int(v.get("pixel_offset", off))
             vs[i].pixel_offset = po
             self.pixel_offsets.append(po)
             self.shapes.append((int(v["height"]), int(v["width"])))
             off = max(off, po + int(v["height"]) * int(v["width"]))
-        h = ctypes.c_void_p()
-        N.check(lib.fe_batch_create(ctypes.byref(desc), sc, len(scenes), vs, len(views),
-                                    ctypes.byref(h)))
-        self._h = h
-        self.n_pixels = int(lib.fe_batch_pixels(h))
-        self.scratch_bytes = int(lib.fe_batch_scratch_bytes(h))
+        return sc, len(scenes), vs, len(views)
+
+    def _sizes(self):
+        lib = N.load()
+        self.n_pixels = int(lib.fe_batch_pixels(self._h))
+        self.scratch_bytes = int(lib.fe_batch_scratch_bytes(self._h))
+
+    def reset(self, scenes, views):
+        """Re-plan for new scenes/views, reusing the device buffers (they only grow)."""
+        sc, nsc, vs, nvs = self._tables(scenes, views)
+        N.check(N.load().fe_batch_reset(self._h, sc, nsc, vs, nvs, _stream()))
+        self._sizes()
 
     def close(self):
         if getattr(self, "_h", None) and self._h.value:

@@ -1,0 +1,106 @@
+"""Autotuner for the blend configuration of batched renders.
+
+Three knobs change the work and its mapping onto the GPU:
+
+* ``tile``  -- screen tile of the binning and of one blend work item (8x8, 16x16 or 32x8):
+  smaller tiles cull more precisely (fewer evaluations) but produce more keys to sort and
+  gather;
+* ``px``    -- pixels of one tile row per thread (1, 2, 4): shares each record's shared-memory
+  loads and row-constant polynomial terms across more evaluations, at the cost of registers;
+* ``chunk`` -- record pairs per shared-memory stage of the TMA ring (8, 16, 32).
+
+``Autotuner.tune`` times every candidate on the actual batch (median of per-stage CUDA-event
+timings of the whole pipeline, not just the blend) and caches the fastest per workload bucket
+(mean pixels per view, mean Gaussians per view and number of views, each on a log2 scale) in a
+JSON file (``FE_AUTOTUNE_CACHE`` or ``~/.cache/fuzzy_ellipses/autotune.json``).
+"""
+
+from __future__ import annotations
+
+import json
+import math
+import os
+import statistics
+import threading
+
+DEFAULT = {"tile": (16, 16), "px": 4, "chunk": 16}
+
+CANDIDATES = [
+    ((8, 8), 1, 16), ((8, 8), 2, 8), ((8, 8), 2, 16),
+    ((16, 16), 2, 16), ((16, 16), 4, 8), ((16, 16), 4, 16), ((16, 16), 4, 32),
+    ((32, 8), 2, 16), ((32, 8), 4, 16), ((32, 8), 4, 32),
+]
+
+
+def bucket(scenes, views):
+    """Workload bucket of a batch: log2 classes of pixels per view, Gaussians per view, views."""
+    n_of = {i: n for i, (_, n) in enumerate(scenes)}
+    pix = sum(int(v["height"]) * int(v["width"]) for v in views) / max(1, len(views))
+    gau = sum(n_of[int(v["scene"])] for v in views) / max(1, len(views))
+    return (f"p{round(math.log2(max(pix, 1)))}_n{round(math.log2(gau + 1))}"
+            f"_v{min(10, int(math.log2(max(1, len(views)))))}")
+
+
+def _cache_path():
+    return os.environ.get("FE_AUTOTUNE_CACHE",
+                          os.path.join(os.path.expanduser("~"), ".cache", "fuzzy_ellipses",
+                                       "autotune.json"))
+
+
+class Autotuner:
+    def __init__(self, path=None, persist=True):
+        self.path = path or _cache_path()
+        self.persist = persist
+        self._lock = threading.Lock()
+        self.table = {}
+        if persist and os.path.exists(self.path):
+            try:
+                with open(self.path) as f:
+                    self.table = json.load(f)
+            except (OSError, ValueError):
+                self.table = {}
+
+    def lookup(self, scenes, views):
+        """Cached best configuration for the batch's bucket, or the default."""
+        e = self.table.get(bucket(scenes, views))
+        if not e:
+            return dict(DEFAULT)
+        return {"tile": tuple(e["tile"]), "px": e["px"], "chunk": e["chunk"]}
+
+    def tune(self, scenes, views, means, prec, logw, candidates=CANDIDATES, reps=5, **batch_kw):
+        """Time every candidate on this batch; cache and return the fastest configuration."""
+        import torch
+
+        from .api import Batch
+
+        results = []
+        for tile, px, chunk in candidates:
+            b = Batch(scenes, views, tile=tile, px=px, chunk=chunk, **batch_kw)
+            depth = torch.empty(b.n_pixels, device=means.device)
+            alpha = torch.empty(b.n_pixels, device=means.device)
+            b.forward(means, prec, logw, depth, alpha)
+            totals, stages = [], []
+            for _ in range(reps):
+                _, _, ms = b.forward_timed(means, prec, logw, depth, alpha)
+                totals.append(sum(ms.values()))
+                stages.append(ms)
+            b.close()
+            med = statistics.median(totals)
+            results.append({"tile": list(tile), "px": px, "chunk": chunk, "ms": med,
+                            "blend_ms": statistics.median(s["blend"] for s in stages)})
+        best = min(results, key=lambda r: r["ms"])
+        key = bucket(scenes, views)
+        with self._lock:
+            self.table[key] = {"tile": best["tile"], "px": best["px"], "chunk": best["chunk"],
+                               "ms": best["ms"]}
+            if self.persist:
+                try:
+                    os.makedirs(os.path.dirname(self.path), exist_ok=True)
+                    tmp = self.path + ".tmp"
+                    with open(tmp, "w") as f:
+                        json.dump(self.table, f, indent=1)
+                    os.replace(tmp, self.path)
+                except OSError:
+                    pass
+        return {"tile": tuple(best["tile"]), "px": best["px"], "chunk": best["chunk"],
+                "ms": best["ms"], "candidates": results, "bucket": key}

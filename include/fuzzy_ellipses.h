@@ -60,6 +60,11 @@ typedef enum fe_cull_mode {
 
 /* Flags for fe_render_desc.flags */
 #define FE_FLAG_SAVE_STATS 1u /* write per-pixel softmax statistics needed by the backward */
+/* Bits 8..15 of flags: record pairs per shared-memory stage of the blend (8, 16 or 32; 0 = 16). */
+#define FE_FLAG_CHUNK(pairs) (((uint32_t)(pairs) & 0xffu) << 8)
+/* Batches only: size the key scratch from the device-side key count (one 8-byte readback and a
+ * stream synchronisation per run) instead of the worst case (views x Gaussians x tiles). */
+#define FE_FLAG_EXACT_KEYS 2u
 
 /* Render descriptor: everything a render needs besides the Gaussian and pose buffers. It is also
  * the opaque payload of the XLA custom call targets (bit-copied; the size and magic are checked).
@@ -186,8 +191,12 @@ typedef struct fe_view {
   float fx, fy, cx, cy;
   float quat[4];          /* scalar first */
   float trans[3];
+  uint32_t flags;         /* FE_VIEW_* */
   int64_t pixel_offset;   /* first pixel of this render in the batch output buffers */
 } fe_view;
+
+/* fe_view.flags: the backward skips this view (its cotangents are zero). */
+#define FE_VIEW_NO_GRAD 1u
 
 typedef struct fe_scene {
   int64_t gauss_offset;   /* first Gaussian of the scene in the concatenated arrays */
@@ -203,6 +212,10 @@ typedef struct fe_batch fe_batch;
  * fields are ignored. */
 int fe_batch_create(const fe_render_desc *desc, const fe_scene *scenes, int32_t n_scenes,
                     const fe_view *views, int32_t n_views, fe_batch **out);
+/* Re-plan an existing batch for new scenes/views, reusing (and only growing) its device buffers.
+ * Synchronises `stream` first (the previous run may still read the old tables). */
+int fe_batch_reset(fe_batch *b, const fe_scene *scenes, int32_t n_scenes, const fe_view *views,
+                   int32_t n_views, fe_stream_t stream);
 void fe_batch_destroy(fe_batch *b);
 /* Total output pixels of the batch (sum of H*W). */
 int64_t fe_batch_pixels(const fe_batch *b);
@@ -235,7 +248,8 @@ int fe_batch_fwd_timed(fe_batch *b, const float *d_means, const float *d_prec, c
                        fe_stream_t stream);
 /* Number of kernels one fe_batch_fwd launches. */
 int fe_batch_launch_count(const fe_batch *b);
-/* Pipe-throughput microbenchmark: kind 0 = FP32 FMA, kind 1 = MUFU ex2; operations per second.
+/* Pipe-throughput microbenchmark: kind 0 = FP32 FMA, kind 1 = MUFU ex2, kind 2 = packed f32x2
+ * FMA (two FMAs per instruction); operations per second.
  * Allocates (and frees) 1 MiB of scratch. No reference counterpart. */
 int fe_bench_peak(int kind, int iters, double *ops_per_second, fe_stream_t stream);
 

@@ -1,5 +1,9 @@
 """Batched renders of uneven scenes and cameras equal the plain per-call renders; the batch runs
-without host synchronisation and replays from a CUDA graph."""
+without host synchronisation and replays from a CUDA graph.
+
+The blend evaluates records in pairs taken from the global key list, so a view's records pair
+up differently inside a batch than alone and its float32 sums are associated differently: the
+two agree to rounding (checked at 1e-6), and each is bit-for-bit repeatable."""
 
 import numpy as np
 import pytest
@@ -41,9 +45,11 @@ def test_batch_equals_single_renders(cuda_device, tile):
         for c in cams:
             d1, a1 = fe.render_forward(ms, ps, ws, c.fx, c.fy, c.cx, c.cy, c.quat, c.trans,
                                        c.height, c.width, tile=tile)
-            assert torch.equal(b.view_image(depth, vi), d1)
-            assert torch.equal(b.view_image(alpha, vi), a1)
+            torch.testing.assert_close(b.view_image(depth, vi), d1, rtol=1e-6, atol=1e-7)
+            torch.testing.assert_close(b.view_image(alpha, vi), a1, rtol=0, atol=1e-6)
             vi += 1
+    depth2, alpha2 = b.forward(m, p, w)
+    assert torch.equal(depth2, depth) and torch.equal(alpha2, alpha)
 
 
 def test_batch_backward_equals_sum_of_single(cuda_device):
