@@ -986,3 +986,113 @@ int fe_bench_peak(int kind, int iters, double* ops_per_second, fe_stream_t strea
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------------------------
+// Forward render with fixed scratch (fe_render_fwd_noalloc)
+// ---------------------------------------------------------------------------------------------
+// Some callers cannot allocate device memory while a render runs:
+//  * an XLA/JAX custom call: XLA's allocator reserves most of the device's memory when the
+//    process starts, so a cudaMalloc inside the call can fail although the request is small, and
+//    memory taken there is invisible to XLA's buffer planning;
+//  * latency-bound loops sharing the device with other streams: cudaFree synchronises the whole
+//    device, so an arena that has to grow stalls every stream of the process.
+// For them the whole scratch of one single-view forward render (records, keys, tile records,
+// sort histograms, tile ranges and the control block) lives in one file-scope device array of
+// FE_NOALLOC_SCRATCH_BYTES per device, resolved once per device with cudaGetSymbolAddress.
+// Requests whose worst-case scratch (every Gaussian on every tile) does not fit are rejected on
+// the host with FE_ERR_SCRATCH_LIMIT before any device work, so the key capacity can never
+// overflow on the device. The entry issues kernels and cudaMemsetAsync/cudaMemcpyAsync on the
+// caller's stream only; it calls no allocating routine of CUDA or of any library.
+
+namespace fe {
+namespace {
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[FE_NOALLOC_SCRATCH_BYTES];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_noalloc_mu;
+char* g_noalloc_base[kMaxDevices] = {};
+
+// Device address of the fixed scratch on the current device (resolved on the first call).
+int noalloc_scratch(char** out) {
+  int dev = 0;
+  FE_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= kMaxDevices)
+    return fail(FE_ERR_UNSUPPORTED, "device ordinal " + std::to_string(dev) + " above 63");
+  std::lock_guard<std::mutex> lk(g_noalloc_mu);
+  if (!g_noalloc_base[dev]) {
+    void* p = nullptr;
+    FE_CUDA(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+    g_noalloc_base[dev] = static_cast<char*>(p);
+  }
+  *out = g_noalloc_base[dev];
+  return FE_OK;
+}
+
+}  // namespace
+}  // namespace fe
+
+extern "C" {
+
+int fe_render_fwd_noalloc(const fe_render_desc* d, const float* means, const float* prec,
+                          const float* logw, const float* quat, const float* trans, float* depth,
+                          float* alpha, float* stats, uint32_t* device_error,
+                          fe_stream_t stream_) {
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream_);
+  int rc = check_desc(d);
+  if (rc) return rc;
+  if (!depth || !alpha || !quat || !trans)
+    return fail(FE_ERR_INVALID_ARGUMENT, "NULL output or pose pointer");
+  const int64_t npix = (int64_t)d->height * d->width;
+  if (d->n_gaussians == 0) {
+    FE_CUDA(cudaMemsetAsync(depth, 0, sizeof(float) * npix, st));
+    FE_CUDA(cudaMemsetAsync(alpha, 0, sizeof(float) * npix, st));
+    if (stats) FE_CUDA(cudaMemsetAsync(stats, 0, sizeof(float) * 3 * npix, st));
+    if (device_error) FE_CUDA(cudaMemsetAsync(device_error, 0, sizeof(uint32_t), st));
+    return FE_OK;
+  }
+  if (!means || !prec || !logw) return fail(FE_ERR_INVALID_ARGUMENT, "NULL Gaussian pointer");
+
+  Pipeline p = single_view_pipeline(d, means, prec, logw, quat, trans);
+  const int64_t worst = p.n_rec * p.n_tiles;
+  const size_t rec_bytes = carve_rec(nullptr, p.n_rec, p.n_tiles, p.n_pix, false,
+                                     [](const RecSpace&) {});
+  const size_t key_bytes = carve_keys(nullptr, worst, [](const KeySpace&) {});
+  if (worst > INT64_C(0xffffffff) || rec_bytes + key_bytes > (size_t)FE_NOALLOC_SCRATCH_BYTES)
+    return fail(FE_ERR_SCRATCH_LIMIT,
+                "fe_render_fwd_noalloc: " + std::to_string(p.n_rec) + " Gaussians x " +
+                    std::to_string(p.n_tiles) + " tiles need " +
+                    std::to_string(rec_bytes + key_bytes) +
+                    " bytes of worst-case scratch; the fixed scratch holds " +
+                    std::to_string((size_t)FE_NOALLOC_SCRATCH_BYTES) + " bytes");
+
+  char* base = nullptr;
+  rc = noalloc_scratch(&base);
+  if (rc) return rc;
+  RecSpace rs;
+  KeySpace ks;
+  carve_rec(base, p.n_rec, p.n_tiles, p.n_pix, false, [&](const RecSpace& s) { rs = s; });
+  carve_keys(base + rec_bytes, worst, [&](const KeySpace& s) { ks = s; });
+
+  // Must start at zero on every call: the control block (key counters, device error word and
+  // the blend's tile counter) and the tile ranges (tiles without keys keep an empty range).
+  FE_CUDA(cudaMemsetAsync(rs.ctrl, 0, sizeof(Control), st));
+  FE_CUDA(cudaMemsetAsync(rs.ranges, 0, sizeof(uint2) * (size_t)p.n_tiles, st));
+  launch_preprocess(p.va, p.n_rec, p.means, p.prec, p.logw, p.quat, nullptr, p.trans, p.cull_mode,
+                    p.cull_param, p.tile_w, p.tile_h, rs.recs, rs.rects, rs.touched, st);
+  launch_scan(rs.touched, rs.incl, p.n_rec, worst, rs.scan_tmp, rs.ctrl, st);
+  launch_emit_keys(p.va, rs.incl, rs.rects, p.n_rec, rs.ctrl, ks.keys_a, worst, st);
+  uint64_t* sorted =
+      launch_sort(ks.keys_a, ks.keys_b, bits_for(p.n_tiles), rs.ctrl, worst, ks.hist, st);
+  launch_ranges_gather(p.va, sorted, rs.ctrl, worst, rs.recs, p.tile_w, p.tile_h, rs.ranges,
+                       ks.trec, st);
+  launch_blend_fwd(p.va, p.tile_w, p.tile_h, p.px, p.chunk, p.n_tiles, ks.trec, rs.ranges,
+                   p.beta2, p.beta3, depth, alpha, stats, npix, rs.ctrl, st);
+  if (device_error)
+    FE_CUDA(cudaMemcpyAsync(device_error, &rs.ctrl->error, sizeof(uint32_t),
+                            cudaMemcpyDeviceToDevice, st));
+  FE_CUDA(cudaGetLastError());
+  return FE_OK;
+}
+
+}  // extern "C"

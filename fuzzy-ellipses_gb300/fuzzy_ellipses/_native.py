@@ -88,6 +88,7 @@ PROTOTYPES = {
     "fe_status_string": (ctypes.c_char_p, [ctypes.c_int]),
     "fe_render_desc_init": (None, [ctypes.POINTER(RenderDesc), I32, I32, I32, F32, F32, F32, F32]),
     "fe_render_fwd": (ctypes.c_int, [ctypes.POINTER(RenderDesc)] + [P] * 8 + [P]),
+    "fe_render_fwd_noalloc": (ctypes.c_int, [ctypes.POINTER(RenderDesc)] + [P] * 9 + [P]),
     "fe_render_bwd": (ctypes.c_int, [ctypes.POINTER(RenderDesc)] + [P] * 13 + [P]),
     "fe_render_binning": (ctypes.c_int, [ctypes.POINTER(RenderDesc)] + [P] * 6 + [I64, P,
                                                                                 ctypes.POINTER(I64), P]),

@@ -253,6 +253,29 @@ int fe_batch_launch_count(const fe_batch *b);
  * Allocates (and frees) 1 MiB of scratch. No reference counterpart. */
 int fe_bench_peak(int kind, int iters, double *ops_per_second, fe_stream_t stream);
 
+/* Forward render of one view that allocates nothing: the same pipeline and results as
+ * fe_render_fwd (same arguments), with all scratch in a fixed file-scope device array of
+ * FE_NOALLOC_SCRATCH_BYTES per device instead of the per-(device, stream) arena.
+ * No counterpart in the reference (whose forwardJAX, rasterizer_impl.cu:174-344, takes scratch
+ * from a GpuMemoryPool that calls cudaFree/cudaMalloc whenever a request outgrows it,
+ * rasterizer_impl.cu:47-79). For callers that cannot allocate during a call, e.g. an XLA custom
+ * call under XLA's preallocating allocator.
+ *   Limit: requests whose worst-case scratch (n_gaussians x tiles keys) exceeds
+ *     FE_NOALLOC_SCRATCH_BYTES return FE_ERR_SCRATCH_LIMIT before any device work (96 bytes
+ *     per Gaussian-tile pair, about 1.39M pairs: 1000 Gaussians on a 640x480 image with 16x16
+ *     tiles fit, 1200 do not).
+ *   Set-up: the first call on a device resolves the array's address (cudaGetSymbolAddress) and
+ *     loads the library's kernels; make it during set-up, before any stream capture begins.
+ *   Concurrency: one scratch per device, so calls on one device must not overlap -- issue them
+ *     on one stream or order them; overlapping calls race on the scratch.
+ *   d_device_error: optional device word receiving the call's device-side error (FE_DEVERR_*),
+ *     stream-ordered; NULL to skip. */
+#define FE_NOALLOC_SCRATCH_BYTES (128u << 20)
+int fe_render_fwd_noalloc(const fe_render_desc *desc, const float *d_means, const float *d_prec,
+                          const float *d_logw, const float *d_quat, const float *d_trans,
+                          float *d_depth, float *d_alpha, float *d_stats, uint32_t *d_device_error,
+                          fe_stream_t stream);
+
 /* Synchronise `stream` and return the device-side error word of the arena used by calls on that
  * stream (0 = no error; see FE_DEVERR_*), clearing it. */
 int fe_check_device_status(fe_stream_t stream, uint32_t *device_error);
