@@ -462,22 +462,36 @@ def serve_bench(fe, dev, n_requests=200, plain_requests=60, seed=0):
     renders = sum(len(r.cameras) for r in reqs)
 
     def run(arrival_gaps):
+        # A streaming consumer: each result is taken as it completes (latency recorded, one pixel
+        # read) and released, so the server's pinned result buffers are recycled.
+        lat, done = [], threading.Semaphore(0)
+        lock = threading.Lock()
+
+        def consume(fut):
+            r = fut.result()
+            with lock:
+                lat.append(r.latency)
+                _ = float(r.alpha[0][0, 0])
+            done.release()
+
         with serve.RenderServer(device=dev, lanes=3) as srv:
-            for r in reqs[:6]:
-                srv.submit(r).result()
+            for r in reqs[:4] + [q for q in reqs if q.backward][:4]:
+                srv.submit(r).result(timeout=300)
+            srv.reset_stats()
             t0 = time.perf_counter()
-            futs = []
             for r, gap in zip(reqs, arrival_gaps):
                 if gap > 0:
                     time.sleep(gap)
-                futs.append(srv.submit(r))
-            res = [f.result() for f in futs]
+                srv.submit(r).add_done_callback(consume)
+            for _ in reqs:
+                if not done.acquire(timeout=300):
+                    raise RuntimeError("served request did not complete")
             wall = time.perf_counter() - t0
-            batches = srv.stats()["batches"]
-        lat = sorted(x.latency for x in res)
+            st = srv.stats()
+        lat.sort()
         return {"renders_per_s": renders / wall, "requests_per_s": len(reqs) / wall,
                 "p50_ms": 1e3 * lat[len(lat) // 2], "p99_ms": 1e3 * lat[min(len(lat) - 1, int(0.99 * len(lat)))],
-                "batches": batches, "wall_s": wall}
+                "batches": st["batches"], "wall_s": wall, "lane_busy_s": st["busy_s"]}
 
     sat = run([0.0] * len(reqs))
     rate = 0.5 * sat["requests_per_s"]

@@ -287,6 +287,10 @@ Pipeline single_view_pipeline(const fe_render_desc* d, const float* means, const
 }
 
 }  // namespace
+
+// Error reporting shared with the other host translation units of the library.
+int set_last_error(int code, const std::string& msg) { return fail(code, msg); }
+
 }  // namespace fe
 
 using namespace fe;
@@ -434,6 +438,22 @@ int fe_render_binning(const fe_render_desc* d, const float* means, const float* 
     FE_CUDA(cudaMemcpyAsync(keys, sorted, sizeof(uint64_t) * (size_t)K, cudaMemcpyDeviceToDevice, st));
   FE_CUDA(cudaMemcpyAsync(ranges, rs.ranges, sizeof(uint2) * (size_t)p.n_tiles,
                           cudaMemcpyDeviceToDevice, st));
+  FE_CUDA(cudaGetLastError());
+  return FE_OK;
+}
+
+int fe_silhouette_bce(const float* alpha, const float* target, const int64_t* seg_end,
+                      int32_t n_seg, int64_t n_pix, float* galpha, double* loss,
+                      fe_stream_t stream_) {
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream_);
+  if (n_pix < 0 || n_seg < 0 || (n_pix > 0 && n_seg == 0))
+    return fail(FE_ERR_INVALID_ARGUMENT, "fe_silhouette_bce: bad pixel or segment count");
+  if (n_seg > 0 && (!seg_end || !loss))
+    return fail(FE_ERR_INVALID_ARGUMENT, "fe_silhouette_bce: NULL segment or loss pointer");
+  if (n_pix > 0 && (!alpha || !target || !galpha))
+    return fail(FE_ERR_INVALID_ARGUMENT, "fe_silhouette_bce: NULL pixel buffer");
+  if (n_seg > 0) FE_CUDA(cudaMemsetAsync(loss, 0, sizeof(double) * (size_t)n_seg, st));
+  launch_silhouette_bce(alpha, target, seg_end, n_seg, n_pix, galpha, loss, st);
   FE_CUDA(cudaGetLastError());
   return FE_OK;
 }
@@ -752,7 +772,10 @@ int commit_batch(fe_batch* b, cudaStream_t st) {
     if (rc) return rc;
     carve_keys(b->keys.ptr, b->cap, [&](const KeySpace& s_) { b->ks = s_; });
   }
-  FE_CUDA(cudaStreamSynchronize(st));  // host tables may be rewritten by the next reset
+  // Host tables may be rewritten right away: a copy from pageable memory returns once its
+  // source is staged. Creation uploads on the legacy stream, which does not order the caller's
+  // non-blocking streams, so it waits for the upload.
+  if (!st) FE_CUDA(cudaStreamSynchronize(st));
   return FE_OK;
 }
 
@@ -798,7 +821,8 @@ int fe_batch_reset(fe_batch* b, const fe_scene* scenes, int32_t n_scenes, const 
                    int32_t n_views, fe_stream_t stream_) {
   if (!b) return fail(FE_ERR_INVALID_ARGUMENT, "NULL batch");
   cudaStream_t st = reinterpret_cast<cudaStream_t>(stream_);
-  FE_CUDA(cudaStreamSynchronize(st));  // the previous run may still read the tables
+  // No synchronisation: the new tables reach the device by copies ordered on `st` after the
+  // previous run, and buffers that must grow wait for `st` before they are freed.
   int rc = plan_batch(b, scenes, n_scenes, views, n_views);
   if (rc) return rc;
   return commit_batch(b, st);

@@ -67,4 +67,12 @@ void launch_record_vjp(const ViewsArg& va, int64_t n_rec, const float* means, co
                        const RecGrad* rgrad, float* gmeans, float* gprec, float* glogw,
                        cudaStream_t st);
 
+// loss.cu
+// Silhouette BCE of renders stored back to back (render s = pixels [seg_end[s-1], seg_end[s]),
+// seg_end on the device, increasing, seg_end[n_seg-1] == n_pix): adds each render's mean loss to
+// loss[s] (float64, zeroed by the caller) and writes dL_s/dalpha to galpha.
+void launch_silhouette_bce(const float* alpha, const float* target, const int64_t* seg_end,
+                           int n_seg, int64_t n_pix, float* galpha, double* loss,
+                           cudaStream_t st);
+
 }  // namespace fe

@@ -10,6 +10,8 @@ import ctypes
 import os
 import threading
 
+import numpy as np
+
 _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "_lib", "libfuzzy_ellipses.so")
 
@@ -21,6 +23,7 @@ FE_DEVERR_CAPACITY = 1
 FE_DEVERR_TIMEOUT = 2
 FE_FLAG_EXACT_KEYS = 2
 FE_VIEW_NO_GRAD = 1
+FE_ERR_OUT_OF_MEMORY = 4
 
 
 def flag_chunk(pairs):
@@ -71,9 +74,47 @@ class View(ctypes.Structure):
                 ("flags", ctypes.c_uint32), ("pixel_offset", ctypes.c_int64)]
 
 
+# numpy mirror of fe_view: a structured array of this dtype is passed to the library as is.
+VIEW_DTYPE = np.dtype(View)
+
+
 class SceneEntry(ctypes.Structure):
     """Mirror of ``fe_scene``."""
     _fields_ = [("gauss_offset", ctypes.c_int64), ("n", ctypes.c_int32), ("reserved", ctypes.c_int32)]
+
+
+class ServerConfig(ctypes.Structure):
+    """Mirror of ``fe_server_config``."""
+    _fields_ = [("lanes", ctypes.c_int32), ("max_batch_views", ctypes.c_int32),
+                ("max_batch_pixels", ctypes.c_int64), ("hbm_budget_bytes", ctypes.c_int64),
+                ("desc", RenderDesc)]
+
+
+class Request(ctypes.Structure):
+    """Mirror of ``fe_request``."""
+    _fields_ = [("n_gaussians", ctypes.c_int32), ("n_views", ctypes.c_int32),
+                ("means", ctypes.c_void_p), ("prec", ctypes.c_void_p), ("logw", ctypes.c_void_p),
+                ("views", ctypes.c_void_p), ("targets", ctypes.c_void_p),
+                ("depth", ctypes.c_void_p), ("alpha", ctypes.c_void_p),
+                ("grad_means", ctypes.c_void_p), ("grad_prec", ctypes.c_void_p),
+                ("grad_logw", ctypes.c_void_p), ("loss", ctypes.c_void_p),
+                ("user_tag", ctypes.c_uint64)]
+
+
+class Completion(ctypes.Structure):
+    """Mirror of ``fe_completion``."""
+    _fields_ = [("id", ctypes.c_uint64), ("user_tag", ctypes.c_uint64), ("status", ctypes.c_int32),
+                ("n_views", ctypes.c_int32), ("submitted_s", ctypes.c_double),
+                ("started_s", ctypes.c_double), ("finished_s", ctypes.c_double),
+                ("message", ctypes.c_char * 160)]
+
+
+class ServerStats(ctypes.Structure):
+    """Mirror of ``fe_server_stats``."""
+    _fields_ = [("submitted", ctypes.c_int64), ("completed", ctypes.c_int64),
+                ("renders", ctypes.c_int64), ("batches", ctypes.c_int64),
+                ("queued", ctypes.c_int64), ("p50_latency_s", ctypes.c_double),
+                ("p99_latency_s", ctypes.c_double), ("busy_s", ctypes.c_double)]
 
 
 P = ctypes.c_void_p
@@ -89,6 +130,7 @@ PROTOTYPES = {
     "fe_render_desc_init": (None, [ctypes.POINTER(RenderDesc), I32, I32, I32, F32, F32, F32, F32]),
     "fe_render_fwd": (ctypes.c_int, [ctypes.POINTER(RenderDesc)] + [P] * 8 + [P]),
     "fe_render_fwd_noalloc": (ctypes.c_int, [ctypes.POINTER(RenderDesc)] + [P] * 9 + [P]),
+    "fe_silhouette_bce": (ctypes.c_int, [P, P, P, I32, I64, P, P, P]),
     "fe_render_bwd": (ctypes.c_int, [ctypes.POINTER(RenderDesc)] + [P] * 13 + [P]),
     "fe_render_binning": (ctypes.c_int, [ctypes.POINTER(RenderDesc)] + [P] * 6 + [I64, P,
                                                                                 ctypes.POINTER(I64), P]),
@@ -112,6 +154,15 @@ PROTOTYPES = {
     "fe_batch_fwd_timed": (ctypes.c_int, [P] + [P] * 6 + [ctypes.POINTER(ctypes.c_float), P]),
     "fe_batch_launch_count": (ctypes.c_int, [P]),
     "fe_bench_peak": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_double), P]),
+    "fe_server_config_init": (None, [ctypes.POINTER(ServerConfig)]),
+    "fe_server_create": (ctypes.c_int, [ctypes.POINTER(ServerConfig), ctypes.c_int, ctypes.POINTER(P)]),
+    "fe_server_submit": (ctypes.c_int, [P, ctypes.POINTER(Request), ctypes.POINTER(ctypes.c_uint64)]),
+    "fe_server_wait": (ctypes.c_int, [P, ctypes.POINTER(Completion), I32, I32, ctypes.POINTER(I32)]),
+    "fe_server_stats_get": (ctypes.c_int, [P, ctypes.POINTER(ServerStats)]),
+    "fe_server_stats_reset": (None, [P]),
+    "fe_server_close": (ctypes.c_int, [P]),
+    "fe_server_destroy": (None, [P]),
+    "fe_request_footprint": (I64, [ctypes.POINTER(Request), I32, I32]),
 }
 
 _lib = None

@@ -147,6 +147,30 @@ def render_binning(means, prec, logw, fx, fy, cx, cy, quat, t, height, width, *,
     return keys[:nk.value], ranges.to(torch.int64) & 0xFFFFFFFF
 
 
+def silhouette_bce(alpha, target, seg_end, galpha=None, loss=None):
+    """Per-render mean silhouette BCE and its alpha cotangent in one kernel.
+
+    ``alpha``/``target``: flat float32 device buffers of the renders stored back to back;
+    ``seg_end``: int64 device tensor of each render's end pixel (the last equals alpha's size).
+    Returns ``(loss (R,) float64, galpha)`` with galpha = dL_r/dalpha per pixel (the loss of the
+    reference's shape-from-silhouette loop, shape_from_silhouette.ipynb cell 12)."""
+    lib = N.load()
+    n_pix = alpha.numel()
+    if target.numel() != n_pix or not (alpha.is_contiguous() and target.is_contiguous()):
+        raise ValueError("alpha and target must be contiguous with the same size")
+    if alpha.dtype != torch.float32 or target.dtype != torch.float32:
+        raise ValueError("alpha and target must be float32")
+    if seg_end.dtype != torch.int64 or not seg_end.is_contiguous():
+        raise ValueError("seg_end must be a contiguous int64 tensor")
+    if galpha is None:
+        galpha = torch.empty_like(alpha)
+    if loss is None:
+        loss = torch.empty(seg_end.numel(), dtype=torch.float64, device=alpha.device)
+    N.check(lib.fe_silhouette_bce(_ptr(alpha), _ptr(target), _ptr(seg_end), seg_end.numel(),
+                                  n_pix, _ptr(galpha), _ptr(loss), _stream()))
+    return loss, galpha
+
+
 def bench_peak(kind):
     """Measured pipe throughput (operations/s): 'fma' (FP32 FMA), 'ex2' (MUFU ex2) or 'fma2'
     (packed f32x2 FMA, two FMAs per instruction)."""
@@ -279,7 +303,9 @@ class Batch:
 
     ``scenes``: list of (gauss_offset, n) into concatenated Gaussian arrays.
     ``views``: list of dicts with keys scene, height, width, fx, fy, cx, cy, quat, trans and
-    optionally pixel_offset (default: packed in order) and no_grad (skip in the backward).
+    optionally pixel_offset (default: packed in order) and no_grad (skip in the backward); or a
+    structured array of ``_native.VIEW_DTYPE`` (the C ``fe_view`` layout, flags included), whose
+    renders are always packed in order (its pixel_offset field is overwritten).
     By default the plan reserves scratch for the worst-case key count, so ``forward`` performs no
     host synchronisation and can be captured in a CUDA graph; ``exact_keys=True`` sizes the key
     scratch from the device-side count instead (one 8-byte readback per run).
@@ -305,6 +331,8 @@ class Batch:
         for i, (off, n) in enumerate(scenes):
             sc[i].gauss_offset = int(off)
             sc[i].n = int(n)
+        if isinstance(views, np.ndarray):
+            return (sc, len(scenes)) + self._array_tables(views)
         vs = (N.View * max(1, len(views)))()
         off = 0
         self.pixel_offsets = []
@@ -326,6 +354,18 @@ class Batch:
             self.shapes.append((int(v["height"]), int(v["width"])))
             off = max(off, po + int(v["height"]) * int(v["width"]))
         return sc, len(scenes), vs, len(views)
+
+    def _array_tables(self, views):
+        arr = np.require(views, dtype=N.VIEW_DTYPE, requirements=["C", "W"])
+        h = arr["height"].astype(np.int64)
+        w = arr["width"].astype(np.int64)
+        ends = np.cumsum(h * w)
+        arr["pixel_offset"] = ends - h * w
+        self.pixel_offsets = arr["pixel_offset"].tolist()
+        self.shapes = list(zip(h.tolist(), w.tolist()))
+        if len(arr) == 0:
+            return (N.View * 1)(), 0
+        return (N.View * len(arr)).from_buffer(arr), len(arr)
 
     def _sizes(self):
         lib = N.load()

@@ -1,18 +1,16 @@
-"""Continuous-batching render server.
+"""Continuous-batching render server: a Python front end of the native server (``fe_server_*``).
 
 Requests (a scene of Gaussians plus 1..k cameras; optionally target silhouettes, which turns the
 request into forward + backward of the silhouette binary cross-entropy, as the reference's
 shape-from-silhouette loop computes with ``jax.grad``, shape_from_silhouette.ipynb cell 12)
-arrive at any time through ``submit``. The server
-
-* admits a request when its estimated device footprint fits the HBM budget, uploading its scene
-  parameters to the device once (they stay resident until the request completes);
-* runs ``lanes`` worker threads, each with its own CUDA stream and reusable batch plan
-  (``Batch.reset`` grows its scratch only); a free lane takes every admitted request that fits its
-  view and pixel limits, in arrival order, and renders them as one batch, so requests that arrive
-  while other batches are on the GPU join the next batch and batches overlap on the device;
-* returns per-request depth/alpha images (and loss and gradients) through futures and records
-  each request's latency (submission to completion).
+arrive at any time through ``submit`` and complete through futures. The batching runs in the
+library's own lane threads (no Python, no GIL): each lane has a CUDA stream and a reusable batch
+plan; a free lane takes the queued requests in arrival order while they fit its view and pixel
+limits and the HBM budget (estimated device bytes of all in-flight batches), renders them as one
+batch, evaluates the loss and backward of the backward requests in the same batch, and writes
+every output straight into the request's own NumPy arrays. This front end validates requests,
+allocates their outputs, keeps their arrays alive until completion and resolves the futures from
+one collector thread.
 
 A request's results do not depend on which other requests shared its batch beyond float32
 rounding (tested to 1e-6).
@@ -20,20 +18,19 @@ rounding (tested to 1e-6).
 
 from __future__ import annotations
 
-import collections
 import concurrent.futures
+import ctypes
 import dataclasses
 import math
 import threading
-import time
 
 import numpy as np
 import torch
 
-from . import api
+from . import _native as N
 
 __all__ = ["RenderRequest", "RenderResult", "RenderServer", "estimate_footprint",
-           "bce_alpha_grad"]
+           "bce_alpha_grad", "bce_terms"]
 
 CLIP_ALPHA = 3e-8
 
@@ -73,7 +70,8 @@ class RenderResult:
 
 
 def estimate_footprint(req, tile=16):
-    """Upper estimate of a request's device bytes (scene, records, keys, outputs)."""
+    """Upper estimate of a request's device bytes (scene, records, keys, outputs); the same
+    formula as the library's admission unit ``fe_request_footprint``."""
     n, views = req.n, len(req.cameras)
     pix = sum(c.height * c.width for c in req.cameras)
     tiles = sum(math.ceil(c.height / tile) * math.ceil(c.width / tile) for c in req.cameras)
@@ -82,10 +80,10 @@ def estimate_footprint(req, tile=16):
     return 52 * n + views * n * (96 + 16 + (96 if req.backward else 0)) + 88 * keys + per_pix * pix
 
 
-def bce_alpha_grad(alpha, target, count):
-    """d/dalpha of mean(-(t log a + (1-t) log(1-a))) with a clamped to [3e-8, 1-3e-8]
-    (shape_from_silhouette.ipynb cell 12); the gradient is zero where the clamp is active.
-    Returns (loss_sum, grad) with the gradient in float32.
+def bce_terms(alpha, target):
+    """Per-pixel silhouette BCE -(t log a + (1-t) log(1-a)) with a clamped to [3e-8, 1-3e-8]
+    (shape_from_silhouette.ipynb cell 12) and its derivative in alpha (zero where the clamp is
+    active), both float64.
 
     Evaluated in float64: in float32 the upper bound 1-3e-8 rounds to 1.0, so the clamp would
     leave saturated pixels (alpha == 1.0, which the render produces once the summed weight
@@ -93,228 +91,190 @@ def bce_alpha_grad(alpha, target, count):
     a64 = alpha.double()
     t64 = target.double()
     a = a64.clamp(CLIP_ALPHA, 1.0 - CLIP_ALPHA)
-    loss = -(t64 * torch.log(a) + (1.0 - t64) * torch.log(1.0 - a)).sum()
+    terms = -(t64 * torch.log(a) + (1.0 - t64) * torch.log(1.0 - a))
     inside = (a64 > CLIP_ALPHA) & (a64 < 1.0 - CLIP_ALPHA)
-    g = torch.where(inside, (-t64 / a + (1.0 - t64) / (1.0 - a)) / count,
-                    torch.zeros_like(a))
-    return loss, g.float()
+    d = torch.where(inside, -t64 / a + (1.0 - t64) / (1.0 - a), torch.zeros_like(a))
+    return terms, d
 
 
-class _Admitted:
-    __slots__ = ("req", "future", "submitted", "bytes", "dev", "ready", "tgt", "host")
+def bce_alpha_grad(alpha, target, count):
+    """Loss sum and float32 gradient of mean-over-``count`` BCE (see ``bce_terms``)."""
+    terms, d = bce_terms(alpha, target)
+    return terms.sum(), (d / count).float()
 
-    def __init__(self, req, future, submitted, nbytes):
-        self.req, self.future, self.submitted, self.bytes = req, future, submitted, nbytes
-        self.dev = None
-        self.ready = None
-        self.tgt = None
-        self.host = None  # pinned staging, kept alive until the upload has run
+
+def _validate(req):
+    """Reject a malformed request at submission, before it can share a batch with others."""
+    n = req.n
+    if req.means.shape != (n, 3) or np.shape(req.prec) != (n, 3, 3) or np.shape(req.logw) != (n,):
+        raise ValueError("means, prec and logw must have shapes (N,3), (N,3,3) and (N,)")
+    if not req.cameras:
+        raise ValueError("a request needs at least one camera")
+    for c in req.cameras:
+        if not (int(c.height) >= 1 and int(c.width) >= 1):
+            raise ValueError("camera image sizes must be positive")
+        if not (math.isfinite(c.fx) and math.isfinite(c.fy) and c.fx != 0 and c.fy != 0):
+            raise ValueError("camera focal lengths must be finite and non-zero")
+    if req.targets is not None:
+        if len(req.targets) != len(req.cameras):
+            raise ValueError("one target silhouette per camera")
+        for t, c in zip(req.targets, req.cameras):
+            if np.shape(t) != (c.height, c.width):
+                raise ValueError("target silhouette shape must be (height, width) of its camera")
+
+
+def _view_table(req):
+    """The request's cameras as an ``fe_view`` structured array (scene and flags set per batch)."""
+    cams = req.cameras
+    v = np.zeros(len(cams), N.VIEW_DTYPE)
+    v["height"] = [c.height for c in cams]
+    v["width"] = [c.width for c in cams]
+    v["fx"] = [c.fx for c in cams]
+    v["fy"] = [c.fy for c in cams]
+    v["cx"] = [c.cx for c in cams]
+    v["cy"] = [c.cy for c in cams]
+    v["quat"] = np.asarray([np.asarray(c.quat, np.float32) for c in cams]).reshape(-1, 4)
+    v["trans"] = np.asarray([np.asarray(c.trans, np.float32) for c in cams]).reshape(-1, 3)
+    if not req.backward:
+        v["flags"] = N.FE_VIEW_NO_GRAD
+    return v
 
 
 class RenderServer:
     def __init__(self, device=None, hbm_budget_bytes=16 << 30, max_batch_views=1024,
                  max_batch_pixels=48 << 20, lanes=2, tile=(16, 16), px=0, chunk=0,
                  beta2=21.4, beta3=2.66, cull="eps", cull_param=None):
-        self.device = (torch.device("cuda", torch.cuda.current_device()) if device is None
-                       else torch.device(device))
-        self.budget = int(hbm_budget_bytes)
-        self.max_views = int(max_batch_views)
-        self.max_pixels = int(max_batch_pixels)
-        self.cfg = dict(tile=tuple(tile), px=px, chunk=chunk, beta2=beta2, beta3=beta3,
-                        cull=cull, cull_param=cull_param)
-        self._lock = threading.Condition()
-        self._pending = collections.deque()   # waiting for budget
-        self._ready = collections.deque()     # admitted, waiting for a lane
-        self._in_use = 0
+        dev = torch.device("cuda" if device is None else device)
+        if dev.type != "cuda":
+            raise ValueError(f"RenderServer needs a CUDA device, got {dev}")
+        self.device = dev if dev.index is not None else torch.device(
+            "cuda", torch.cuda.current_device())
+        self.tile = tuple(tile)
+        lib = N.load()
+        cfg = N.ServerConfig()
+        lib.fe_server_config_init(ctypes.byref(cfg))
+        cfg.lanes = int(lanes)
+        cfg.max_batch_views = int(max_batch_views)
+        cfg.max_batch_pixels = int(max_batch_pixels)
+        cfg.hbm_budget_bytes = int(hbm_budget_bytes)
+        cfg.desc = N.make_desc(0, 1, 1, 1.0, 1.0, 0.0, 0.0, beta2, beta3, cull, cull_param, tile,
+                               flags=N.flag_chunk(chunk), px=px)
+        h = ctypes.c_void_p()
+        N.check(lib.fe_server_create(ctypes.byref(cfg), self.device.index, ctypes.byref(h)))
+        self._h = h
+        self._lock = threading.Lock()
+        self._inflight = {}   # user tag -> (future, request, outputs, keep-alive objects)
+        self._tag = 0
         self._closed = False
-        self._upload_stream = torch.cuda.Stream(device=self.device)
-        self.latencies = []
-        self.completed = 0
-        self.renders = 0
-        self.batches = 0
-        self._lanes = [threading.Thread(target=self._lane, args=(i,), daemon=True)
-                       for i in range(lanes)]
-        for t in self._lanes:
-            t.start()
+        self._collector = threading.Thread(target=self._collect, daemon=True)
+        self._collector.start()
 
-    # -- submission and admission ------------------------------------------------------------
+    # -- submission ------------------------------------------------------------------------------
     def submit(self, req: RenderRequest) -> concurrent.futures.Future:
+        _validate(req)
+        if self._closed:
+            raise RuntimeError("server is closed")
+        n = req.n
+        means = np.ascontiguousarray(req.means, dtype=np.float32)
+        prec = np.ascontiguousarray(req.prec, dtype=np.float32)
+        logw = np.ascontiguousarray(req.logw, dtype=np.float32)
+        views = _view_table(req)
+        pixels = int((views["height"].astype(np.int64) * views["width"]).sum())
+        out = {"depth": np.empty(pixels, np.float32), "alpha": np.empty(pixels, np.float32)}
+        keep = [means, prec, logw, views]
+        r = N.Request()
+        r.n_gaussians, r.n_views = n, len(req.cameras)
+        r.means, r.prec, r.logw = means.ctypes.data, prec.ctypes.data, logw.ctypes.data
+        r.views = views.ctypes.data
+        r.depth, r.alpha = out["depth"].ctypes.data, out["alpha"].ctypes.data
+        if req.backward:
+            targets = [np.ascontiguousarray(t, dtype=np.float32) for t in req.targets]
+            tptr = (ctypes.c_void_p * len(targets))(*[t.ctypes.data for t in targets])
+            keep += [targets, tptr]
+            out.update(grad_means=np.empty((n, 3), np.float32),
+                       grad_prec=np.empty((n, 3, 3), np.float32),
+                       grad_logw=np.empty(n, np.float32), loss=np.empty(1, np.float64))
+            r.targets = ctypes.cast(tptr, ctypes.c_void_p)
+            r.grad_means = out["grad_means"].ctypes.data
+            r.grad_prec = out["grad_prec"].ctypes.data
+            r.grad_logw = out["grad_logw"].ctypes.data
+            r.loss = out["loss"].ctypes.data
         fut = concurrent.futures.Future()
-        nbytes = estimate_footprint(req, self.cfg["tile"][0])
-        item = _Admitted(req, fut, time.perf_counter(), nbytes)
         with self._lock:
-            if self._closed:
-                raise RuntimeError("server is closed")
-            if nbytes > self.budget:
-                fut.set_exception(MemoryError(
-                    f"request needs ~{nbytes} device bytes, over the budget {self.budget}"))
+            self._tag += 1
+            tag = self._tag
+            self._inflight[tag] = (fut, req, out, keep)
+        r.user_tag = tag
+        rid = ctypes.c_uint64()
+        rc = N.load().fe_server_submit(self._h, ctypes.byref(r), ctypes.byref(rid))
+        if rc != 0:
+            with self._lock:
+                self._inflight.pop(tag, None)
+            msg = N.load().fe_last_error_message().decode(errors="replace")
+            if rc == N.FE_ERR_OUT_OF_MEMORY:
+                fut.set_exception(MemoryError(msg))
                 return fut
-            self._pending.append(item)
-            self._admit_locked()
+            raise N.FEError(rc, msg)
         return fut
 
-    def _admit_locked(self):
-        while self._pending and self._in_use + self._pending[0].bytes <= self.budget:
-            item = self._pending.popleft()
-            self._in_use += item.bytes
-            self._upload(item)
-            self._ready.append(item)
-            self._lock.notify_all()
-
-    def _upload(self, item):
-        # Scene parameters (and targets) go to the device once, on the upload stream.
-        req = item.req
-        with torch.cuda.stream(self._upload_stream):
-            host = [torch.from_numpy(np.ascontiguousarray(x, dtype=np.float32)).pin_memory()
-                    for x in (req.means, req.prec, req.logw)]
-            item.dev = [h.to(self.device, non_blocking=True) for h in host]
-            if req.targets is not None:
-                t = np.concatenate([np.asarray(x, np.float32).ravel() for x in req.targets])
-                host.append(torch.from_numpy(t).pin_memory())
-                item.tgt = host[-1].to(self.device, non_blocking=True)
-            ev = torch.cuda.Event()
-            ev.record(self._upload_stream)
-        item.ready = ev
-        item.host = host
-
-    # -- lanes ---------------------------------------------------------------------------------
-    def _take_batch(self):
-        with self._lock:
-            while not self._ready and not self._closed:
-                self._lock.wait()
-            if not self._ready:
-                return None
-            batch, views, pixels = [], 0, 0
-            while self._ready:
-                r = self._ready[0].req
-                nv = len(r.cameras)
-                npx = sum(c.height * c.width for c in r.cameras)
-                if batch and (views + nv > self.max_views or pixels + npx > self.max_pixels):
-                    break
-                batch.append(self._ready.popleft())
-                views += nv
-                pixels += npx
-            return batch
-
-    def _lane(self, lane_id):
-        torch.cuda.set_device(self.device)
-        stream = torch.cuda.Stream(device=self.device)
-        plan = None
+    # -- completions -----------------------------------------------------------------------------
+    def _collect(self):
+        lib = N.load()
+        buf = (N.Completion * 64)()
+        count = ctypes.c_int32()
         while True:
-            items = self._take_batch()
-            if items is None:
-                break
-            started = time.perf_counter()
-            try:
-                with torch.cuda.stream(stream):
-                    plan = self._run(items, plan, stream, started)
-            except Exception as e:  # deliver the failure to every request of the batch
-                for it in items:
-                    if not it.future.done():
-                        it.future.set_exception(e)
-            with self._lock:
-                for it in items:
-                    self._in_use -= it.bytes
-                self._admit_locked()
-        if plan is not None:
-            plan.close()
-
-    def _run(self, items, plan, stream, started):
-        for it in items:
-            stream.wait_event(it.ready)
-        scenes, views, off = [], [], 0
-        for si, it in enumerate(items):
-            scenes.append((off, it.req.n))
-            off += it.req.n
-            for c in it.req.cameras:
-                views.append(dict(scene=si, height=c.height, width=c.width, fx=c.fx, fy=c.fy,
-                                  cx=c.cx, cy=c.cy, quat=c.quat, trans=c.trans,
-                                  no_grad=not it.req.backward))
-        means = torch.cat([it.dev[0] for it in items])
-        prec = torch.cat([it.dev[1] for it in items])
-        logw = torch.cat([it.dev[2] for it in items])
-        cfg = self.cfg
-        if plan is None:
-            plan = api.Batch(scenes, views, cfg["beta2"], cfg["beta3"], cull=cfg["cull"],
-                             cull_param=cfg["cull_param"], tile=cfg["tile"], px=cfg["px"],
-                             chunk=cfg["chunk"], exact_keys=True)
-        else:
-            plan.reset(scenes, views)
-        any_bwd = any(it.req.backward for it in items)
-        npx = plan.n_pixels
-        depth = torch.empty(npx, device=self.device)
-        alpha = torch.empty(npx, device=self.device)
-        stats = torch.empty(3 * npx, device=self.device) if any_bwd else None
-        plan.forward(means, prec, logw, depth, alpha, stats)
-        losses = {}
-        grads = None
-        if any_bwd:
-            galpha = torch.zeros(npx, device=self.device)
-            vi = 0
-            for k, it in enumerate(items):
-                nv = len(it.req.cameras)
-                if it.req.backward:
-                    lo = plan.pixel_offsets[vi]
-                    hi = plan.pixel_offsets[vi + nv - 1] + plan.shapes[vi + nv - 1][0] * plan.shapes[vi + nv - 1][1]
-                    loss, g = bce_alpha_grad(alpha[lo:hi], it.tgt, hi - lo)
-                    galpha[lo:hi] = g
-                    losses[k] = loss / (hi - lo)
-                vi += nv
-            grads = plan.backward(means, prec, logw, depth, alpha, stats, None, galpha)
-        # Results to pinned host memory, then complete the futures.
-        depth_h = torch.empty(npx, dtype=torch.float32, pin_memory=True)
-        alpha_h = torch.empty(npx, dtype=torch.float32, pin_memory=True)
-        depth_h.copy_(depth, non_blocking=True)
-        alpha_h.copy_(alpha, non_blocking=True)
-        if grads is not None:
-            grads_h = [torch.empty(g.shape, dtype=torch.float32, pin_memory=True) for g in grads]
-            for h, g in zip(grads_h, grads):
-                h.copy_(g, non_blocking=True)
-            loss_h = {k: v.to("cpu", non_blocking=True) for k, v in losses.items()}
-        stream.synchronize()
-        finished = time.perf_counter()
-        dn, an = depth_h.numpy(), alpha_h.numpy()
-        vi, goff = 0, 0
-        for k, it in enumerate(items):
-            d_list, a_list = [], []
-            for c in it.req.cameras:
-                lo = plan.pixel_offsets[vi]
-                h, w = plan.shapes[vi]
-                d_list.append(dn[lo:lo + h * w].reshape(h, w).copy())
-                a_list.append(an[lo:lo + h * w].reshape(h, w).copy())
-                vi += 1
-            n = it.req.n
-            res = RenderResult(d_list, a_list, None, None, None, None, it.submitted, started,
-                               finished)
-            if it.req.backward:
-                res.loss = float(loss_h[k])
-                res.grad_means = grads_h[0][goff:goff + n].numpy().copy()
-                res.grad_prec = grads_h[1][goff:goff + n].numpy().copy()
-                res.grad_logw = grads_h[2][goff:goff + n].numpy().copy()
-            goff += n
-            with self._lock:
-                self.latencies.append(res.latency)
-                self.completed += 1
-                self.renders += len(it.req.cameras)
-            it.future.set_result(res)
-        with self._lock:
-            self.batches += 1
-        return plan
+            N.check(lib.fe_server_wait(self._h, buf, 64, 200, ctypes.byref(count)))
+            if count.value < 0:
+                return
+            for i in range(count.value):
+                c = buf[i]
+                with self._lock:
+                    fut, req, out, _ = self._inflight.pop(c.user_tag)
+                if c.status != 0:
+                    fut.set_exception(N.FEError(c.status, c.message.decode(errors="replace")))
+                    continue
+                d_list, a_list, o = [], [], 0
+                for cam in req.cameras:
+                    hw = cam.height * cam.width
+                    d_list.append(out["depth"][o:o + hw].reshape(cam.height, cam.width))
+                    a_list.append(out["alpha"][o:o + hw].reshape(cam.height, cam.width))
+                    o += hw
+                res = RenderResult(d_list, a_list, None, None, None, None, c.submitted_s,
+                                   c.started_s, c.finished_s)
+                if req.backward:
+                    res.loss = float(out["loss"][0])
+                    res.grad_means = out["grad_means"]
+                    res.grad_prec = out["grad_prec"]
+                    res.grad_logw = out["grad_logw"]
+                fut.set_result(res)
 
     # -- reporting and shutdown ----------------------------------------------------------------
     def stats(self):
-        with self._lock:
-            lat = sorted(self.latencies)
-        q = (lambda p: lat[min(len(lat) - 1, int(p * len(lat)))] if lat else None)
-        return {"completed": self.completed, "renders": self.renders, "batches": self.batches,
-                "p50_s": q(0.50), "p99_s": q(0.99)}
+        st = N.ServerStats()
+        N.check(N.load().fe_server_stats_get(self._h, ctypes.byref(st)))
+        return {"submitted": st.submitted, "completed": st.completed, "renders": st.renders,
+                "batches": st.batches, "queued": st.queued, "p50_s": st.p50_latency_s,
+                "p99_s": st.p99_latency_s, "busy_s": st.busy_s}
+
+    def reset_stats(self):
+        """Forget latencies and counters (e.g. after a warm-up)."""
+        N.load().fe_server_stats_reset(self._h)
 
     def close(self):
-        with self._lock:
-            self._closed = True
-            self._lock.notify_all()
-        for t in self._lanes:
-            t.join()
+        if self._closed:
+            return
+        self._closed = True
+        lib = N.load()
+        N.check(lib.fe_server_close(self._h))   # finishes the queued requests
+        self._collector.join()
+        lib.fe_server_destroy(self._h)
+        self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
     def __enter__(self):
         return self

@@ -213,7 +213,9 @@ typedef struct fe_batch fe_batch;
 int fe_batch_create(const fe_render_desc *desc, const fe_scene *scenes, int32_t n_scenes,
                     const fe_view *views, int32_t n_views, fe_batch **out);
 /* Re-plan an existing batch for new scenes/views, reusing (and only growing) its device buffers.
- * Synchronises `stream` first (the previous run may still read the old tables). */
+ * Does not synchronise: the new tables are uploaded on `stream`, ordered after the batch's
+ * previous runs, so a batch's runs and resets must be issued on one stream (or ordered by the
+ * caller). Buffers that must grow wait for `stream` before the old ones are freed. */
 int fe_batch_reset(fe_batch *b, const fe_scene *scenes, int32_t n_scenes, const fe_view *views,
                    int32_t n_views, fe_stream_t stream);
 void fe_batch_destroy(fe_batch *b);
@@ -248,6 +250,79 @@ int fe_batch_fwd_timed(fe_batch *b, const float *d_means, const float *d_prec, c
                        fe_stream_t stream);
 /* Number of kernels one fe_batch_fwd launches. */
 int fe_batch_launch_count(const fe_batch *b);
+/* ---------------------------------------------------------------------------------------------
+ * Continuous-batching render server. No reference counterpart: the reference renders one camera
+ * per call (rasterize_main.cu:29-114) and leaves batching and serving to the caller.
+ * Requests (one scene of Gaussians, 1..k cameras, optionally per-camera target silhouettes that
+ * add the silhouette-BCE loss and its gradients) are queued by fe_server_submit and rendered by
+ * `lanes` worker threads, each with its own CUDA stream and batch plan: a free lane takes the
+ * queued requests in arrival order while they fit its view and pixel limits and the HBM budget,
+ * and renders them as one batch (fe_batch_*), so concurrent requests share launches. Inputs are
+ * read from, and outputs written to, the caller's host memory directly; both must stay valid
+ * until the request's completion is returned by fe_server_wait.
+ * ------------------------------------------------------------------------------------------- */
+typedef struct fe_server fe_server;
+
+typedef struct fe_server_config {
+  int32_t lanes;             /* worker threads (streams), >= 1 */
+  int32_t max_batch_views;   /* cameras per batch */
+  int64_t max_batch_pixels;  /* output pixels per batch */
+  int64_t hbm_budget_bytes;  /* estimated device bytes of all in-flight batches together */
+  fe_render_desc desc;       /* beta2/beta3, cull, tile, px_per_thread, chunk flags; sizes ignored */
+} fe_server_config;
+
+typedef struct fe_request {
+  int32_t n_gaussians;
+  int32_t n_views;
+  const float *means;              /* host (N,3) */
+  const float *prec;               /* host (N,3,3) upper-triangular factor */
+  const float *logw;               /* host (N) */
+  const fe_view *views;            /* n_views cameras; scene, flags, pixel_offset are ignored */
+  const float *const *targets;     /* NULL: forward only; else n_views host (H,W) silhouettes */
+  float *depth;                    /* host output: the renders' depth, back to back */
+  float *alpha;                    /* host output: the renders' alpha, back to back */
+  float *grad_means;               /* host outputs with targets (may be NULL): dL/dmeans (N,3), */
+  float *grad_prec;                /*   dL/dprec (N,3,3), dL/dlogw (N) of the mean BCE over the */
+  float *grad_logw;                /*   request's pixels */
+  double *loss;                    /* host output with targets: the mean BCE (1 value) */
+  uint64_t user_tag;               /* returned in the completion */
+} fe_request;
+
+typedef struct fe_completion {
+  uint64_t id;                /* from fe_server_submit */
+  uint64_t user_tag;
+  int32_t status;             /* FE_OK or the failure of the request's batch */
+  int32_t n_views;
+  double submitted_s, started_s, finished_s;  /* seconds since the server was created */
+  char message[160];          /* failure message ("" on success) */
+} fe_completion;
+
+typedef struct fe_server_stats {
+  int64_t submitted, completed, renders, batches, queued;
+  double p50_latency_s, p99_latency_s;  /* over completed requests since the last reset */
+  double busy_s;                        /* lane time spent in batches, summed over lanes */
+} fe_server_stats;
+
+/* Defaults: 2 lanes, 1024 views and 48 Mi pixels per batch, 16 GiB budget, fe_render_desc_init. */
+void fe_server_config_init(fe_server_config *cfg);
+/* Starts the lanes on CUDA device `device`. */
+int fe_server_create(const fe_server_config *cfg, int device, fe_server **out);
+/* Validates and queues a request; *id identifies its completion. FE_ERR_OUT_OF_MEMORY when the
+ * request alone exceeds the HBM budget (see fe_request_footprint). Never blocks on the GPU. */
+int fe_server_submit(fe_server *s, const fe_request *req, uint64_t *id);
+/* Up to `max` completions into `out`, waiting up to timeout_ms for the first; *n_out = count,
+ * or -1 once the server is closed and every request has completed and been returned. */
+int fe_server_wait(fe_server *s, fe_completion *out, int32_t max, int32_t timeout_ms,
+                   int32_t *n_out);
+int fe_server_stats_get(fe_server *s, fe_server_stats *out);
+void fe_server_stats_reset(fe_server *s);
+/* Stop accepting requests, finish the queued ones and stop the lanes (blocks). */
+int fe_server_close(fe_server *s);
+/* Close (if needed) and free the server; completions not yet returned are dropped. */
+void fe_server_destroy(fe_server *s);
+/* Estimated device bytes of a request (the admission unit). Host only. */
+int64_t fe_request_footprint(const fe_request *req, int32_t tile_w, int32_t tile_h);
+
 /* Pipe-throughput microbenchmark: kind 0 = FP32 FMA, kind 1 = MUFU ex2, kind 2 = packed f32x2
  * FMA (two FMAs per instruction); operations per second.
  * Allocates (and frees) 1 MiB of scratch. No reference counterpart. */
@@ -275,6 +350,17 @@ int fe_render_fwd_noalloc(const fe_render_desc *desc, const float *d_means, cons
                           const float *d_logw, const float *d_quat, const float *d_trans,
                           float *d_depth, float *d_alpha, float *d_stats, uint32_t *d_device_error,
                           fe_stream_t stream);
+
+/* Silhouette binary cross-entropy of renders stored back to back in one pixel buffer, the loss
+ * of the reference's shape-from-silhouette loop (shape_from_silhouette.ipynb cell 12: mean over
+ * pixels of -(t log a + (1-t) log(1-a)) with a clamped to [3e-8, 1-3e-8]), which the reference
+ * evaluates in JAX; one kernel here. Render s owns pixels [d_seg_end[s-1], d_seg_end[s])
+ * (d_seg_end: n_seg increasing int64 on the device, the last equal to n_pix).
+ * Writes d_loss[s] = render s's mean loss (float64, n_seg) and d_galpha = dL_s/dalpha per pixel
+ * (zero where the clamp is active), the cotangent fe_render_bwd / fe_batch_bwd take. */
+int fe_silhouette_bce(const float *d_alpha, const float *d_target, const int64_t *d_seg_end,
+                      int32_t n_seg, int64_t n_pix, float *d_galpha, double *d_loss,
+                      fe_stream_t stream);
 
 /* Synchronise `stream` and return the device-side error word of the arena used by calls on that
  * stream (0 = no error; see FE_DEVERR_*), clearing it. */

@@ -143,3 +143,48 @@ def test_autotuner_picks_a_candidate(cuda_device, tmp_path):
             ref = a.clone()
         assert torch.allclose(a, ref, atol=2e-6, rtol=0)
         b.close()
+
+
+def test_device_without_index_and_malformed_request(cuda_device):
+    req = small_stream(1, seed=4)[0]
+    with serve.RenderServer(device="cuda", lanes=1) as srv:
+        assert srv.device.index is not None
+        res = srv.submit(req).result(timeout=120)
+        assert len(res.alpha) == len(req.cameras)
+    # A malformed request is rejected at submission and does not disturb the next one.
+    bad = serve.RenderRequest(req.means, req.prec, req.logw,
+                              [S.Camera(32, 32, 0.0, 0.0, 16.0, 16.0, *S.look_at([0.5, 0, 0]))])
+    with serve.RenderServer(device=cuda_device, lanes=1) as srv:
+        with pytest.raises(ValueError):
+            srv.submit(bad)
+        ok = srv.submit(req).result(timeout=120)
+        assert len(ok.alpha) == len(req.cameras)
+
+
+def test_fused_silhouette_bce_matches_float64(cuda_device):
+    # Renders of ragged sizes back to back (boundaries inside warps), alphas at and around the
+    # clamp bounds, soft and binary targets.
+    rng = np.random.default_rng(7)
+    sizes = [1, 37, 128, 1000, 4099, 3]
+    n = sum(sizes)
+    a = rng.uniform(size=n).astype(np.float32)
+    special = np.array([0.0, 1.0, 1e-9, 3e-8, 1 - 1e-8, 0.99999994, 1e-30, 0.5], np.float32)
+    a[rng.choice(n, 400, replace=False)] = rng.choice(special, 400)
+    t = (rng.uniform(size=n) > 0.6).astype(np.float32)
+    t[::7] = rng.uniform(size=t[::7].size)
+    alpha, target = torch.from_numpy(a).to(cuda_device), torch.from_numpy(t).to(cuda_device)
+    ends = torch.tensor(np.cumsum(sizes), dtype=torch.int64, device=cuda_device)
+    loss, galpha = fe.api.silhouette_bce(alpha, target, ends)
+    terms, d = serve.bce_terms(alpha, target)
+    lo = 0
+    for s, hi in enumerate(np.cumsum(sizes)):
+        ref = float(terms[lo:hi].mean())
+        assert abs(float(loss[s]) - ref) <= 1e-6 * abs(ref) + 1e-9
+        # float32 evaluation of -t/a + (1-t)/(1-a): error relative to the terms' magnitudes
+        # (the two terms cancel for soft targets)
+        a64 = alpha[lo:hi].double().clamp(3e-8, 1 - 3e-8)
+        t64 = target[lo:hi].double()
+        scale = (t64 / a64 + (1 - t64) / (1 - a64)) / (hi - lo)
+        err = (galpha[lo:hi].double() - d[lo:hi] / (hi - lo)).abs()
+        assert bool((err <= 1e-6 * scale + 1e-30).all())
+        lo = hi

@@ -1,6 +1,9 @@
 """Host-side logic of the autotuner and the server (no GPU)."""
 
+import ctypes
+
 import numpy as np
+import pytest
 
 from fuzzy_ellipses import autotune, serve
 from fuzzy_ellipses import synthetic as S
@@ -46,3 +49,54 @@ def test_bce_gradient_matches_autograd():
     loss1, g1 = serve.bce_alpha_grad(torch.ones(3), torch.zeros(3), 3)
     assert torch.isfinite(loss1) and abs(float(loss1) / 3 + np.log(3e-8)) < 1e-6
     assert float(g1.abs().max()) == 0.0
+
+
+def test_malformed_requests_are_rejected_on_the_host():
+    rng = np.random.default_rng(3)
+    sc = S.random_gaussians(10, 0.1, rng)
+    cam = S.Camera(32, 40, 40.0, 40.0, 20.0, 16.0, *S.look_at([0.5, 0, 0]))
+    serve._validate(serve.RenderRequest(sc.means, sc.prec, sc.logw, [cam]))
+    bad_cam = S.Camera(32, 40, 0.0, 40.0, 20.0, 16.0, *S.look_at([0.5, 0, 0]))
+    cases = [serve.RenderRequest(sc.means, sc.prec, sc.logw, []),
+             serve.RenderRequest(sc.means, sc.prec, sc.logw, [bad_cam]),
+             serve.RenderRequest(sc.means[:5], sc.prec, sc.logw, [cam]),
+             serve.RenderRequest(sc.means, sc.prec, sc.logw, [cam], [np.zeros((40, 32))])]
+    for r in cases:
+        with pytest.raises(ValueError):
+            serve._validate(r)
+
+
+def test_view_table_matches_the_c_layout():
+    from fuzzy_ellipses import _native as N
+    rng = np.random.default_rng(4)
+    sc = S.random_gaussians(10, 0.1, rng)
+    cams = [S.Camera(30 + i, 50, 60.0, 61.0, 25.0, 15.0, *S.look_at([0.5, 0.1 * i, 0]))
+            for i in range(3)]
+    v = serve._view_table(serve.RenderRequest(sc.means, sc.prec, sc.logw, cams))
+    assert v.dtype.itemsize == ctypes.sizeof(N.View)
+    c = (N.View * 3).from_buffer(v)
+    assert [c[i].height for i in range(3)] == [30, 31, 32]
+    assert abs(c[2].fy - 61.0) < 1e-6 and c[1].flags == N.FE_VIEW_NO_GRAD
+    assert np.allclose(list(c[2].quat), cams[2].quat) and np.allclose(list(c[2].trans), cams[2].trans)
+
+
+def test_footprint_matches_the_library_admission_unit():
+    from fuzzy_ellipses import _native as N
+    lib = N.load()
+    rng = np.random.default_rng(5)
+    for bwd in (False, True):
+        for n, nv, side in ((20, 1, 96), (700, 5, 211), (2000, 32, 480)):
+            sc = S.random_gaussians(n, 0.1, rng)
+            cams = [S.Camera(side, side + 7, float(side), float(side), side / 2, side / 2,
+                             *S.look_at([0.5, 0.0, 0.1 * i])) for i in range(nv)]
+            tg = [np.zeros((side, side + 7), np.float32) for _ in cams] if bwd else None
+            req = serve.RenderRequest(sc.means, sc.prec, sc.logw, cams, tg)
+            views = serve._view_table(req)
+            r = N.Request()
+            r.n_gaussians, r.n_views = n, nv
+            r.views = views.ctypes.data
+            tptr = (ctypes.c_void_p * nv)(*([1] * nv))
+            r.targets = ctypes.cast(tptr, ctypes.c_void_p) if bwd else None
+            for tile in (8, 16):
+                assert lib.fe_request_footprint(ctypes.byref(r), tile, tile) == \
+                    serve.estimate_footprint(req, tile)

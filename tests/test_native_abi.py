@@ -36,15 +36,20 @@ def test_struct_layouts_match_c(tmp_path):
     prog = tmp_path / "sizes.c"
     prog.write_text(
         '#include <stdio.h>\n#include <stddef.h>\n#include "fuzzy_ellipses.h"\n'
-        "int main(void){printf(\"%zu %zu %zu %zu %zu %zu\\n\", sizeof(fe_render_desc),"
+        "int main(void){printf(\"%zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu\\n\", sizeof(fe_render_desc),"
         " sizeof(fe_legacy_desc), sizeof(fe_view), sizeof(fe_scene),"
-        " offsetof(fe_view, pixel_offset), offsetof(fe_render_desc, tile_w));return 0;}\n")
+        " offsetof(fe_view, pixel_offset), offsetof(fe_render_desc, tile_w),"
+        " sizeof(fe_server_config), offsetof(fe_server_config, desc), sizeof(fe_request),"
+        " offsetof(fe_request, user_tag), sizeof(fe_completion), sizeof(fe_server_stats));return 0;}\n")
     exe = tmp_path / "sizes"
     subprocess.run(["gcc", "-I", os.path.join(ROOT, "include"), str(prog), "-o", str(exe)], check=True)
     out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split()
     assert [int(x) for x in out] == [ctypes.sizeof(N.RenderDesc), ctypes.sizeof(N.LegacyDesc),
                                      ctypes.sizeof(N.View), ctypes.sizeof(N.SceneEntry),
-                                     N.View.pixel_offset.offset, N.RenderDesc.tile_w.offset]
+                                     N.View.pixel_offset.offset, N.RenderDesc.tile_w.offset,
+                                     ctypes.sizeof(N.ServerConfig), N.ServerConfig.desc.offset,
+                                     ctypes.sizeof(N.Request), N.Request.user_tag.offset,
+                                     ctypes.sizeof(N.Completion), ctypes.sizeof(N.ServerStats)]
     assert ctypes.sizeof(N.LegacyDesc) == 20  # the reference's RasterizeDescriptor: 3 int + 2 float
 
 
