@@ -102,6 +102,7 @@ struct fe_server {
   uint64_t next_id = 1;
   int64_t submitted = 0, completed = 0, renders = 0, batches = 0;
   double busy_s = 0;
+  double phase_s[6] = {0, 0, 0, 0, 0, 0};
   std::vector<double> latencies;
   std::vector<std::thread> lanes;
   std::mutex close_mu;
@@ -149,6 +150,13 @@ struct Lane {
   cudaStream_t st = nullptr;
   fe_batch* plan = nullptr;
   LaneBuf gauss, pix, tgt, grads, small;
+  double phase[6] = {0, 0, 0, 0, 0, 0};
+  double mark = 0;
+  void tick(int p) {
+    const double t = s->now();
+    phase[p] += t - mark;
+    mark = t;
+  }
 
 #define LANE_CUDA(call)                                                              \
   do {                                                                               \
@@ -158,6 +166,7 @@ struct Lane {
   } while (0)
 
   int run(std::vector<Request*>& batch) {
+    mark = s->now();
     std::stable_partition(batch.begin(), batch.end(),
                           [](const Request* q) { return q->r.targets != nullptr; });
     const int nr = (int)batch.size();
@@ -208,6 +217,7 @@ struct Lane {
       LANE_CUDA(cudaMemcpyAsync(prec + 9 * goff[k], r.prec, 36 * n, cudaMemcpyHostToDevice, st));
       LANE_CUDA(cudaMemcpyAsync(logw + goff[k], r.logw, 4 * n, cudaMemcpyHostToDevice, st));
     }
+    tick(0);
 
     if (!plan) {
       fe_render_desc d = s->cfg.desc;
@@ -221,8 +231,10 @@ struct Lane {
       rc = fe_batch_reset(plan, scenes.data(), nr, views.data(), (int32_t)views.size(), st);
       if (rc) return rc;
     }
+    tick(1);
     rc = fe_batch_fwd(plan, means, prec, logw, depth, alpha, stats, st);
     if (rc) return rc;
+    tick(2);
 
     double* loss = nullptr;
     if (n_bwd) {
@@ -255,6 +267,7 @@ struct Lane {
       rc = fe_batch_bwd(plan, means, prec, logw, depth, alpha, stats, nullptr, galpha, gm,
                         gm + 3 * G, gm + 12 * G, st);
       if (rc) return rc;
+      tick(3);
     }
 
     // Outputs straight into the callers' memory.
@@ -280,6 +293,7 @@ struct Lane {
     }
     (void)gb;
     LANE_CUDA(cudaStreamSynchronize(st));
+    tick(4);
     int64_t nk = 0, wk = 0;
     uint32_t err = 0;
     rc = fe_batch_status(plan, st, &nk, &wk, &err);
@@ -288,6 +302,7 @@ struct Lane {
       return set_last_error(FE_ERR_DEVICE_TIMEOUT, "a bounded device wait gave up");
     if (err & FE_DEVERR_CAPACITY)
       return set_last_error(FE_ERR_CAPACITY, "key capacity exceeded");
+    tick(5);
     return FE_OK;
   }
 #undef LANE_CUDA
@@ -327,6 +342,10 @@ struct Lane {
         }
         s->batches += 1;
         s->busy_s += finished - started;
+        for (int p = 0; p < 6; ++p) {
+          s->phase_s[p] += phase[p];
+          phase[p] = 0;
+        }
       }
       s->cv_done.notify_all();
       s->cv_work.notify_all();
@@ -479,6 +498,7 @@ int fe_server_stats_get(fe_server* s, fe_server_stats* out) {
     out->batches = s->batches;
     out->queued = (int64_t)s->queue.size();
     out->busy_s = s->busy_s;
+    for (int p = 0; p < 6; ++p) out->phase_s[p] = s->phase_s[p];
     lat = s->latencies;
   }
   out->p50_latency_s = quantile(lat, 0.50);
@@ -491,6 +511,7 @@ void fe_server_stats_reset(fe_server* s) {
   std::lock_guard<std::mutex> lk(s->mu);
   s->submitted = s->completed = s->renders = s->batches = 0;
   s->busy_s = 0;
+  for (int p = 0; p < 6; ++p) s->phase_s[p] = 0;
   s->latencies.clear();
 }
 

@@ -114,7 +114,8 @@ class ServerStats(ctypes.Structure):
     _fields_ = [("submitted", ctypes.c_int64), ("completed", ctypes.c_int64),
                 ("renders", ctypes.c_int64), ("batches", ctypes.c_int64),
                 ("queued", ctypes.c_int64), ("p50_latency_s", ctypes.c_double),
-                ("p99_latency_s", ctypes.c_double), ("busy_s", ctypes.c_double)]
+                ("p99_latency_s", ctypes.c_double), ("busy_s", ctypes.c_double),
+                ("phase_s", ctypes.c_double * 6)]
 
 
 P = ctypes.c_void_p

@@ -9,8 +9,9 @@ plan; a free lane takes the queued requests in arrival order while they fit its 
 limits and the HBM budget (estimated device bytes of all in-flight batches), renders them as one
 batch, evaluates the loss and backward of the backward requests in the same batch, and writes
 every output straight into the request's own NumPy arrays. This front end validates requests,
-allocates their outputs, keeps their arrays alive until completion and resolves the futures from
-one collector thread.
+allocates their outputs (one pinned block per request, recycled through torch's pinned-memory
+cache once the client drops the result), keeps their arrays alive until completion and resolves
+the futures from one collector thread.
 
 A request's results do not depend on which other requests shared its batch beyond float32
 rounding (tested to 1e-6).
@@ -180,7 +181,19 @@ class RenderServer:
         logw = np.ascontiguousarray(req.logw, dtype=np.float32)
         views = _view_table(req)
         pixels = int((views["height"].astype(np.int64) * views["width"]).sum())
-        out = {"depth": np.empty(pixels, np.float32), "alpha": np.empty(pixels, np.float32)}
+        # Outputs in one pinned block per request: [loss (f64) | depth | alpha | grads]. The
+        # lanes' copies into it are asynchronous at full link speed (no page faults), and the
+        # block returns to torch's pinned-memory cache once the result arrays are dropped.
+        n_out = 2 * pixels + ((2 + 13 * n) if req.backward else 0)
+        block = torch.empty(n_out, dtype=torch.float32, pin_memory=True).numpy()
+        o = 2 if req.backward else 0
+        out = {"depth": block[o:o + pixels], "alpha": block[o + pixels:o + 2 * pixels]}
+        if req.backward:
+            g = o + 2 * pixels
+            out.update(loss=block[0:2].view(np.float64),
+                       grad_means=block[g:g + 3 * n].reshape(n, 3),
+                       grad_prec=block[g + 3 * n:g + 12 * n].reshape(n, 3, 3),
+                       grad_logw=block[g + 12 * n:g + 13 * n])
         keep = [means, prec, logw, views]
         r = N.Request()
         r.n_gaussians, r.n_views = n, len(req.cameras)
@@ -191,9 +204,6 @@ class RenderServer:
             targets = [np.ascontiguousarray(t, dtype=np.float32) for t in req.targets]
             tptr = (ctypes.c_void_p * len(targets))(*[t.ctypes.data for t in targets])
             keep += [targets, tptr]
-            out.update(grad_means=np.empty((n, 3), np.float32),
-                       grad_prec=np.empty((n, 3, 3), np.float32),
-                       grad_logw=np.empty(n, np.float32), loss=np.empty(1, np.float64))
             r.targets = ctypes.cast(tptr, ctypes.c_void_p)
             r.grad_means = out["grad_means"].ctypes.data
             r.grad_prec = out["grad_prec"].ctypes.data
@@ -254,7 +264,10 @@ class RenderServer:
         N.check(N.load().fe_server_stats_get(self._h, ctypes.byref(st)))
         return {"submitted": st.submitted, "completed": st.completed, "renders": st.renders,
                 "batches": st.batches, "queued": st.queued, "p50_s": st.p50_latency_s,
-                "p99_s": st.p99_latency_s, "busy_s": st.busy_s}
+                "p99_s": st.p99_latency_s, "busy_s": st.busy_s,
+                "phase_s": dict(zip(self.PHASES, [round(x, 6) for x in st.phase_s]))}
+
+    PHASES = ("upload", "plan", "forward", "loss_backward", "download", "finish")
 
     def reset_stats(self):
         """Forget latencies and counters (e.g. after a warm-up)."""

@@ -301,6 +301,9 @@ typedef struct fe_server_stats {
   int64_t submitted, completed, renders, batches, queued;
   double p50_latency_s, p99_latency_s;  /* over completed requests since the last reset */
   double busy_s;                        /* lane time spent in batches, summed over lanes */
+  /* lane time by phase, summed over lanes: 0 upload, 1 plan, 2 forward (with its key-count
+   * readback), 3 loss + backward, 4 download (copies into the callers' memory), 5 finish */
+  double phase_s[6];
 } fe_server_stats;
 
 /* Defaults: 2 lanes, 1024 views and 48 Mi pixels per batch, 16 GiB budget, fe_render_desc_init. */
