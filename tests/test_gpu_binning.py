@@ -96,3 +96,53 @@ def test_legacy_rasterize_matches_culled_oracle(cuda_device):
                              [0, 0, 0], [np.array(l, np.int64) for l in lists], 8, 8)
     ea, ed = parity_errors(z.cpu().numpy(), a.cpu().numpy(), dc, ac)
     assert ea <= 2 * TOL_ALPHA and ed <= TOL_DEPTH_REL, (ea, ed)
+
+
+@pytest.mark.parametrize("tile", [(8, 8), (16, 16), (32, 8)])
+def test_product_tile_sets_match_float64_screen_bounds(cuda_device, tile):
+    """Every Gaussian's tiles in the product binning (float32) form the rectangle of the float64
+    restatement of its k-sigma screen bound; boundary cases may differ by one tile row/column."""
+    from oracle import screen_bounds as SB
+    scene, cams = S.config1(seed=2)
+    m, p, w = [torch.from_numpy(x).to(cuda_device) for x in (scene.means, scene.prec, scene.logw)]
+    exact, total = 0, 0
+    for c in cams[:6]:
+        keys, _ = fe.render_binning(m, p, w, c.fx, c.fy, c.cx, c.cy, c.quat, c.trans, c.height,
+                                    c.width, tile=tile)
+        k = keys.cpu().numpy().astype(np.uint64)
+        tiles = (k >> np.uint64(32)).astype(np.int64)
+        gid = (k & np.uint64(0xFFFFFFFF)).astype(np.int64)
+        gx = -(-c.width // tile[0])
+        rect = SB.tile_rects(scene.means, scene.prec, scene.logw, c, *tile)
+        for g in range(scene.n):
+            t = tiles[gid == g]
+            x0, y0, x1, y1 = rect[g]
+            want = {(ty * gx + tx) for ty in range(y0, y1) for tx in range(x0, x1)}
+            got = set(t.tolist())
+            total += 1
+            if got == want:
+                exact += 1
+                continue
+            tx, ty = t % gx, t // gx
+            if len(t):
+                assert tx.min() >= x0 - 1 and tx.max() <= x1 and ty.min() >= y0 - 1 and ty.max() <= y1
+            assert len(got ^ want) <= max(x1 - x0, y1 - y0, 1) + 2
+    assert exact >= 0.999 * total
+
+
+def test_eval_counts_match_float64_screen_bounds(cuda_device):
+    """The benchmark's unit (evaluations of a tile-binned render) from the GPU binning equals the
+    float64 restatement's count on the 16-camera workload."""
+    from oracle import screen_bounds as SB
+    scene, cams = S.config1(seed=0)
+    m, p, w = [torch.from_numpy(x).to(cuda_device) for x in (scene.means, scene.prec, scene.logw)]
+    for c in cams:
+        _, ranges = fe.render_binning(m, p, w, c.fx, c.fy, c.cx, c.cy, c.quat, c.trans,
+                                      c.height, c.width, tile=(8, 8))
+        r = ranges.cpu().numpy()
+        gx = (c.width + 7) // 8
+        t = np.arange(r.shape[0])
+        pix = np.minimum(8, c.width - 8 * (t % gx)) * np.minimum(8, c.height - 8 * (t // gx))
+        gpu = int(((r[:, 1] - r[:, 0]) * pix).sum())
+        cpu = SB.evals_per_render(scene.means, scene.prec, scene.logw, c)
+        assert abs(gpu - cpu) <= 1e-4 * cpu

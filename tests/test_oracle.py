@@ -109,3 +109,38 @@ def test_culled_equals_dense_with_full_lists():
     assert np.allclose(a, a_ref, atol=1e-14)
     mask = a_ref > 1e-6
     assert np.allclose(d[mask], d_ref[mask], rtol=1e-12)
+
+
+def test_screen_bounds_contain_the_k_sigma_ellipsoid():
+    """The float64 screen bound encloses the projections of points sampled on each Gaussian's
+    k-sigma ellipsoid surface (k^2 = 2 (logw - ln 1e-7)) in front of the camera, and is tight:
+    some sampled point lands in each edge tile row/column."""
+    import math
+
+    from fuzzy_ellipses import synthetic as S
+    from oracle import screen_bounds as SB
+    rng = np.random.default_rng(0)
+    scene = S.random_gaussians(40, 0.1, rng)
+    cam = S.Camera(240, 320, 300.0, 300.0, 160.0, 120.0, *S.look_at([0.6, 0.1, 0.2]))
+    rect = SB.tile_rects(scene.means, scene.prec, scene.logw, cam, 8, 8)
+    R = O.quat_to_rot(cam.quat)
+    for g in range(scene.n):
+        k = math.sqrt(2 * (scene.logw[g] - math.log(1e-7)))
+        U = np.triu(scene.prec[g].astype(np.float64))
+        L = np.linalg.inv(U.T)  # Sigma = (U U^T)^-1 = L L^T: surface points mean + k L d
+        d = rng.normal(size=(4000, 3))
+        d /= np.linalg.norm(d, axis=1, keepdims=True)
+        pts = scene.means[g] + k * d @ L.T
+        pc = (pts - cam.trans) @ R.T
+        assert (pc[:, 2] > 0).all()
+        u = cam.fx * pc[:, 0] / pc[:, 2] + cam.cx
+        v = cam.fy * pc[:, 1] / pc[:, 2] + cam.cy
+        inside = (u >= 0) & (u < cam.width) & (v >= 0) & (v < cam.height)
+        if not inside.any():
+            continue
+        tx, ty = np.floor(u[inside] / 8).astype(int), np.floor(v[inside] / 8).astype(int)
+        x0, y0, x1, y1 = rect[g]
+        assert tx.min() >= x0 and tx.max() < x1 and ty.min() >= y0 and ty.max() < y1
+        if inside.all():  # tight: the samples reach the rectangle's edge tiles (within one)
+            assert tx.min() <= x0 + 1 and tx.max() >= x1 - 2
+            assert ty.min() <= y0 + 1 and ty.max() >= y1 - 2
