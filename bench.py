@@ -41,6 +41,12 @@ WORKLOAD = ("N=1000 Gaussians (means U[-0.3,0.3]^3 m, scales logU[0.005,0.03] m,
 # the logit and the three accumulations) and 3 MUFU operations (rcp and two ex2).
 PER_EVAL_FMA = 22
 PER_EVAL_MUFU = 3
+# Backward, counted from blend_bwd_kernel's per-pixel loop: 37 FMA-pipe operations (pixel
+# offsets 2, the three row-folded polynomials 5, peak and logits 5, chain rule 14, row moments
+# of the coefficient gradients 11) and 3 MUFU (rcp, ex2 of the density, ex2 of the softmax
+# weight).
+PER_EVAL_BWD_FMA = 37
+PER_EVAL_BWD_MUFU = 3
 
 
 def parse():
@@ -51,9 +57,12 @@ def parse():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-serve", action="store_true")
+    ap.add_argument("--serve-only", action="store_true",
+                    help="run only the served mixed-request workload and print its JSON")
     ap.add_argument("--profile-step", action="store_true",
-                    help="build the workload, warm up, run one batched forward step and exit "
-                         "(the command the committed ncu summaries capture)")
+                    help="build the workload, warm up, run one batched forward step, then one "
+                         "forward with statistics and its backward, and exit (the command the "
+                         "committed ncu summaries capture)")
     return ap.parse_args()
 
 
@@ -240,6 +249,12 @@ def main():
     if args.impl == "reference":
         run_reference(args)
         return
+    if args.serve_only:
+        import torch
+
+        import fuzzy_ellipses as fe
+        print(json.dumps(serve_bench(fe, torch.device("cuda", 0))), flush=True)
+        return
     import torch
 
     import fuzzy_ellipses as fe
@@ -263,7 +278,8 @@ def main():
         tuner = fe.autotune.Autotuner(persist=False)
         tuned = tuner.tune([(0, scene.n)], views, m, p, w, reps=3)
         cfg = {k: tuned[k] for k in ("tile", "px", "chunk")}
-    batch = fe.Batch([(0, scene.n)], views, tile=cfg["tile"], px=cfg["px"], chunk=cfg["chunk"])
+    batch = fe.Batch([(0, scene.n)], views, tile=cfg["tile"], px=cfg["px"], chunk=cfg["chunk"],
+                     keep_binning=True)
     per_cam_evals = count_evals(fe, cams, mpw) if not args.profile_step else [0] * len(cams)
     e_step = float(sum(per_cam_evals))
     depth = torch.empty(batch.n_pixels, device=dev)
@@ -274,6 +290,15 @@ def main():
         batch.forward(m, p, w, depth, alpha)
     if args.profile_step:
         batch.forward(m, p, w, depth, alpha)
+        torch.cuda.synchronize()
+        assert batch.status()["device_error"] == 0
+        # then one differentiable step: forward with statistics and the backward
+        stats = torch.empty(3 * batch.n_pixels, device=dev)
+        batch.forward(m, p, w, depth, alpha, stats)
+        gen = torch.Generator(device=dev).manual_seed(1)
+        gdep = torch.randn(batch.n_pixels, device=dev, generator=gen) * 1e-3
+        galp = torch.randn(batch.n_pixels, device=dev, generator=gen) * 1e-3
+        batch.backward(m, p, w, depth, alpha, stats, gdep, galp)
         torch.cuda.synchronize()
         assert batch.status()["device_error"] == 0
         return
@@ -380,6 +405,34 @@ def main():
     e2e_s = (time.perf_counter() - t0) / args.steps
     e2e_value = e_step / e2e_s / 1e6
 
+    # ---- backward of the same step (recompute-based), CUDA events, L2 flushed between ------
+    stats = torch.empty(3 * batch.n_pixels, device=dev)
+    batch.forward(m, p, w, depth, alpha, stats)
+    gen = torch.Generator(device=dev).manual_seed(1)
+    gdep = torch.randn(batch.n_pixels, device=dev, generator=gen) * 1e-3
+    galp = torch.randn(batch.n_pixels, device=dev, generator=gen) * 1e-3
+    for _ in range(3):
+        batch.backward(m, p, w, depth, alpha, stats, gdep, galp)
+    b_start = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    b_end = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    for i in range(args.steps):
+        flush.fill_(i & 0xFF)
+        b_start[i].record()
+        batch.backward(m, p, w, depth, alpha, stats, gdep, galp)
+        b_end[i].record()
+    torch.cuda.synchronize()
+    bwd_ms = statistics.median(a.elapsed_time(b) for a, b in zip(b_start, b_end))
+    bwd_evals_s = e_step / (bwd_ms * 1e-3)
+    bwd_peak = min(fma_ops / PER_EVAL_BWD_FMA, ex2_ops / PER_EVAL_BWD_MUFU)
+    backward = {"ms_per_step": bwd_ms, "evals_per_s": bwd_evals_s,
+                "roofline": {"bound": "fma+xu", "achieved": bwd_evals_s / 1e9,
+                             "peak": bwd_peak / 1e9, "unit": "Gevals/s",
+                             "frac": bwd_evals_s / bwd_peak,
+                             "per_eval": {"fma_pipe": PER_EVAL_BWD_FMA, "mufu": PER_EVAL_BWD_MUFU},
+                             "scope": "whole backward (pixel prep, per-key recompute and "
+                                      "coefficient gradients, record VJP) of the 16-view step, "
+                                      "reusing the forward's binning"}}
+
     # ---- served mixed requests vs the plain per-call drop-in ------------------------------
     served = None if args.no_serve else serve_bench(fe, dev)
 
@@ -425,6 +478,7 @@ def main():
         "num_keys": nk,
         "evals_per_camera": per_cam_evals,
         "cpu_baseline": cpu,
+        "backward": backward,
         "served": served,
         "autotune": tuned and {"bucket": tuned["bucket"],
                                "candidates_ms": {f"{c['tile'][0]}x{c['tile'][1]}/px{c['px']}/ch{c['chunk']}": round(c["ms"], 4)

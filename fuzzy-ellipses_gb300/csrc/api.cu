@@ -396,8 +396,8 @@ int fe_render_bwd(const fe_render_desc* d, const float* means, const float* prec
   if (rc) return rc;
   FE_CUDA(cudaMemsetAsync(rs.rgrad, 0, sizeof(RecGrad) * (size_t)p.n_rec, st));
   launch_pixel_prep(p.va, p.n_pix, depth, stats, p.n_pix, gdepth, galpha, rs.pix, st);
-  launch_blend_bwd(p.va, p.tile_w, p.tile_h, sorted, rs.ctrl, cap, ks.trec, rs.recs, rs.pix,
-                   p.beta2, p.beta3, rs.rgrad, st);
+  launch_blend_bwd(p.va, p.tile_w, p.tile_h, p.n_tiles, sorted, rs.ranges, ks.trec, rs.recs,
+                   rs.pix, p.beta2, p.beta3, rs.rgrad, rs.ctrl, st);
   launch_record_vjp(p.va, p.n_rec, means, prec, quat, trans, rs.recs, rs.rgrad, gmeans, gprec,
                     glogw, st);
   FE_CUDA(cudaGetLastError());
@@ -676,6 +676,9 @@ struct fe_batch {
   fe_render_desc desc{};
   int tile_w = 16, tile_h = 16;
   bool exact = false;  // size key scratch from the device-side count (one readback per run)
+  bool keep_binning = false;  // reuse the last forward's binning in the backward
+  bool binned = false;        // the scratch holds the binning of the last forward of ...
+  const float* binned_for[3] = {nullptr, nullptr, nullptr};  // ... these Gaussian arrays
   int32_t n_views = 0;
   DevBuf tables;  // ViewDev[n_views] | quat[4 n_views] | trans[3 n_views]
   ViewDev* views_d = nullptr;
@@ -796,6 +799,7 @@ int fe_batch_create(const fe_render_desc* desc, const fe_scene* scenes, int32_t 
   fe_batch* b = new fe_batch();
   b->desc = *desc;
   b->exact = (desc->flags & FE_FLAG_EXACT_KEYS) != 0;
+  b->keep_binning = (desc->flags & FE_FLAG_KEEP_BINNING) != 0;
   tile_shape(desc, b->tile_w, b->tile_h);
   rc = plan_batch(b, scenes, n_scenes, views, n_views);
   if (rc) {
@@ -823,6 +827,7 @@ int fe_batch_reset(fe_batch* b, const fe_scene* scenes, int32_t n_scenes, const 
   cudaStream_t st = reinterpret_cast<cudaStream_t>(stream_);
   // No synchronisation: the new tables reach the device by copies ordered on `st` after the
   // previous run, and buffers that must grow wait for `st` before they are freed.
+  b->binned = false;
   int rc = plan_batch(b, scenes, n_scenes, views, n_views);
   if (rc) return rc;
   return commit_batch(b, st);
@@ -844,6 +849,14 @@ int64_t fe_batch_scratch_bytes(const fe_batch* b) {
 }
 
 }  // extern "C"
+
+// Remember which Gaussian arrays the batch's current binning belongs to (FE_FLAG_KEEP_BINNING).
+static void note_binning(fe_batch* b, const float* means, const float* prec, const float* logw) {
+  b->binned = true;
+  b->binned_for[0] = means;
+  b->binned_for[1] = prec;
+  b->binned_for[2] = logw;
+}
 
 static Pipeline batch_pipeline(fe_batch* b, const float* means, const float* prec,
                                const float* logw) {
@@ -912,8 +925,10 @@ int fe_batch_fwd(fe_batch* b, const float* means, const float* prec, const float
   Pipeline p = batch_pipeline(b, means, prec, logw);
   if (p.n_rec > 0 && (!means || !prec || !logw))
     return fail(FE_ERR_INVALID_ARGUMENT, "NULL Gaussian pointer");
+  b->binned = false;
   int rc = batch_binning(b, p, st, nullptr);
   if (rc) return rc;
+  note_binning(b, means, prec, logw);
   launch_blend_fwd(p.va, p.tile_w, p.tile_h, p.px, p.chunk, p.n_tiles, b->ks.trec, b->rs.ranges,
                    p.beta2, p.beta3, depth, alpha, stats, p.n_pix, b->rs.ctrl, st);
   FE_CUDA(cudaGetLastError());
@@ -932,12 +947,20 @@ int fe_batch_bwd(fe_batch* b, const float* means, const float* prec, const float
   FE_CUDA(cudaMemsetAsync(gmeans, 0, sizeof(float) * 3 * (size_t)b->n_gauss, st));
   FE_CUDA(cudaMemsetAsync(gprec, 0, sizeof(float) * 9 * (size_t)b->n_gauss, st));
   FE_CUDA(cudaMemsetAsync(glogw, 0, sizeof(float) * (size_t)b->n_gauss, st));
-  int rc = batch_binning(b, p, st, nullptr);
-  if (rc) return rc;
+  if (b->keep_binning && b->binned && b->binned_for[0] == means && b->binned_for[1] == prec &&
+      b->binned_for[2] == logw) {
+    // Reuse the forward's binning; only the blend's tile counter must start again at zero.
+    FE_CUDA(cudaMemsetAsync(&b->rs.ctrl->next_tile, 0, sizeof(uint32_t), st));
+  } else {
+    b->binned = false;
+    int rc = batch_binning(b, p, st, nullptr);
+    if (rc) return rc;
+    note_binning(b, means, prec, logw);
+  }
   FE_CUDA(cudaMemsetAsync(b->rs.rgrad, 0, sizeof(RecGrad) * (size_t)p.n_rec, st));
   launch_pixel_prep(p.va, p.n_pix, depth, stats, p.n_pix, gdepth, galpha, b->rs.pix, st);
-  launch_blend_bwd(p.va, p.tile_w, p.tile_h, b->sorted, b->rs.ctrl, b->cap, b->ks.trec,
-                   b->rs.recs, b->rs.pix, p.beta2, p.beta3, b->rs.rgrad, st);
+  launch_blend_bwd(p.va, p.tile_w, p.tile_h, p.n_tiles, b->sorted, b->rs.ranges, b->ks.trec,
+                   b->rs.recs, b->rs.pix, p.beta2, p.beta3, b->rs.rgrad, b->rs.ctrl, st);
   launch_record_vjp(p.va, p.n_rec, means, prec, p.quat, p.trans, b->rs.recs, b->rs.rgrad, gmeans,
                     gprec, glogw, st);
   FE_CUDA(cudaGetLastError());
@@ -975,11 +998,13 @@ int fe_batch_fwd_timed(fe_batch* b, const float* means, const float* prec, const
   Pipeline p = batch_pipeline(b, means, prec, logw);
   cudaEvent_t ev[7];
   for (auto& e : ev) FE_CUDA(cudaEventCreate(&e));
+  b->binned = false;
   int rc = batch_binning(b, p, st, ev);
   if (rc) {
     for (auto& e : ev) cudaEventDestroy(e);
     return rc;
   }
+  note_binning(b, means, prec, logw);
   launch_blend_fwd(p.va, p.tile_w, p.tile_h, p.px, p.chunk, p.n_tiles, b->ks.trec, b->rs.ranges,
                    p.beta2, p.beta3, depth, alpha, stats, p.n_pix, b->rs.ctrl, st);
   FE_CUDA(cudaEventRecord(ev[6], st));

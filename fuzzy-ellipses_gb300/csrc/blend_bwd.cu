@@ -8,13 +8,17 @@
 // Per pixel, with e = 2^(l-m) the unnormalised softmax weight and eA = 2^s2 the peak density:
 //   dL/ds = dL/dalpha (1-alpha) eA + beta3 (dL/ddepth / W) e (z - depth)      (s natural log)
 //   dL/dz = (dL/ddepth / W) e (1 - beta2 (z - depth))
-// Parallelisation is transposed with respect to the forward: one thread per (tile, Gaussian)
-// key loops over the tile's pixels and accumulates the gradient of its 16 tile-polynomial
-// coefficients in registers (no cross-thread reductions), maps them back through the tile
-// re-expansion to record space and adds them to the record's accumulator. A per-record kernel
+// Parallelisation is transposed with respect to the forward: persistent warps take tiles from a
+// device counter and stage the tile's per-pixel data in shared memory; each (tile, Gaussian) key
+// gets one or more lanes that loop over the tile's pixels and accumulate the gradient of its 16
+// tile-polynomial coefficients in registers (lanes sharing a key combine by shuffles), map them
+// back through the tile re-expansion to record space and add them to the record's accumulator
+// (vector reductions). A per-record kernel
 // then applies the chain rule of the preprocess (camera transform, cofactors, cross products)
 // and accumulates d/dmeans, d/dprec (upper triangle only, as jax.grad through triu gives) and
 // d/dlogw over the views of a scene.
+#include <algorithm>
+
 #include "fe_kernels.cuh"
 
 namespace fe {
@@ -40,103 +44,243 @@ __device__ __forceinline__ void red_add_v4(float* addr, float a, float b, float 
                : "memory");
 }
 
+constexpr int kBwdWarps = 4;
+
+// Per-warp shared-memory slice: the tile's per-pixel data as four planes (depth, softmax max m,
+// dL/ddepth / W, dL/dalpha (1-alpha)), so that one 64-bit load gives the same field of two
+// adjacent pixels for the packed arithmetic. Rows are padded to TW + 2 floats (8-byte aligned
+// pairs; lanes of one key reading different rows of the same columns hit different banks).
 template <int TW, int TH>
-__global__ void __launch_bounds__(128) blend_bwd_kernel(
-    ViewsArg va, const uint64_t* __restrict__ keys, const Control* __restrict__ ctrl,
-    const TilePair* __restrict__ trec, const GaussRec* __restrict__ recs,
-    const float4* __restrict__ pix, float nb2, float beta3, float beta2, RecGrad* __restrict__ rgrad) {
-  const int64_t K = (int64_t)ctrl->num_keys;
-  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < K;
-       k += (int64_t)gridDim.x * blockDim.x) {
-    const uint64_t key = keys[k];
-    const uint32_t tile = (uint32_t)(key >> 32);
-    const uint32_t gid = (uint32_t)key;
+struct alignas(16) BwdSlice {
+  static constexpr int ROW = TW + 2;
+  static_assert((TH * ROW) % 2 == 0 && ROW % 2 == 0, "pairs must stay 8-byte aligned");
+  float plane[4][TH * ROW];
+};
+
+// Persistent warps: each warp takes a tile from the device counter, stages the tile's pixel data
+// in its shared-memory slice and processes the tile's keys in groups of up to 32. A group of n
+// keys gets s = 32 / n lanes per key (s a power of two), which split the tile's rows; their
+// partial sums are combined with shuffles. Pixels are evaluated in adjacent pairs with packed
+// f32x2 arithmetic (one instruction for both pixels; rcp and ex2 per pixel).
+template <int TW, int TH>
+__global__ void __launch_bounds__(32 * kBwdWarps) blend_bwd_kernel(
+    ViewsArg va, uint32_t n_tiles, const uint64_t* __restrict__ keys,
+    const uint2* __restrict__ ranges, const TilePair* __restrict__ trec,
+    const GaussRec* __restrict__ recs, const float4* __restrict__ pix, float nb2, float beta3,
+    float beta2, RecGrad* __restrict__ rgrad, Control* ctrl) {
+  using Slice = BwdSlice<TW, TH>;
+  __shared__ Slice slices[kBwdWarps];
+  const unsigned full = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  Slice& sl = slices[threadIdx.x >> 5];
+  const f2_t B3 = f2_pack(beta3, beta3), NB2 = f2_pack(nb2, nb2);
+  const f2_t NEGB2 = f2_pack(-beta2, -beta2), ONE = f2_pack(1.f, 1.f), TWO = f2_pack(2.f, 2.f);
+  const f2_t LN2 = f2_pack(kLn2, kLn2);
+  for (;;) {
+    uint32_t tile = 0;
+    if (lane == 0) tile = atomicAdd(&ctrl->next_tile, 1u);
+    tile = __shfl_sync(full, tile, 0);
+    if (tile >= n_tiles) break;
+    const uint2 range = ranges[tile];
+    if (range.y <= range.x) continue;
     const int vi = find_view<&ViewDev::tile_base>(va, tile);
     const ViewDev& V = view_at(va, vi);
     if (V.flags & FE_VIEW_NO_GRAD) continue;
     const int lt = (int)(tile - V.tile_base);
     const int tx = lt % V.gx, ty = lt / V.gx;
-    // Record k lives in slot k%2 of pair k/2 (field i at float offset 2*i + slot).
-    const float* tf = reinterpret_cast<const float*>(trec + (k >> 1)) + (k & 1);
-    const float V0 = tf[0], V1 = tf[2], V2 = tf[4], V3 = tf[6], V4 = tf[8], V5 = tf[10];
-    const float P0 = tf[12], P1 = tf[14], P2 = tf[16];
-    const float N0 = tf[18], N1 = tf[20], N2 = tf[22], N3 = tf[24], N4 = tf[26], N5 = tf[28];
-    const float C = tf[30], cu = tf[32], cvv = tf[34];
-
-    float gV[6] = {0, 0, 0, 0, 0, 0}, gP[3] = {0, 0, 0}, gN[6] = {0, 0, 0, 0, 0, 0}, gC = 0.f;
     const int xs = min(TW, V.W - tx * TW), ys = min(TH, V.H - ty * TH);
-    for (int ly = 0; ly < ys; ++ly) {
-      const float dv = ly - 0.5f * (TH - 1), dv2 = dv * dv;
-      const float ev = dv - cvv, ev2 = ev * ev;
-      const float4* prow = pix + V.pix_base + (int64_t)(ty * TH + ly) * V.W + tx * TW;
-      for (int lx = 0; lx < xs; ++lx) {
-        const float du = lx - 0.5f * (TW - 1), du2 = du * du, dudv = du * dv;
-        const float eu = du - cu, eu2 = eu * eu, euev = eu * ev;
-        const float4 px = prow[lx];  // depth, m, gD/W, gA(1-alpha)
-        const float vsv = fmaf(V5, dv2, fmaf(V4, dudv, fmaf(V3, du2, fmaf(V2, dv, fmaf(V1, du, V0)))));
-        const float psv = fmaf(P2, dv, fmaf(P1, du, P0));
-        const float nq = fmaf(N5, ev2, fmaf(N4, euev, fmaf(N3, eu2, fmaf(N2, ev, fmaf(N1, eu, N0)))));
-        const float qi = rcp_approx(vsv);
-        const float z = psv * qi;
-        const float s2 = fmaf(nq, qi, C);
-        const float eA = ex2_approx(s2);
-        const float l = fmaf(beta3, s2, nb2 * z);
-        const float e = z > 0.f ? ex2_approx(l - px.y) : 0.f;
-        const float we = px.z * e;                 // dL/ddepth * softmax weight
-        const float zd = z - px.x;
-        const float gs = fmaf(px.w, eA, beta3 * we * zd);       // dL/ds (natural)
-        const float gz = we * fmaf(-beta2, zd, 1.f);            // dL/dz
-        const float gs2 = gs * kLn2;                            // dL/ds2
-        const float gnq = gs2 * qi;
-        const float gq = fmaf(gs2, nq, gz * psv);
-        const float gpsv = gz * qi;
-        const float gvsv = -gq * qi * qi;
-        gC += gs2;
-        gV[0] += gvsv; gV[1] = fmaf(gvsv, du, gV[1]); gV[2] = fmaf(gvsv, dv, gV[2]);
-        gV[3] = fmaf(gvsv, du2, gV[3]); gV[4] = fmaf(gvsv, dudv, gV[4]); gV[5] = fmaf(gvsv, dv2, gV[5]);
-        gP[0] += gpsv; gP[1] = fmaf(gpsv, du, gP[1]); gP[2] = fmaf(gpsv, dv, gP[2]);
-        gN[0] += gnq; gN[1] = fmaf(gnq, eu, gN[1]); gN[2] = fmaf(gnq, ev, gN[2]);
-        gN[3] = fmaf(gnq, eu2, gN[3]); gN[4] = fmaf(gnq, euev, gN[4]); gN[5] = fmaf(gnq, ev2, gN[5]);
-      }
-    }
 
-    // Back through the tile re-expansion (binning.cu tile_record) to record space.
-    const GaussRec g = recs[V.rec_base + gid];
-    const float tcx = tx * TW + 0.5f * (TW - 1), tcy = ty * TH + 0.5f * (TH - 1);
-    const float du = tcx - g.uc, dv = tcy - g.vc;
-    // Same choice of expansion centre as the gather (binning.cu tile_record).
-    const bool near = fabsf(du) <= kNearCentre && fabsf(dv) <= kNearCentre;
-    const float kn = -0.5f * kLog2e;
-    float a0[3], y0[3];
-#pragma unroll
-    for (int c = 0; c < 3; ++c) {
-      a0[c] = fmaf(dv, g.a2[c], fmaf(du, g.a1[c], g.a0[c]));
-      y0[c] = near ? g.y0[c] : fmaf(dv, g.y2[c], fmaf(du, g.y1[c], g.y0[c]));
-    }
-    float ga0[3], ga1[3], ga2[3], gb[3], gy0[3], gy1[3], gy2[3];
-#pragma unroll
-    for (int c = 0; c < 3; ++c) {
-      ga0[c] = 2.f * (gV[0] * a0[c] + gV[1] * g.a1[c] + gV[2] * g.a2[c]) + gP[0] * g.b[c];
-      ga1[c] = 2.f * (gV[1] * a0[c] + gV[3] * g.a1[c] + gV[4] * g.a2[c]) + gP[1] * g.b[c];
-      ga2[c] = 2.f * (gV[2] * a0[c] + gV[4] * g.a1[c] + gV[5] * g.a2[c]) + gP[2] * g.b[c];
-      gb[c] = gP[0] * a0[c] + gP[1] * g.a1[c] + gP[2] * g.a2[c];
-      gy0[c] = 2.f * kn * (gN[0] * y0[c] + gN[1] * g.y1[c] + gN[2] * g.y2[c]);
-      gy1[c] = 2.f * kn * (gN[1] * y0[c] + gN[3] * g.y1[c] + gN[4] * g.y2[c]);
-      gy2[c] = 2.f * kn * (gN[2] * y0[c] + gN[4] * g.y1[c] + gN[5] * g.y2[c]);
-      ga1[c] = fmaf(du, ga0[c], ga1[c]);
-      ga2[c] = fmaf(dv, ga0[c], ga2[c]);
-      if (!near) {
-        gy1[c] = fmaf(du, gy0[c], gy1[c]);
-        gy2[c] = fmaf(dv, gy0[c], gy2[c]);
+    __syncwarp();  // the previous tile's readers are done with the slice
+    for (int q = lane; q < TW * TH; q += 32) {
+      const int ly = q / TW, lx = q - ly * TW;
+      if (lx < xs && ly < ys) {
+        const float4 v = pix[V.pix_base + (int64_t)(ty * TH + ly) * V.W + tx * TW + lx];
+        const int o = ly * Slice::ROW + lx;
+        sl.plane[0][o] = v.x;
+        sl.plane[1][o] = v.y;
+        sl.plane[2][o] = v.z;
+        sl.plane[3][o] = v.w;
       }
     }
-    float* dst = reinterpret_cast<float*>(rgrad + (V.rec_base + gid));
-    red_add_v4(dst + 0, ga0[0], ga0[1], ga0[2], ga1[0]);
-    red_add_v4(dst + 4, ga1[1], ga1[2], ga2[0], ga2[1]);
-    red_add_v4(dst + 8, ga2[2], gb[0], gb[1], gb[2]);
-    red_add_v4(dst + 12, gy0[0], gy0[1], gy0[2], gy1[0]);
-    red_add_v4(dst + 16, gy1[1], gy1[2], gy2[0], gy2[1]);
-    red_add_v4(dst + 20, gy2[2], gC, 0.f, 0.f);
+    __syncwarp();
+
+    for (uint32_t base = range.x; base < range.y; base += 32) {
+      const int cnt = (int)min(32u, range.y - base);
+      int ls = 0;  // log2 of the lanes per key
+      while ((cnt << (ls + 1)) <= 32) ++ls;
+      const int s = 1 << ls;
+      const int kl = lane >> ls, sub = lane & (s - 1);
+      const bool active = kl < cnt;
+      const uint64_t k = base + (uint32_t)(active ? kl : 0);
+
+      // Coefficient gradients: gV over the basis [1, du, dv, du^2, du dv, dv^2] of vsv, gP over
+      // [1, du, dv] of psv, gN over [1, eu, ev, eu^2, eu ev, ev^2] of nq (eu = du - cu,
+      // ev = dv - cv). Within a row dv and ev are constant, so the row's polynomials are folded
+      // to quadratics in du / eu and the pixel loop only accumulates the row moments
+      // S* = sum h du^k with h = -dL/dvsv, Q* = sum dL/dpsv du^k, T* = sum dL/dnq eu^k; the row
+      // end maps them onto the basis.
+      float gV[6] = {0, 0, 0, 0, 0, 0}, gP[3] = {0, 0, 0}, gN[6] = {0, 0, 0, 0, 0, 0}, gC = 0.f;
+      // Record k lives in slot k%2 of pair k/2 (field i at float offset 2*i + slot).
+      const float* tf = reinterpret_cast<const float*>(trec + (k >> 1)) + (k & 1);
+      if (active) {
+        const float V0 = tf[0], V1 = tf[2], V2 = tf[4], V3 = tf[6], V4 = tf[8], V5 = tf[10];
+        const float P0 = tf[12], P1 = tf[14], P2 = tf[16];
+        const float N0 = tf[18], N1 = tf[20], N2 = tf[22], N3 = tf[24], N4 = tf[26], N5 = tf[28];
+        const float C = tf[30], cu = tf[32], cvv = tf[34];
+        const f2_t V3p = f2_pack(V3, V3), P1p = f2_pack(P1, P1), N3p = f2_pack(N3, N3);
+        const f2_t Cp = f2_pack(C, C), CUp = f2_pack(cu, cu);
+        for (int ly = sub; ly < ys; ly += s) {
+          const float dv = ly - 0.5f * (TH - 1), dv2 = dv * dv;
+          const float ev = dv - cvv, ev2 = ev * ev;
+          const float rv0 = fmaf(V5, dv2, fmaf(V2, dv, V0)), rv1 = fmaf(V4, dv, V1);
+          const float rp0 = fmaf(P2, dv, P0);
+          const float rn0 = fmaf(N5, ev2, fmaf(N2, ev, N0)), rn1 = fmaf(N4, ev, N1);
+          const f2_t RV0 = f2_pack(rv0, rv0), RV1 = f2_pack(rv1, rv1), RP0 = f2_pack(rp0, rp0);
+          const f2_t RN0 = f2_pack(rn0, rn0), RN1 = f2_pack(rn1, rn1);
+          f2_t S0 = 0, S1 = 0, S2 = 0, Q0 = 0, Q1 = 0, T0 = 0, T1 = 0, T2 = 0, G = 0;
+          const int o = ly * Slice::ROW;
+          const f2_t* pd = reinterpret_cast<const f2_t*>(&sl.plane[0][o]);
+          const f2_t* pm = reinterpret_cast<const f2_t*>(&sl.plane[1][o]);
+          const f2_t* pz = reinterpret_cast<const f2_t*>(&sl.plane[2][o]);
+          const f2_t* pa = reinterpret_cast<const f2_t*>(&sl.plane[3][o]);
+          f2_t du = f2_pack(-0.5f * (TW - 1), 1.f - 0.5f * (TW - 1));
+          const int pairs = xs >> 1;
+#pragma unroll 2
+          for (int j = 0; j < pairs; ++j, du = add2(du, TWO)) {
+            const f2_t D = pd[j], M = pm[j], GDW = pz[j], GA = pa[j];
+            const f2_t eu = sub2(du, CUp);
+            const f2_t vsv = fma2(fma2(V3p, du, RV1), du, RV0);
+            const f2_t psv = fma2(P1p, du, RP0);
+            const f2_t nq = fma2(fma2(N3p, eu, RN1), eu, RN0);
+            float va, vb;
+            f2_unpack(vsv, va, vb);
+            const f2_t qi = f2_pack(rcp_approx(va), rcp_approx(vb));
+            const f2_t z = mul2(psv, qi);
+            const f2_t s2 = fma2(nq, qi, Cp);
+            float sa, sb;
+            f2_unpack(s2, sa, sb);
+            const f2_t eA = f2_pack(ex2_approx(sa), ex2_approx(sb));
+            const f2_t lm = sub2(fma2(B3, s2, mul2(NB2, z)), M);
+            float la, lb, za, zb;
+            f2_unpack(lm, la, lb);
+            f2_unpack(z, za, zb);
+            const f2_t e = f2_pack(za > 0.f ? ex2_approx(la) : 0.f, zb > 0.f ? ex2_approx(lb) : 0.f);
+            const f2_t we = mul2(GDW, e);                            // dL/ddepth * weight
+            const f2_t zd = sub2(z, D);
+            const f2_t gs = fma2(GA, eA, mul2(mul2(B3, we), zd));    // dL/ds (natural)
+            const f2_t gz = mul2(we, fma2(NEGB2, zd, ONE));           // dL/dz
+            const f2_t gs2 = mul2(gs, LN2);                           // dL/ds2
+            const f2_t gnq = mul2(gs2, qi);
+            const f2_t gq = fma2(gs2, nq, mul2(gz, psv));
+            const f2_t gpsv = mul2(gz, qi);
+            const f2_t h = mul2(mul2(gq, qi), qi);                    // -dL/dvsv
+            G = add2(G, gs2);
+            const f2_t tv = mul2(h, du), tn = mul2(gnq, eu);
+            S0 = add2(S0, h); S1 = add2(S1, tv); S2 = fma2(tv, du, S2);
+            Q0 = add2(Q0, gpsv); Q1 = fma2(gpsv, du, Q1);
+            T0 = add2(T0, gnq); T1 = add2(T1, tn); T2 = fma2(tn, eu, T2);
+          }
+          float s0, s1, s2v, q0, q1, t0, t1, t2, gc;
+          {
+            float a, b;
+            f2_unpack(S0, a, b); s0 = a + b;
+            f2_unpack(S1, a, b); s1 = a + b;
+            f2_unpack(S2, a, b); s2v = a + b;
+            f2_unpack(Q0, a, b); q0 = a + b;
+            f2_unpack(Q1, a, b); q1 = a + b;
+            f2_unpack(T0, a, b); t0 = a + b;
+            f2_unpack(T1, a, b); t1 = a + b;
+            f2_unpack(T2, a, b); t2 = a + b;
+            f2_unpack(G, a, b); gc = a + b;
+          }
+          if (xs & 1) {  // the odd last column
+            const int lx = xs - 1;
+            const float du1 = lx - 0.5f * (TW - 1), eu = du1 - cu;
+            const float D = sl.plane[0][o + lx], M = sl.plane[1][o + lx];
+            const float GDW = sl.plane[2][o + lx], GA = sl.plane[3][o + lx];
+            const float vsv = fmaf(fmaf(V3, du1, rv1), du1, rv0);
+            const float psv = fmaf(P1, du1, rp0);
+            const float nq = fmaf(fmaf(N3, eu, rn1), eu, rn0);
+            const float qi = rcp_approx(vsv);
+            const float z = psv * qi;
+            const float s2 = fmaf(nq, qi, C);
+            const float eA = ex2_approx(s2);
+            const float l = fmaf(beta3, s2, nb2 * z);
+            const float e = z > 0.f ? ex2_approx(l - M) : 0.f;
+            const float we = GDW * e;
+            const float zd = z - D;
+            const float gs = fmaf(GA, eA, beta3 * we * zd);
+            const float gz = we * fmaf(-beta2, zd, 1.f);
+            const float gs2 = gs * kLn2;
+            const float gnq = gs2 * qi;
+            const float gq = fmaf(gs2, nq, gz * psv);
+            const float gpsv = gz * qi;
+            const float h = gq * qi * qi;
+            gc += gs2;
+            const float tv = h * du1, tn = gnq * eu;
+            s0 += h; s1 += tv; s2v = fmaf(tv, du1, s2v);
+            q0 += gpsv; q1 = fmaf(gpsv, du1, q1);
+            t0 += gnq; t1 += tn; t2 = fmaf(tn, eu, t2);
+          }
+          gC += gc;
+          gV[0] -= s0; gV[1] -= s1; gV[2] = fmaf(-dv, s0, gV[2]);
+          gV[3] -= s2v; gV[4] = fmaf(-dv, s1, gV[4]); gV[5] = fmaf(-dv2, s0, gV[5]);
+          gP[0] += q0; gP[1] += q1; gP[2] = fmaf(dv, q0, gP[2]);
+          gN[0] += t0; gN[1] += t1; gN[2] = fmaf(ev, t0, gN[2]);
+          gN[3] += t2; gN[4] = fmaf(ev, t1, gN[4]); gN[5] = fmaf(ev2, t0, gN[5]);
+        }
+      }
+      // Combine the s lanes of each key (all lanes take part; idle lanes hold zeros).
+      for (int o = 1; o < s; o <<= 1) {
+#pragma unroll
+        for (int i = 0; i < 6; ++i) gV[i] += __shfl_xor_sync(full, gV[i], o);
+#pragma unroll
+        for (int i = 0; i < 3; ++i) gP[i] += __shfl_xor_sync(full, gP[i], o);
+#pragma unroll
+        for (int i = 0; i < 6; ++i) gN[i] += __shfl_xor_sync(full, gN[i], o);
+        gC += __shfl_xor_sync(full, gC, o);
+      }
+      if (!active || sub != 0) continue;
+      const uint32_t gid = (uint32_t)keys[k];
+
+      // Back through the tile re-expansion (binning.cu tile_record) to record space.
+      const GaussRec g = recs[V.rec_base + gid];
+      const float tcx = tx * TW + 0.5f * (TW - 1), tcy = ty * TH + 0.5f * (TH - 1);
+      const float du = tcx - g.uc, dv = tcy - g.vc;
+      // Same choice of expansion centre as the gather (binning.cu tile_record).
+      const bool near = fabsf(du) <= kNearCentre && fabsf(dv) <= kNearCentre;
+      const float kn = -0.5f * kLog2e;
+      float a0[3], y0[3];
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        a0[c] = fmaf(dv, g.a2[c], fmaf(du, g.a1[c], g.a0[c]));
+        y0[c] = near ? g.y0[c] : fmaf(dv, g.y2[c], fmaf(du, g.y1[c], g.y0[c]));
+      }
+      float ga0[3], ga1[3], ga2[3], gb[3], gy0[3], gy1[3], gy2[3];
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        ga0[c] = 2.f * (gV[0] * a0[c] + gV[1] * g.a1[c] + gV[2] * g.a2[c]) + gP[0] * g.b[c];
+        ga1[c] = 2.f * (gV[1] * a0[c] + gV[3] * g.a1[c] + gV[4] * g.a2[c]) + gP[1] * g.b[c];
+        ga2[c] = 2.f * (gV[2] * a0[c] + gV[4] * g.a1[c] + gV[5] * g.a2[c]) + gP[2] * g.b[c];
+        gb[c] = gP[0] * a0[c] + gP[1] * g.a1[c] + gP[2] * g.a2[c];
+        gy0[c] = 2.f * kn * (gN[0] * y0[c] + gN[1] * g.y1[c] + gN[2] * g.y2[c]);
+        gy1[c] = 2.f * kn * (gN[1] * y0[c] + gN[3] * g.y1[c] + gN[4] * g.y2[c]);
+        gy2[c] = 2.f * kn * (gN[2] * y0[c] + gN[4] * g.y1[c] + gN[5] * g.y2[c]);
+        ga1[c] = fmaf(du, ga0[c], ga1[c]);
+        ga2[c] = fmaf(dv, ga0[c], ga2[c]);
+        if (!near) {
+          gy1[c] = fmaf(du, gy0[c], gy1[c]);
+          gy2[c] = fmaf(dv, gy0[c], gy2[c]);
+        }
+      }
+      float* dst = reinterpret_cast<float*>(rgrad + (V.rec_base + gid));
+      red_add_v4(dst + 0, ga0[0], ga0[1], ga0[2], ga1[0]);
+      red_add_v4(dst + 4, ga1[1], ga1[2], ga2[0], ga2[1]);
+      red_add_v4(dst + 8, ga2[2], gb[0], gb[1], gb[2]);
+      red_add_v4(dst + 12, gy0[0], gy0[1], gy0[2], gy1[0]);
+      red_add_v4(dst + 16, gy1[1], gy1[2], gy2[0], gy2[1]);
+      red_add_v4(dst + 20, gy2[2], gC, 0.f, 0.f);
+    }
   }
 }
 
@@ -238,14 +382,23 @@ __global__ void record_vjp_kernel(ViewsArg va, int64_t n_rec, const float* __res
 }
 
 template <int TW, int TH>
-void launch_bwd_tiles(const ViewsArg& va, const uint64_t* keys, const Control* ctrl,
-                      int64_t capacity, const TilePair* trec, const GaussRec* recs,
-                      const float4* pix, float beta2, float beta3, RecGrad* rgrad,
+void launch_bwd_tiles(const ViewsArg& va, int64_t n_tiles, const uint64_t* keys,
+                      const uint2* ranges, const TilePair* trec, const GaussRec* recs,
+                      const float4* pix, float beta2, float beta3, RecGrad* rgrad, Control* ctrl,
                       cudaStream_t st) {
-  const int64_t want = (capacity + 127) / 128;
-  const int blocks = (int)(want < 152 * 16 ? (want < 1 ? 1 : want) : 152 * 16);
-  blend_bwd_kernel<TW, TH><<<blocks, 128, 0, st>>>(va, keys, ctrl, trec, recs, pix,
-                                                   -beta2 * kLog2e, beta3, beta2, rgrad);
+  constexpr auto kern = blend_bwd_kernel<TW, TH>;
+  static int resident = 0;
+  if (resident == 0) {
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 32 * kBwdWarps, 0);
+    resident = sms * (per_sm > 0 ? per_sm : 1);
+  }
+  const int64_t grid =
+      std::max<int64_t>(1, std::min<int64_t>((n_tiles + kBwdWarps - 1) / kBwdWarps, resident));
+  kern<<<(unsigned)grid, 32 * kBwdWarps, 0, st>>>(va, (uint32_t)n_tiles, keys, ranges, trec, recs,
+                                                  pix, -beta2 * kLog2e, beta3, beta2, rgrad, ctrl);
 }
 
 }  // namespace
@@ -260,16 +413,17 @@ void launch_pixel_prep(const ViewsArg& va, int64_t n_pix, const float* depth, co
       va, n_pix, depth, stats, stats_stride, grad_depth, grad_alpha, pix);
 }
 
-void launch_blend_bwd(const ViewsArg& va, int tile_w, int tile_h, const uint64_t* keys,
-                      const Control* ctrl, int64_t capacity, const TilePair* trec,
+void launch_blend_bwd(const ViewsArg& va, int tile_w, int tile_h, int64_t n_tiles,
+                      const uint64_t* keys, const uint2* ranges, const TilePair* trec,
                       const GaussRec* recs, const float4* pix, float beta2, float beta3,
-                      RecGrad* rgrad, cudaStream_t st) {
+                      RecGrad* rgrad, Control* ctrl, cudaStream_t st) {
+  if (n_tiles <= 0) return;
   if (tile_w == 8 && tile_h == 8)
-    launch_bwd_tiles<8, 8>(va, keys, ctrl, capacity, trec, recs, pix, beta2, beta3, rgrad, st);
+    launch_bwd_tiles<8, 8>(va, n_tiles, keys, ranges, trec, recs, pix, beta2, beta3, rgrad, ctrl, st);
   else if (tile_w == 32 && tile_h == 8)
-    launch_bwd_tiles<32, 8>(va, keys, ctrl, capacity, trec, recs, pix, beta2, beta3, rgrad, st);
+    launch_bwd_tiles<32, 8>(va, n_tiles, keys, ranges, trec, recs, pix, beta2, beta3, rgrad, ctrl, st);
   else
-    launch_bwd_tiles<16, 16>(va, keys, ctrl, capacity, trec, recs, pix, beta2, beta3, rgrad, st);
+    launch_bwd_tiles<16, 16>(va, n_tiles, keys, ranges, trec, recs, pix, beta2, beta3, rgrad, ctrl, st);
 }
 
 void launch_record_vjp(const ViewsArg& va, int64_t n_rec, const float* means, const float* prec,

@@ -267,15 +267,15 @@ __global__ void __launch_bounds__(BlendShape<TW, TH, PX, CH>::NT) blend_fwd_kern
   }
 }
 
-// Resident CTAs of one kernel instance on the current device (queried once per instance).
-template <class K>
-int resident_ctas(K kernel, int threads) {
+// CTAs of `Kern` resident on the current device (queried once per kernel instantiation).
+template <auto Kern>
+int resident_ctas(int threads) {
   static int cached = 0;
   if (cached == 0) {
     int dev = 0, sms = 0, per_sm = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, Kern, threads, 0);
     cached = sms * (per_sm > 0 ? per_sm : 1);
   }
   return cached;
@@ -286,8 +286,8 @@ void launch_tiles(const ViewsArg& va, int64_t n_tiles, const TilePair* trec, con
                   float nb2, float beta3, float* depth, float* alpha, float* stats,
                   int64_t stats_stride, Control* ctrl, cudaStream_t st) {
   constexpr int NT = BlendShape<TW, TH, PX, CH>::NT;
-  auto kern = blend_fwd_kernel<TW, TH, PX, CH>;
-  const int64_t grid = std::min<int64_t>(n_tiles, resident_ctas(kern, NT));
+  constexpr auto kern = blend_fwd_kernel<TW, TH, PX, CH>;
+  const int64_t grid = std::min<int64_t>(n_tiles, resident_ctas<kern>(NT));
   kern<<<(unsigned)grid, NT, 0, st>>>(va, (uint32_t)n_tiles, trec, ranges, nb2, beta3, depth,
                                       alpha, stats, stats_stride, ctrl);
 }

@@ -57,10 +57,10 @@ void launch_blend_fwd(const ViewsArg& va, int tile_w, int tile_h, int px, int ch
 void launch_pixel_prep(const ViewsArg& va, int64_t n_pix, const float* depth, const float* stats,
                        int64_t stats_stride, const float* grad_depth, const float* grad_alpha,
                        float4* pix, cudaStream_t st);
-void launch_blend_bwd(const ViewsArg& va, int tile_w, int tile_h, const uint64_t* keys,
-                      const Control* ctrl, int64_t capacity, const TilePair* trec,
+void launch_blend_bwd(const ViewsArg& va, int tile_w, int tile_h, int64_t n_tiles,
+                      const uint64_t* keys, const uint2* ranges, const TilePair* trec,
                       const GaussRec* recs, const float4* pix, float beta2, float beta3,
-                      RecGrad* rgrad, cudaStream_t st);
+                      RecGrad* rgrad, Control* ctrl, cudaStream_t st);
 // Gradients are accumulated (atomically) into gmeans/gprec/glogw, which must be zeroed first.
 void launch_record_vjp(const ViewsArg& va, int64_t n_rec, const float* means, const float* prec,
                        const float* quat, const float* trans, const GaussRec* recs,

@@ -221,7 +221,7 @@ struct Lane {
 
     if (!plan) {
       fe_render_desc d = s->cfg.desc;
-      d.flags |= FE_FLAG_EXACT_KEYS;
+      d.flags |= FE_FLAG_EXACT_KEYS | FE_FLAG_KEEP_BINNING;  // backward right after forward
       rc = fe_batch_create(&d, scenes.data(), nr, views.data(), (int32_t)views.size(), &plan);
       if (rc) {
         plan = nullptr;

@@ -65,6 +65,11 @@ typedef enum fe_cull_mode {
 /* Batches only: size the key scratch from the device-side key count (one 8-byte readback and a
  * stream synchronisation per run) instead of the worst case (views x Gaussians x tiles). */
 #define FE_FLAG_EXACT_KEYS 2u
+/* Batches only: keep the binning (keys, tile records, ranges) of the last fe_batch_fwd and reuse
+ * it in an fe_batch_bwd that gets the same Gaussian pointers with no fe_batch_reset in between,
+ * instead of recomputing it. The caller guarantees that the Gaussian data did not change between
+ * the two calls. */
+#define FE_FLAG_KEEP_BINNING 4u
 
 /* Render descriptor: everything a render needs besides the Gaussian and pose buffers. It is also
  * the opaque payload of the XLA custom call targets (bit-copied; the size and magic are checked).

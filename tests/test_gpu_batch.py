@@ -16,7 +16,7 @@ from tests.helpers import scene_to_dev
 pytestmark = pytest.mark.gpu
 
 
-def make_batch(dev, n_scenes=6, seed=0, tile=(16, 16)):
+def make_batch(dev, n_scenes=6, seed=0, tile=(16, 16), **kw):
     items = S.config3(seed=seed, n_scenes=n_scenes)
     means, prec, logw, scenes, views = [], [], [], [], []
     off = 0
@@ -27,7 +27,7 @@ def make_batch(dev, n_scenes=6, seed=0, tile=(16, 16)):
         for c in cams:
             views.append(dict(scene=si, height=c.height, width=c.width, fx=c.fx, fy=c.fy, cx=c.cx,
                               cy=c.cy, quat=c.quat, trans=c.trans))
-    b = fe.Batch(scenes, views, tile=tile)
+    b = fe.Batch(scenes, views, tile=tile, **kw)
     tens = [torch.from_numpy(np.concatenate(x)).to(dev) for x in (means, prec, logw)]
     return b, items, views, tens
 
@@ -95,3 +95,33 @@ def test_batch_replays_from_cuda_graph(cuda_device):
     g.replay()
     torch.cuda.synchronize()
     assert torch.equal(depth, ref_d) and torch.equal(alpha, ref_a)
+
+
+def test_backward_reusing_the_forward_binning_equals_recomputing(cuda_device):
+    """FE_FLAG_KEEP_BINNING: the backward right after a forward on the same tensors reuses its
+    binning and gives the same gradients; a backward on other tensors recomputes."""
+    dev = cuda_device
+    ref, _, _, (m, p, w) = make_batch(dev, n_scenes=4, seed=2)
+    keep, _, _, _ = make_batch(dev, n_scenes=4, seed=2, keep_binning=True)
+    gen = torch.Generator(device=dev).manual_seed(3)
+    outs = []
+    for b in (ref, keep):
+        stats = torch.empty(3 * b.n_pixels, device=dev)
+        depth, alpha = b.forward(m, p, w, stats=stats)
+        gd = torch.randn(b.n_pixels, device=dev, generator=gen) * 1e-2
+        ga = torch.randn(b.n_pixels, device=dev, generator=gen)
+        gen.manual_seed(3)
+        outs.append(b.backward(m, p, w, depth, alpha, stats, gd, ga))
+    # (the record gradients are accumulated with atomics: equal up to summation order)
+    for x, y in zip(*outs):
+        assert float((x - y).norm()) <= 1e-5 * float(y.norm()) + 1e-12
+    # Other tensors (same values, new storage): the kept binning is not used for them.
+    m2, p2, w2 = m.clone() * 1.0001, p.clone(), w.clone()
+    stats = torch.empty(3 * keep.n_pixels, device=dev)
+    depth, alpha = ref.forward(m2, p2, w2, stats=stats)
+    gd = torch.randn(keep.n_pixels, device=dev, generator=gen) * 1e-2
+    ga = torch.randn(keep.n_pixels, device=dev, generator=gen)
+    g_ref = ref.backward(m2, p2, w2, depth, alpha, stats, gd, ga)
+    g_keep = keep.backward(m2, p2, w2, depth, alpha, stats, gd, ga)  # last forward was on m, p, w
+    for x, y in zip(g_ref, g_keep):
+        assert float((x - y).norm()) <= 1e-5 * float(y.norm()) + 1e-12

@@ -67,22 +67,25 @@ def test_silhouette_bce_gradients_match_float64_autograd(cuda_device, cfg2):
     assert torch.all(torch.tril(gp, -1) == 0)  # like jax.grad through triu
 
 
-def test_depth_gradients_match_float64_autograd(cuda_device):
+@pytest.mark.parametrize("H,W,tile", [(64, 64, (16, 16)), (37, 53, (16, 16)), (29, 45, (8, 8)),
+                                      (41, 77, (32, 8))])
+def test_depth_gradients_match_float64_autograd(cuda_device, H, W, tile):
+    """Ragged sizes (odd widths, partial edge tiles) on every tile shape."""
     scene, cams = S.config0(seed=1)
     c = cams[0]
-    H = W = 64
-    f, cx = 64.0, 32.0
+    f = float(max(H, W))
+    cx, cy = W / 2, H / 2
     dev = cuda_device
-    _, a_ref = O.render_pinhole(scene.means, scene.prec, scene.logw, H, W, f, f, cx, cx, c.quat, c.trans)
+    _, a_ref = O.render_pinhole(scene.means, scene.prec, scene.logw, H, W, f, f, cx, cy, c.quat, c.trans)
     gen = torch.Generator().manual_seed(0)
     # Depth cotangents only where depth is meaningful (alpha > 1e-2), alpha cotangents everywhere.
     gd = torch.randn(H, W, generator=gen, dtype=torch.float64) * torch.from_numpy(a_ref > 1e-2)
     ga = torch.randn(H, W, generator=gen, dtype=torch.float64)
     m, p, w = [t.clone().requires_grad_() for t in scene_to_dev(scene, dev)]
-    d, a = fe.render(m, p, w, f, f, cx, cx, c.quat, c.trans, H, W)
+    d, a = fe.render(m, p, w, f, f, cx, cy, c.quat, c.trans, H, W, tile=tile)
     (d.double() * gd.to(dev) + a.double() * ga.to(dev)).sum().backward()
     m64, p64, w64 = [torch.from_numpy(x).double().requires_grad_() for x in (scene.means, scene.prec, scene.logw)]
-    d64, a64 = OT.render_pinhole(m64, p64, w64, H, W, f, f, cx, cx,
+    d64, a64 = OT.render_pinhole(m64, p64, w64, H, W, f, f, cx, cy,
                                  torch.from_numpy(c.quat).double(), torch.from_numpy(c.trans).double())
     (d64 * gd + a64 * ga).sum().backward()
     assert rel(m.grad.double().cpu(), m64.grad) < GRAD_TOL
