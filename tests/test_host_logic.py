@@ -100,3 +100,14 @@ def test_footprint_matches_the_library_admission_unit():
             for tile in (8, 16):
                 assert lib.fe_request_footprint(ctypes.byref(r), tile, tile) == \
                     serve.estimate_footprint(req, tile)
+
+
+def test_jax_binding_reports_missing_jax():
+    import importlib
+    try:
+        import jax  # noqa: F401
+        pytest.skip("jax is installed: the binding is importable")
+    except ImportError:
+        pass
+    with pytest.raises(ImportError, match="JAX"):
+        importlib.import_module("fuzzy_ellipses.jax_ops")
