@@ -458,6 +458,28 @@ int fe_silhouette_bce(const float* alpha, const float* target, const int64_t* se
   return FE_OK;
 }
 
+int fe_gmm_log_likelihood(const float* means, const float* prec, const float* logw, int32_t n,
+                          const float* points, int64_t n_points, float* point_ll, float* res,
+                          double* total, fe_stream_t stream_) {
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream_);
+  if (n < 1 || n_points < 0)
+    return fail(FE_ERR_INVALID_ARGUMENT, "fe_gmm_log_likelihood: need n >= 1 and n_points >= 0");
+  if (!means || !prec || !logw || (n_points > 0 && (!points || !point_ll)))
+    return fail(FE_ERR_INVALID_ARGUMENT, "fe_gmm_log_likelihood: NULL argument");
+  if (total) FE_CUDA(cudaMemsetAsync(total, 0, sizeof(double), st));
+  if (n_points == 0) return FE_OK;
+  Arena* a = nullptr;
+  int rc = arena_for(st, &a);
+  if (rc) return rc;
+  // The records' scratch is the front of the arena's record buffer.
+  rc = a->rec.reserve(gmm_scratch_bytes(n), st);
+  if (rc) return rc;
+  launch_gmm_log_likelihood(n, means, prec, logw, n_points, points, point_ll, res, total,
+                            a->rec.ptr, st);
+  FE_CUDA(cudaGetLastError());
+  return FE_OK;
+}
+
 int fe_check_device_status(fe_stream_t stream_, uint32_t* device_error) {
   cudaStream_t st = reinterpret_cast<cudaStream_t>(stream_);
   Arena* a = nullptr;

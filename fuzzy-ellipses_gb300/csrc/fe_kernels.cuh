@@ -75,4 +75,14 @@ void launch_silhouette_bce(const float* alpha, const float* target, const int64_
                            int n_seg, int64_t n_pix, float* galpha, double* loss,
                            cudaStream_t st);
 
+// gmm.cu
+// Log-likelihood of points under the mixture (fm_render.py log_likelihood): point_ll[j] =
+// logsumexp_i r_ij; res (n x n_points, row per Gaussian) receives r_ij when non-NULL; total
+// (float64, zeroed by the caller) accumulates sum_j point_ll[j] when non-NULL.
+// scratch: gmm_scratch_bytes(n) bytes of device memory.
+size_t gmm_scratch_bytes(int n);
+void launch_gmm_log_likelihood(int n, const float* means, const float* prec, const float* logw,
+                               int64_t n_points, const float* points, float* point_ll,
+                               float* res, double* total, void* scratch, cudaStream_t st);
+
 }  // namespace fe

@@ -9,7 +9,8 @@ Gaussian precision factor and a (quaternion, translation) pose like ``baseline/f
 
 from . import autotune, serve, synthetic  # noqa: F401
 from ._native import FEError, NativeLibraryMissing, load as load_native  # noqa: F401
-from .api import (Batch, bench_peak, device_status, projection_matrix, rasterize, reference_binning,  # noqa: F401
-                     reference_num_stds, render, render_binning, render_forward)
+from .api import (Batch, bench_peak, device_status, gmm_log_likelihood,  # noqa: F401
+                  projection_matrix, rasterize, reference_binning, reference_num_stds, render,
+                  render_binning, render_forward, silhouette_bce)
 
 __version__ = "0.1.0"

@@ -171,6 +171,30 @@ def silhouette_bce(alpha, target, seg_end, galpha=None, loss=None):
     return loss, galpha
 
 
+def gmm_log_likelihood(means, prec, logw, points, *, return_matrix=False):
+    """Log-likelihood of points (P, 3) under the mixture (the reference's ``log_likelihood``,
+    baseline/fm_render.py:231-259): returns ``(nll, point_ll)`` -- the mean negative
+    log-likelihood (float64 scalar tensor, the reference's first output) and the per-point
+    log-likelihoods (P,) -- plus, with ``return_matrix=True``, the per-(Gaussian, point) log
+    terms (N, P) (the reference's second output)."""
+    lib = N.load()
+    n = _check_inputs(means, prec, logw)
+    if n < 1:
+        raise ValueError("need at least one Gaussian")
+    if points.dtype != torch.float32 or points.dim() != 2 or points.shape[1] != 3:
+        raise ValueError("points must be float32 of shape (P, 3)")
+    points = points.contiguous()
+    P = points.shape[0]
+    dev = means.device
+    point_ll = torch.empty(P, device=dev)
+    total = torch.empty(1, dtype=torch.float64, device=dev)
+    res = torch.empty((n, P), device=dev) if return_matrix else None
+    N.check(lib.fe_gmm_log_likelihood(_ptr(means), _ptr(prec), _ptr(logw), n, _ptr(points), P,
+                                      _ptr(point_ll), _ptr(res), _ptr(total), _stream()))
+    nll = -total[0] / max(P, 1)
+    return (nll, point_ll, res) if return_matrix else (nll, point_ll)
+
+
 def bench_peak(kind):
     """Measured pipe throughput (operations/s): 'fma' (FP32 FMA), 'ex2' (MUFU ex2) or 'fma2'
     (packed f32x2 FMA, two FMAs per instruction)."""

@@ -370,6 +370,19 @@ int fe_silhouette_bce(const float *d_alpha, const float *d_target, const int64_t
                       int32_t n_seg, int64_t n_pix, float *d_galpha, double *d_loss,
                       fe_stream_t stream);
 
+/* Log-likelihood of 3-D points under the Gaussian mixture: the reference's log_likelihood
+ * (baseline/fm_render.py:231-259), which evaluates it in JAX. For Gaussians i (d_means (n,3),
+ * d_prec (n,3,3) with only the upper triangle read, Sigma^-1 = U U^T, d_logw (n) unnormalised
+ * log weights) and points j (d_points (n_points,3)):
+ *   r_ij = log softmax(logw)_i + log|det U_i| - (|U_i^T (mu_i - x_j)|^2 + 3 log(2 pi)) / 2
+ * writes d_point_ll[j] = logsumexp_i r_ij, d_res[i * n_points + j] = r_ij when d_res is not NULL
+ * (the reference's second output, transposed: n x n_points), and d_total (float64) = sum_j
+ * d_point_ll[j] when not NULL (the reference's first output is -d_total / n_points). Uses the
+ * per-stream arena for 48 B of scratch per Gaussian. */
+int fe_gmm_log_likelihood(const float *d_means, const float *d_prec, const float *d_logw,
+                          int32_t n, const float *d_points, int64_t n_points, float *d_point_ll,
+                          float *d_res, double *d_total, fe_stream_t stream);
+
 /* Synchronise `stream` and return the device-side error word of the arena used by calls on that
  * stream (0 = no error; see FE_DEVERR_*), clearing it. */
 int fe_check_device_status(fe_stream_t stream, uint32_t *device_error);

@@ -144,3 +144,25 @@ def test_screen_bounds_contain_the_k_sigma_ellipsoid():
         if inside.all():  # tight: the samples reach the rectangle's edge tiles (within one)
             assert tx.min() <= x0 + 1 and tx.max() >= x1 - 2
             assert ty.min() <= y0 + 1 and ty.max() >= y1 - 2
+
+
+def test_gmm_oracle_matches_sklearn_score_samples():
+    """The restated log_likelihood equals scikit-learn's GaussianMixture.score_samples with the
+    same weights, means and precision Cholesky factors (fm_render's prec_full is sklearn's
+    precisions_cholesky_ convention)."""
+    sk = pytest.importorskip("sklearn.mixture")
+    from fuzzy_ellipses import synthetic as S
+    from oracle import gmm_np
+    rng = np.random.default_rng(4)
+    sc = S.random_gaussians(12, 0.2, rng)
+    pts = rng.uniform(-0.3, 0.3, size=(500, 3))
+    nll, res, lse = gmm_np.log_likelihood(sc.means, sc.prec, sc.logw, pts)
+    g = sk.GaussianMixture(n_components=12, covariance_type="full")
+    w = np.exp(sc.logw.astype(np.float64))
+    g.weights_ = w / w.sum()
+    g.means_ = sc.means.astype(np.float64)
+    g.precisions_cholesky_ = np.triu(sc.prec.astype(np.float64))
+    ref = g.score_samples(pts)
+    assert np.allclose(lse, ref, rtol=1e-10, atol=1e-9)
+    assert abs(nll + ref.mean()) < 1e-9 * abs(ref.mean())
+    assert res.shape == (12, 500)
