@@ -480,6 +480,55 @@ int fe_gmm_log_likelihood(const float* means, const float* prec, const float* lo
   return FE_OK;
 }
 
+int fe_prec_from_scale_rot(const float* scales, const float* quats, int64_t n, float* prec,
+                           fe_stream_t stream_) {
+  if (n < 0 || (n > 0 && (!scales || !quats || !prec)))
+    return fail(FE_ERR_INVALID_ARGUMENT, "fe_prec_from_scale_rot: bad arguments");
+  launch_prec_from_scale_rot(n, scales, quats, prec, reinterpret_cast<cudaStream_t>(stream_));
+  FE_CUDA(cudaGetLastError());
+  return FE_OK;
+}
+
+int fe_prec_from_scale_rot_bwd(const float* scales, const float* quats, int64_t n,
+                               const float* grad_prec, float* grad_scales, float* grad_quats,
+                               fe_stream_t stream_) {
+  if (n < 0 || (n > 0 && (!scales || !quats || !grad_prec || !grad_scales || !grad_quats)))
+    return fail(FE_ERR_INVALID_ARGUMENT, "fe_prec_from_scale_rot_bwd: bad arguments");
+  launch_prec_from_scale_rot_bwd(n, scales, quats, grad_prec, grad_scales, grad_quats,
+                                 reinterpret_cast<cudaStream_t>(stream_));
+  FE_CUDA(cudaGetLastError());
+  return FE_OK;
+}
+
+int fe_transform_points(const float* points, int64_t n, const float* pose, int32_t inverse,
+                        float* out, fe_stream_t stream_) {
+  if (n < 0 || !pose || (n > 0 && (!points || !out)))
+    return fail(FE_ERR_INVALID_ARGUMENT, "fe_transform_points: bad arguments");
+  launch_transform_points(n, points, pose, inverse ? 1 : 0, out,
+                          reinterpret_cast<cudaStream_t>(stream_));
+  FE_CUDA(cudaGetLastError());
+  return FE_OK;
+}
+
+int fe_transform_points_bwd(const float* points, int64_t n, const float* pose, int32_t inverse,
+                            const float* grad_out, float* grad_points, float* grad_pose,
+                            fe_stream_t stream_) {
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream_);
+  if (n < 0 || !pose || (n > 0 && (!points || !grad_out)))
+    return fail(FE_ERR_INVALID_ARGUMENT, "fe_transform_points_bwd: bad arguments");
+  Arena* a = nullptr;
+  int rc = arena_for(st, &a);
+  if (rc) return rc;
+  rc = a->rec.reserve(12 * sizeof(double), st);
+  if (rc) return rc;
+  double* gacc = reinterpret_cast<double*>(a->rec.ptr);
+  FE_CUDA(cudaMemsetAsync(gacc, 0, 12 * sizeof(double), st));
+  launch_transform_points_bwd(n, points, pose, inverse ? 1 : 0, grad_out, grad_points, grad_pose,
+                              gacc, st);
+  FE_CUDA(cudaGetLastError());
+  return FE_OK;
+}
+
 int fe_check_device_status(fe_stream_t stream_, uint32_t* device_error) {
   cudaStream_t st = reinterpret_cast<cudaStream_t>(stream_);
   Arena* a = nullptr;

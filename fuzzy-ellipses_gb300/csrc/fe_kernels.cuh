@@ -85,4 +85,20 @@ void launch_gmm_log_likelihood(int n, const float* means, const float* prec, con
                                int64_t n_points, const float* points, float* point_ll,
                                float* res, double* total, void* scratch, cudaStream_t st);
 
+// adapters.cu
+// Upper precision factor (n,3,3) from scales (n,3) and scalar-first quaternions (n,4), and its
+// backward (gradients of the upper-triangle entries to scales and quaternions).
+void launch_prec_from_scale_rot(int64_t n, const float* scales, const float* quats, float* prec,
+                                cudaStream_t st);
+void launch_prec_from_scale_rot_bwd(int64_t n, const float* scales, const float* quats,
+                                    const float* gprec, float* gscales, float* gquats,
+                                    cudaStream_t st);
+// out = R(q) p + t (inverse = 0) or R(q)^T p + t (inverse = 1), pose = [t(3), q(4)]; the backward
+// writes dL/dpoints (if non-NULL) and dL/dpose (7, if non-NULL) using gacc (12 doubles, zeroed).
+void launch_transform_points(int64_t n, const float* points, const float* pose, int inverse,
+                             float* out, cudaStream_t st);
+void launch_transform_points_bwd(int64_t n, const float* points, const float* pose, int inverse,
+                                 const float* gout, float* gpoints, float* gpose, double* gacc,
+                                 cudaStream_t st);
+
 }  // namespace fe

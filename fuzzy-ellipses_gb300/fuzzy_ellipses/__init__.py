@@ -7,7 +7,7 @@ Gaussian precision factor and a (quaternion, translation) pose like ``baseline/f
 ``_lib/libfuzzy_ellipses.so``; there is no CPU path.
 """
 
-from . import autotune, serve, synthetic  # noqa: F401
+from . import adapters, autotune, serve, synthetic  # noqa: F401
 from ._native import FEError, NativeLibraryMissing, load as load_native  # noqa: F401
 from .api import (Batch, bench_peak, device_status, gmm_log_likelihood,  # noqa: F401
                   projection_matrix, rasterize, reference_binning, reference_num_stds, render,

@@ -134,6 +134,10 @@ PROTOTYPES = {
     "fe_render_fwd_noalloc": (ctypes.c_int, [ctypes.POINTER(RenderDesc)] + [P] * 9 + [P]),
     "fe_silhouette_bce": (ctypes.c_int, [P, P, P, I32, I64, P, P, P]),
     "fe_gmm_log_likelihood": (ctypes.c_int, [P, P, P, I32, P, I64, P, P, P, P]),
+    "fe_prec_from_scale_rot": (ctypes.c_int, [P, P, I64, P, P]),
+    "fe_prec_from_scale_rot_bwd": (ctypes.c_int, [P, P, I64, P, P, P, P]),
+    "fe_transform_points": (ctypes.c_int, [P, I64, P, I32, P, P]),
+    "fe_transform_points_bwd": (ctypes.c_int, [P, I64, P, I32, P, P, P, P]),
     "fe_render_bwd": (ctypes.c_int, [ctypes.POINTER(RenderDesc)] + [P] * 13 + [P]),
     "fe_render_binning": (ctypes.c_int, [ctypes.POINTER(RenderDesc)] + [P] * 6 + [I64, P,
                                                                                 ctypes.POINTER(I64), P]),

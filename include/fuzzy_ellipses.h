@@ -383,6 +383,29 @@ int fe_gmm_log_likelihood(const float *d_means, const float *d_prec, const float
                           int32_t n, const float *d_points, int64_t n_points, float *d_point_ll,
                           float *d_res, double *d_total, fe_stream_t stream);
 
+/* Scene-parameter adapters (device kernels, float64 inside).
+ * fe_prec_from_scale_rot: the renderer's upper-triangular precision factor U (n,3,3, row-major,
+ * zeros below the diagonal; U U^T = Sigma^-1) of Sigma = R(q) diag(s)^2 R(q)^T from scales (n,3)
+ * and scalar-first quaternions (n,4) -- the covariance of the reference's prec_from_rotscale
+ * (utils/sfs_utils.py:207-213) and CUDA rasterizer (forward.cu computeCov3D). (The reference's
+ * prec_from_rotscale returns the lower factor cholesky(Sigma^-1), of which fm_render's triu keeps
+ * only the diagonal; this is the factor the renderer's convention needs.)
+ * fe_prec_from_scale_rot_bwd: gradients of the upper-triangle entries to scales and quaternions. */
+int fe_prec_from_scale_rot(const float *d_scales, const float *d_quats, int64_t n, float *d_prec,
+                           fe_stream_t stream);
+int fe_prec_from_scale_rot_bwd(const float *d_scales, const float *d_quats, int64_t n,
+                               const float *d_grad_prec, float *d_grad_scales,
+                               float *d_grad_quats, fe_stream_t stream);
+/* Rigid transform of points (n,3) by a pose d_pose = [t(3), q(4)] (scalar-first quaternion, the
+ * reference's layout): out = R(q) p + t (inverse = 0; transform_points_jittable,
+ * utils/sfs_utils.py:171-172) or R(q)^T p + t (inverse = 1; transform_points_by_inv_jittable,
+ * :182-184). The backward writes dL/dpoints (when not NULL) and dL/dpose (7, when not NULL). */
+int fe_transform_points(const float *d_points, int64_t n, const float *d_pose, int32_t inverse,
+                        float *d_out, fe_stream_t stream);
+int fe_transform_points_bwd(const float *d_points, int64_t n, const float *d_pose,
+                            int32_t inverse, const float *d_grad_out, float *d_grad_points,
+                            float *d_grad_pose, fe_stream_t stream);
+
 /* Synchronise `stream` and return the device-side error word of the arena used by calls on that
  * stream (0 = no error; see FE_DEVERR_*), clearing it. */
 int fe_check_device_status(fe_stream_t stream, uint32_t *device_error);

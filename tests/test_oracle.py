@@ -166,3 +166,23 @@ def test_gmm_oracle_matches_sklearn_score_samples():
     assert np.allclose(lse, ref, rtol=1e-10, atol=1e-9)
     assert abs(nll + ref.mean()) < 1e-9 * abs(ref.mean())
     assert res.shape == (12, 500)
+
+
+def test_adapter_oracle_factor_is_upper_and_inverts_the_covariance():
+    import torch
+
+    from oracle import adapters_torch as AT
+    g = torch.Generator().manual_seed(0)
+    s = torch.rand(50, 3, generator=g, dtype=torch.float64) * 0.03 + 0.005
+    q = torch.randn(50, 4, generator=g, dtype=torch.float64)
+    U = AT.prec_from_scale_rot(s, q)
+    assert torch.all(torch.tril(U, -1) == 0)
+    R = AT.quat_to_rot(q)
+    cov = (R * s[:, None, :] ** 2) @ R.transpose(-1, -2)
+    eye = torch.eye(3, dtype=torch.float64).expand(50, 3, 3)
+    assert torch.allclose(U @ U.transpose(-1, -2) @ cov, eye, atol=1e-9)
+    # the pose transforms agree with rotating by R / R^T
+    pose = torch.cat([torch.randn(3, generator=g, dtype=torch.float64), q[0]])
+    p = torch.randn(10, 3, generator=g, dtype=torch.float64)
+    assert torch.allclose(AT.transform_points(pose, p), (R[0] @ p.T).T + pose[:3])
+    assert torch.allclose(AT.transform_points_by_inv(pose, p), (R[0].T @ p.T).T + pose[:3])
