@@ -529,6 +529,58 @@ int fe_transform_points_bwd(const float* points, int64_t n, const float* pose, i
   return FE_OK;
 }
 
+void fe_pixlist_desc_init(fe_pixlist_desc* d, int32_t n, int32_t n_poses, int64_t n_rays,
+                          float inv_f) {
+  std::memset(d, 0, sizeof(*d));
+  d->magic = FE_DESC_MAGIC;
+  d->version = FE_DESC_VERSION;
+  d->n_gaussians = n;
+  d->n_poses = n_poses;
+  d->n_rays = n_rays;
+  d->inv_f = inv_f;
+  d->beta2 = 21.4f;
+  d->beta3 = 2.66f;
+  d->cull_mode = FE_CULL_EPS;
+  d->cull_param = kDefaultCullEps;
+}
+
+int fe_render_pixels(const fe_pixlist_desc* d, const float* means, const float* prec,
+                     const float* logw, const float* poses, const float* rays,
+                     const float* features, float* depth, float* alpha, float* flow_next,
+                     float* flow_prev, float* out_features, float* weights,
+                     fe_stream_t stream_) {
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream_);
+  if (!d) return fail(FE_ERR_INVALID_ARGUMENT, "descriptor is NULL");
+  if (d->magic != FE_DESC_MAGIC || d->version != FE_DESC_VERSION)
+    return fail(FE_ERR_DESCRIPTOR, "pixel-list descriptor magic/version mismatch");
+  if (d->n_gaussians < 0 || d->n_poses < 1 || d->n_rays < 0)
+    return fail(FE_ERR_INVALID_ARGUMENT, "need n_gaussians >= 0, n_poses >= 1, n_rays >= 0");
+  if (!(d->inv_f != 0.f) || !std::isfinite(d->inv_f))
+    return fail(FE_ERR_INVALID_ARGUMENT, "inv_f must be finite and non-zero");
+  if (d->cull_mode != FE_CULL_EPS && d->cull_mode != FE_CULL_NSTD)
+    return fail(FE_ERR_INVALID_ARGUMENT, "unknown cull mode");
+  if (d->n_features < 0 || d->n_features > 16)
+    return fail(FE_ERR_UNSUPPORTED, "n_features must be in [0, 16]");
+  if ((d->n_features > 0) != (features != nullptr) || (out_features && d->n_features == 0))
+    return fail(FE_ERR_INVALID_ARGUMENT, "features and n_features must be given together");
+  if (d->n_rays == 0) return FE_OK;
+  if (!poses || !rays || !depth || !alpha ||
+      (d->n_gaussians > 0 && (!means || !prec || !logw)))
+    return fail(FE_ERR_INVALID_ARGUMENT, "NULL argument");
+  Arena* a = nullptr;
+  int rc = arena_for(st, &a);
+  if (rc) return rc;
+  rc = a->rec.reserve(std::max<size_t>(pixlist_scratch_bytes(d->n_gaussians, d->n_poses), 256),
+                      st);
+  if (rc) return rc;
+  launch_render_pixels(d->n_gaussians, d->n_poses, means, prec, logw, poses, d->n_rays, rays,
+                       d->inv_f, d->beta2, d->beta3, d->cull_mode, d->cull_param, features,
+                       d->n_features, depth, alpha, flow_next, flow_prev, out_features, weights,
+                       a->rec.ptr, st);
+  FE_CUDA(cudaGetLastError());
+  return FE_OK;
+}
+
 int fe_check_device_status(fe_stream_t stream_, uint32_t* device_error) {
   cudaStream_t st = reinterpret_cast<cudaStream_t>(stream_);
   Arena* a = nullptr;

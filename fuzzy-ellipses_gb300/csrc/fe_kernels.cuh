@@ -101,4 +101,16 @@ void launch_transform_points_bwd(int64_t n, const float* points, const float* po
                                  const float* gout, float* gpoints, float* gpose, double* gacc,
                                  cudaStream_t st);
 
+// pixlist.cu
+// Multi-pose pixel-list render (fm_render.py render_func_idx_quattrans[_flow]); scratch:
+// pixlist_scratch_bytes(n, n_poses). feats (n x nf, nf <= 16), flows, out_feats and weights
+// (n x n_rays) are optional (NULL).
+size_t pixlist_scratch_bytes(int n, int n_poses);
+void launch_render_pixels(int n, int n_poses, const float* means, const float* prec,
+                          const float* logw, const float* poses, int64_t n_rays, const float* rays,
+                          float inv_f, float beta2, float beta3, int cull_mode, float cull_param,
+                          const float* feats, int nf, float* depth, float* alpha,
+                          float* flow_next, float* flow_prev, float* out_feats, float* weights,
+                          void* scratch, cudaStream_t st);
+
 }  // namespace fe

@@ -10,6 +10,7 @@
 //    computeCov3D :65-122, computeCov2D :21-60 and auxiliary.h:46-61,144-169), restated with
 //    explicitly rounded float operations so the compiler cannot contract them, which makes its
 //    tile rectangles bit-reproducible (the reference built with -fmad=false computes the same).
+#include "fe_footprint.cuh"
 #include "fe_kernels.cuh"
 
 namespace fe {
@@ -107,110 +108,31 @@ __device__ __forceinline__ int clamp_tile(double x, int lo, int hi) {
 // Exact-projection binning (float32, cancellation-free forms)
 // ------------------------------------------------------------------------------------------
 
-// Record and footprint of one (Gaussian, view) pair in float32.
-//   M = U^T R^T (a = M rays_cam), Y = cof(M), det M = U00 U11 U22 (R is a rotation).
-//   Camera-frame covariance: Sc = Yh^T Yh with Yh = Y / det M = M^-T (entries of order sigma).
-//   The k-sigma ellipsoid's outline is the conic whose dual is C = k2 Sc - p p^T (p: camera-frame
-//   mean, k2 = k^2). Its vertical tangents x = (c02 +- sqrt(D)) / c22 use
-//     D = c02^2 - c00 c22 = k2 (|pz Yh0 - px Yh2|^2 - k2 |Yh0 x Yh2|^2)
-//   (Yh0, Yh2: columns of Yh), where the p^4 terms cancel analytically; likewise for y.
+// Record and tile footprint of one (Gaussian, view) pair in float32 (fe_footprint.cuh).
 __device__ __forceinline__ void footprint_and_record(
     const float* mean, const float* prec, float logw, const float* R, const float* t,
     const ViewDev& V, int cull_mode, float cull_param, int tile_w, int tile_h, GaussRec& rec,
     int& tx0, int& ty0, int& tx1, int& ty1) {
-  const float U00 = prec[0], U01 = prec[1], U02 = prec[2], U11 = prec[4], U12 = prec[5],
-              U22 = prec[8];
-  const V3<float> p = v3(mean[0] - t[0], mean[1] - t[1], mean[2] - t[2]);
-  const V3<float> pc = matvec(R, p);
-  // M[i][j] = sum_{k<=i} U[k][i] R[j][k]
-  float M[9];
-#pragma unroll
-  for (int j = 0; j < 3; ++j) {
-    M[0 * 3 + j] = U00 * R[j * 3 + 0];
-    M[1 * 3 + j] = U01 * R[j * 3 + 0] + U11 * R[j * 3 + 1];
-    M[2 * 3 + j] = U02 * R[j * 3 + 0] + U12 * R[j * 3 + 1] + U22 * R[j * 3 + 2];
-  }
-  float Y[9];
-  cofactor3(M, Y);
-  const float detM = U00 * U11 * U22;
-
-  // Cut-off radius.
-  float k2;
-  if (cull_mode == FE_CULL_EPS) {
-    const float eps = cull_param > 0.f ? cull_param : kDefaultCullEps;
-    k2 = 2.f * (logw - logf(eps));
-  } else {
-    const float k = cull_param > 0.f ? cull_param : 3.f;
-    k2 = k * k;
-  }
+  const CamTerms ct = camera_terms(mean, prec, R, t);
+  const float k2 = cutoff_k2(logw, cull_mode, cull_param);
   tx0 = ty0 = tx1 = ty1 = 0;
   if (k2 > 0.f) {
-    bool full = !(detM != 0.f) || !isfinite(detM);
-    if (!full) {
-      const float inv = 1.f / detM;
-      float Yh[9];
-#pragma unroll
-      for (int q = 0; q < 9; ++q) Yh[q] = Y[q] * inv;
-      // Columns c of Yh: Yh[0*3+c], Yh[1*3+c], Yh[2*3+c].
-      auto col = [&](int c) { return v3(Yh[c], Yh[3 + c], Yh[6 + c]); };
-      const V3<float> y0 = col(0), y1 = col(1), y2 = col(2);
-      const float s02 = dot(y0, y2), s12 = dot(y1, y2), s22 = dot(y2, y2);
-      const float c22 = k2 * s22 - pc.z * pc.z;
-      full = !(c22 < 0.f);
-      if (!full) {
-        const V3<float> ex = pc.z * y0 - pc.x * y2, ey = pc.z * y1 - pc.y * y2;
-        const V3<float> xx = cross(y0, y2), xy = cross(y1, y2);
-        const float dx = fmaxf(k2 * (dot(ex, ex) - k2 * dot(xx, xx)), 0.f);
-        const float dy = fmaxf(k2 * (dot(ey, ey) - k2 * dot(xy, xy)), 0.f);
-        const float c02 = k2 * s02 - pc.x * pc.z, c12 = k2 * s12 - pc.y * pc.z;
-        const float sx = sqrtf(dx), sy = sqrtf(dy);
-        const float xa = (c02 + sx) / c22, xb = (c02 - sx) / c22;
-        const float ya = (c12 + sy) / c22, yb = (c12 - sy) / c22;
-        const float ulo = fmaf(V.fx, fminf(xa, xb), V.cx), uhi = fmaf(V.fx, fmaxf(xa, xb), V.cx);
-        const float vlo = fmaf(V.fy, fminf(ya, yb), V.cy), vhi = fmaf(V.fy, fmaxf(ya, yb), V.cy);
-        // Conservative margin covers the float32 rounding of the bounds (of order 1e-5 px).
-        const float margin = 0.02f;
-        full = !(isfinite(ulo) && isfinite(uhi) && isfinite(vlo) && isfinite(vhi));
-        if (!full) {
-          tx0 = clamp_tile(floorf((ulo - margin) / tile_w), 0, V.gx);
-          tx1 = clamp_tile(floorf((uhi + margin) / tile_w) + 1.f, 0, V.gx);
-          ty0 = clamp_tile(floorf((vlo - margin) / tile_h), 0, V.gy);
-          ty1 = clamp_tile(floorf((vhi + margin) / tile_h) + 1.f, 0, V.gy);
-        }
-      }
-    }
-    if (full) {
+    float ulo = 0.f, uhi = 0.f, vlo = 0.f, vhi = 0.f;
+    if (screen_bounds(ct, k2, V.fx, V.fy, V.cx, V.cy, ulo, uhi, vlo, vhi) == kFootBounded) {
+      // Conservative margin covers the float32 rounding of the bounds (of order 1e-5 px).
+      const float margin = 0.02f;
+      tx0 = clamp_tile(floorf((ulo - margin) / tile_w), 0, V.gx);
+      tx1 = clamp_tile(floorf((uhi + margin) / tile_w) + 1.f, 0, V.gx);
+      ty0 = clamp_tile(floorf((vlo - margin) / tile_h), 0, V.gy);
+      ty1 = clamp_tile(floorf((vhi + margin) / tile_h) + 1.f, 0, V.gy);
+    } else {
       tx0 = 0; ty0 = 0; tx1 = V.gx; ty1 = V.gy;
     }
   }
   if (tx1 <= tx0 || ty1 <= ty0) tx0 = ty0 = tx1 = ty1 = 0;
-
   // Record around the projected mean (image centre when the projection is unbounded).
-  float uc = 0.5f * V.W, vc = 0.5f * V.H;
-  if (fabsf(pc.z) > 1e-6f * sqrtf(dot(pc, pc))) {
-    const float u0 = fmaf(V.fx, pc.x / pc.z, V.cx), v0 = fmaf(V.fy, pc.y / pc.z, V.cy);
-    if (isfinite(u0) && isfinite(v0)) {
-      uc = fminf(fmaxf(u0, -1.f * V.W), 2.f * V.W);
-      vc = fminf(fmaxf(v0, -1.f * V.H), 2.f * V.H);
-    }
-  }
-  const float ifx = 1.f / V.fx, ify = 1.f / V.fy;
-  const V3<float> r0 = v3((uc - V.cx) * ifx, (vc - V.cy) * ify, 1.f);
-  const V3<float> a0 = matvec(M, r0), b = matvec(M, pc);
-  const V3<float> c0 = cross(r0, pc);
-  const V3<float> y0 = matvec(Y, c0);
-  const V3<float> y1 = matvec(Y, v3(0.f, -pc.z * ifx, pc.y * ifx));
-  const V3<float> y2 = matvec(Y, v3(pc.z * ify, 0.f, -pc.x * ify));
-  rec.a0[0] = a0.x; rec.a0[1] = a0.y; rec.a0[2] = a0.z;
-  rec.a1[0] = M[0] * ifx; rec.a1[1] = M[3] * ifx; rec.a1[2] = M[6] * ifx;
-  rec.a2[0] = M[1] * ify; rec.a2[1] = M[4] * ify; rec.a2[2] = M[7] * ify;
-  rec.b[0] = b.x; rec.b[1] = b.y; rec.b[2] = b.z;
-  rec.y0[0] = y0.x; rec.y0[1] = y0.y; rec.y0[2] = y0.z;
-  rec.y1[0] = y1.x; rec.y1[1] = y1.y; rec.y1[2] = y1.z;
-  rec.y2[0] = y2.x; rec.y2[1] = y2.y; rec.y2[2] = y2.z;
-  rec.uc = uc;
-  rec.vc = vc;
-  rec.c2 = logw * kLog2e;
+  make_record(ct, logw, V.fx, V.fy, V.cx, V.cy, 0.5f * V.W, 0.5f * V.H, -1.f * V.W, 2.f * V.W,
+              -1.f * V.H, 2.f * V.H, rec);
 }
 
 __global__ void __launch_bounds__(64) preprocess_kernel(

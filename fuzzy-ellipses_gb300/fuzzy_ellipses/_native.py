@@ -84,6 +84,15 @@ class SceneEntry(ctypes.Structure):
     _fields_ = [("gauss_offset", ctypes.c_int64), ("n", ctypes.c_int32), ("reserved", ctypes.c_int32)]
 
 
+class PixlistDesc(ctypes.Structure):
+    """Mirror of ``fe_pixlist_desc``."""
+    _fields_ = [("magic", ctypes.c_uint32), ("version", ctypes.c_uint32),
+                ("n_gaussians", ctypes.c_int32), ("n_poses", ctypes.c_int32),
+                ("n_rays", ctypes.c_int64), ("inv_f", ctypes.c_float), ("beta2", ctypes.c_float),
+                ("beta3", ctypes.c_float), ("cull_mode", ctypes.c_int32),
+                ("cull_param", ctypes.c_float), ("n_features", ctypes.c_int32)]
+
+
 class ServerConfig(ctypes.Structure):
     """Mirror of ``fe_server_config``."""
     _fields_ = [("lanes", ctypes.c_int32), ("max_batch_views", ctypes.c_int32),
@@ -134,6 +143,8 @@ PROTOTYPES = {
     "fe_render_fwd_noalloc": (ctypes.c_int, [ctypes.POINTER(RenderDesc)] + [P] * 9 + [P]),
     "fe_silhouette_bce": (ctypes.c_int, [P, P, P, I32, I64, P, P, P]),
     "fe_gmm_log_likelihood": (ctypes.c_int, [P, P, P, I32, P, I64, P, P, P, P]),
+    "fe_pixlist_desc_init": (None, [ctypes.POINTER(PixlistDesc), I32, I32, I64, F32]),
+    "fe_render_pixels": (ctypes.c_int, [ctypes.POINTER(PixlistDesc)] + [P] * 12 + [P]),
     "fe_prec_from_scale_rot": (ctypes.c_int, [P, P, I64, P, P]),
     "fe_prec_from_scale_rot_bwd": (ctypes.c_int, [P, P, I64, P, P, P, P]),
     "fe_transform_points": (ctypes.c_int, [P, I64, P, I32, P, P]),

@@ -171,6 +171,51 @@ def silhouette_bce(alpha, target, seg_end, galpha=None, loss=None):
     return loss, galpha
 
 
+def render_pixels(means, prec, logw, pixel_posei, inv_f, poses, beta2=21.4, beta3=2.66, *,
+                  flow=False, weights=False, features=None, cull="eps", cull_param=None):
+    """Multi-pose pixel-list render (baseline/fm_render.py:151-224 ``render_func_idx_quattrans``
+    and, with ``flow=True``, ``render_func_idx_quattrans_flow``).
+
+    ``pixel_posei`` (P, 4): rows (x, y, c, pose) -- the camera ray is (x inv_f, y inv_f, c) of
+    pose ``pose``; ``poses`` (n_poses, 7): quaternion (scalar first) and translation.
+    Returns ``(depth, alpha, None, w)`` or, with ``flow=True``, ``(depth, alpha, None, w, flowp,
+    flowm)`` as the reference does; ``w`` is the dense (N, P) softmax weight matrix when
+    ``weights=True``, else None. With ``features`` (N, F), F <= 16, the softmax-weighted features
+    (P, F) are appended to the tuple. Forward only."""
+    lib = N.load()
+    n = _check_inputs(means, prec, logw)
+    dev = means.device
+    rays = pixel_posei.to(device=dev, dtype=torch.float32).contiguous()
+    ps = poses.to(device=dev, dtype=torch.float32).contiguous()
+    if rays.dim() != 2 or rays.shape[1] != 4 or ps.dim() != 2 or ps.shape[1] != 7:
+        raise ValueError("pixel_posei must be (P, 4) and poses (n_poses, 7)")
+    P = rays.shape[0]
+    d = N.PixlistDesc()
+    lib.fe_pixlist_desc_init(ctypes.byref(d), n, ps.shape[0], P, float(inv_f))
+    d.beta2, d.beta3 = float(beta2), float(beta3)
+    if cull == "eps":
+        d.cull_mode, d.cull_param = N.FE_CULL_EPS, (1e-7 if cull_param is None else float(cull_param))
+    else:
+        d.cull_mode, d.cull_param = N.FE_CULL_NSTD, (3.0 if cull_param is None else float(cull_param))
+    feats = None
+    if features is not None:
+        feats = features.to(device=dev, dtype=torch.float32).contiguous()
+        if feats.dim() != 2 or feats.shape[0] != n:
+            raise ValueError("features must be (N, F)")
+        d.n_features = feats.shape[1]
+    depth = torch.empty(P, device=dev)
+    alpha = torch.empty(P, device=dev)
+    fp = torch.empty((P, 2), device=dev) if flow else None
+    fm = torch.empty((P, 2), device=dev) if flow else None
+    of = torch.empty((P, d.n_features), device=dev) if feats is not None else None
+    w = torch.empty((n, P), device=dev) if weights else None
+    N.check(lib.fe_render_pixels(ctypes.byref(d), _ptr(means), _ptr(prec), _ptr(logw), _ptr(ps),
+                                 _ptr(rays), _ptr(feats), _ptr(depth), _ptr(alpha), _ptr(fp),
+                                 _ptr(fm), _ptr(of), _ptr(w), _stream()))
+    out = (depth, alpha, None, w) + ((fp, fm) if flow else ())
+    return out + ((of,) if feats is not None else ())
+
+
 def gmm_log_likelihood(means, prec, logw, points, *, return_matrix=False):
     """Log-likelihood of points (P, 3) under the mixture (the reference's ``log_likelihood``,
     baseline/fm_render.py:231-259): returns ``(nll, point_ll)`` -- the mean negative

@@ -383,6 +383,39 @@ int fe_gmm_log_likelihood(const float *d_means, const float *d_prec, const float
                           int32_t n, const float *d_points, int64_t n_points, float *d_point_ll,
                           float *d_res, double *d_total, fe_stream_t stream);
 
+/* Multi-pose pixel-list render with optical flow: the reference's render_func_idx_quattrans and
+ * render_func_idx_quattrans_flow (baseline/fm_render.py:151-224, whose render_func_rays calls pass
+ * the Gaussians where the rays belong; the intended argument order is used here).
+ *   d_rays (n_rays, 4): the reference's pixel_posei rows (x, y, c, pose); the camera ray is
+ *     (x inv_f, y inv_f, c) of pose `pose` (truncated to an integer and clamped to the poses);
+ *   d_poses (n_poses, 7): quaternion (4, scalar first) and translation (3) per pose;
+ *   d_features (n, n_features) or NULL: per-Gaussian features (n_features <= 16);
+ * outputs per ray: d_depth, d_alpha; optional (NULL to skip): d_flow_next / d_flow_prev
+ * (n_rays, 2) the flow to poses pose+1 / pose-1 (clamped), d_out_features (n_rays, n_features)
+ * the softmax-weighted features, d_weights (n, n_rays) the dense softmax weights (fm_render's w).
+ * Gaussians are culled per ray at the renderer's k-sigma screen bound. Uses the per-stream arena
+ * (112 B per Gaussian and pose). */
+typedef struct fe_pixlist_desc {
+  uint32_t magic;      /* FE_DESC_MAGIC */
+  uint32_t version;    /* FE_DESC_VERSION */
+  int32_t n_gaussians;
+  int32_t n_poses;
+  int64_t n_rays;
+  float inv_f;         /* inverse focal length (the reference's invF) */
+  float beta2, beta3;
+  int32_t cull_mode;   /* fe_cull_mode */
+  float cull_param;
+  int32_t n_features;
+} fe_pixlist_desc;
+
+void fe_pixlist_desc_init(fe_pixlist_desc *desc, int32_t n, int32_t n_poses, int64_t n_rays,
+                          float inv_f);
+int fe_render_pixels(const fe_pixlist_desc *desc, const float *d_means, const float *d_prec,
+                     const float *d_logw, const float *d_poses, const float *d_rays,
+                     const float *d_features, float *d_depth, float *d_alpha, float *d_flow_next,
+                     float *d_flow_prev, float *d_out_features, float *d_weights,
+                     fe_stream_t stream);
+
 /* Scene-parameter adapters (device kernels, float64 inside).
  * fe_prec_from_scale_rot: the renderer's upper-triangular precision factor U (n,3,3, row-major,
  * zeros below the diagonal; U U^T = Sigma^-1) of Sigma = R(q) diag(s)^2 R(q)^T from scales (n,3)

@@ -207,3 +207,45 @@ def render_culled(means, prec_full, weights_log, height, width, fx, fy, cx, cy, 
             depth.ravel()[pix] = d
             alpha.ravel()[pix] = a
     return depth, alpha
+
+
+def _pose_rays(pixel_posei, invF, poses):
+    pp = np.asarray(pixel_posei, dtype=np.float64)
+    poses = np.asarray(poses, dtype=np.float64)
+    rots = np.stack([quat_to_rot(p[:4]) for p in poses])               # :157
+    idx = np.clip(pp[:, 3].astype(int), 0, len(poses) - 1)              # astype(int); JAX clamps
+    rays = pp[:, :3] * np.array([invF, invF, 1.0])                      # :160
+    rw = np.einsum("pi,pij->pj", rays, rots[idx])                       # ray @ rot_mats[idx]
+    return pp, poses, rots, idx, rays, rw
+
+
+def render_func_idx_quattrans(means, prec_full, weights_log, pixel_posei, invF, poses, beta_2,
+                              beta_3, return_weights=False):
+    """``fm_render.py:151-167`` with the intended argument order of its render_func_rays call."""
+    _, poses, _, idx, _, rw = _pose_rays(pixel_posei, invF, poses)
+    csr = np.stack([rw, poses[idx, 4:]], 1)
+    return render_func_rays(csr, means, prec_full, weights_log, beta_2, beta_3,
+                            return_weights=return_weights)
+
+
+def flow_from_depth(pixel_posei, invF, poses, depth):
+    """Per-ray forward / backward flow of ``fm_render.py:186-222`` for given depths."""
+    pp, poses, rots, idx, rays, _ = _pose_rays(pixel_posei, invF, poses)
+    n = len(poses)
+    pt1 = rays * np.asarray(depth, dtype=np.float64)[:, None]
+    world = np.einsum("pi,pij->pj", pt1, rots[idx]) + poses[idx, 4:]
+    out = []
+    for nb in (np.minimum(idx + 1, n - 1), np.maximum(idx - 1, 0)):
+        pt2 = np.einsum("pj,pij->pi", world - poses[nb, 4:], rots[nb])   # (world - t) @ R^T
+        coord = pt2[:, :2] / (pt2[:, 2:3] * invF)
+        out.append(-(coord - pp[:, :2]))
+    return out[0], out[1]
+
+
+def render_func_idx_quattrans_flow(means, prec_full, weights_log, pixel_posei, invF, poses,
+                                   beta_2, beta_3, return_weights=False):
+    """``fm_render.py:171-224`` (argument order fixed as above)."""
+    d, a, nrm, w = render_func_idx_quattrans(means, prec_full, weights_log, pixel_posei, invF,
+                                             poses, beta_2, beta_3, return_weights)
+    fp, fm = flow_from_depth(pixel_posei, invF, poses, d)
+    return d, a, nrm, w, fp, fm

@@ -186,3 +186,31 @@ def test_adapter_oracle_factor_is_upper_and_inverts_the_covariance():
     p = torch.randn(10, 3, generator=g, dtype=torch.float64)
     assert torch.allclose(AT.transform_points(pose, p), (R[0] @ p.T).T + pose[:3])
     assert torch.allclose(AT.transform_points_by_inv(pose, p), (R[0].T @ p.T).T + pose[:3])
+
+
+def test_pixel_list_oracle_matches_image_oracle_and_flow_is_consistent():
+    """One pose's full pixel grid through render_func_idx_quattrans equals render_pinhole; the
+    flow to the same pose is zero; for two poses differing by a sideways translation dx the flow
+    of a point at depth z is the disparity -dx f / z."""
+    from fuzzy_ellipses import synthetic as S
+    scene, cams = S.config0(seed=2)
+    c = cams[0]
+    H = W = 24
+    f = 24.0
+    inv_f = 1.0 / f
+    v, u = np.mgrid[0:H, 0:W]
+    pp = np.stack([u.ravel() - W / 2, v.ravel() - H / 2, np.ones(H * W), np.zeros(H * W)], 1)
+    pose = np.concatenate([c.quat, c.trans])[None]
+    d, a, _, _ = O.render_func_idx_quattrans(scene.means, scene.prec, scene.logw, pp, inv_f, pose,
+                                             21.4, 2.66)
+    d2, a2 = O.render_pinhole(scene.means, scene.prec, scene.logw, H, W, f, f, W / 2, H / 2,
+                              c.quat, c.trans)
+    assert np.allclose(d, d2.ravel(), rtol=1e-12, atol=1e-12)
+    assert np.allclose(a, a2.ravel(), rtol=1e-12, atol=1e-12)
+    fp, fm = O.flow_from_depth(pp, inv_f, pose, d)
+    assert np.allclose(fp, 0, atol=1e-9) and np.allclose(fm, 0, atol=1e-9)
+    # sideways translation along the camera x axis (world = camera frame with identity rotation)
+    poses = np.array([[1, 0, 0, 0, 0, 0, -1.0], [1, 0, 0, 0, 0.05, 0, -1.0]])
+    z = np.full(H * W, 0.8)
+    fp, _ = O.flow_from_depth(pp, inv_f, poses, z)
+    assert np.allclose(fp[:, 0], 0.05 * f / 0.8, rtol=1e-9) and np.allclose(fp[:, 1], 0, atol=1e-9)
