@@ -57,6 +57,7 @@ def parse():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-serve", action="store_true")
+    ap.add_argument("--no-next", action="store_true")
     ap.add_argument("--serve-only", action="store_true",
                     help="run only the served mixed-request workload and print its JSON")
     ap.add_argument("--profile-step", action="store_true",
@@ -433,6 +434,10 @@ def main():
                                       "coefficient gradients, record VJP) of the 16-view step, "
                                       "reusing the forward's binning"}}
 
+    # ---- the kernels beyond the render path ------------------------------------------------
+    next_rows = None if args.no_next else next_rows_bench(fe, dev, scene, cams, fma_ops, ex2_ops,
+                                                          peaks["hbm_gbs"])
+
     # ---- served mixed requests vs the plain per-call drop-in ------------------------------
     served = None if args.no_serve else serve_bench(fe, dev)
 
@@ -479,6 +484,7 @@ def main():
         "evals_per_camera": per_cam_evals,
         "cpu_baseline": cpu,
         "backward": backward,
+        "next_rows": next_rows,
         "served": served,
         "autotune": tuned and {"bucket": tuned["bucket"],
                                "candidates_ms": {f"{c['tile'][0]}x{c['tile'][1]}/px{c['px']}/ch{c['chunk']}": round(c["ms"], 4)
@@ -586,6 +592,81 @@ def serve_bench(fe, dev, n_requests=200, plain_requests=60, seed=0):
             "saturating": sat, "poisson_half_load": poisson,
             "plain_per_call_renders_per_s": plain_rs,
             "served_over_plain": sat["renders_per_s"] / plain_rs}
+
+
+def _event_ms(fn, reps=5, warm=2, calls=10):
+    """Median CUDA-event time (ms) per call of fn() on the current stream, timing `calls`
+    back-to-back calls between two events so that host launch overhead overlaps device work."""
+    import torch
+    for _ in range(warm):
+        fn()
+    ts = []
+    for _ in range(reps):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        for _ in range(calls):
+            fn()
+        b.record()
+        torch.cuda.synchronize()
+        ts.append(a.elapsed_time(b) / calls)
+    return statistics.median(ts)
+
+
+# GMM log-likelihood per (point, Gaussian): 3 subtractions, 6 for U^T p, 3 for the squared norm,
+# 1 for the log-density, 2 for the online logsumexp = 15 FMA-pipe operations and 1 ex2.
+PER_PAIR_GMM_FMA = 15
+PER_PAIR_GMM_MUFU = 1
+
+
+def next_rows_bench(fe, dev, scene, cams, fma_ops, ex2_ops, hbm_gbs):
+    """Throughput of the kernels beyond the render path: GMM log-likelihood, the multi-pose
+    pixel-list renderer with flow, and the scene-parameter adapters."""
+    import torch
+    out = {}
+    m, p, w = [torch.from_numpy(x).to(dev) for x in (scene.means, scene.prec, scene.logw)]
+    g = torch.Generator(device=dev).manual_seed(0)
+    # GMM: 1000 Gaussians, 2^21 points uniform in the scene's box
+    pts = (torch.rand((1 << 21, 3), device=dev, generator=g) - 0.5) * 0.6
+    ms = _event_ms(lambda: fe.gmm_log_likelihood(m, p, w, pts))
+    pairs = pts.shape[0] * scene.n
+    peak = min(fma_ops / PER_PAIR_GMM_FMA, ex2_ops / PER_PAIR_GMM_MUFU)
+    out["gmm_log_likelihood"] = {
+        "workload": f"{scene.n} Gaussians x {pts.shape[0]} points", "ms": ms,
+        "pairs_per_s": pairs / (ms * 1e-3),
+        "roofline": {"bound": "fma+xu", "achieved": pairs / (ms * 1e-3) / 1e9,
+                     "peak": peak / 1e9, "unit": "Gpairs/s", "frac": pairs / (ms * 1e-3) / peak,
+                     "per_pair": {"fma_pipe": PER_PAIR_GMM_FMA, "mufu": PER_PAIR_GMM_MUFU}}}
+    # Pixel list: every other pixel of the 16 cameras, poses interleaved per camera, with flow
+    H, W = cams[0].height, cams[0].width
+    v, u = np.mgrid[0:H:2, 0:W:2]
+    rays = np.concatenate([np.stack([u.ravel() - cams[0].cx, v.ravel() - cams[0].cy,
+                                     np.ones(u.size), np.full(u.size, k)], 1)
+                           for k in range(len(cams))]).astype(np.float32)
+    poses = np.stack([np.concatenate([c.quat, c.trans]) for c in cams]).astype(np.float32)
+    rays_d = torch.from_numpy(rays).to(dev)
+    poses_d = torch.from_numpy(poses).to(dev)
+    ms = _event_ms(lambda: fe.render_pixels(m, p, w, rays_d, 1.0 / cams[0].fx, poses_d, flow=True))
+    out["render_pixels"] = {"workload": f"{len(rays)} rays over {len(cams)} poses "
+                                        f"({H}x{W} at stride 2), N={scene.n}, with flow",
+                            "ms": ms, "rays_per_s": len(rays) / (ms * 1e-3)}
+    # Adapters: precision factors of 2^20 Gaussians; a pose transform of 2^23 points
+    n_g = 1 << 20
+    sc = torch.exp(torch.empty((n_g, 3), device=dev).uniform_(np.log(0.005), np.log(0.03), generator=g))
+    qs = torch.randn((n_g, 4), device=dev, generator=g)
+    ms = _event_ms(lambda: fe.adapters.prec_from_scale_rot(sc, qs))
+    out["prec_from_scale_rot"] = {"workload": f"{n_g} Gaussians", "ms": ms,
+                                  "gaussians_per_s": n_g / (ms * 1e-3),
+                                  "hbm_gbs": n_g * (28 + 36) / (ms * 1e-3) / 1e9,
+                                  "bound": "float64 arithmetic (FP64 rate)"}
+    n_p = 1 << 25
+    pp = torch.randn((n_p, 3), device=dev, generator=g)
+    pose = torch.tensor([0.01, 0.02, 0.03, 0.9, 0.1, 0.2, 0.3], device=dev)
+    ms = _event_ms(lambda: fe.adapters.transform_points(pose, pp))
+    gbs = n_p * 24 / (ms * 1e-3) / 1e9
+    out["transform_points"] = {"workload": f"{n_p} points", "ms": ms, "hbm_gbs": gbs,
+                               "roofline": {"bound": "hbm", "achieved": gbs, "peak": hbm_gbs,
+                                            "unit": "GB/s", "frac": gbs / hbm_gbs}}
+    return out
 
 
 def batch_tiles(cams, tw, th):

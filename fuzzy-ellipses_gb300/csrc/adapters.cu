@@ -177,19 +177,39 @@ __global__ void prec_from_scale_rot_bwd_kernel(int64_t n, const float* __restric
 }
 
 // out = M p + t with M = R (inverse = false) or R^T (inverse = true); pose = [t(3), q(4)].
+// The rotation is built in float64 once per thread; the per-point arithmetic is float32, as in
+// the reference (jnp.einsum in float32), so the kernel streams at memory speed.
 __global__ void transform_points_kernel(int64_t n, const float* __restrict__ points,
                                         const float* __restrict__ pose, int inverse,
                                         float* __restrict__ out) {
   const Rot R = make_rot(pose + 3);
-  double M[9];
+  float M[9];
   for (int r = 0; r < 3; ++r)
-    for (int c = 0; c < 3; ++c) M[3 * r + c] = inverse ? R.r[3 * c + r] : R.r[3 * r + c];
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
-       i += (int64_t)gridDim.x * blockDim.x) {
-    const double p0 = points[3 * i], p1 = points[3 * i + 1], p2 = points[3 * i + 2];
-    for (int r = 0; r < 3; ++r)
-      out[3 * i + r] = (float)(M[3 * r] * p0 + M[3 * r + 1] * p1 + M[3 * r + 2] * p2 + pose[r]);
+    for (int c = 0; c < 3; ++c) M[3 * r + c] = (float)(inverse ? R.r[3 * c + r] : R.r[3 * r + c]);
+  const float t0 = pose[0], t1 = pose[1], t2 = pose[2];
+  auto xf = [&](const float* p, float* o) {
+    o[0] = fmaf(M[2], p[2], fmaf(M[1], p[1], fmaf(M[0], p[0], t0)));
+    o[1] = fmaf(M[5], p[2], fmaf(M[4], p[1], fmaf(M[3], p[0], t1)));
+    o[2] = fmaf(M[8], p[2], fmaf(M[7], p[1], fmaf(M[6], p[0], t2)));
+  };
+  // Groups of four points are three 16-byte words (both buffers are 16-byte aligned).
+  const int64_t groups = n >> 2;
+  const float4* in4 = reinterpret_cast<const float4*>(points);
+  float4* out4 = reinterpret_cast<float4*>(out);
+  for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < groups;
+       g += (int64_t)gridDim.x * blockDim.x) {
+    const float4 a = in4[3 * g], b = in4[3 * g + 1], c = in4[3 * g + 2];
+    const float p[12] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w, c.x, c.y, c.z, c.w};
+    float o[12];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) xf(p + 3 * q, o + 3 * q);
+    out4[3 * g] = make_float4(o[0], o[1], o[2], o[3]);
+    out4[3 * g + 1] = make_float4(o[4], o[5], o[6], o[7]);
+    out4[3 * g + 2] = make_float4(o[8], o[9], o[10], o[11]);
   }
+  const int64_t tail = groups << 2;
+  const int64_t i = tail + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < n) xf(points + 3 * i, out + 3 * i);
 }
 
 // dL/dp = M^T g; dL/dt = sum g; dL/dM = sum g p^T -> dL/dR (transposed when inverse) -> dL/dq.
@@ -200,26 +220,27 @@ __global__ void transform_points_bwd_kernel(int64_t n, const float* __restrict__
                                             float* __restrict__ gpoints,
                                             double* __restrict__ gacc) {
   const Rot R = make_rot(pose + 3);
-  double M[9];
+  float M[9];
   for (int r = 0; r < 3; ++r)
-    for (int c = 0; c < 3; ++c) M[3 * r + c] = inverse ? R.r[3 * c + r] : R.r[3 * r + c];
-  double acc[12] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};  // dL/dt (3), dL/dM (9)
+    for (int c = 0; c < 3; ++c) M[3 * r + c] = (float)(inverse ? R.r[3 * c + r] : R.r[3 * r + c]);
+  // Per-thread float32 partial sums (a thread sees n / (grid x block) points), then float64.
+  float acc[12] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};  // dL/dt (3), dL/dM (9)
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x) {
-    const double g[3] = {gout[3 * i], gout[3 * i + 1], gout[3 * i + 2]};
-    const double p[3] = {points[3 * i], points[3 * i + 1], points[3 * i + 2]};
+    const float g[3] = {gout[3 * i], gout[3 * i + 1], gout[3 * i + 2]};
+    const float p[3] = {points[3 * i], points[3 * i + 1], points[3 * i + 2]};
     if (gpoints)
       for (int c = 0; c < 3; ++c)
-        gpoints[3 * i + c] = (float)(M[c] * g[0] + M[3 + c] * g[1] + M[6 + c] * g[2]);
+        gpoints[3 * i + c] = fmaf(M[6 + c], g[2], fmaf(M[3 + c], g[1], M[c] * g[0]));
     for (int r = 0; r < 3; ++r) {
       acc[r] += g[r];
-      for (int c = 0; c < 3; ++c) acc[3 + 3 * r + c] += g[r] * p[c];
+      for (int c = 0; c < 3; ++c) acc[3 + 3 * r + c] = fmaf(g[r], p[c], acc[3 + 3 * r + c]);
     }
   }
   __shared__ double red[12][32];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
   for (int k = 0; k < 12; ++k) {
-    double v = acc[k];
+    double v = (double)acc[k];
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
     if (lane == 0) red[k][wid] = v;
   }
@@ -270,7 +291,8 @@ void launch_prec_from_scale_rot_bwd(int64_t n, const float* scales, const float*
 void launch_transform_points(int64_t n, const float* points, const float* pose, int inverse,
                              float* out, cudaStream_t st) {
   if (n <= 0) return;
-  transform_points_kernel<<<grid_for_n(n, 256), 256, 0, st>>>(n, points, pose, inverse, out);
+  transform_points_kernel<<<grid_for_n((n + 3) / 4, 256), 256, 0, st>>>(n, points, pose, inverse,
+                                                                        out);
 }
 
 void launch_transform_points_bwd(int64_t n, const float* points, const float* pose, int inverse,

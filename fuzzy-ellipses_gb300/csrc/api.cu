@@ -504,6 +504,8 @@ int fe_transform_points(const float* points, int64_t n, const float* pose, int32
                         float* out, fe_stream_t stream_) {
   if (n < 0 || !pose || (n > 0 && (!points || !out)))
     return fail(FE_ERR_INVALID_ARGUMENT, "fe_transform_points: bad arguments");
+  if ((reinterpret_cast<uintptr_t>(points) | reinterpret_cast<uintptr_t>(out)) & 15)
+    return fail(FE_ERR_INVALID_ARGUMENT, "fe_transform_points: buffers must be 16-byte aligned");
   launch_transform_points(n, points, pose, inverse ? 1 : 0, out,
                           reinterpret_cast<cudaStream_t>(stream_));
   FE_CUDA(cudaGetLastError());

@@ -432,7 +432,8 @@ int fe_prec_from_scale_rot_bwd(const float *d_scales, const float *d_quats, int6
 /* Rigid transform of points (n,3) by a pose d_pose = [t(3), q(4)] (scalar-first quaternion, the
  * reference's layout): out = R(q) p + t (inverse = 0; transform_points_jittable,
  * utils/sfs_utils.py:171-172) or R(q)^T p + t (inverse = 1; transform_points_by_inv_jittable,
- * :182-184). The backward writes dL/dpoints (when not NULL) and dL/dpose (7, when not NULL). */
+ * :182-184). The backward writes dL/dpoints (when not NULL) and dL/dpose (7, when not NULL).
+ * d_points and d_out must be 16-byte aligned (as every CUDA allocation is). */
 int fe_transform_points(const float *d_points, int64_t n, const float *d_pose, int32_t inverse,
                         float *d_out, fe_stream_t stream);
 int fe_transform_points_bwd(const float *d_points, int64_t n, const float *d_pose,

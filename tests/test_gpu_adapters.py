@@ -54,10 +54,10 @@ def test_prec_from_scale_rot_backward_matches_autograd(cuda_device):
 @pytest.mark.parametrize("inverse", [False, True])
 def test_transform_points_forward_and_backward(cuda_device, inverse):
     g = torch.Generator().manual_seed(3)
-    pts = torch.randn(10000, 3, generator=g, dtype=torch.float64).float()
+    pts = torch.randn(10003, 3, generator=g, dtype=torch.float64).float()  # a ragged tail
     pose = torch.cat([torch.randn(3, generator=g, dtype=torch.float64),
                       torch.randn(4, generator=g, dtype=torch.float64)]).float()
-    G = torch.randn(10000, 3, generator=g, dtype=torch.float64)
+    G = torch.randn(10003, 3, generator=g, dtype=torch.float64)
     f = A.transform_points_by_inv if inverse else A.transform_points
     fr = AT.transform_points_by_inv if inverse else AT.transform_points
     pd = pts.to(cuda_device).requires_grad_()
