@@ -61,6 +61,9 @@ __device__ __forceinline__ void issue_chunk(BlendSmem<CH>& sm, int stage, const 
 template <int TW, int TH, int PX, int CH>
 struct BlendShape {
   static constexpr int NT = TW * TH / PX;
+  // Resident CTAs per SM the register budget is sized for: 24 warps (768 threads) per SM, at
+  // most 16 CTAs (one-warp CTAs would otherwise be squeezed into spilling).
+  static constexpr int MIN_CTAS = (768 / NT) < 16 ? (768 / NT) : 16;
   static constexpr int CW = TW / PX;
   static constexpr int GP = PX >= 4 ? 2 : 4;
   static_assert(TW % PX == 0, "PX must divide the tile width");
@@ -72,7 +75,8 @@ struct BlendShape {
 constexpr float kNoLogit = -1e30f;
 
 template <int TW, int TH, int PX, int CH>
-__global__ void __launch_bounds__(BlendShape<TW, TH, PX, CH>::NT) blend_fwd_kernel(
+__global__ void __launch_bounds__(BlendShape<TW, TH, PX, CH>::NT,
+                                  BlendShape<TW, TH, PX, CH>::MIN_CTAS) blend_fwd_kernel(
     ViewsArg va, uint32_t n_tiles, const TilePair* __restrict__ trec,
     const uint2* __restrict__ ranges, float nb2, float beta3, float* __restrict__ depth,
     float* __restrict__ alpha, float* __restrict__ stats, int64_t stats_stride,
