@@ -67,6 +67,18 @@ def parse():
     return ap.parse_args()
 
 
+def job_value(dev_s, units_per_step, steps, world, device):
+    """Whole-job throughput of independent replicas (weak scaling): all ranks' units over the
+    slowest rank's device time. Returns (value in millions of units per second, that time)."""
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        t = torch.tensor([dev_s], device=device, dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        dev_s = float(t.item())
+    return world * units_per_step * steps / dev_s / 1e6, dev_s
+
+
 def dist_env():
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -261,11 +273,11 @@ def main():
     import fuzzy_ellipses as fe
 
     rank, world, local = dist_env()
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl")
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
+    if world > 1:  # independent replicas; the process group only carries the barriers and timing
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
     scene, cams, mpw = build_workload(dev)
     m, p, w = mpw
     H, W = cams[0].height, cams[0].width
@@ -329,12 +341,7 @@ def main():
     wall = time.perf_counter() - t_wall
     clocks = sampler.stop()
     step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
-    dev_s = sum(step_ms) / 1e3
-    if world > 1:
-        t = torch.tensor([dev_s], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        dev_s = float(t.item())
-    value = world * e_step * args.steps / dev_s / 1e6
+    value, dev_s = job_value(sum(step_ms) / 1e3, e_step, args.steps, world, dev)
     renders_s = world * len(cams) * args.steps / dev_s
 
     if rank != 0:
