@@ -216,3 +216,29 @@ def test_subpixel_gaussians(cuda_device, tile):
     d, a = render_np(cuda_device, scene, cam, tile=tile)
     ea, ed = parity_errors(d, a, d_ref, a_ref)
     assert ea <= TOL_ALPHA and ed <= TOL_DEPTH_REL, (ea, ed)
+
+
+def test_large_scene_beyond_the_key_budget(cuda_device):
+    """24,000 Gaussians at 1280x720 with 16x16 tiles: the worst-case key plan (N x tiles = 86 M
+    keys, ~8 GB of key scratch) exceeds the 4 GiB key budget, so the plain call reads the exact
+    key count back and sizes the keys from it. Sampled pixels against the float64 oracle; the
+    backward goes through the same path."""
+    rng = np.random.default_rng(21)
+    scene = S.random_gaussians(24000, 0.35, rng)
+    cam = S.Camera(720, 1280, 900.0, 900.0, 640.0, 360.0, *S.look_at([0.2, -0.3, 1.1]))
+    m, p, w = scene_to_dev(scene, cuda_device)
+    depth, alpha = fe.render_forward(m, p, w, cam.fx, cam.fy, cam.cx, cam.cy, cam.quat, cam.trans,
+                                     cam.height, cam.width)
+    assert fe.device_status() == 0
+    pix = rng.choice(cam.height * cam.width, 600, replace=False)
+    d_ref, a_ref = oracle_pixels(scene, cam, pix)
+    ea, ed = parity_errors(depth.cpu().numpy().ravel()[pix], alpha.cpu().numpy().ravel()[pix],
+                           d_ref, a_ref)
+    assert ea <= TOL_ALPHA and ed <= TOL_DEPTH_REL, (ea, ed)
+    mr, pr, wr = [t.clone().requires_grad_() for t in (m, p, w)]
+    d2, a2 = fe.render(mr, pr, wr, cam.fx, cam.fy, cam.cx, cam.cy, cam.quat, cam.trans,
+                       cam.height, cam.width)
+    assert torch.equal(a2.detach(), alpha)
+    a2.sum().backward()
+    for g in (mr.grad, pr.grad, wr.grad):
+        assert torch.isfinite(g).all() and float(g.abs().sum()) > 0
