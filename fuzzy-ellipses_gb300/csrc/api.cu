@@ -404,6 +404,39 @@ int fe_render_bwd(const fe_render_desc* d, const float* means, const float* prec
   return FE_OK;
 }
 
+int fe_render_features(const fe_render_desc* d, const float* means, const float* prec,
+                       const float* logw, const float* quat, const float* trans,
+                       const float* stats, const float* features, int32_t n_features,
+                       float* out, fe_stream_t stream_) {
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream_);
+  int rc = check_desc(d);
+  if (rc) return rc;
+  if (n_features < 1) return fail(FE_ERR_INVALID_ARGUMENT, "n_features must be >= 1");
+  if (!stats || !features || !out || !quat || !trans)
+    return fail(FE_ERR_INVALID_ARGUMENT, "NULL pointer");
+  const int64_t npix = (int64_t)d->height * d->width;
+  if (d->n_gaussians == 0) {
+    FE_CUDA(cudaMemsetAsync(out, 0, sizeof(float) * npix * n_features, st));
+    return FE_OK;
+  }
+  if (!means || !prec || !logw) return fail(FE_ERR_INVALID_ARGUMENT, "NULL Gaussian pointer");
+  Arena* a = nullptr;
+  rc = arena_for(st, &a);
+  if (rc) return rc;
+  Pipeline p = single_view_pipeline(d, means, prec, logw, quat, trans);
+  RecSpace rs;
+  KeySpace ks;
+  int64_t cap = 0;
+  uint64_t* sorted = nullptr;
+  rc = run_binning(p, p.n_rec * p.n_tiles, a->rec, a->keys, a->h_pinned, false, st, rs, ks, cap,
+                   sorted);
+  if (rc) return rc;
+  launch_features(p.va, p.tile_w, p.tile_h, p.n_tiles, sorted, rs.ranges, ks.trec, stats, npix,
+                  p.beta2, p.beta3, features, n_features, out, rs.ctrl, st);
+  FE_CUDA(cudaGetLastError());
+  return FE_OK;
+}
+
 int fe_render_binning(const fe_render_desc* d, const float* means, const float* prec,
                       const float* logw, const float* quat, const float* trans, uint64_t* keys,
                       int64_t key_capacity, uint32_t* ranges, int64_t* h_num_keys,

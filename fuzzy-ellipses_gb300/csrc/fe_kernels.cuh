@@ -113,4 +113,11 @@ void launch_render_pixels(int n, int n_poses, const float* means, const float* p
                           float* flow_next, float* flow_prev, float* out_feats, float* weights,
                           void* scratch, cudaStream_t st);
 
+// features.cu
+// Softmax-weighted features (nf per Gaussian) of an image render from the forward's statistics.
+void launch_features(const ViewsArg& va, int tile_w, int tile_h, int64_t n_tiles,
+                     const uint64_t* keys, const uint2* ranges, const TilePair* trec,
+                     const float* stats, int64_t stats_stride, float beta2, float beta3,
+                     const float* feats, int nf, float* out, Control* ctrl, cudaStream_t st);
+
 }  // namespace fe

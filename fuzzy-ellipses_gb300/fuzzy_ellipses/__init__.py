@@ -11,6 +11,7 @@ from . import adapters, autotune, serve, synthetic  # noqa: F401
 from ._native import FEError, NativeLibraryMissing, load as load_native  # noqa: F401
 from .api import (Batch, bench_peak, device_status, gmm_log_likelihood,  # noqa: F401
                   projection_matrix, rasterize, reference_binning, reference_num_stds, render,
-                  render_binning, render_forward, render_pixels, silhouette_bce)
+                  render_binning, render_features, render_forward, render_pixels,
+                  silhouette_bce)
 
 __version__ = "0.1.0"

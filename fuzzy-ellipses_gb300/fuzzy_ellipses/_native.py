@@ -141,6 +141,7 @@ PROTOTYPES = {
     "fe_render_desc_init": (None, [ctypes.POINTER(RenderDesc), I32, I32, I32, F32, F32, F32, F32]),
     "fe_render_fwd": (ctypes.c_int, [ctypes.POINTER(RenderDesc)] + [P] * 8 + [P]),
     "fe_render_fwd_noalloc": (ctypes.c_int, [ctypes.POINTER(RenderDesc)] + [P] * 9 + [P]),
+    "fe_render_features": (ctypes.c_int, [ctypes.POINTER(RenderDesc)] + [P] * 7 + [I32, P, P]),
     "fe_silhouette_bce": (ctypes.c_int, [P, P, P, I32, I64, P, P, P]),
     "fe_gmm_log_likelihood": (ctypes.c_int, [P, P, P, I32, P, I64, P, P, P, P]),
     "fe_pixlist_desc_init": (None, [ctypes.POINTER(PixlistDesc), I32, I32, I64, F32]),

@@ -125,6 +125,32 @@ def render_forward(means, prec, logw, fx, fy, cx, cy, quat, t, height, width, be
     return out
 
 
+def render_features(means, prec, logw, features, fx, fy, cx, cy, quat, t, height, width,
+                    beta2=21.4, beta3=2.66, *, cull="eps", cull_param=None, tile=(16, 16)):
+    """Depth, alpha (H, W) and the softmax-weighted features (H, W, F) of one pinhole camera:
+    feature(pixel) = sum_i w_i f_i with fm_render's normalised weights w (fm_render.py:95-109).
+    ``features`` (N, F) float32. Forward only."""
+    lib = N.load()
+    n = _check_inputs(means, prec, logw)
+    dev = means.device
+    feats = features.to(device=dev, dtype=torch.float32).contiguous()
+    if feats.dim() != 2 or feats.shape[0] != n or feats.shape[1] < 1:
+        raise ValueError("features must be (N, F) with F >= 1")
+    q = _as_dev(quat, dev, (4,))
+    tt = _as_dev(t, dev, (3,))
+    desc = N.make_desc(n, height, width, fx, fy, cx, cy, beta2, beta3, cull, cull_param, tile)
+    depth = torch.empty((height, width), device=dev)
+    alpha = torch.empty((height, width), device=dev)
+    stats = torch.empty((3, height, width), device=dev)
+    out = torch.empty((height, width, feats.shape[1]), device=dev)
+    N.check(lib.fe_render_fwd(ctypes.byref(desc), _ptr(means), _ptr(prec), _ptr(logw), _ptr(q),
+                              _ptr(tt), _ptr(depth), _ptr(alpha), _ptr(stats), _stream()))
+    N.check(lib.fe_render_features(ctypes.byref(desc), _ptr(means), _ptr(prec), _ptr(logw),
+                                   _ptr(q), _ptr(tt), _ptr(stats), _ptr(feats), feats.shape[1],
+                                   _ptr(out), _stream()))
+    return depth, alpha, out
+
+
 def render_binning(means, prec, logw, fx, fy, cx, cy, quat, t, height, width, *, cull="eps",
                    cull_param=None, tile=(16, 16), key_capacity=None):
     """The tile binning ``render`` uses: returns (keys (K,) int64 holding (tile << 32 | gaussian),

@@ -128,6 +128,16 @@ int fe_render_binning(const fe_render_desc *desc, const float *d_means, const fl
                       uint64_t *d_keys, int64_t key_capacity, uint32_t *d_ranges,
                       int64_t *h_num_keys, fe_stream_t stream);
 
+/* Softmax-weighted per-Gaussian features of an image render: out (H,W,n_features) =
+ * sum_i w_i f_i with fm_render's normalised weights w (baseline/fm_render.py:95-109, which returns
+ * w "to compute color, DINO features, or any other per-Gaussian property"). d_stats must come
+ * from fe_render_fwd with the same descriptor, Gaussians and pose; d_features (n, n_features).
+ * Recomputes the binning and evaluates each key's weight per pixel; no weight matrix is formed. */
+int fe_render_features(const fe_render_desc *desc, const float *d_means, const float *d_prec,
+                       const float *d_logw, const float *d_quat, const float *d_trans,
+                       const float *d_stats, const float *d_features, int32_t n_features,
+                       float *d_out, fe_stream_t stream);
+
 /* XLA custom-call targets (api_version 2: status-returning), registered under the names
  * "fe_render_fwd" and "fe_render_bwd". opaque = an fe_render_desc.
  * fwd buffers: [means, prec, logw, quat, trans, depth, alpha, stats]
