@@ -27,8 +27,8 @@ struct GmmRec {
 
 constexpr float kHalfLog2Pi3 = 2.7568155996140185f;  // 1.5 ln(2 pi)
 constexpr int kGmmThreads = 256;
-constexpr int kGmmChunk = 512;  // Gaussians per shared-memory stage
-constexpr int kGmmPts = 2;      // points per thread
+constexpr int kGmmChunk = 512;  // Gaussians per shared-memory stage (40 KB)
+constexpr int kGmmPts = 4;      // points per thread (two packed pairs)
 
 __global__ void __launch_bounds__(1024) gmm_prep_kernel(int n, const float* __restrict__ means,
                                                         const float* __restrict__ prec,
@@ -76,49 +76,98 @@ __global__ void __launch_bounds__(1024) gmm_prep_kernel(int n, const float* __re
   }
 }
 
+// A prepared Gaussian with every field duplicated, so that one 8-byte shared-memory load gives a
+// packed f32x2 operand for two points.
+struct GmmRec2 {
+  f2_t mx, my, mz, u00, u01, u02, u11, u12, u22, c2;
+};
+
+// Four points per thread as two packed pairs; Gaussians are consumed in groups of four so that
+// the running maximum of each point's logsumexp is updated once per group.
 __global__ void __launch_bounds__(kGmmThreads) gmm_ll_kernel(
     int n, const GmmRec* __restrict__ gs, int64_t n_points, const float* __restrict__ points,
     float* __restrict__ point_ll, float* __restrict__ res, double* __restrict__ total) {
-  __shared__ GmmRec sg[kGmmChunk];
-  const float kNegHalfLog2e = -0.5f * kLog2e;
+  constexpr int kPairs = kGmmPts / 2;
+  constexpr int kGroup = 4;
+  __shared__ GmmRec2 sg[kGmmChunk];
+  const f2_t NH = f2_pack(-0.5f * kLog2e, -0.5f * kLog2e);
   for (int64_t base = (int64_t)blockIdx.x * kGmmThreads * kGmmPts; base < n_points;
        base += (int64_t)gridDim.x * kGmmThreads * kGmmPts) {
-    float px[kGmmPts], py[kGmmPts], pz[kGmmPts], m[kGmmPts], acc[kGmmPts];
+    f2_t PX[kPairs], PY[kPairs], PZ[kPairs];
+    float m[kGmmPts], acc[kGmmPts];
     int64_t j[kGmmPts];
 #pragma unroll
     for (int q = 0; q < kGmmPts; ++q) {
       j[q] = base + threadIdx.x + (int64_t)q * kGmmThreads;
-      const bool ok = j[q] < n_points;
-      px[q] = ok ? points[3 * j[q]] : 0.f;
-      py[q] = ok ? points[3 * j[q] + 1] : 0.f;
-      pz[q] = ok ? points[3 * j[q] + 2] : 0.f;
       m[q] = -INFINITY;
       acc[q] = 0.f;
+    }
+#pragma unroll
+    for (int h = 0; h < kPairs; ++h) {
+      float c[2][3];
+#pragma unroll
+      for (int t = 0; t < 2; ++t) {
+        const int q = 2 * h + t;
+        const bool ok = j[q] < n_points;
+        c[t][0] = ok ? points[3 * j[q]] : 0.f;
+        c[t][1] = ok ? points[3 * j[q] + 1] : 0.f;
+        c[t][2] = ok ? points[3 * j[q] + 2] : 0.f;
+      }
+      PX[h] = f2_pack(c[0][0], c[1][0]);
+      PY[h] = f2_pack(c[0][1], c[1][1]);
+      PZ[h] = f2_pack(c[0][2], c[1][2]);
     }
     for (int c0 = 0; c0 < n; c0 += kGmmChunk) {
       const int cn = min(kGmmChunk, n - c0);
       __syncthreads();
-      for (int i = threadIdx.x; i < cn; i += kGmmThreads) sg[i] = gs[c0 + i];
+      for (int i = threadIdx.x; i < cn; i += kGmmThreads) {
+        const GmmRec g = gs[c0 + i];
+        GmmRec2 d;
+        d.mx = f2_pack(g.mx, g.mx); d.my = f2_pack(g.my, g.my); d.mz = f2_pack(g.mz, g.mz);
+        d.u00 = f2_pack(g.u00, g.u00); d.u01 = f2_pack(g.u01, g.u01);
+        d.u02 = f2_pack(g.u02, g.u02); d.u11 = f2_pack(g.u11, g.u11);
+        d.u12 = f2_pack(g.u12, g.u12); d.u22 = f2_pack(g.u22, g.u22);
+        d.c2 = f2_pack(g.c2, g.c2);
+        sg[i] = d;
+      }
       __syncthreads();
-      for (int i = 0; i < cn; ++i) {
-        const GmmRec g = sg[i];
+      for (int i0 = 0; i0 < cn; i0 += kGroup) {
+        const int gn = min(kGroup, cn - i0);
+        float r[kGroup][kGmmPts];
+#pragma unroll
+        for (int k = 0; k < kGroup; ++k) {
+          if (k < gn) {
+            const GmmRec2& g = sg[i0 + k];
+#pragma unroll
+            for (int h = 0; h < kPairs; ++h) {
+              const f2_t p0 = sub2(g.mx, PX[h]), p1 = sub2(g.my, PY[h]), p2 = sub2(g.mz, PZ[h]);
+              const f2_t q0 = mul2(g.u00, p0);
+              const f2_t q1 = fma2(g.u11, p1, mul2(g.u01, p0));
+              const f2_t q2 = fma2(g.u22, p2, fma2(g.u12, p1, mul2(g.u02, p0)));
+              const f2_t d = fma2(q2, q2, fma2(q1, q1, mul2(q0, q0)));
+              f2_unpack(fma2(NH, d, g.c2), r[k][2 * h], r[k][2 * h + 1]);  // log2 densities
+            }
+          } else {
+#pragma unroll
+            for (int q = 0; q < kGmmPts; ++q) r[k][q] = -INFINITY;
+          }
+        }
 #pragma unroll
         for (int q = 0; q < kGmmPts; ++q) {
-          const float p0 = g.mx - px[q], p1 = g.my - py[q], p2 = g.mz - pz[q];
-          const float q0 = g.u00 * p0;
-          const float q1 = fmaf(g.u11, p1, g.u01 * p0);
-          const float q2 = fmaf(g.u22, p2, fmaf(g.u12, p1, g.u02 * p0));
-          const float d = fmaf(q2, q2, fmaf(q1, q1, q0 * q0));
-          const float r2 = fmaf(kNegHalfLog2e, d, g.c2);  // log2 of the component density
-          if (res && j[q] < n_points) res[(int64_t)(c0 + i) * n_points + j[q]] = r2 * kLn2;
-          if (r2 > m[q]) {
-            acc[q] = fmaf(acc[q], ex2_approx(m[q] - r2), 1.f);
-            m[q] = r2;
-          } else if (r2 > -INFINITY) {  // a -inf component adds nothing (and -inf - -inf is NaN)
-            acc[q] += ex2_approx(r2 - m[q]);
-          } else if (r2 != r2) {
-            acc[q] = r2;  // NaN input propagates
+          if (res && j[q] < n_points)
+            for (int k = 0; k < gn; ++k) res[(int64_t)(c0 + i0 + k) * n_points + j[q]] = r[k][q] * kLn2;
+          float gmax = r[0][q];
+#pragma unroll
+          for (int k = 1; k < kGroup; ++k) gmax = fmaxf(gmax, r[k][q]);
+          if (gmax > m[q]) {
+            acc[q] *= ex2_approx(m[q] - gmax);  // (0 while m is -inf: acc is 0 then)
+            m[q] = gmax;
           }
+          if (m[q] > -INFINITY) {  // all-(-inf) so far adds nothing (and -inf - -inf is NaN)
+#pragma unroll
+            for (int k = 0; k < kGroup; ++k) acc[q] += ex2_approx(r[k][q] - m[q]);
+          }
+          if (gmax != gmax) acc[q] = gmax;  // NaN input propagates
         }
       }
     }
