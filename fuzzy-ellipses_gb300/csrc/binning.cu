@@ -194,13 +194,16 @@ __global__ void __launch_bounds__(1024) scan_small_kernel(const uint32_t* __rest
   }
 }
 
-// Number of sort blocks that receive keys: at least 2048 keys per block, at most the grid.
+// Number of sort blocks that receive keys: at least kSortKeysPerBlock keys per block, at most the
+// grid.
+constexpr int kSortKeysPerBlock = 2048;
 __device__ __forceinline__ int sort_blocks_used(int64_t K, int grid) {
-  const int64_t b = (K + 2047) / 2048;
+  const int64_t b = (K + kSortKeysPerBlock - 1) / kSortKeysPerBlock;
   return (int)(b < 1 ? 1 : (b > grid ? grid : b));
 }
 
-// Per-block digit histograms, block-major: hist[b * 256 + digit].
+// Per-block digit histograms, digit-major: hist[digit * grid + b] (grid = the launch grid), so
+// that each digit's counts are contiguous for the scan.
 __global__ void sort_hist_kernel(const uint64_t* __restrict__ keys, const Control* __restrict__ ctrl,
                                  int shift, uint32_t* __restrict__ hist) {
   __shared__ uint32_t cnt[256];
@@ -211,36 +214,39 @@ __global__ void sort_hist_kernel(const uint64_t* __restrict__ keys, const Contro
   const int64_t s = blockIdx.x * chunk, e = min(K, s + chunk);
   cnt[threadIdx.x] = 0;
   __syncthreads();
+#pragma unroll 4
   for (int64_t i = s + threadIdx.x; i < e; i += kSortThreads)
     atomicAdd(&cnt[(uint32_t)(keys[i] >> shift) & 255u], 1u);
   __syncthreads();
-  hist[blockIdx.x * 256 + threadIdx.x] = cnt[threadIdx.x];
+  hist[threadIdx.x * gridDim.x + blockIdx.x] = cnt[threadIdx.x];
 }
 
-// One block per digit: exclusive scan of that digit's per-block counts (in block order), written
-// back in place; the digit total goes to row `grid` of hist. Each thread owns a contiguous run
-// of blocks so the scan keeps block order.
+// One block per digit: exclusive scan of that digit's per-block counts (in block order, one
+// contiguous row of hist), written back in place; the digit total goes to hist[256 * grid + d].
+// Each thread owns a contiguous run of blocks so the scan keeps block order.
 __global__ void sort_scan_kernel(uint32_t* __restrict__ hist, const Control* __restrict__ ctrl,
                                  int grid) {
   __shared__ uint32_t ws[kScanThreads / 32];
   const int nb = sort_blocks_used((int64_t)ctrl->num_keys, grid);
   const int d = blockIdx.x;
+  uint32_t* row = hist + (int64_t)d * grid;
   const int per = (nb + kScanThreads - 1) / kScanThreads;
   const int b0 = threadIdx.x * per, b1 = min(nb, b0 + per);
   uint32_t run = 0;
-  for (int b = b0; b < b1; ++b) run += hist[b * 256 + d];
+  for (int b = b0; b < b1; ++b) run += row[b];
   uint32_t ex;
   const uint32_t total = block_exclusive_scan<uint32_t>(run, ex, ws);
   for (int b = b0; b < b1; ++b) {
-    const uint32_t c = hist[b * 256 + d];
-    hist[b * 256 + d] = ex;
+    const uint32_t c = row[b];
+    row[b] = ex;
     ex += c;
   }
   if (threadIdx.x == 0) hist[grid * 256 + d] = total;
 }
 
 // Stable scatter: keys are taken in order 256 at a time; ranks within a 256-key slice come from
-// warp match-any groups plus per-warp digit counts scanned across warps in warp order.
+// warp match-any groups plus per-warp digit counts scanned across warps in warp order. Digit
+// bases: the scanned digit totals plus this block's row entries of the digit-major hist.
 __global__ void sort_scatter_kernel(const uint64_t* __restrict__ in, uint64_t* __restrict__ out,
                                     const Control* __restrict__ ctrl, int shift,
                                     const uint32_t* __restrict__ hist) {
@@ -258,15 +264,18 @@ __global__ void sort_scatter_kernel(const uint64_t* __restrict__ in, uint64_t* _
     // Digit bases: exclusive scan of the 256 digit totals.
     uint32_t base;
     block_exclusive_scan<uint32_t>(hist[gridDim.x * 256 + tid], base, ws);
-    off[tid] = base + hist[blockIdx.x * 256 + tid];
+    off[tid] = base + hist[tid * gridDim.x + blockIdx.x];
   }
   const uint32_t lt_mask = (1u << lane) - 1u;
+  // The next slice's key is loaded one iteration ahead, so the ranking below does not wait on it.
+  uint64_t next = (s + tid < e) ? in[s + tid] : 0ull;
   for (int64_t base = s; base < e; base += kSortThreads) {
 #pragma unroll
     for (int w = 0; w < kSortWarps; ++w) wc[w][tid] = 0;
     const int64_t i = base + tid;
     const bool valid = i < e;
-    const uint64_t key = valid ? in[i] : 0ull;
+    const uint64_t key = next;
+    next = (i + kSortThreads < e) ? in[i + kSortThreads] : 0ull;
     const uint32_t d = valid ? ((uint32_t)(key >> shift) & 255u) : 256u;
     const uint32_t peers = __match_any_sync(0xffffffffu, d);
     const uint32_t rank = __popc(peers & lt_mask);
@@ -391,7 +400,7 @@ inline int grid_for(int64_t work, int threads, int cap) {
 }  // namespace
 
 int scan_grid(int64_t n) { return grid_for(n, 4 * kScanThreads, 1024); }
-int sort_grid(int64_t key_capacity) { return grid_for(key_capacity, 2048, 2 * 152); }
+int sort_grid(int64_t key_capacity) { return grid_for(key_capacity, kSortKeysPerBlock, 2 * 152); }
 
 void launch_scan(const uint32_t* touched, uint32_t* incl, int64_t n, int64_t capacity,
                  unsigned long long* scratch, Control* ctrl, cudaStream_t st) {
