@@ -556,7 +556,7 @@ def _silhouette(h, w):
     return (((u - w / 2) ** 2 + (v - h / 2) ** 2) < (0.3 * min(h, w)) ** 2).astype(np.float32)
 
 
-def serve_bench(fe, dev, n_requests=200, plain_requests=60, seed=0):
+def serve_bench(fe, dev, n_requests=500, plain_requests=60, seed=0):
     """Served mixed requests (N log-uniform in [20, 2000], 1-32 poses, sides 96-480, 30% with a
     silhouette-BCE backward): saturating arrivals for throughput, Poisson arrivals at half that
     rate for latency; the plain per-call drop-in (one fe_render_fwd / autograd render per camera,
