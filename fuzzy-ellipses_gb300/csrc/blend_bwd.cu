@@ -387,14 +387,7 @@ void launch_bwd_tiles(const ViewsArg& va, int64_t n_tiles, const uint64_t* keys,
                       const float4* pix, float beta2, float beta3, RecGrad* rgrad, Control* ctrl,
                       cudaStream_t st) {
   constexpr auto kern = blend_bwd_kernel<TW, TH>;
-  static int resident = 0;
-  if (resident == 0) {
-    int dev = 0, sms = 0, per_sm = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 32 * kBwdWarps, 0);
-    resident = sms * (per_sm > 0 ? per_sm : 1);
-  }
+  const int resident = resident_ctas<kern>(32 * kBwdWarps);
   const int64_t grid =
       std::max<int64_t>(1, std::min<int64_t>((n_tiles + kBwdWarps - 1) / kBwdWarps, resident));
   kern<<<(unsigned)grid, 32 * kBwdWarps, 0, st>>>(va, (uint32_t)n_tiles, keys, ranges, trec, recs,

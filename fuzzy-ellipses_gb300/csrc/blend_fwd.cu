@@ -271,20 +271,6 @@ __global__ void __launch_bounds__(BlendShape<TW, TH, PX, CH>::NT,
   }
 }
 
-// CTAs of `Kern` resident on the current device (queried once per kernel instantiation).
-template <auto Kern>
-int resident_ctas(int threads) {
-  static int cached = 0;
-  if (cached == 0) {
-    int dev = 0, sms = 0, per_sm = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, Kern, threads, 0);
-    cached = sms * (per_sm > 0 ? per_sm : 1);
-  }
-  return cached;
-}
-
 template <int TW, int TH, int PX, int CH>
 void launch_tiles(const ViewsArg& va, int64_t n_tiles, const TilePair* trec, const uint2* ranges,
                   float nb2, float beta3, float* depth, float* alpha, float* stats,

@@ -1,6 +1,7 @@
 // fe_common.cuh -- types, constants and inline-PTX helpers shared by the renderer's kernels.
 #pragma once
 
+#include <atomic>
 #include <cstdint>
 #include <cuda_runtime.h>
 
@@ -324,6 +325,26 @@ __device__ __forceinline__ void quat_to_rot(const float* q, T* r) {
   r[0] = T(1) - (yY + zZ); r[1] = xY - wZ; r[2] = xZ + wY;
   r[3] = xY + wZ; r[4] = T(1) - (xX + zZ); r[5] = yZ - wX;
   r[6] = xZ - wY; r[7] = yZ + wX; r[8] = T(1) - (xX + yY);
+}
+
+// CTAs of kernel `Kern` (with `threads` threads) resident on the current device, queried once per
+// (kernel, device); safe to call from several host threads.
+template <auto Kern>
+inline int resident_ctas(int threads) {
+  constexpr int kMaxDevices = 64;
+  static std::atomic<int> cache[kMaxDevices];
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev < 0 || dev >= kMaxDevices) dev = 0;
+  int v = cache[dev].load(std::memory_order_relaxed);
+  if (v == 0) {
+    int sms = 0, per_sm = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, Kern, threads, 0);
+    v = (sms > 0 ? sms : 1) * (per_sm > 0 ? per_sm : 1);
+    cache[dev].store(v, std::memory_order_relaxed);
+  }
+  return v;
 }
 
 }  // namespace fe

@@ -104,14 +104,7 @@ void launch_tiles(const ViewsArg& va, int64_t n_tiles, const uint64_t* keys, con
                   float beta3, const float* feats, int nf, float* out, Control* ctrl,
                   cudaStream_t st) {
   constexpr auto kern = features_kernel<TW, TH>;
-  static int resident = 0;
-  if (resident == 0) {
-    int dev = 0, sms = 0, per_sm = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 32 * kFeatWarps, 0);
-    resident = sms * (per_sm > 0 ? per_sm : 1);
-  }
+  const int resident = resident_ctas<kern>(32 * kFeatWarps);
   const int64_t grid =
       std::max<int64_t>(1, std::min<int64_t>((n_tiles + kFeatWarps - 1) / kFeatWarps, resident));
   kern<<<(unsigned)grid, 32 * kFeatWarps, 0, st>>>(va, (uint32_t)n_tiles, keys, ranges, trec,
