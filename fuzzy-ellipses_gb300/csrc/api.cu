@@ -616,6 +616,27 @@ int fe_render_pixels(const fe_pixlist_desc* d, const float* means, const float* 
   return FE_OK;
 }
 
+int fe_selftest_bounded_wait(uint64_t limit_ns, uint32_t* h_status, uint64_t* h_elapsed_ns,
+                             fe_stream_t stream_) {
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream_);
+  if (!h_status || !h_elapsed_ns) return fail(FE_ERR_INVALID_ARGUMENT, "NULL output");
+  if (limit_ns < 1000 || limit_ns > 1000000000ull)
+    return fail(FE_ERR_INVALID_ARGUMENT, "limit_ns must be in [1 us, 1 s]");
+  Arena* a = nullptr;
+  int rc = arena_for(st, &a);
+  if (rc) return rc;
+  rc = a->rec.reserve(256, st);
+  if (rc) return rc;
+  uint32_t* status = reinterpret_cast<uint32_t*>(a->rec.ptr);
+  unsigned long long* elapsed = reinterpret_cast<unsigned long long*>(a->rec.ptr + 64);
+  launch_wait_selftest(limit_ns, status, elapsed, st);
+  FE_CUDA(cudaGetLastError());
+  FE_CUDA(cudaMemcpyAsync(h_status, status, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+  FE_CUDA(cudaMemcpyAsync(h_elapsed_ns, elapsed, sizeof(uint64_t), cudaMemcpyDeviceToHost, st));
+  FE_CUDA(cudaStreamSynchronize(st));
+  return FE_OK;
+}
+
 int fe_check_device_status(fe_stream_t stream_, uint32_t* device_error) {
   cudaStream_t st = reinterpret_cast<cudaStream_t>(stream_);
   Arena* a = nullptr;

@@ -120,4 +120,8 @@ void launch_features(const ViewsArg& va, int tile_w, int tile_h, int64_t n_tiles
                      const float* stats, int64_t stats_stride, float beta2, float beta3,
                      const float* feats, int nf, float* out, Control* ctrl, cudaStream_t st);
 
+// profiling.cu
+void launch_wait_selftest(unsigned long long limit_ns, uint32_t* status,
+                          unsigned long long* elapsed_ns, cudaStream_t st);
+
 }  // namespace fe

@@ -58,7 +58,32 @@ __global__ void __launch_bounds__(256) peak_fma2_kernel(float* out, int iters, f
   if (s == 12345.678f) out[blockIdx.x] = s;
 }
 
+// Failure-detection self-test: one block waits on an mbarrier that nothing ever arrives at,
+// through the same bounded wait the blend uses for its TMA copies. The wait must give up after
+// limit_ns and report FE_DEVERR_TIMEOUT, leaving the context usable.
+__global__ void wait_selftest_kernel(unsigned long long limit_ns, uint32_t* status,
+                                     unsigned long long* elapsed_ns) {
+  __shared__ uint64_t bar;
+  if (threadIdx.x == 0) {
+    mbar_init(&bar, 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+  const unsigned long long t0 = global_timer_ns();
+  const bool completed = mbar_wait_bounded(&bar, 0, limit_ns);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    *status = completed ? 0u : FE_DEVERR_TIMEOUT;
+    *elapsed_ns = global_timer_ns() - t0;
+  }
+}
+
 }  // namespace
+
+void launch_wait_selftest(unsigned long long limit_ns, uint32_t* status,
+                          unsigned long long* elapsed_ns, cudaStream_t st) {
+  wait_selftest_kernel<<<1, 32, 0, st>>>(limit_ns, status, elapsed_ns);
+}
 
 // Returns pipe operations per second: kind 0 = FFMA (one FMA per op), kind 1 = MUFU.EX2
 // (the ex2 kernel also issues one FADD per op, on the FMA pipe), kind 2 = packed f32x2 FMA

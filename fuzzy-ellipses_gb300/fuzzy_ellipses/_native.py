@@ -173,6 +173,8 @@ PROTOTYPES = {
     "fe_batch_fwd_timed": (ctypes.c_int, [P] + [P] * 6 + [ctypes.POINTER(ctypes.c_float), P]),
     "fe_batch_launch_count": (ctypes.c_int, [P]),
     "fe_bench_peak": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_double), P]),
+    "fe_selftest_bounded_wait": (ctypes.c_int, [ctypes.c_uint64, ctypes.POINTER(ctypes.c_uint32),
+                                                ctypes.POINTER(ctypes.c_uint64), P]),
     "fe_server_config_init": (None, [ctypes.POINTER(ServerConfig)]),
     "fe_server_create": (ctypes.c_int, [ctypes.POINTER(ServerConfig), ctypes.c_int, ctypes.POINTER(P)]),
     "fe_server_submit": (ctypes.c_int, [P, ctypes.POINTER(Request), ctypes.POINTER(ctypes.c_uint64)]),

@@ -457,6 +457,14 @@ int fe_check_device_status(fe_stream_t stream, uint32_t *device_error);
 #define FE_DEVERR_CAPACITY 1u /* more keys than planned */
 #define FE_DEVERR_TIMEOUT 2u  /* a bounded mbarrier wait gave up */
 
+/* Failure-detection self-test (no reference counterpart): one block waits on an mbarrier that
+ * nothing arrives at, through the same bounded wait the blend uses for its TMA copies, with the
+ * limit limit_ns (1 us .. 1 s). Synchronises `stream`; *h_status receives FE_DEVERR_TIMEOUT when
+ * the wait gave up (the expected outcome) and *h_elapsed_ns the time the wait took. The context
+ * stays usable afterwards. */
+int fe_selftest_bounded_wait(uint64_t limit_ns, uint32_t *h_status, uint64_t *h_elapsed_ns,
+                             fe_stream_t stream);
+
 /* Message for the most recent error on the calling thread. */
 const char *fe_last_error_message(void);
 const char *fe_status_string(int status);
