@@ -872,6 +872,17 @@ struct fe_batch {
   KeySpace ks{};
   uint64_t* sorted = nullptr;
   unsigned long long* h_pinned = nullptr;
+  // fe_batch_fwd_host: device staging of the Gaussians and images, the band plan, and the
+  // batch's second compute stream and copy stream with their events (created on first use).
+  struct HostBand {
+    int64_t t0, t1;  // global tiles [t0, t1): whole tile rows
+    int64_t p0, p1;  // the contiguous output pixels [p0, p1) of those rows
+  };
+  DevBuf io;
+  std::vector<HostBand> bands;
+  cudaStream_t s_comp = nullptr, s_copy = nullptr;
+  cudaEvent_t ev_bin = nullptr, ev_copy = nullptr;
+  std::vector<cudaEvent_t> band_ev;
 };
 
 namespace {
@@ -887,6 +898,7 @@ int plan_batch(fe_batch* b, const fe_scene* scenes, int32_t n_scenes, const fe_v
         !(v.fx != 0.f) || !(v.fy != 0.f) || scenes[v.scene].n < 0 || scenes[v.scene].gauss_offset < 0)
       return fail(FE_ERR_INVALID_ARGUMENT, "bad view " + std::to_string(i));
   }
+  b->bands.clear();
   b->views_h.assign(n_views, ViewDev{});
   b->quat_h.assign(4 * (size_t)n_views, 0.f);
   b->trans_h.assign(3 * (size_t)n_views, 0.f);
@@ -1018,6 +1030,12 @@ void fe_batch_destroy(fe_batch* b) {
   cudaFree(b->rec.ptr);
   cudaFree(b->keys.ptr);
   if (b->h_pinned) cudaFreeHost(b->h_pinned);
+  cudaFree(b->io.ptr);
+  for (cudaEvent_t e : b->band_ev) cudaEventDestroy(e);
+  if (b->ev_bin) cudaEventDestroy(b->ev_bin);
+  if (b->ev_copy) cudaEventDestroy(b->ev_copy);
+  if (b->s_comp) cudaStreamDestroy(b->s_comp);
+  if (b->s_copy) cudaStreamDestroy(b->s_copy);
   delete b;
 }
 
@@ -1095,6 +1113,38 @@ static int batch_binning(fe_batch* b, const Pipeline& p, cudaStream_t st, cudaEv
   return FE_OK;
 }
 
+// Bands of whole tile rows for fe_batch_fwd_host: about kHostBandPixels output pixels each (at
+// most kMaxHostBands per batch), each covering a contiguous range of output pixels (a band ends
+// where the next view's pixels do not follow on).
+constexpr int64_t kHostBandPixels = INT64_C(1) << 19;
+constexpr int64_t kMaxHostBands = 8;
+
+static void plan_host_bands(fe_batch* b) {
+  b->bands.clear();
+  const int64_t k =
+      std::min(kMaxHostBands, std::max<int64_t>(1, (b->n_pix + kHostBandPixels - 1) / kHostBandPixels));
+  const int64_t target = std::max<int64_t>(1, (b->n_tiles + k - 1) / k);
+  fe_batch::HostBand cur{0, 0, 0, 0};
+  bool open = false;
+  for (const ViewDev& V : b->views_h) {
+    for (int ty = 0; ty < V.gy; ++ty) {
+      const int64_t t = V.tile_base + (int64_t)ty * V.gx;
+      const int64_t px = V.pix_base + (int64_t)std::min(ty * b->tile_h, V.H) * V.W;
+      if (open && (cur.p1 != px || cur.t1 != t || cur.t1 - cur.t0 >= target)) {
+        b->bands.push_back(cur);
+        open = false;
+      }
+      if (!open) {
+        cur = {t, t, px, px};
+        open = true;
+      }
+      cur.t1 = t + V.gx;
+      cur.p1 = V.pix_base + (int64_t)std::min((ty + 1) * b->tile_h, V.H) * V.W;
+    }
+  }
+  if (open) b->bands.push_back(cur);
+}
+
 extern "C" {
 
 int fe_batch_fwd(fe_batch* b, const float* means, const float* prec, const float* logw,
@@ -1111,6 +1161,78 @@ int fe_batch_fwd(fe_batch* b, const float* means, const float* prec, const float
   launch_blend_fwd(p.va, p.tile_w, p.tile_h, p.px, p.chunk, p.n_tiles, b->ks.trec, b->rs.ranges,
                    p.beta2, p.beta3, depth, alpha, stats, p.n_pix, b->rs.ctrl, st);
   FE_CUDA(cudaGetLastError());
+  return FE_OK;
+}
+
+int fe_batch_fwd_host(fe_batch* b, const float* h_means, const float* h_prec,
+                      const float* h_logw, float* h_depth, float* h_alpha, fe_stream_t stream_) {
+  if (!b || !h_depth || !h_alpha) return fail(FE_ERR_INVALID_ARGUMENT, "NULL argument");
+  const int64_t n = b->n_gauss;
+  if (n > 0 && (!h_means || !h_prec || !h_logw))
+    return fail(FE_ERR_INVALID_ARGUMENT, "NULL Gaussian pointer");
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream_);
+  if (b->bands.empty()) plan_host_bands(b);
+  const int nb = (int)b->bands.size();
+
+  Carver c{nullptr};
+  c.take<float>(3 * n); c.take<float>(9 * n); c.take<float>(n);
+  c.take<float>(b->n_pix); c.take<float>(b->n_pix); c.take<uint32_t>(nb);
+  int rc = b->io.reserve(c.off, st);
+  if (rc) return rc;
+  Carver t{b->io.ptr};
+  float* m_d = t.take<float>(3 * n);
+  float* p_d = t.take<float>(9 * n);
+  float* w_d = t.take<float>(n);
+  float* dep_d = t.take<float>(b->n_pix);
+  float* alp_d = t.take<float>(b->n_pix);
+  uint32_t* ctr = t.take<uint32_t>(nb);
+  if (!b->s_comp) {
+    FE_CUDA(cudaStreamCreateWithFlags(&b->s_comp, cudaStreamNonBlocking));
+    FE_CUDA(cudaStreamCreateWithFlags(&b->s_copy, cudaStreamNonBlocking));
+    FE_CUDA(cudaEventCreateWithFlags(&b->ev_bin, cudaEventDisableTiming));
+    FE_CUDA(cudaEventCreateWithFlags(&b->ev_copy, cudaEventDisableTiming));
+  }
+  while ((int)b->band_ev.size() < nb) {
+    cudaEvent_t e;
+    FE_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    b->band_ev.push_back(e);
+  }
+
+  if (n > 0) {
+    FE_CUDA(cudaMemcpyAsync(m_d, h_means, sizeof(float) * 3 * n, cudaMemcpyHostToDevice, st));
+    FE_CUDA(cudaMemcpyAsync(p_d, h_prec, sizeof(float) * 9 * n, cudaMemcpyHostToDevice, st));
+    FE_CUDA(cudaMemcpyAsync(w_d, h_logw, sizeof(float) * n, cudaMemcpyHostToDevice, st));
+  }
+  Pipeline p = batch_pipeline(b, m_d, p_d, w_d);
+  b->binned = false;
+  rc = batch_binning(b, p, st, nullptr);
+  if (rc) return rc;
+  note_binning(b, m_d, p_d, w_d);
+  FE_CUDA(cudaMemsetAsync(ctr, 0, sizeof(uint32_t) * nb, st));
+  FE_CUDA(cudaEventRecord(b->ev_bin, st));
+  FE_CUDA(cudaStreamWaitEvent(b->s_comp, b->ev_bin, 0));
+  // Every band's blend is enqueued before any copy, so copies into pageable memory (which hold
+  // the calling thread) cannot delay the renders.
+  for (int j = 0; j < nb; ++j) {
+    const fe_batch::HostBand& hb = b->bands[j];
+    cudaStream_t sj = (j & 1) ? b->s_comp : st;
+    launch_blend_fwd_band(p.va, p.tile_w, p.tile_h, p.px, p.chunk, hb.t0, hb.t1, ctr + j,
+                          b->ks.trec, b->rs.ranges, p.beta2, p.beta3, dep_d, alp_d, nullptr,
+                          p.n_pix, b->rs.ctrl, sj);
+    FE_CUDA(cudaGetLastError());
+    FE_CUDA(cudaEventRecord(b->band_ev[j], sj));
+  }
+  for (int j = 0; j < nb; ++j) {
+    const fe_batch::HostBand& hb = b->bands[j];
+    const size_t bytes = sizeof(float) * (size_t)(hb.p1 - hb.p0);
+    FE_CUDA(cudaStreamWaitEvent(b->s_copy, b->band_ev[j], 0));
+    FE_CUDA(cudaMemcpyAsync(h_depth + hb.p0, dep_d + hb.p0, bytes, cudaMemcpyDeviceToHost,
+                            b->s_copy));
+    FE_CUDA(cudaMemcpyAsync(h_alpha + hb.p0, alp_d + hb.p0, bytes, cudaMemcpyDeviceToHost,
+                            b->s_copy));
+  }
+  FE_CUDA(cudaEventRecord(b->ev_copy, b->s_copy));
+  FE_CUDA(cudaStreamWaitEvent(st, b->ev_copy, 0));
   return FE_OK;
 }
 

@@ -144,20 +144,34 @@ __global__ void emit_keys_kernel(ViewsArg va, const uint32_t* __restrict__ incl,
   }
 }
 
-// Single-CTA inclusive scan for small inputs: 1024 threads x 4 consecutive values per pass.
+// Single-CTA inclusive scan for small inputs: 1024 threads x 16 consecutive values per pass
+// (16-byte loads and stores when the arrays are aligned), all loads of a pass issued up front.
 __global__ void __launch_bounds__(1024) scan_small_kernel(const uint32_t* __restrict__ in,
                                                           uint32_t* __restrict__ out, int64_t n,
                                                           int64_t capacity,
                                                           Control* __restrict__ ctrl) {
+  constexpr int kPer = 16;
   __shared__ unsigned long long ws[32];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const bool vec = ((reinterpret_cast<uintptr_t>(in) | reinterpret_cast<uintptr_t>(out)) & 15) == 0;
   unsigned long long carry = 0;
-  for (int64_t base = 0; base < n; base += 4096) {
-    const int64_t i0 = base + 4 * threadIdx.x;
-    uint32_t v[4];
+  for (int64_t base = 0; base < n; base += 1024 * kPer) {
+    const int64_t i0 = base + (int64_t)kPer * threadIdx.x;
+    const bool whole = vec && i0 + kPer <= n;
+    uint32_t v[kPer];
+    if (whole) {
 #pragma unroll
-    for (int k = 0; k < 4; ++k) v[k] = i0 + k < n ? in[i0 + k] : 0u;
-    unsigned long long t = (unsigned long long)v[0] + v[1] + v[2] + v[3];
+      for (int q = 0; q < kPer / 4; ++q) {
+        const uint4 w = reinterpret_cast<const uint4*>(in + i0)[q];
+        v[4 * q] = w.x; v[4 * q + 1] = w.y; v[4 * q + 2] = w.z; v[4 * q + 3] = w.w;
+      }
+    } else {
+#pragma unroll
+      for (int q = 0; q < kPer; ++q) v[q] = i0 + q < n ? in[i0 + q] : 0u;
+    }
+    unsigned long long t = 0;
+#pragma unroll
+    for (int q = 0; q < kPer; ++q) t += v[q];
     unsigned long long x = t;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
@@ -178,10 +192,21 @@ __global__ void __launch_bounds__(1024) scan_small_kernel(const uint32_t* __rest
     __syncthreads();
     unsigned long long run = carry + (warp ? ws[warp - 1] : 0ull) + x - t;
     const unsigned long long total = ws[31];
+    uint32_t r[kPer];
 #pragma unroll
-    for (int k = 0; k < 4; ++k) {
-      run += v[k];
-      if (i0 + k < n) out[i0 + k] = run > 0xffffffffull ? 0xffffffffu : (uint32_t)run;
+    for (int q = 0; q < kPer; ++q) {
+      run += v[q];
+      r[q] = run > 0xffffffffull ? 0xffffffffu : (uint32_t)run;
+    }
+    if (whole) {
+#pragma unroll
+      for (int q = 0; q < kPer / 4; ++q)
+        reinterpret_cast<uint4*>(out + i0)[q] =
+            make_uint4(r[4 * q], r[4 * q + 1], r[4 * q + 2], r[4 * q + 3]);
+    } else {
+#pragma unroll
+      for (int q = 0; q < kPer; ++q)
+        if (i0 + q < n) out[i0 + q] = r[q];
     }
     carry += total;
     __syncthreads();
@@ -348,48 +373,113 @@ __device__ __forceinline__ void null_tile_record(TileRec& t) {
   t.front = 1.f;
 }
 
-// One thread per pair of sorted keys: tile ranges, and the two tile records written as one
-// pair-interleaved TilePair (ten 16-byte stores).
-__global__ void ranges_gather_kernel(ViewsArg va, const uint64_t* __restrict__ keys,
-                                     const Control* __restrict__ ctrl,
-                                     const GaussRec* __restrict__ recs, int tile_w, int tile_h,
-                                     uint2* __restrict__ ranges, TilePair* __restrict__ trec) {
+// Gather block: one sorted key per thread, kGatherThreads / 2 TilePairs per iteration.
+constexpr int kGatherThreads = 256;
+constexpr int kGatherPairs = kGatherThreads / 2;
+constexpr int kGatherParts = (int)(sizeof(GaussRec) / 16);  // 16-byte parts of a GaussRec
+constexpr int kRecWords = 28;  // GaussRec stride in shared memory (96 B + 16 B: conflict-free)
+
+struct GatherSmem {
+  union {
+    float rec[kGatherThreads * kRecWords];  // the block's source records (28 KB)
+    TilePair out[kGatherPairs];             // the block's output pairs (20 KB)
+  } u;
+  int64_t src[kGatherThreads];  // record index of each thread's key, -1 when out of range
+};
+
+// Tile ranges, and every key's tile record, written pair-interleaved. Per iteration a block takes
+// kGatherThreads consecutive keys: the source records are fetched cooperatively (consecutive
+// lanes read consecutive 16-byte parts, so a warp touches ~5 records per load instead of 32),
+// each thread expands its own record, the two records of a pair are interleaved with lane
+// shuffles into conflict-free 16-byte shared stores, and one TMA bulk store writes the block's
+// 20 KB of TilePairs to global memory. trec == nullptr computes the ranges only.
+__global__ void __launch_bounds__(kGatherThreads, 4) ranges_gather_kernel(
+    ViewsArg va, const uint64_t* __restrict__ keys, const Control* __restrict__ ctrl,
+    const GaussRec* __restrict__ recs, int tile_w, int tile_h, uint2* __restrict__ ranges,
+    TilePair* __restrict__ trec) {
+  __shared__ __align__(128) GatherSmem sm;
+  const unsigned full = 0xffffffffu;
+  const int tid = threadIdx.x, lane = tid & 31;
+  const bool odd = (tid & 1) != 0;
   const int64_t K = (int64_t)ctrl->num_keys;
   const int64_t npairs = (K + 1) >> 1;
-  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < npairs;
-       p += (int64_t)gridDim.x * blockDim.x) {
-    TileRec t[2];
-#pragma unroll
-    for (int sl = 0; sl < 2; ++sl) {
-      const int64_t k = 2 * p + sl;
-      if (k >= K) {
-        null_tile_record(t[sl]);
-        continue;
-      }
-      const uint64_t key = keys[k];
-      const uint32_t tile = (uint32_t)(key >> 32);
-      const uint32_t gid = (uint32_t)key;
-      if (k == 0 || (uint32_t)(keys[k - 1] >> 32) != tile) ranges[tile].x = (uint32_t)k;
-      if (k == K - 1 || (uint32_t)(keys[k + 1] >> 32) != tile) ranges[tile].y = (uint32_t)(k + 1);
-      if (trec) {
-        const int vi = find_view<&ViewDev::tile_base>(va, tile);
-        const ViewDev& V = view_at(va, vi);
-        const int lt = (int)(tile - V.tile_base);
-        const int tx = lt % V.gx, ty = lt / V.gx;
-        const float hw = 0.5f * (tile_w - 1), hh = 0.5f * (tile_h - 1);
-        const GaussRec g = recs[V.rec_base + gid];
-        tile_record(g, tx * tile_w + hw - g.uc, ty * tile_h + hh - g.vc, hw, hh, t[sl]);
-      }
+  for (int64_t p0 = (int64_t)blockIdx.x * kGatherPairs; p0 < npairs;
+       p0 += (int64_t)gridDim.x * kGatherPairs) {
+    const int64_t k = 2 * p0 + tid;
+    const bool valid = k < K;
+    const uint64_t key = valid ? keys[k] : 0ull;
+    const uint32_t tile = (uint32_t)(key >> 32);
+    uint32_t prev = __shfl_up_sync(full, tile, 1);
+    uint32_t next = __shfl_down_sync(full, tile, 1);
+    if (valid) {
+      if (lane == 0 && k > 0) prev = (uint32_t)(keys[k - 1] >> 32);
+      if (lane == 31 && k + 1 < K) next = (uint32_t)(keys[k + 1] >> 32);
+      if (k == 0 || prev != tile) ranges[tile].x = (uint32_t)k;
+      if (k == K - 1 || next != tile) ranges[tile].y = (uint32_t)(k + 1);
     }
-    if (trec) {
-      const float* a = reinterpret_cast<const float*>(&t[0]);
-      const float* b = reinterpret_cast<const float*>(&t[1]);
-      float4* dst = reinterpret_cast<float4*>(trec + p);
+    if (trec == nullptr) continue;
+
+    int tx = 0, ty = 0;
+    int64_t src = -1;
+    if (valid) {
+      const int vi = find_view<&ViewDev::tile_base>(va, tile);
+      const ViewDev& V = view_at(va, vi);
+      const int lt = (int)(tile - V.tile_base);
+      tx = lt % V.gx;
+      ty = lt / V.gx;
+      src = V.rec_base + (int64_t)(uint32_t)key;
+    }
+    sm.src[tid] = src;
+    if (tid == 0) bulk_wait_group_read0();  // the previous store has read u.out (aliases u.rec)
+    __syncthreads();
 #pragma unroll
-      for (int j = 0; j < kRecFields / 2; ++j)
-        dst[j] = make_float4(a[2 * j], b[2 * j], a[2 * j + 1], b[2 * j + 1]);
+    for (int e = tid; e < kGatherThreads * kGatherParts; e += kGatherThreads) {
+      const int r = e / kGatherParts, part = e - r * kGatherParts;
+      const int64_t s = sm.src[r];
+      if (s >= 0)
+        *reinterpret_cast<float4*>(&sm.u.rec[r * kRecWords + 4 * part]) =
+            reinterpret_cast<const float4*>(recs + s)[part];
+    }
+    __syncthreads();
+    GaussRec g;
+    if (valid) {
+      float4* gd = reinterpret_cast<float4*>(&g);
+#pragma unroll
+      for (int part = 0; part < kGatherParts; ++part)
+        gd[part] = *reinterpret_cast<const float4*>(&sm.u.rec[tid * kRecWords + 4 * part]);
+    }
+    __syncthreads();  // every record read before u.out (aliased) is written
+
+    TileRec t;
+    if (valid) {
+      const float hw = 0.5f * (tile_w - 1), hh = 0.5f * (tile_h - 1);
+      tile_record(g, tx * tile_w + hw - g.uc, ty * tile_h + hh - g.vc, hw, hh, t);
+    } else {
+      null_tile_record(t);
+    }
+    // Even lane: record a (slot 0) of the pair; odd lane: record b (slot 1). Float4 j of the pair
+    // is (a[2j], b[2j], a[2j+1], b[2j+1]); the even lane writes j = 0..4, the odd lane j = 5..9.
+    const float* mine = reinterpret_cast<const float*>(&t);
+    float other[kRecFields / 2];
+#pragma unroll
+    for (int i = 0; i < kRecFields / 2; ++i)
+      other[i] = __shfl_xor_sync(full, odd ? mine[i] : mine[kRecFields / 2 + i], 1);
+    float4* dst = reinterpret_cast<float4*>(&sm.u.out[tid >> 1]) + (odd ? kRecFields / 4 : 0);
+#pragma unroll
+    for (int m = 0; m < kRecFields / 4; ++m) {
+      const int h = kRecFields / 2 + 2 * m;
+      dst[m] = odd ? make_float4(other[2 * m], mine[h], other[2 * m + 1], mine[h + 1])
+                   : make_float4(mine[2 * m], other[2 * m], mine[2 * m + 1], other[2 * m + 1]);
+    }
+    fence_proxy_async_smem();
+    __syncthreads();
+    if (tid == 0) {
+      const int64_t np = min((int64_t)kGatherPairs, npairs - p0);
+      bulk_store_s2g(trec + p0, sm.u.out, (uint32_t)(np * sizeof(TilePair)));
+      bulk_commit_group();
     }
   }
+  if (trec != nullptr && tid == 0) bulk_wait_group0();
 }
 
 inline int grid_for(int64_t work, int threads, int cap) {
@@ -440,15 +530,19 @@ uint64_t* launch_sort(uint64_t* a, uint64_t* b, int key_bits, const Control* ctr
 void launch_ranges_gather(const ViewsArg& va, const uint64_t* keys, const Control* ctrl,
                           int64_t capacity, const GaussRec* recs, int tile_w, int tile_h,
                           uint2* ranges, TilePair* trec, cudaStream_t st) {
-  ranges_gather_kernel<<<grid_for((capacity + 1) / 2, 256, 4 * 152 * 8), 256, 0, st>>>(
-      va, keys, ctrl, recs, tile_w, tile_h, ranges, trec);
+  const int grid = grid_for((capacity + 1) / 2, kGatherPairs,
+                            resident_ctas<ranges_gather_kernel>(kGatherThreads));
+  ranges_gather_kernel<<<grid, kGatherThreads, 0, st>>>(va, keys, ctrl, recs, tile_w, tile_h,
+                                                        ranges, trec);
 }
 
 void launch_ranges(const uint64_t* keys, const Control* ctrl, int64_t capacity, uint2* ranges,
                    cudaStream_t st) {
   ViewsArg va{};
-  ranges_gather_kernel<<<grid_for((capacity + 1) / 2, 256, 4 * 152 * 8), 256, 0, st>>>(
-      va, keys, ctrl, nullptr, 8, 8, ranges, nullptr);
+  const int grid = grid_for((capacity + 1) / 2, kGatherPairs,
+                            resident_ctas<ranges_gather_kernel>(kGatherThreads));
+  ranges_gather_kernel<<<grid, kGatherThreads, 0, st>>>(va, keys, ctrl, nullptr, 8, 8, ranges,
+                                                        nullptr);
 }
 
 }  // namespace fe

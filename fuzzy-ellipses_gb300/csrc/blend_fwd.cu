@@ -74,13 +74,87 @@ struct BlendShape {
 // Initial running max: finite, far below any logit, so logit - max is never inf - inf.
 constexpr float kNoLogit = -1e30f;
 
+// One group of GP record pairs for the thread's PX pixels: evaluate every logit, raise the running
+// maxima once (rescaling W and Z), then accumulate. MASK applies the z > 0 mask to the logits.
+template <int PX, int GP, bool MASK>
+__device__ __forceinline__ void blend_group(const TilePair* grp, const f2_t (&DU)[PX], f2_t DV,
+                                            f2_t DVSQ, f2_t B3, f2_t NB2, f2_t (&A2)[PX],
+                                            f2_t (&W2)[PX], f2_t (&Z2)[PX], float (&m)[PX]) {
+  f2_t ll[GP][PX], zz[GP][PX];
+  float cmax[PX];
+#pragma unroll
+  for (int k = 0; k < PX; ++k) cmax[k] = -INFINITY;
+#pragma unroll
+  for (int q = 0; q < GP; ++q) {
+    const ulonglong2* rp = reinterpret_cast<const ulonglong2*>(grp + q);
+    const ulonglong2 r0 = rp[0], r1 = rp[1], r2 = rp[2], r3 = rp[3], r4 = rp[4];
+    const ulonglong2 r5 = rp[5], r6 = rp[6], r7 = rp[7], r8 = rp[8];
+    // V0..V5 = r0.x r0.y r1.x r1.y r2.x r2.y; P0..P2 = r3.x r3.y r4.x;
+    // N0..N5 = r4.y r5.x r5.y r6.x r6.y r7.x; C = r7.y; cu = r8.x; cv = r8.y.
+    // Row-constant parts first, shared by the thread's PX pixels.
+    const f2_t bv = fma2(r2.y, DVSQ, fma2(r1.x, DV, r0.x));
+    const f2_t cv = fma2(r2.x, DV, r0.y);
+    const f2_t bp = fma2(r4.x, DV, r3.x);
+    const f2_t ev = sub2(DV, r8.y);
+    const f2_t bn = fma2(mul2(r7.x, ev), ev, fma2(r5.y, ev, r4.y));
+    const f2_t cn = fma2(r6.y, ev, r5.x);
+#pragma unroll
+    for (int k = 0; k < PX; ++k) {
+      const f2_t vsv = fma2(fma2(r1.y, DU[k], cv), DU[k], bv);
+      const f2_t psv = fma2(r3.y, DU[k], bp);
+      const f2_t eu = sub2(DU[k], r8.x);
+      const f2_t nq = fma2(fma2(r6.x, eu, cn), eu, bn);
+      float va, vb;
+      f2_unpack(vsv, va, vb);
+      const f2_t qi = f2_pack(rcp_approx(va), rcp_approx(vb));
+      const f2_t z = mul2(psv, qi);
+      const f2_t s2 = fma2(nq, qi, r7.y);
+      float sa, sb;
+      f2_unpack(s2, sa, sb);
+      A2[k] = add2(A2[k], f2_pack(ex2_approx(sa), ex2_approx(sb)));
+      f2_t l = fma2(B3, s2, mul2(NB2, z));
+      float l0, l1;
+      f2_unpack(l, l0, l1);
+      if (MASK) {
+        float z0, z1;
+        f2_unpack(z, z0, z1);
+        l0 = z0 > 0.f ? l0 : -INFINITY;
+        l1 = z1 > 0.f ? l1 : -INFINITY;
+        l = f2_pack(l0, l1);
+      }
+      ll[q][k] = l;
+      zz[q][k] = z;
+      cmax[k] = max3f(cmax[k], l0, l1);
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < PX; ++k) {
+    if (cmax[k] > m[k]) {
+      const float sc = ex2_approx(m[k] - cmax[k]);
+      const f2_t S = f2_pack(sc, sc);
+      W2[k] = mul2(W2[k], S);
+      Z2[k] = mul2(Z2[k], S);
+      m[k] = cmax[k];
+    }
+    const f2_t M = f2_pack(m[k], m[k]);
+#pragma unroll
+    for (int q = 0; q < GP; ++q) {
+      float d0, d1;
+      f2_unpack(sub2(ll[q][k], M), d0, d1);
+      const f2_t e = f2_pack(ex2_approx(d0), ex2_approx(d1));
+      W2[k] = add2(W2[k], e);
+      Z2[k] = fma2(e, zz[q][k], Z2[k]);
+    }
+  }
+}
+
 template <int TW, int TH, int PX, int CH>
 __global__ void __launch_bounds__(BlendShape<TW, TH, PX, CH>::NT,
                                   BlendShape<TW, TH, PX, CH>::MIN_CTAS) blend_fwd_kernel(
-    ViewsArg va, uint32_t n_tiles, const TilePair* __restrict__ trec,
-    const uint2* __restrict__ ranges, float nb2, float beta3, float* __restrict__ depth,
-    float* __restrict__ alpha, float* __restrict__ stats, int64_t stats_stride,
-    Control* __restrict__ ctrl) {
+    ViewsArg va, uint32_t tile_begin, uint32_t tile_end, uint32_t* __restrict__ counter,
+    const TilePair* __restrict__ trec, const uint2* __restrict__ ranges, float nb2, float beta3,
+    float* __restrict__ depth, float* __restrict__ alpha, float* __restrict__ stats,
+    int64_t stats_stride, Control* __restrict__ ctrl) {
   using Sh = BlendShape<TW, TH, PX, CH>;
   constexpr int GP = Sh::GP;
   __shared__ __align__(128) BlendSmem<CH> sm;
@@ -106,10 +180,10 @@ __global__ void __launch_bounds__(BlendShape<TW, TH, PX, CH>::NT,
   uint32_t phase = 0;  // bit s: parity of the next completion to wait for on stage s
 
   while (true) {
-    if (tid == 0) sm.tile = atomicAdd(&ctrl->next_tile, 1u);
+    if (tid == 0) sm.tile = tile_begin + atomicAdd(counter, 1u);
     __syncthreads();
     const uint32_t tile = sm.tile;
-    if (tile >= n_tiles) break;
+    if (tile >= tile_end) break;
     const int vi = find_view<&ViewDev::tile_base>(va, tile);
     const int gx = view_at(va, vi).gx;
     const int lt = (int)(tile - view_at(va, vi).tile_base);
@@ -167,76 +241,18 @@ __global__ void __launch_bounds__(BlendShape<TW, TH, PX, CH>::NT,
           break;
         }
         for (int j = 0; j < padded; j += GP) {
-          float la[GP][PX], lb[GP][PX];
-          f2_t zz[GP][PX];
-          float cmax[PX];
-#pragma unroll
-          for (int k = 0; k < PX; ++k) cmax[k] = -INFINITY;
+          // Uniform over the CTA: the z > 0 mask is only evaluated for groups holding a record
+          // whose psv is not positive over the whole tile (null slots included).
+          bool need_mask = false;
 #pragma unroll
           for (int q = 0; q < GP; ++q) {
-            const ulonglong2* rp = reinterpret_cast<const ulonglong2*>(&sm.buf[stage][j + q]);
-            const ulonglong2 r0 = rp[0], r1 = rp[1], r2 = rp[2], r3 = rp[3], r4 = rp[4];
-            const ulonglong2 r5 = rp[5], r6 = rp[6], r7 = rp[7], r8 = rp[8], r9 = rp[9];
-            // V0..V5 = r0.x r0.y r1.x r1.y r2.x r2.y; P0..P2 = r3.x r3.y r4.x;
-            // N0..N5 = r4.y r5.x r5.y r6.x r6.y r7.x; C = r7.y; cu = r8.x; cv = r8.y;
-            // front = r9.x. Row-constant parts first, shared by the thread's PX pixels.
-            const f2_t bv = fma2(r2.y, DVSQ, fma2(r1.x, DV, r0.x));
-            const f2_t cv = fma2(r2.x, DV, r0.y);
-            const f2_t bp = fma2(r4.x, DV, r3.x);
-            const f2_t ev = sub2(DV, r8.y);
-            const f2_t bn = fma2(mul2(r7.x, ev), ev, fma2(r5.y, ev, r4.y));
-            const f2_t cn = fma2(r6.y, ev, r5.x);
-            float fa, fb;
-            f2_unpack(r9.x, fa, fb);
-            const bool masked = !(fa != 0.f && fb != 0.f);
-#pragma unroll
-            for (int k = 0; k < PX; ++k) {
-              const f2_t vsv = fma2(fma2(r1.y, DU[k], cv), DU[k], bv);
-              const f2_t psv = fma2(r3.y, DU[k], bp);
-              const f2_t eu = sub2(DU[k], r8.x);
-              const f2_t nq = fma2(fma2(r6.x, eu, cn), eu, bn);
-              float va, vb;
-              f2_unpack(vsv, va, vb);
-              const f2_t qi = f2_pack(rcp_approx(va), rcp_approx(vb));
-              const f2_t z = mul2(psv, qi);
-              const f2_t s2 = fma2(nq, qi, r7.y);
-              float sa, sb;
-              f2_unpack(s2, sa, sb);
-              A2[k] = add2(A2[k], f2_pack(ex2_approx(sa), ex2_approx(sb)));
-              const f2_t l = fma2(B3, s2, mul2(NB2, z));
-              float l0, l1;
-              f2_unpack(l, l0, l1);
-              if (masked) {
-                float z0, z1;
-                f2_unpack(z, z0, z1);
-                l0 = z0 > 0.f ? l0 : -INFINITY;
-                l1 = z1 > 0.f ? l1 : -INFINITY;
-              }
-              la[q][k] = l0;
-              lb[q][k] = l1;
-              zz[q][k] = z;
-              cmax[k] = fmaxf(cmax[k], fmaxf(l0, l1));
-            }
+            const float2 fr = sm.buf[stage][j + q].f[18];
+            need_mask |= !(fr.x != 0.f && fr.y != 0.f);
           }
-#pragma unroll
-          for (int k = 0; k < PX; ++k) {
-            if (cmax[k] > m[k]) {
-              const float sc = ex2_approx(m[k] - cmax[k]);
-              const f2_t S = f2_pack(sc, sc);
-              W2[k] = mul2(W2[k], S);
-              Z2[k] = mul2(Z2[k], S);
-              m[k] = cmax[k];
-            }
-            const f2_t M = f2_pack(m[k], m[k]);
-#pragma unroll
-            for (int q = 0; q < GP; ++q) {
-              float d0, d1;
-              f2_unpack(sub2(f2_pack(la[q][k], lb[q][k]), M), d0, d1);
-              const f2_t e = f2_pack(ex2_approx(d0), ex2_approx(d1));
-              W2[k] = add2(W2[k], e);
-              Z2[k] = fma2(e, zz[q][k], Z2[k]);
-            }
-          }
+          if (need_mask)
+            blend_group<PX, GP, true>(&sm.buf[stage][j], DU, DV, DVSQ, B3, NB2, A2, W2, Z2, m);
+          else
+            blend_group<PX, GP, false>(&sm.buf[stage][j], DU, DV, DVSQ, B3, NB2, A2, W2, Z2, m);
         }
         fence_proxy_async_smem();
         __syncthreads();
@@ -272,44 +288,47 @@ __global__ void __launch_bounds__(BlendShape<TW, TH, PX, CH>::NT,
 }
 
 template <int TW, int TH, int PX, int CH>
-void launch_tiles(const ViewsArg& va, int64_t n_tiles, const TilePair* trec, const uint2* ranges,
-                  float nb2, float beta3, float* depth, float* alpha, float* stats,
-                  int64_t stats_stride, Control* ctrl, cudaStream_t st) {
+void launch_tiles(const ViewsArg& va, int64_t tile_begin, int64_t tile_end, uint32_t* counter,
+                  const TilePair* trec, const uint2* ranges, float nb2, float beta3, float* depth,
+                  float* alpha, float* stats, int64_t stats_stride, Control* ctrl,
+                  cudaStream_t st) {
   constexpr int NT = BlendShape<TW, TH, PX, CH>::NT;
   constexpr auto kern = blend_fwd_kernel<TW, TH, PX, CH>;
-  const int64_t grid = std::min<int64_t>(n_tiles, resident_ctas<kern>(NT));
-  kern<<<(unsigned)grid, NT, 0, st>>>(va, (uint32_t)n_tiles, trec, ranges, nb2, beta3, depth,
-                                      alpha, stats, stats_stride, ctrl);
+  const int64_t grid = std::min<int64_t>(tile_end - tile_begin, resident_ctas<kern>(NT));
+  kern<<<(unsigned)grid, NT, 0, st>>>(va, (uint32_t)tile_begin, (uint32_t)tile_end, counter, trec,
+                                      ranges, nb2, beta3, depth, alpha, stats, stats_stride, ctrl);
 }
 
 template <int TW, int TH, int PX>
-void launch_chunk(int chunk, const ViewsArg& va, int64_t n_tiles, const TilePair* trec,
-                  const uint2* ranges, float nb2, float beta3, float* depth, float* alpha,
-                  float* stats, int64_t stats_stride, Control* ctrl, cudaStream_t st) {
+void launch_chunk(int chunk, const ViewsArg& va, int64_t tile_begin, int64_t tile_end,
+                  uint32_t* counter, const TilePair* trec, const uint2* ranges, float nb2,
+                  float beta3, float* depth, float* alpha, float* stats, int64_t stats_stride,
+                  Control* ctrl, cudaStream_t st) {
   if (chunk == 8)
-    launch_tiles<TW, TH, PX, 8>(va, n_tiles, trec, ranges, nb2, beta3, depth, alpha, stats,
-                                stats_stride, ctrl, st);
+    launch_tiles<TW, TH, PX, 8>(va, tile_begin, tile_end, counter, trec, ranges, nb2, beta3, depth,
+                                alpha, stats, stats_stride, ctrl, st);
   else if (chunk == 32)
-    launch_tiles<TW, TH, PX, 32>(va, n_tiles, trec, ranges, nb2, beta3, depth, alpha, stats,
-                                 stats_stride, ctrl, st);
+    launch_tiles<TW, TH, PX, 32>(va, tile_begin, tile_end, counter, trec, ranges, nb2, beta3,
+                                 depth, alpha, stats, stats_stride, ctrl, st);
   else
-    launch_tiles<TW, TH, PX, 16>(va, n_tiles, trec, ranges, nb2, beta3, depth, alpha, stats,
-                                 stats_stride, ctrl, st);
+    launch_tiles<TW, TH, PX, 16>(va, tile_begin, tile_end, counter, trec, ranges, nb2, beta3,
+                                 depth, alpha, stats, stats_stride, ctrl, st);
 }
 
 }  // namespace
 
 // Pixels per thread: px in {1, 2, 4} (8x8 tiles: 1, 2); 0 selects the default for the tile.
 // Chunk: record pairs per shared-memory stage, 8, 16 or 32; 0 selects 16.
-void launch_blend_fwd(const ViewsArg& va, int tile_w, int tile_h, int px, int chunk,
-                      int64_t n_tiles, const TilePair* trec, const uint2* ranges, float beta2,
-                      float beta3, float* depth, float* alpha, float* stats,
-                      int64_t stats_stride, Control* ctrl, cudaStream_t st) {
-  if (n_tiles <= 0) return;
+void launch_blend_fwd_band(const ViewsArg& va, int tile_w, int tile_h, int px, int chunk,
+                           int64_t tile_begin, int64_t tile_end, uint32_t* counter,
+                           const TilePair* trec, const uint2* ranges, float beta2, float beta3,
+                           float* depth, float* alpha, float* stats, int64_t stats_stride,
+                           Control* ctrl, cudaStream_t st) {
+  if (tile_end <= tile_begin) return;
   const float nb2 = -beta2 * kLog2e;
 #define FE_BLEND(TW_, TH_, PX_)                                                                 \
-  launch_chunk<TW_, TH_, PX_>(chunk, va, n_tiles, trec, ranges, nb2, beta3, depth, alpha,     \
-                              stats, stats_stride, ctrl, st)
+  launch_chunk<TW_, TH_, PX_>(chunk, va, tile_begin, tile_end, counter, trec, ranges, nb2, beta3, \
+                              depth, alpha, stats, stats_stride, ctrl, st)
   if (tile_w == 8 && tile_h == 8) {
     if (px == 1) FE_BLEND(8, 8, 1); else FE_BLEND(8, 8, 2);
   } else if (tile_w == 32 && tile_h == 8) {
@@ -318,6 +337,14 @@ void launch_blend_fwd(const ViewsArg& va, int tile_w, int tile_h, int px, int ch
     if (px == 1) FE_BLEND(16, 16, 1); else if (px == 2) FE_BLEND(16, 16, 2); else FE_BLEND(16, 16, 4);
   }
 #undef FE_BLEND
+}
+
+void launch_blend_fwd(const ViewsArg& va, int tile_w, int tile_h, int px, int chunk,
+                      int64_t n_tiles, const TilePair* trec, const uint2* ranges, float beta2,
+                      float beta3, float* depth, float* alpha, float* stats,
+                      int64_t stats_stride, Control* ctrl, cudaStream_t st) {
+  launch_blend_fwd_band(va, tile_w, tile_h, px, chunk, 0, n_tiles, &ctrl->next_tile, trec, ranges,
+                        beta2, beta3, depth, alpha, stats, stats_stride, ctrl, st);
 }
 
 }  // namespace fe

@@ -52,6 +52,13 @@ void launch_blend_fwd(const ViewsArg& va, int tile_w, int tile_h, int px, int ch
                       const TilePair* trec, const uint2* ranges, float beta2, float beta3,
                       float* depth, float* alpha, float* stats, int64_t stats_stride,
                       Control* ctrl, cudaStream_t st);
+// The blend over global tiles [tile_begin, tile_end) only, taking tiles from `counter` (zero at
+// launch); bands with their own counters may run concurrently on different streams.
+void launch_blend_fwd_band(const ViewsArg& va, int tile_w, int tile_h, int px, int chunk,
+                           int64_t tile_begin, int64_t tile_end, uint32_t* counter,
+                           const TilePair* trec, const uint2* ranges, float beta2, float beta3,
+                           float* depth, float* alpha, float* stats, int64_t stats_stride,
+                           Control* ctrl, cudaStream_t st);
 
 // blend_bwd.cu
 void launch_pixel_prep(const ViewsArg& va, int64_t n_pix, const float* depth, const float* stats,

@@ -166,6 +166,7 @@ PROTOTYPES = {
     "fe_batch_pixels": (I64, [P]),
     "fe_batch_scratch_bytes": (I64, [P]),
     "fe_batch_fwd": (ctypes.c_int, [P] + [P] * 6 + [P]),
+    "fe_batch_fwd_host": (ctypes.c_int, [P] + [P] * 5 + [P]),
     "fe_batch_bwd": (ctypes.c_int, [P] + [P] * 11 + [P]),
     "fe_batch_status": (ctypes.c_int, [P, P, ctypes.POINTER(I64), ctypes.POINTER(I64),
                                        ctypes.POINTER(ctypes.c_uint32)]),

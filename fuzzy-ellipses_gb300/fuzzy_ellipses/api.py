@@ -498,6 +498,28 @@ class Batch:
                                  _ptr(alpha), _ptr(stats), _stream()))
         return depth, alpha
 
+    def forward_host(self, means, prec, logw, depth=None, alpha=None):
+        """forward() from host tensors to host tensors (fe_batch_fwd_host): the Gaussians are
+        copied in, the blend runs in bands whose outputs are copied back while the next bands
+        render. Outputs default to new pinned tensors; returns after the copies have landed."""
+        lib = N.load()
+        host = [t.detach().contiguous().float() for t in (means, prec, logw)]
+        for t in host:
+            if t.is_cuda:
+                raise ValueError("forward_host takes host (CPU) tensors")
+        if depth is None:
+            depth = torch.empty(self.n_pixels, dtype=torch.float32).pin_memory()
+        if alpha is None:
+            alpha = torch.empty(self.n_pixels, dtype=torch.float32).pin_memory()
+        for t in (depth, alpha):
+            if t.is_cuda or t.dtype != torch.float32 or not t.is_contiguous() or \
+                    t.numel() < self.n_pixels:
+                raise ValueError("outputs must be contiguous float32 host tensors of n_pixels")
+        N.check(lib.fe_batch_fwd_host(self._h, _ptr(host[0]), _ptr(host[1]), _ptr(host[2]),
+                                      _ptr(depth), _ptr(alpha), _stream()))
+        torch.cuda.current_stream().synchronize()
+        return depth, alpha
+
     def backward(self, means, prec, logw, depth, alpha, stats, gdepth, galpha):
         lib = N.load()
         gm, gp, gw = torch.empty_like(means), torch.empty_like(prec), torch.empty_like(logw)

@@ -125,3 +125,49 @@ def test_backward_reusing_the_forward_binning_equals_recomputing(cuda_device):
     g_keep = keep.backward(m2, p2, w2, depth, alpha, stats, gd, ga)  # last forward was on m, p, w
     for x, y in zip(g_ref, g_keep):
         assert float((x - y).norm()) <= 1e-5 * float(y.norm()) + 1e-12
+
+
+def _host_forward_matches(b, m, p, w, pinned=True):
+    depth, alpha = b.forward(m, p, w)
+    torch.cuda.synchronize()
+    if pinned:
+        hd, ha = b.forward_host(m.cpu(), p.cpu(), w.cpu())
+        assert hd.is_pinned() and ha.is_pinned()
+    else:
+        hd = torch.full((b.n_pixels,), -7.0)
+        ha = torch.full((b.n_pixels,), -7.0)
+        b.forward_host(m.cpu(), p.cpu(), w.cpu(), hd, ha)
+    # The banded blend evaluates every tile exactly as the one-launch blend does.
+    assert torch.equal(hd, depth.cpu()) and torch.equal(ha, alpha.cpu())
+    st = b.status()
+    assert st["device_error"] == 0
+
+
+@pytest.mark.parametrize("pinned", [True, False])
+def test_forward_host_equals_device_forward(cuda_device, pinned):
+    b, items, views, (m, p, w) = make_batch(cuda_device, n_scenes=6, seed=3)
+    _host_forward_matches(b, m, p, w, pinned)
+    _host_forward_matches(b, m, p, w, pinned)  # repeat: counters, streams and events reused
+
+
+def test_forward_host_bands_within_and_across_views(cuda_device):
+    dev = cuda_device
+    scene, cams = S.config1(seed=0)
+    m, p, w = [torch.from_numpy(x).to(dev) for x in (scene.means, scene.prec, scene.logw)]
+    # 16 views of 640x480: several bands, each ending at a view or tile-row boundary.
+    views = [dict(scene=0, height=c.height, width=c.width, fx=c.fx, fy=c.fy, cx=c.cx, cy=c.cy,
+                  quat=c.quat, trans=c.trans) for c in cams]
+    b = fe.Batch([(0, scene.n)], views, tile=(16, 16))
+    _host_forward_matches(b, m, p, w)
+    # One large view (1280x968: the last tile row is partial): bands of tile rows inside it.
+    c = cams[0]
+    big = [dict(scene=0, height=968, width=1280, fx=2 * c.fx, fy=2 * c.fy, cx=640.0, cy=484.0,
+                quat=c.quat, trans=c.trans)]
+    b.reset([(0, scene.n)], big)
+    _host_forward_matches(b, m, p, w)
+    # Views laid out in reverse order in the output: no band spans two views.
+    n_px = [v["height"] * v["width"] for v in views[:5]]
+    offs = np.cumsum([0] + n_px[::-1][:-1])[::-1]
+    rev = [dict(v, pixel_offset=int(o)) for v, o in zip(views[:5], offs)]
+    b2 = fe.Batch([(0, scene.n)], rev, tile=(32, 8))
+    _host_forward_matches(b2, m, p, w)
