@@ -380,9 +380,13 @@ def main():
     passes = (max(1, int(np.ceil(np.log2(batch_tiles(cams, *cfg["tile"]))))) + 7) // 8
     hbm = {
         "preprocess": (52 * scene.n + len(cams) * scene.n * (96 + 8 + 4)) / (stages["preprocess"] * 1e-3) / 1e9,
-        "sort": (16 * nk * passes) / (stages["sort"] * 1e-3) / 1e9,
+        "emit": (8 * nk) / (stages["emit"] * 1e-3) / 1e9,
         "gather": (8 * nk + 64 * nk) / (stages["gather"] * 1e-3) / 1e9,
     }
+    # The tile-major binning writes the keys in order (its "sort" stage is empty); the emit +
+    # radix sort path moves 16 B per key per pass.
+    if stages["sort"] > 1e-3:
+        hbm["sort"] = (16 * nk * passes) / (stages["sort"] * 1e-3) / 1e9
 
     # ---- plain per-call drop-in on device-resident inputs ----------------------------------
     outs = [(torch.empty(H, W, device=dev), torch.empty(H, W, device=dev)) for _ in cams]

@@ -110,6 +110,7 @@ struct RecSpace {
   uint32_t* incl;
   unsigned long long* scan_tmp;
   uint2* ranges;
+  unsigned long long* row_tot;  // tile-major binning: keys per tile row (row slots)
   float4* pix;     // backward only
   RecGrad* rgrad;  // backward only
 };
@@ -131,8 +132,9 @@ size_t carve_rec(char* base, int64_t n_rec, int64_t n_tiles, int64_t n_pix, bool
   s.rects = c.take<TileRect>(n_rec);
   s.touched = c.take<uint32_t>(n_rec);
   s.incl = c.take<uint32_t>(n_rec);
-  s.scan_tmp = c.take<unsigned long long>(scan_grid(n_rec));
+  s.scan_tmp = c.take<unsigned long long>(scan_grid(std::max(n_rec, n_tiles)));
   s.ranges = c.take<uint2>(n_tiles);
+  s.row_tot = c.take<unsigned long long>(n_tiles);
   s.pix = bwd ? c.take<float4>(n_pix) : nullptr;
   s.rgrad = bwd ? c.take<RecGrad>(n_rec) : nullptr;
   out(s);
@@ -213,11 +215,37 @@ struct Pipeline {
   int tile_w, tile_h;
   int px;     // pixels per thread in the blend (0 = default)
   int chunk;  // record pairs per shared-memory stage in the blend (0 = default)
+  bool radix;  // FE_FLAG_RADIX_BINNING: emit + sort even where tile-major binning applies
   int cull_mode;
   float cull_param;
   float beta2, beta3;
   const float *means, *prec, *logw, *quat, *trans;
 };
+
+// Tile-major binning (tile_rows_kernel) filters every view's rectangles once per tile row; it is
+// used when every view is at most kMaxRowTiles tiles wide and that filtering stays small next to
+// the records (the emit + radix sort path otherwise).
+struct RowPlan {
+  bool ok = false;
+  int max_gy = 0;
+  int n_views = 0;
+};
+
+RowPlan row_plan(const ViewDev* views, int n_views) {
+  RowPlan r;
+  r.n_views = n_views;
+  r.ok = n_views >= 1 && n_views <= 65535;
+  int64_t tests = 0, n_rec = 0;
+  for (int i = 0; i < n_views; ++i) {
+    const ViewDev& V = views[i];
+    if (V.gx > kMaxRowTiles || V.gy > 65535) r.ok = false;
+    r.max_gy = std::max(r.max_gy, (int)V.gy);
+    tests += (int64_t)V.gy * V.n;
+    n_rec += V.n;
+  }
+  if (tests > std::max<int64_t>(INT64_C(1) << 24, 64 * n_rec)) r.ok = false;
+  return r;
+}
 
 int run_binning(const Pipeline& p, int64_t worst, DevBuf& recbuf, DevBuf& keybuf,
                 unsigned long long* h_pinned, bool bwd, cudaStream_t st, RecSpace& rs,
@@ -234,11 +262,20 @@ int run_binning(const Pipeline& p, int64_t worst, DevBuf& recbuf, DevBuf& keybuf
   FE_CUDA(cudaMemsetAsync(rs.ranges, 0, sizeof(uint2) * (size_t)p.n_tiles, st));
   launch_preprocess(p.va, p.n_rec, p.means, p.prec, p.logw, p.quat, nullptr, p.trans, p.cull_mode,
                     p.cull_param, p.tile_w, p.tile_h, rs.recs, rs.rects, rs.touched, st);
+  // The single-view pipelines describe their view on the host (va.one).
+  const RowPlan rp = (p.va.table || p.radix) ? RowPlan{} : row_plan(&p.va.one, 1);
   if (exact) {
     cap = worst;
+    if (rp.ok)
+      launch_tile_binning_count(p.va, rp.n_views, rp.max_gy, rs.rects, rs.row_tot, cap, rs.ctrl,
+                                st);
   } else {
-    // Scan with an unbounded capacity first, read the count back, then size the keys.
-    launch_scan(rs.touched, rs.incl, p.n_rec, INT64_C(0xffffffff), rs.scan_tmp, rs.ctrl, st);
+    // Count with an unbounded capacity first, read the count back, then size the keys.
+    if (rp.ok)
+      launch_tile_binning_count(p.va, rp.n_views, rp.max_gy, rs.rects, rs.row_tot,
+                                INT64_C(0xffffffff), rs.ctrl, st);
+    else
+      launch_scan(rs.touched, rs.incl, p.n_rec, INT64_C(0xffffffff), rs.scan_tmp, rs.ctrl, st);
     FE_CUDA(cudaMemcpyAsync(h_pinned, &rs.ctrl->want_keys, sizeof(unsigned long long),
                             cudaMemcpyDeviceToHost, st));
     FE_CUDA(cudaStreamSynchronize(st));
@@ -249,11 +286,19 @@ int run_binning(const Pipeline& p, int64_t worst, DevBuf& recbuf, DevBuf& keybuf
   rc = keybuf.reserve(key_bytes, st);
   if (rc) return rc;
   carve_keys(keybuf.ptr, cap, [&](const KeySpace& s) { ks = s; });
-  if (exact) launch_scan(rs.touched, rs.incl, p.n_rec, cap, rs.scan_tmp, rs.ctrl, st);
-  launch_emit_keys(p.va, rs.incl, rs.rects, p.n_rec, rs.ctrl, ks.keys_a, cap, st);
-  sorted = launch_sort(ks.keys_a, ks.keys_b, bits_for(p.n_tiles), rs.ctrl, cap, ks.hist, st);
-  launch_ranges_gather(p.va, sorted, rs.ctrl, cap, rs.recs, p.tile_w, p.tile_h, rs.ranges,
-                       ks.trec, st);
+  if (exact && !rp.ok) launch_scan(rs.touched, rs.incl, p.n_rec, cap, rs.scan_tmp, rs.ctrl, st);
+  if (rp.ok) {
+    launch_tile_binning_emit(p.va, rp.n_views, rp.max_gy, rs.rects, rs.row_tot, rs.ctrl,
+                             rs.ranges, ks.keys_a, st);
+    sorted = ks.keys_a;
+    launch_ranges_gather(p.va, sorted, rs.ctrl, cap, rs.recs, p.tile_w, p.tile_h, nullptr,
+                         ks.trec, st);
+  } else {
+    launch_emit_keys(p.va, rs.incl, rs.rects, p.n_rec, rs.ctrl, ks.keys_a, cap, st);
+    sorted = launch_sort(ks.keys_a, ks.keys_b, bits_for(p.n_tiles), rs.ctrl, cap, ks.hist, st);
+    launch_ranges_gather(p.va, sorted, rs.ctrl, cap, rs.recs, p.tile_w, p.tile_h, rs.ranges,
+                         ks.trec, st);
+  }
   return FE_OK;
 }
 
@@ -278,6 +323,7 @@ Pipeline single_view_pipeline(const fe_render_desc* d, const float* means, const
   p.tile_h = th;
   p.px = (int)d->px_per_thread;
   p.chunk = (int)(d->flags >> 8) & 0xff;
+  p.radix = (d->flags & FE_FLAG_RADIX_BINNING) != 0;
   p.cull_mode = d->cull_mode;
   p.cull_param = d->cull_param;
   p.beta2 = d->beta2;
@@ -883,6 +929,7 @@ struct fe_batch {
   cudaStream_t s_comp = nullptr, s_copy = nullptr;
   cudaEvent_t ev_bin = nullptr, ev_copy = nullptr;
   std::vector<cudaEvent_t> band_ev;
+  RowPlan rows;  // tile-major binning plan (rows.ok) or the emit + sort path
 };
 
 namespace {
@@ -933,6 +980,7 @@ int plan_batch(fe_batch* b, const fe_scene* scenes, int32_t n_scenes, const fe_v
   b->n_tiles = tiles;
   b->n_pix = pix_end;
   b->worst = worst;
+  b->rows = row_plan(b->views_h.data(), n_views);
   return FE_OK;
 }
 
@@ -954,10 +1002,13 @@ int commit_batch(fe_batch* b, cudaStream_t st) {
                           cudaMemcpyHostToDevice, st));
   FE_CUDA(cudaMemcpyAsync(b->trans_d, b->trans_h.data(), sizeof(float) * b->trans_h.size(),
                           cudaMemcpyHostToDevice, st));
-  const size_t rb = carve_rec(nullptr, b->n_rec, b->n_tiles, b->n_pix, true, [](const RecSpace&) {});
+  // (ranges and row totals: sized for the tiles and for the tile-major binning's row slots)
+  const int64_t tile_slots =
+      std::max<int64_t>(b->n_tiles, (int64_t)b->rows.n_views * b->rows.max_gy);
+  const size_t rb = carve_rec(nullptr, b->n_rec, tile_slots, b->n_pix, true, [](const RecSpace&) {});
   rc = b->rec.reserve(rb, st);
   if (rc) return rc;
-  carve_rec(b->rec.ptr, b->n_rec, b->n_tiles, b->n_pix, true, [&](const RecSpace& s_) { b->rs = s_; });
+  carve_rec(b->rec.ptr, b->n_rec, tile_slots, b->n_pix, true, [&](const RecSpace& s_) { b->rs = s_; });
   if (!b->exact) {
     const int64_t budget_keys = (int64_t)(key_budget_bytes() / kBytesPerKey);
     b->cap = std::max<int64_t>(1, std::min<int64_t>({b->worst, budget_keys, INT64_C(0xffffffff)}));
@@ -1067,6 +1118,7 @@ static Pipeline batch_pipeline(fe_batch* b, const float* means, const float* pre
   p.tile_h = b->tile_h;
   p.px = (int)b->desc.px_per_thread;
   p.chunk = (int)(b->desc.flags >> 8) & 0xff;
+  p.radix = (b->desc.flags & FE_FLAG_RADIX_BINNING) != 0;
   p.cull_mode = b->desc.cull_mode;
   p.cull_param = b->desc.cull_param;
   p.beta2 = b->desc.beta2;
@@ -1085,8 +1137,13 @@ static int batch_binning(fe_batch* b, const Pipeline& p, cudaStream_t st, cudaEv
   launch_preprocess(p.va, p.n_rec, p.means, p.prec, p.logw, p.quat, nullptr, p.trans, p.cull_mode,
                     p.cull_param, p.tile_w, p.tile_h, rs.recs, rs.rects, rs.touched, st);
   if (ev) FE_CUDA(cudaEventRecord(ev[1], st));
+  const RowPlan rp = p.radix ? RowPlan{} : b->rows;
   if (b->exact) {
-    launch_scan(rs.touched, rs.incl, p.n_rec, INT64_C(0xffffffff), rs.scan_tmp, rs.ctrl, st);
+    if (rp.ok)
+      launch_tile_binning_count(p.va, rp.n_views, rp.max_gy, rs.rects, rs.row_tot,
+                                INT64_C(0xffffffff), rs.ctrl, st);
+    else
+      launch_scan(rs.touched, rs.incl, p.n_rec, INT64_C(0xffffffff), rs.scan_tmp, rs.ctrl, st);
     FE_CUDA(cudaMemcpyAsync(b->h_pinned, &rs.ctrl->want_keys, sizeof(unsigned long long),
                             cudaMemcpyDeviceToHost, st));
     FE_CUDA(cudaStreamSynchronize(st));
@@ -1098,17 +1155,30 @@ static int batch_binning(fe_batch* b, const Pipeline& p, cudaStream_t st, cudaEv
       b->cap = K + K / 4;
       carve_keys(b->keys.ptr, b->cap, [&](const KeySpace& s_) { b->ks = s_; });
     }
+  } else if (rp.ok) {
+    launch_tile_binning_count(p.va, rp.n_views, rp.max_gy, rs.rects, rs.row_tot, b->cap, rs.ctrl,
+                              st);
   } else {
     launch_scan(rs.touched, rs.incl, p.n_rec, b->cap, rs.scan_tmp, rs.ctrl, st);
   }
   if (ev) FE_CUDA(cudaEventRecord(ev[2], st));
   const KeySpace& ks = b->ks;
-  launch_emit_keys(p.va, rs.incl, rs.rects, p.n_rec, rs.ctrl, ks.keys_a, b->cap, st);
-  if (ev) FE_CUDA(cudaEventRecord(ev[3], st));
-  b->sorted = launch_sort(ks.keys_a, ks.keys_b, bits_for(p.n_tiles), rs.ctrl, b->cap, ks.hist, st);
-  if (ev) FE_CUDA(cudaEventRecord(ev[4], st));
-  launch_ranges_gather(p.va, b->sorted, rs.ctrl, b->cap, rs.recs, p.tile_w, p.tile_h, rs.ranges,
-                       ks.trec, st);
+  if (rp.ok) {
+    launch_tile_binning_emit(p.va, rp.n_views, rp.max_gy, rs.rects, rs.row_tot, rs.ctrl,
+                             rs.ranges, ks.keys_a, st);
+    if (ev) FE_CUDA(cudaEventRecord(ev[3], st));
+    b->sorted = ks.keys_a;
+    if (ev) FE_CUDA(cudaEventRecord(ev[4], st));
+    launch_ranges_gather(p.va, b->sorted, rs.ctrl, b->cap, rs.recs, p.tile_w, p.tile_h, nullptr,
+                         ks.trec, st);
+  } else {
+    launch_emit_keys(p.va, rs.incl, rs.rects, p.n_rec, rs.ctrl, ks.keys_a, b->cap, st);
+    if (ev) FE_CUDA(cudaEventRecord(ev[3], st));
+    b->sorted = launch_sort(ks.keys_a, ks.keys_b, bits_for(p.n_tiles), rs.ctrl, b->cap, ks.hist, st);
+    if (ev) FE_CUDA(cudaEventRecord(ev[4], st));
+    launch_ranges_gather(p.va, b->sorted, rs.ctrl, b->cap, rs.recs, p.tile_w, p.tile_h, rs.ranges,
+                         ks.trec, st);
+  }
   if (ev) FE_CUDA(cudaEventRecord(ev[5], st));
   return FE_OK;
 }
@@ -1430,12 +1500,22 @@ int fe_render_fwd_noalloc(const fe_render_desc* d, const float* means, const flo
   FE_CUDA(cudaMemsetAsync(rs.ranges, 0, sizeof(uint2) * (size_t)p.n_tiles, st));
   launch_preprocess(p.va, p.n_rec, p.means, p.prec, p.logw, p.quat, nullptr, p.trans, p.cull_mode,
                     p.cull_param, p.tile_w, p.tile_h, rs.recs, rs.rects, rs.touched, st);
-  launch_scan(rs.touched, rs.incl, p.n_rec, worst, rs.scan_tmp, rs.ctrl, st);
-  launch_emit_keys(p.va, rs.incl, rs.rects, p.n_rec, rs.ctrl, ks.keys_a, worst, st);
-  uint64_t* sorted =
-      launch_sort(ks.keys_a, ks.keys_b, bits_for(p.n_tiles), rs.ctrl, worst, ks.hist, st);
-  launch_ranges_gather(p.va, sorted, rs.ctrl, worst, rs.recs, p.tile_w, p.tile_h, rs.ranges,
-                       ks.trec, st);
+  const RowPlan rp = p.radix ? RowPlan{} : row_plan(&p.va.one, 1);
+  if (rp.ok) {
+    launch_tile_binning_count(p.va, rp.n_views, rp.max_gy, rs.rects, rs.row_tot, worst, rs.ctrl,
+                              st);
+    launch_tile_binning_emit(p.va, rp.n_views, rp.max_gy, rs.rects, rs.row_tot, rs.ctrl,
+                             rs.ranges, ks.keys_a, st);
+    launch_ranges_gather(p.va, ks.keys_a, rs.ctrl, worst, rs.recs, p.tile_w, p.tile_h, nullptr,
+                         ks.trec, st);
+  } else {
+    launch_scan(rs.touched, rs.incl, p.n_rec, worst, rs.scan_tmp, rs.ctrl, st);
+    launch_emit_keys(p.va, rs.incl, rs.rects, p.n_rec, rs.ctrl, ks.keys_a, worst, st);
+    uint64_t* sorted =
+        launch_sort(ks.keys_a, ks.keys_b, bits_for(p.n_tiles), rs.ctrl, worst, ks.hist, st);
+    launch_ranges_gather(p.va, sorted, rs.ctrl, worst, rs.recs, p.tile_w, p.tile_h, rs.ranges,
+                         ks.trec, st);
+  }
   launch_blend_fwd(p.va, p.tile_w, p.tile_h, p.px, p.chunk, p.n_tiles, ks.trec, rs.ranges,
                    p.beta2, p.beta3, depth, alpha, stats, npix, rs.ctrl, st);
   if (device_error)

@@ -373,45 +373,49 @@ __device__ __forceinline__ void null_tile_record(TileRec& t) {
   t.front = 1.f;
 }
 
-// Gather block: one sorted key per thread, kGatherThreads / 2 TilePairs per iteration.
-constexpr int kGatherThreads = 256;
-constexpr int kGatherPairs = kGatherThreads / 2;
-constexpr int kGatherParts = (int)(sizeof(GaussRec) / 16);  // 16-byte parts of a GaussRec
+// Gather: each warp takes 32 consecutive sorted keys (16 TilePairs) at a time and works on its
+// own slice of shared memory, so the only barriers are warp barriers.
+constexpr int kGatherWarps = 8;
+constexpr int kGatherThreads = 32 * kGatherWarps;
+constexpr int kGatherParts = (int)(sizeof(GaussRec) / 16);  // 16-byte parts of a GaussRec (6)
 constexpr int kRecWords = 28;  // GaussRec stride in shared memory (96 B + 16 B: conflict-free)
+constexpr int kLoadRecs = 32 / kGatherParts;  // records fetched per cooperative load (5)
 
-struct GatherSmem {
+struct GatherWarpSmem {
   union {
-    float rec[kGatherThreads * kRecWords];  // the block's source records (28 KB)
-    TilePair out[kGatherPairs];             // the block's output pairs (20 KB)
+    float rec[32 * kRecWords];  // the warp's 32 source records (3.5 KB)
+    TilePair out[16];           // the warp's 16 output pairs (2.5 KB)
   } u;
-  int64_t src[kGatherThreads];  // record index of each thread's key, -1 when out of range
 };
 
-// Tile ranges, and every key's tile record, written pair-interleaved. Per iteration a block takes
-// kGatherThreads consecutive keys: the source records are fetched cooperatively (consecutive
-// lanes read consecutive 16-byte parts, so a warp touches ~5 records per load instead of 32),
-// each thread expands its own record, the two records of a pair are interleaved with lane
-// shuffles into conflict-free 16-byte shared stores, and one TMA bulk store writes the block's
-// 20 KB of TilePairs to global memory. trec == nullptr computes the ranges only.
+// Tile ranges, and every key's tile record, written pair-interleaved. Per 32 keys a warp
+//  - reads the keys (coalesced) and writes the range ends found among them,
+//  - fetches the 32 source records cooperatively: in each round lanes 0..29 read the six
+//    16-byte parts of five records, so a load instruction touches 5 records instead of 32,
+//  - expands each lane's record around its tile and stores it into its slot of the pair,
+//  - writes its 16 pairs (2.5 KB) with one TMA bulk store, which runs while the warp goes on.
+// trec == nullptr computes the ranges only.
 __global__ void __launch_bounds__(kGatherThreads, 4) ranges_gather_kernel(
     ViewsArg va, const uint64_t* __restrict__ keys, const Control* __restrict__ ctrl,
     const GaussRec* __restrict__ recs, int tile_w, int tile_h, uint2* __restrict__ ranges,
     TilePair* __restrict__ trec) {
-  __shared__ __align__(128) GatherSmem sm;
+  __shared__ __align__(128) GatherWarpSmem wsm[kGatherWarps];
   const unsigned full = 0xffffffffu;
-  const int tid = threadIdx.x, lane = tid & 31;
-  const bool odd = (tid & 1) != 0;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  GatherWarpSmem& sm = wsm[warp];
+  const int sub = lane / kGatherParts, part = lane - sub * kGatherParts;
   const int64_t K = (int64_t)ctrl->num_keys;
   const int64_t npairs = (K + 1) >> 1;
-  for (int64_t p0 = (int64_t)blockIdx.x * kGatherPairs; p0 < npairs;
-       p0 += (int64_t)gridDim.x * kGatherPairs) {
-    const int64_t k = 2 * p0 + tid;
+  const float hw = 0.5f * (tile_w - 1), hh = 0.5f * (tile_h - 1);
+  for (int64_t p0 = ((int64_t)blockIdx.x * kGatherWarps + warp) * 16; p0 < npairs;
+       p0 += (int64_t)gridDim.x * kGatherWarps * 16) {
+    const int64_t k = 2 * p0 + lane;  // lane 0's key always exists (2 p0 < K)
     const bool valid = k < K;
     const uint64_t key = valid ? keys[k] : 0ull;
     const uint32_t tile = (uint32_t)(key >> 32);
     uint32_t prev = __shfl_up_sync(full, tile, 1);
     uint32_t next = __shfl_down_sync(full, tile, 1);
-    if (valid) {
+    if (valid && ranges != nullptr) {
       if (lane == 0 && k > 0) prev = (uint32_t)(keys[k - 1] >> 32);
       if (lane == 31 && k + 1 < K) next = (uint32_t)(keys[k + 1] >> 32);
       if (k == 0 || prev != tile) ranges[tile].x = (uint32_t)k;
@@ -419,67 +423,309 @@ __global__ void __launch_bounds__(kGatherThreads, 4) ranges_gather_kernel(
     }
     if (trec == nullptr) continue;
 
-    int tx = 0, ty = 0;
-    int64_t src = -1;
-    if (valid) {
-      const int vi = find_view<&ViewDev::tile_base>(va, tile);
-      const ViewDev& V = view_at(va, vi);
-      const int lt = (int)(tile - V.tile_base);
-      tx = lt % V.gx;
-      ty = lt / V.gx;
-      src = V.rec_base + (int64_t)(uint32_t)key;
+    // View of each key: the keys are sorted by tile, so the warp's keys almost always share
+    // lane 0's view; lanes past its last tile search for their own.
+    int v0 = 0;
+    if (lane == 0) v0 = find_view<&ViewDev::tile_base>(va, tile);
+    v0 = __shfl_sync(full, v0, 0);
+    int vi = v0;
+    if (va.table != nullptr && v0 + 1 < va.count && valid &&
+        (int64_t)tile >= va.table[v0 + 1].tile_base)
+      vi = find_view<&ViewDev::tile_base>(va, tile);
+    const ViewDev& V = view_at(va, vi);
+    // Tile row and column: a float estimate of lt / gx, corrected by one step (exact while
+    // lt / gx < 2^22).
+    const int lt = (int)(tile - V.tile_base);
+    int ty = (int)((float)lt * rcp_approx((float)V.gx));
+    int tx = lt - ty * V.gx;
+    if (tx < 0) {
+      --ty;
+      tx += V.gx;
+    } else if (tx >= V.gx) {
+      ++ty;
+      tx -= V.gx;
     }
-    sm.src[tid] = src;
-    if (tid == 0) bulk_wait_group_read0();  // the previous store has read u.out (aliases u.rec)
-    __syncthreads();
+    const int64_t src = valid ? V.rec_base + (int64_t)(uint32_t)key : -1;
+
+    if (lane == 0) bulk_wait_group_read0();  // the previous store has read u.out (aliases u.rec)
+    __syncwarp();
 #pragma unroll
-    for (int e = tid; e < kGatherThreads * kGatherParts; e += kGatherThreads) {
-      const int r = e / kGatherParts, part = e - r * kGatherParts;
-      const int64_t s = sm.src[r];
-      if (s >= 0)
+    for (int it = 0; it < (32 + kLoadRecs - 1) / kLoadRecs; ++it) {
+      const int r = kLoadRecs * it + sub;
+      const int64_t s = __shfl_sync(full, src, r & 31);
+      if (lane < kLoadRecs * kGatherParts && r < 32 && s >= 0)
         *reinterpret_cast<float4*>(&sm.u.rec[r * kRecWords + 4 * part]) =
             reinterpret_cast<const float4*>(recs + s)[part];
     }
-    __syncthreads();
+    __syncwarp();
     GaussRec g;
     if (valid) {
       float4* gd = reinterpret_cast<float4*>(&g);
 #pragma unroll
-      for (int part = 0; part < kGatherParts; ++part)
-        gd[part] = *reinterpret_cast<const float4*>(&sm.u.rec[tid * kRecWords + 4 * part]);
+      for (int q = 0; q < kGatherParts; ++q)
+        gd[q] = *reinterpret_cast<const float4*>(&sm.u.rec[lane * kRecWords + 4 * q]);
     }
-    __syncthreads();  // every record read before u.out (aliased) is written
+    __syncwarp();  // every record read before u.out (aliased) is written
 
     TileRec t;
-    if (valid) {
-      const float hw = 0.5f * (tile_w - 1), hh = 0.5f * (tile_h - 1);
+    if (valid)
       tile_record(g, tx * tile_w + hw - g.uc, ty * tile_h + hh - g.vc, hw, hh, t);
-    } else {
+    else
       null_tile_record(t);
-    }
-    // Even lane: record a (slot 0) of the pair; odd lane: record b (slot 1). Float4 j of the pair
-    // is (a[2j], b[2j], a[2j+1], b[2j+1]); the even lane writes j = 0..4, the odd lane j = 5..9.
+    // Field i of the even lane's record is f[i].x of pair lane/2, of the odd lane's f[i].y.
     const float* mine = reinterpret_cast<const float*>(&t);
-    float other[kRecFields / 2];
+    float* dst = reinterpret_cast<float*>(&sm.u.out[lane >> 1]) + (lane & 1);
 #pragma unroll
-    for (int i = 0; i < kRecFields / 2; ++i)
-      other[i] = __shfl_xor_sync(full, odd ? mine[i] : mine[kRecFields / 2 + i], 1);
-    float4* dst = reinterpret_cast<float4*>(&sm.u.out[tid >> 1]) + (odd ? kRecFields / 4 : 0);
-#pragma unroll
-    for (int m = 0; m < kRecFields / 4; ++m) {
-      const int h = kRecFields / 2 + 2 * m;
-      dst[m] = odd ? make_float4(other[2 * m], mine[h], other[2 * m + 1], mine[h + 1])
-                   : make_float4(mine[2 * m], other[2 * m], mine[2 * m + 1], other[2 * m + 1]);
-    }
+    for (int i = 0; i < kRecFields; ++i) dst[2 * i] = mine[i];
     fence_proxy_async_smem();
-    __syncthreads();
-    if (tid == 0) {
-      const int64_t np = min((int64_t)kGatherPairs, npairs - p0);
+    __syncwarp();
+    if (lane == 0) {
+      const int64_t np = min((int64_t)16, npairs - p0);
       bulk_store_s2g(trec + p0, sm.u.out, (uint32_t)(np * sizeof(TilePair)));
       bulk_commit_group();
     }
   }
-  if (trec != nullptr && tid == 0) bulk_wait_group0();
+  if (trec != nullptr && lane == 0) bulk_wait_group0();
+}
+
+// ---- Tile-major binning ---------------------------------------------------------------------
+// The keys of a tile are its Gaussians in ascending id: the order the stable sort of the
+// Gaussian-major key list produces. Both kernels run one block per (view, tile row):
+//  row_totals_kernel  the row's key count (sum of the widths of the footprint rectangles that
+//                     cover the row); the last block to finish adds the rows up into the run's
+//                     key count (clamped to the capacity, FE_DEVERR_CAPACITY past it)
+//  tile_emit_kernel   the row's base (the totals of the rows before it), per-tile counts from a
+//                     difference array over the covering rectangles, the tile ranges, and the
+//                     keys: the covering rectangles in id order (order-preserving compaction into
+//                     shared memory), a warp per tile walking them 32 at a time, a ballot giving
+//                     each covering rectangle its slot
+// Row slot = view * gridDim.x + row (gridDim.x = the largest row count of the views).
+constexpr int kRowThreads = kScanThreads;  // block_exclusive_scan works on kScanThreads threads
+constexpr int kRowWarps = kRowThreads / 32;
+constexpr int kRowPer = 4;                          // rectangles per thread per filter segment
+constexpr int kRowSeg = kRowThreads * kRowPer;      // rectangles filtered per segment
+constexpr int kTilesPer = kMaxRowTiles / kRowThreads;  // tiles per thread in the row scans
+constexpr int kTileBlock = 8;  // tiles a warp emits at once
+
+struct RowRect {
+  uint16_t x0, x1;
+  uint32_t gid;
+};
+
+__device__ __forceinline__ bool covers_row(const TileRect& r, int row) {
+  return r.y0 <= row && row < r.y1 && r.x0 < r.x1;
+}
+
+// Sum over the block (kRowThreads threads); every thread gets the result.
+__device__ __forceinline__ unsigned long long block_sum_u64(unsigned long long v,
+                                                            unsigned long long* ws) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  __syncthreads();
+  if (lane == 0) ws[warp] = v;
+  __syncthreads();
+  unsigned long long t = 0;
+#pragma unroll
+  for (int w = 0; w < kRowWarps; ++w) t += ws[w];
+  return t;
+}
+
+__global__ void __launch_bounds__(kRowThreads) row_totals_kernel(
+    ViewsArg va, const TileRect* __restrict__ rects, unsigned long long* __restrict__ row_tot,
+    int64_t capacity, Control* __restrict__ ctrl) {
+  __shared__ unsigned long long ws[kRowWarps];
+  __shared__ bool last;
+  const int tid = threadIdx.x;
+  const unsigned slots = gridDim.x * gridDim.y;
+  const unsigned slot = blockIdx.y * gridDim.x + blockIdx.x;
+  const ViewDev& V = view_at(va, blockIdx.y);
+  const int row = blockIdx.x;
+  unsigned long long sum = 0;
+  if (row < V.gy) {
+    if (V.gx > kMaxRowTiles) {  // the host plans this path only for narrower views
+      if (tid == 0) atomicOr(&ctrl->error, FE_DEVERR_CAPACITY);
+    } else {
+      const TileRect* vr = rects + V.rec_base;
+#pragma unroll 4
+      for (int i = tid; i < V.n; i += kRowThreads) {
+        const TileRect r = vr[i];
+        if (covers_row(r, row)) sum += (unsigned)(r.x1 - r.x0);
+      }
+    }
+  }
+  sum = block_sum_u64(sum, ws);
+  if (tid == 0) {
+    row_tot[slot] = sum;
+    __threadfence();
+    last = atomicAdd(&ctrl->rows_done, 1u) == slots - 1;
+  }
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  unsigned long long tot = 0;
+  for (unsigned s = tid; s < slots; s += kRowThreads) tot += __ldcg(&row_tot[s]);
+  tot = block_sum_u64(tot, ws);
+  if (tid == 0) {
+    const unsigned long long cap = (unsigned long long)capacity;
+    ctrl->want_keys = tot;
+    ctrl->num_keys = tot < cap ? tot : cap;
+    if (tot > cap) atomicOr(&ctrl->error, FE_DEVERR_CAPACITY);
+  }
+}
+
+// Order-preserving compaction of the segment's rectangles that cover `row` into `list`
+// (thread t takes rectangles s0 + kRowPer t .. + kRowPer - 1); returns their number. Ends with a
+// barrier after the list is written.
+__device__ __forceinline__ uint32_t filter_row(const TileRect* __restrict__ vr, int n, int s0,
+                                               int row, RowRect* list, uint32_t* ws) {
+  const int tid = threadIdx.x;
+  TileRect r[kRowPer];
+  uint32_t hits = 0, c = 0;
+#pragma unroll
+  for (int q = 0; q < kRowPer; ++q) {
+    const int i = s0 + kRowPer * tid + q;
+    r[q] = i < n ? vr[i] : TileRect{0, 0, 0, 0};
+    const bool h = covers_row(r[q], row);
+    hits |= (uint32_t)h << q;
+    c += h;
+  }
+  uint32_t at;
+  const uint32_t total = block_exclusive_scan<uint32_t>(c, at, ws);  // ends with a barrier
+#pragma unroll
+  for (int q = 0; q < kRowPer; ++q)
+    if ((hits >> q) & 1u)
+      list[at++] = RowRect{r[q].x0, r[q].x1, (uint32_t)(s0 + kRowPer * tid + q)};
+  __syncthreads();
+  return total;
+}
+
+__global__ void __launch_bounds__(kRowThreads) tile_emit_kernel(
+    ViewsArg va, const TileRect* __restrict__ rects,
+    const unsigned long long* __restrict__ row_tot, const Control* __restrict__ ctrl,
+    uint2* __restrict__ ranges, uint64_t* __restrict__ keys) {
+  __shared__ RowRect list[kRowSeg];
+  __shared__ int diff[kMaxRowTiles + 1];         // +1 at x0, -1 at x1 of every covering rectangle
+  __shared__ uint32_t pos[kMaxRowTiles];  // per tile: next key slot within the row
+  __shared__ unsigned long long wsu[kRowWarps];
+  __shared__ uint32_t ws[kRowWarps];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const unsigned full = 0xffffffffu;
+  const uint32_t lt_mask = (1u << lane) - 1u;
+  const unsigned slot = blockIdx.y * gridDim.x + blockIdx.x;
+  const ViewDev& V = view_at(va, blockIdx.y);
+  const int row = blockIdx.x;
+  if (row >= V.gy || V.gx > kMaxRowTiles) return;  // (uniform over the block)
+  const int gx = V.gx, n = V.n;
+  const int64_t tile0 = V.tile_base + (int64_t)row * gx;
+  const TileRect* vr = rects + V.rec_base;
+  const unsigned long long K = ctrl->num_keys;
+
+  unsigned long long b = 0;
+  for (unsigned s = tid; s < slot; s += kRowThreads) b += row_tot[s];
+  const unsigned long long row_base = block_sum_u64(b, wsu);
+  // Keys of this row: slot p (relative to the row's base) for p < lim.
+  uint64_t* row_keys = keys + row_base;
+  const unsigned long long left = K > row_base ? K - row_base : 0ull;
+  const uint32_t lim = left < 0xffffffffull ? (uint32_t)left : 0xffffffffu;
+  for (int x = tid; x <= gx; x += kRowThreads) diff[x] = 0;
+  __syncthreads();
+  uint32_t total = 0;
+  for (int s0 = 0; s0 < n; s0 += kRowSeg) {
+    total = filter_row(vr, n, s0, row, list, ws);
+    for (uint32_t j = tid; j < total; j += kRowThreads) {
+      atomicAdd(&diff[list[j].x0], 1);
+      atomicAdd(&diff[list[j].x1], -1);
+    }
+    __syncthreads();
+  }
+  // Tile counts (prefix of the difference array) and their exclusive prefix, kTilesPer
+  // consecutive tiles per thread.
+  int cnt[kTilesPer];
+  uint32_t dsum = 0;
+#pragma unroll
+  for (int q = 0; q < kTilesPer; ++q) {
+    const int x = kTilesPer * tid + q;
+    cnt[q] = x < gx ? diff[x] : 0;
+    dsum += (uint32_t)cnt[q];
+  }
+  uint32_t dex;
+  block_exclusive_scan<uint32_t>(dsum, dex, ws);
+  unsigned long long csum = 0;
+  {
+    int run = (int)dex;
+#pragma unroll
+    for (int q = 0; q < kTilesPer; ++q) {
+      run += cnt[q];
+      cnt[q] = run;
+      csum += (unsigned)run;
+    }
+  }
+  unsigned long long cex;
+  {
+    // Exclusive scan of the per-thread count sums (64-bit: a row can hold more than 2^32 keys).
+    unsigned long long x = csum;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const unsigned long long y = __shfl_up_sync(full, x, o);
+      if (lane >= o) x += y;
+    }
+    __syncthreads();
+    if (lane == 31) wsu[warp] = x;
+    __syncthreads();
+    unsigned long long before = 0;
+    for (int w = 0; w < warp; ++w) before += wsu[w];
+    cex = before + x - csum;
+  }
+#pragma unroll
+  for (int q = 0; q < kTilesPer; ++q) {
+    const int x = kTilesPer * tid + q;
+    if (x < gx) {
+      pos[x] = cex < lim ? (uint32_t)cex : lim;  // (slots from lim on are dropped)
+      const unsigned long long lo = min(row_base + cex, K);
+      const unsigned long long hi = min(row_base + cex + (unsigned)cnt[q], K);
+      if (hi > lo) ranges[tile0 + x] = make_uint2((uint32_t)lo, (uint32_t)hi);
+      cex += (unsigned)cnt[q];
+    }
+  }
+  __syncthreads();
+  for (int s0 = 0; s0 < n; s0 += kRowSeg) {
+    if (n > kRowSeg) total = filter_row(vr, n, s0, row, list, ws);  // else still in shared memory
+    // Each warp takes kTileBlock of its tiles at a time (tiles warp + kRowWarps t), keeping their
+    // next slots in registers, and reads each 32-entry chunk of the list once for all of them.
+    for (int xb = warp; xb < gx; xb += kRowWarps * kTileBlock) {
+      uint32_t p[kTileBlock];
+#pragma unroll
+      for (int t = 0; t < kTileBlock; ++t) {
+        const int x = xb + kRowWarps * t;
+        p[t] = x < gx ? (uint32_t)pos[x] : 0u;
+      }
+      for (uint32_t j0 = 0; j0 < total; j0 += 32) {
+        const uint32_t j = j0 + lane;
+        RowRect e{0, 0, 0};
+        if (j < total) e = list[j];
+#pragma unroll
+        for (int t = 0; t < kTileBlock; ++t) {
+          const int x = xb + kRowWarps * t;  // (x >= gx: no rectangle reaches it)
+          const bool cov = e.x0 <= x && x < e.x1;
+          const uint32_t bal = __ballot_sync(full, cov);
+          if (cov) {
+            const uint32_t k = p[t] + __popc(bal & lt_mask);
+            if (k < lim) row_keys[k] = ((uint64_t)(tile0 + x) << 32) | e.gid;
+          }
+          p[t] += __popc(bal);
+        }
+      }
+      if (lane == 0) {
+#pragma unroll
+        for (int t = 0; t < kTileBlock; ++t) {
+          const int x = xb + kRowWarps * t;
+          if (x < gx) pos[x] = p[t];
+        }
+      }
+    }
+    __syncthreads();  // the list is rewritten by the next segment
+  }
 }
 
 inline int grid_for(int64_t work, int threads, int cap) {
@@ -530,16 +776,32 @@ uint64_t* launch_sort(uint64_t* a, uint64_t* b, int key_bits, const Control* ctr
 void launch_ranges_gather(const ViewsArg& va, const uint64_t* keys, const Control* ctrl,
                           int64_t capacity, const GaussRec* recs, int tile_w, int tile_h,
                           uint2* ranges, TilePair* trec, cudaStream_t st) {
-  const int grid = grid_for((capacity + 1) / 2, kGatherPairs,
+  const int grid = grid_for((capacity + 1) / 2, 16 * kGatherWarps,
                             resident_ctas<ranges_gather_kernel>(kGatherThreads));
   ranges_gather_kernel<<<grid, kGatherThreads, 0, st>>>(va, keys, ctrl, recs, tile_w, tile_h,
                                                         ranges, trec);
 }
 
+void launch_tile_binning_count(const ViewsArg& va, int n_views, int max_gy,
+                               const TileRect* rects, unsigned long long* row_tot,
+                               int64_t capacity, Control* ctrl, cudaStream_t st) {
+  if (n_views <= 0 || max_gy <= 0) return;
+  row_totals_kernel<<<dim3((unsigned)max_gy, (unsigned)n_views), kRowThreads, 0, st>>>(
+      va, rects, row_tot, capacity, ctrl);
+}
+
+void launch_tile_binning_emit(const ViewsArg& va, int n_views, int max_gy, const TileRect* rects,
+                              const unsigned long long* row_tot, const Control* ctrl,
+                              uint2* ranges, uint64_t* keys, cudaStream_t st) {
+  if (n_views <= 0 || max_gy <= 0) return;
+  tile_emit_kernel<<<dim3((unsigned)max_gy, (unsigned)n_views), kRowThreads, 0, st>>>(
+      va, rects, row_tot, ctrl, ranges, keys);
+}
+
 void launch_ranges(const uint64_t* keys, const Control* ctrl, int64_t capacity, uint2* ranges,
                    cudaStream_t st) {
   ViewsArg va{};
-  const int grid = grid_for((capacity + 1) / 2, kGatherPairs,
+  const int grid = grid_for((capacity + 1) / 2, 16 * kGatherWarps,
                             resident_ctas<ranges_gather_kernel>(kGatherThreads));
   ranges_gather_kernel<<<grid, kGatherThreads, 0, st>>>(va, keys, ctrl, nullptr, 8, 8, ranges,
                                                         nullptr);

@@ -110,7 +110,8 @@ struct Control {
   unsigned long long want_keys; // keys the run needed
   uint32_t error;               // FE_DEVERR_* bits
   uint32_t next_tile;           // work counter of the persistent blend
-  uint32_t pad[10];
+  uint32_t rows_done;           // tile-major binning: row-total blocks finished
+  uint32_t pad[9];
 };
 
 // View lookup: the plain single-render path passes its one view by value (so it needs no

@@ -36,11 +36,24 @@ void launch_emit_keys(const ViewsArg& va, const uint32_t* incl, const TileRect* 
 // result (a or b). hist: 256 * (sort_grid(capacity) + 1) uint32.
 uint64_t* launch_sort(uint64_t* a, uint64_t* b, int key_bits, const Control* ctrl,
                       int64_t capacity, uint32_t* hist, cudaStream_t st);
-// Tile ranges (ranges must be zeroed beforehand) and the tile-local record stream, key k at
-// trec[k/2] slot k%2 (capacity/2 rounded up pairs).
+// Tile ranges (ranges must be zeroed beforehand; NULL skips them) and the tile-local record
+// stream, key k at trec[k/2] slot k%2 (capacity/2 rounded up pairs).
 void launch_ranges_gather(const ViewsArg& va, const uint64_t* keys, const Control* ctrl,
                           int64_t capacity, const GaussRec* recs, int tile_w, int tile_h,
                           uint2* ranges, TilePair* trec, cudaStream_t st);
+// Tile-major binning for views at most kMaxRowTiles tiles wide (grids: one block per tile row
+// of every view; row_tot: n_views * max_gy entries). The count pass writes every row's key count
+// and the run's key count (clamped to capacity, as launch_scan does); the emit pass writes the
+// keys of every tile in ascending Gaussian id at their place in the sorted order (keys past
+// ctrl->num_keys dropped) and the non-empty tile ranges (ranges zeroed beforehand). Same keys and
+// ranges as emit + stable sort + ranges. ctrl->rows_done must be zero before the count pass.
+constexpr int kMaxRowTiles = 1024;
+void launch_tile_binning_count(const ViewsArg& va, int n_views, int max_gy,
+                               const TileRect* rects, unsigned long long* row_tot,
+                               int64_t capacity, Control* ctrl, cudaStream_t st);
+void launch_tile_binning_emit(const ViewsArg& va, int n_views, int max_gy, const TileRect* rects,
+                              const unsigned long long* row_tot, const Control* ctrl,
+                              uint2* ranges, uint64_t* keys, cudaStream_t st);
 // Ranges only (reference-compatible binning).
 void launch_ranges(const uint64_t* keys, const Control* ctrl, int64_t capacity, uint2* ranges,
                    cudaStream_t st);

@@ -23,6 +23,7 @@ FE_DEVERR_CAPACITY = 1
 FE_DEVERR_TIMEOUT = 2
 FE_FLAG_EXACT_KEYS = 2
 FE_FLAG_KEEP_BINNING = 4
+FE_FLAG_RADIX_BINNING = 8
 FE_VIEW_NO_GRAD = 1
 FE_ERR_OUT_OF_MEMORY = 4
 

@@ -110,14 +110,15 @@ def render(means, prec, logw, fx, fy, cx, cy, quat, t, height, width, beta2=21.4
 
 def render_forward(means, prec, logw, fx, fy, cx, cy, quat, t, height, width, beta2=21.4,
                    beta3=2.66, *, cull="eps", cull_param=None, tile=(16, 16), out=None,
-                   stats=None):
+                   stats=None, binning="tiles"):
     """Non-differentiable forward into optional preallocated ``out=(depth, alpha)``."""
     lib = N.load()
     n = _check_inputs(means, prec, logw)
     dev = means.device
     q = _as_dev(quat, dev, (4,))
     tt = _as_dev(t, dev, (3,))
-    desc = N.make_desc(n, height, width, fx, fy, cx, cy, beta2, beta3, cull, cull_param, tile)
+    desc = N.make_desc(n, height, width, fx, fy, cx, cy, beta2, beta3, cull, cull_param, tile,
+                       flags=_binning_flag(binning))
     if out is None:
         out = (torch.empty((height, width), device=dev), torch.empty((height, width), device=dev))
     N.check(lib.fe_render_fwd(ctypes.byref(desc), _ptr(means), _ptr(prec), _ptr(logw), _ptr(q),
@@ -151,16 +152,24 @@ def render_features(means, prec, logw, features, fx, fy, cx, cy, quat, t, height
     return depth, alpha, out
 
 
+def _binning_flag(binning):
+    if binning not in ("tiles", "radix"):
+        raise ValueError("binning must be 'tiles' or 'radix'")
+    return N.FE_FLAG_RADIX_BINNING if binning == "radix" else 0
+
+
 def render_binning(means, prec, logw, fx, fy, cx, cy, quat, t, height, width, *, cull="eps",
-                   cull_param=None, tile=(16, 16), key_capacity=None):
+                   cull_param=None, tile=(16, 16), key_capacity=None, binning="tiles"):
     """The tile binning ``render`` uses: returns (keys (K,) int64 holding (tile << 32 | gaussian),
-    ranges (T, 2) int64). Synchronises once."""
+    ranges (T, 2) int64). Synchronises once. ``binning="radix"`` forces key emission + radix sort
+    instead of the tile-major binning (same result)."""
     lib = N.load()
     n = _check_inputs(means, prec, logw)
     dev = means.device
     q = _as_dev(quat, dev, (4,))
     tt = _as_dev(t, dev, (3,))
-    desc = N.make_desc(n, height, width, fx, fy, cx, cy, 21.4, 2.66, cull, cull_param, tile)
+    desc = N.make_desc(n, height, width, fx, fy, cx, cy, 21.4, 2.66, cull, cull_param, tile,
+                       flags=_binning_flag(binning))
     gx = (width + tile[0] - 1) // tile[0]
     gy = (height + tile[1] - 1) // tile[1]
     cap = int(key_capacity) if key_capacity is not None else max(1, n * gx * gy)
@@ -411,10 +420,11 @@ class Batch:
     """
 
     def __init__(self, scenes, views, beta2=21.4, beta3=2.66, *, cull="eps", cull_param=None,
-                 tile=(16, 16), px=0, chunk=0, exact_keys=False, keep_binning=False):
+                 tile=(16, 16), px=0, chunk=0, exact_keys=False, keep_binning=False,
+                 binning="tiles"):
         lib = N.load()
         flags = (N.flag_chunk(chunk) | (N.FE_FLAG_EXACT_KEYS if exact_keys else 0)
-                 | (N.FE_FLAG_KEEP_BINNING if keep_binning else 0))
+                 | (N.FE_FLAG_KEEP_BINNING if keep_binning else 0) | _binning_flag(binning))
         desc = N.make_desc(0, 1, 1, 1.0, 1.0, 0.0, 0.0, beta2, beta3, cull, cull_param, tile,
                            flags=flags, px=px)
         sc, nsc, vs, nvs = self._tables(scenes, views)

@@ -70,6 +70,9 @@ typedef enum fe_cull_mode {
  * instead of recomputing it. The caller guarantees that the Gaussian data did not change between
  * the two calls. */
 #define FE_FLAG_KEEP_BINNING 4u
+/* Bin with key emission + radix sort even where the tile-major binning applies (both give the
+ * same keys and ranges; the flag exists to compare them). */
+#define FE_FLAG_RADIX_BINNING 8u
 
 /* Render descriptor: everything a render needs besides the Gaussian and pose buffers. It is also
  * the opaque payload of the XLA custom call targets (bit-copied; the size and magic are checked).
