@@ -247,9 +247,11 @@ RowPlan row_plan(const ViewDev* views, int n_views) {
   return r;
 }
 
+// need_trec: also build the gathered tile-record stream (the backward and the feature pass read
+// it; the forward blend builds its records itself).
 int run_binning(const Pipeline& p, int64_t worst, DevBuf& recbuf, DevBuf& keybuf,
-                unsigned long long* h_pinned, bool bwd, cudaStream_t st, RecSpace& rs,
-                KeySpace& ks, int64_t& cap, uint64_t*& sorted) {
+                unsigned long long* h_pinned, bool bwd, bool need_trec, cudaStream_t st,
+                RecSpace& rs, KeySpace& ks, int64_t& cap, uint64_t*& sorted) {
   size_t rec_bytes = carve_rec(nullptr, p.n_rec, p.n_tiles, p.n_pix, bwd, [](const RecSpace&) {});
   int rc = recbuf.reserve(rec_bytes, st);
   if (rc) return rc;
@@ -291,13 +293,14 @@ int run_binning(const Pipeline& p, int64_t worst, DevBuf& recbuf, DevBuf& keybuf
     launch_tile_binning_emit(p.va, rp.n_views, rp.max_gy, rs.rects, rs.row_tot, rs.ctrl,
                              rs.ranges, ks.keys_a, st);
     sorted = ks.keys_a;
-    launch_ranges_gather(p.va, sorted, rs.ctrl, cap, rs.recs, p.tile_w, p.tile_h, nullptr,
-                         ks.trec, st);
+    if (need_trec)
+      launch_ranges_gather(p.va, sorted, rs.ctrl, cap, rs.recs, p.tile_w, p.tile_h, nullptr,
+                           ks.trec, st);
   } else {
     launch_emit_keys(p.va, rs.incl, rs.rects, p.n_rec, rs.ctrl, ks.keys_a, cap, st);
     sorted = launch_sort(ks.keys_a, ks.keys_b, bits_for(p.n_tiles), rs.ctrl, cap, ks.hist, st);
     launch_ranges_gather(p.va, sorted, rs.ctrl, cap, rs.recs, p.tile_w, p.tile_h, rs.ranges,
-                         ks.trec, st);
+                         need_trec ? ks.trec : nullptr, st);
   }
   return FE_OK;
 }
@@ -403,10 +406,10 @@ int fe_render_fwd(const fe_render_desc* d, const float* means, const float* prec
   KeySpace ks;
   int64_t cap = 0;
   uint64_t* sorted = nullptr;
-  rc = run_binning(p, p.n_rec * p.n_tiles, a->rec, a->keys, a->h_pinned, false, st, rs, ks, cap,
+  rc = run_binning(p, p.n_rec * p.n_tiles, a->rec, a->keys, a->h_pinned, false, false, st, rs, ks, cap,
                    sorted);
   if (rc) return rc;
-  launch_blend_fwd(p.va, p.tile_w, p.tile_h, p.px, p.chunk, p.n_tiles, ks.trec, rs.ranges, p.beta2, p.beta3,
+  launch_blend_fwd(p.va, p.tile_w, p.tile_h, p.px, p.chunk, p.n_tiles, sorted, rs.recs, rs.ranges, p.beta2, p.beta3,
                    depth, alpha, stats, npix, rs.ctrl, st);
   FE_CUDA(cudaGetLastError());
   return FE_OK;
@@ -437,7 +440,7 @@ int fe_render_bwd(const fe_render_desc* d, const float* means, const float* prec
   KeySpace ks;
   int64_t cap = 0;
   uint64_t* sorted = nullptr;
-  rc = run_binning(p, p.n_rec * p.n_tiles, a->rec, a->keys, a->h_pinned, true, st, rs, ks, cap,
+  rc = run_binning(p, p.n_rec * p.n_tiles, a->rec, a->keys, a->h_pinned, true, true, st, rs, ks, cap,
                    sorted);
   if (rc) return rc;
   FE_CUDA(cudaMemsetAsync(rs.rgrad, 0, sizeof(RecGrad) * (size_t)p.n_rec, st));
@@ -474,7 +477,7 @@ int fe_render_features(const fe_render_desc* d, const float* means, const float*
   KeySpace ks;
   int64_t cap = 0;
   uint64_t* sorted = nullptr;
-  rc = run_binning(p, p.n_rec * p.n_tiles, a->rec, a->keys, a->h_pinned, false, st, rs, ks, cap,
+  rc = run_binning(p, p.n_rec * p.n_tiles, a->rec, a->keys, a->h_pinned, false, true, st, rs, ks, cap,
                    sorted);
   if (rc) return rc;
   launch_features(p.va, p.tile_w, p.tile_h, p.n_tiles, sorted, rs.ranges, ks.trec, stats, npix,
@@ -504,7 +507,7 @@ int fe_render_binning(const fe_render_desc* d, const float* means, const float* 
   KeySpace ks;
   int64_t cap = 0;
   uint64_t* sorted = nullptr;
-  rc = run_binning(p, p.n_rec * p.n_tiles, a->rec, a->keys, a->h_pinned, false, st, rs, ks, cap,
+  rc = run_binning(p, p.n_rec * p.n_tiles, a->rec, a->keys, a->h_pinned, false, false, st, rs, ks, cap,
                    sorted);
   if (rc) return rc;
   FE_CUDA(cudaMemcpyAsync(a->h_pinned, &rs.ctrl->num_keys, sizeof(unsigned long long),
@@ -832,8 +835,8 @@ int fe_rasterize_legacy(const fe_legacy_desc* d, const float* means, const float
   carve_keys(a->keys.ptr, cap, [&](const KeySpace& s_) { ks = s_; });
   launch_emit_keys(va, rs.incl, rs.rects, P, rs.ctrl, ks.keys_a, cap, st);
   uint64_t* sorted = launch_sort(ks.keys_a, ks.keys_b, bits_for(T), rs.ctrl, cap, ks.hist, st);
-  launch_ranges_gather(va, sorted, rs.ctrl, cap, rs.recs, 8, 8, rs.ranges, ks.trec, st);
-  launch_blend_fwd(va, 8, 8, 0, 0, T, ks.trec, rs.ranges, 21.4f, 2.66f, out_z, out_alpha, nullptr, 0,
+  launch_ranges_gather(va, sorted, rs.ctrl, cap, rs.recs, 8, 8, rs.ranges, nullptr, st);
+  launch_blend_fwd(va, 8, 8, 0, 0, T, sorted, rs.recs, rs.ranges, 21.4f, 2.66f, out_z, out_alpha, nullptr, 0,
                    rs.ctrl, st);
   FE_CUDA(cudaGetLastError());
   return FE_OK;
@@ -930,6 +933,7 @@ struct fe_batch {
   cudaEvent_t ev_bin = nullptr, ev_copy = nullptr;
   std::vector<cudaEvent_t> band_ev;
   RowPlan rows;  // tile-major binning plan (rows.ok) or the emit + sort path
+  bool trec_ready = false;  // the binning's gathered tile records are built (the backward's input)
 };
 
 namespace {
@@ -1129,7 +1133,10 @@ static Pipeline batch_pipeline(fe_batch* b, const float* means, const float* pre
 
 // Binning of a batch. With exact key sizing the key count is read back after the scan (one
 // 8-byte copy and a stream synchronisation) and the key scratch grows to fit it.
-static int batch_binning(fe_batch* b, const Pipeline& p, cudaStream_t st, cudaEvent_t* ev) {
+// need_trec: also build the gathered tile-record stream (the backward reads it; the forward blend
+// builds its records itself).
+static int batch_binning(fe_batch* b, const Pipeline& p, bool need_trec, cudaStream_t st,
+                         cudaEvent_t* ev) {
   const RecSpace& rs = b->rs;
   FE_CUDA(cudaMemsetAsync(rs.ctrl, 0, sizeof(Control), st));
   FE_CUDA(cudaMemsetAsync(rs.ranges, 0, sizeof(uint2) * (size_t)p.n_tiles, st));
@@ -1169,16 +1176,18 @@ static int batch_binning(fe_batch* b, const Pipeline& p, cudaStream_t st, cudaEv
     if (ev) FE_CUDA(cudaEventRecord(ev[3], st));
     b->sorted = ks.keys_a;
     if (ev) FE_CUDA(cudaEventRecord(ev[4], st));
-    launch_ranges_gather(p.va, b->sorted, rs.ctrl, b->cap, rs.recs, p.tile_w, p.tile_h, nullptr,
-                         ks.trec, st);
+    if (need_trec)
+      launch_ranges_gather(p.va, b->sorted, rs.ctrl, b->cap, rs.recs, p.tile_w, p.tile_h, nullptr,
+                           ks.trec, st);
   } else {
     launch_emit_keys(p.va, rs.incl, rs.rects, p.n_rec, rs.ctrl, ks.keys_a, b->cap, st);
     if (ev) FE_CUDA(cudaEventRecord(ev[3], st));
     b->sorted = launch_sort(ks.keys_a, ks.keys_b, bits_for(p.n_tiles), rs.ctrl, b->cap, ks.hist, st);
     if (ev) FE_CUDA(cudaEventRecord(ev[4], st));
     launch_ranges_gather(p.va, b->sorted, rs.ctrl, b->cap, rs.recs, p.tile_w, p.tile_h, rs.ranges,
-                         ks.trec, st);
+                         need_trec ? ks.trec : nullptr, st);
   }
+  b->trec_ready = need_trec;
   if (ev) FE_CUDA(cudaEventRecord(ev[5], st));
   return FE_OK;
 }
@@ -1225,11 +1234,11 @@ int fe_batch_fwd(fe_batch* b, const float* means, const float* prec, const float
   if (p.n_rec > 0 && (!means || !prec || !logw))
     return fail(FE_ERR_INVALID_ARGUMENT, "NULL Gaussian pointer");
   b->binned = false;
-  int rc = batch_binning(b, p, st, nullptr);
+  int rc = batch_binning(b, p, false, st, nullptr);
   if (rc) return rc;
   note_binning(b, means, prec, logw);
-  launch_blend_fwd(p.va, p.tile_w, p.tile_h, p.px, p.chunk, p.n_tiles, b->ks.trec, b->rs.ranges,
-                   p.beta2, p.beta3, depth, alpha, stats, p.n_pix, b->rs.ctrl, st);
+  launch_blend_fwd(p.va, p.tile_w, p.tile_h, p.px, p.chunk, p.n_tiles, b->sorted, b->rs.recs,
+                   b->rs.ranges, p.beta2, p.beta3, depth, alpha, stats, p.n_pix, b->rs.ctrl, st);
   FE_CUDA(cudaGetLastError());
   return FE_OK;
 }
@@ -1275,7 +1284,7 @@ int fe_batch_fwd_host(fe_batch* b, const float* h_means, const float* h_prec,
   }
   Pipeline p = batch_pipeline(b, m_d, p_d, w_d);
   b->binned = false;
-  rc = batch_binning(b, p, st, nullptr);
+  rc = batch_binning(b, p, false, st, nullptr);
   if (rc) return rc;
   note_binning(b, m_d, p_d, w_d);
   FE_CUDA(cudaMemsetAsync(ctr, 0, sizeof(uint32_t) * nb, st));
@@ -1287,8 +1296,8 @@ int fe_batch_fwd_host(fe_batch* b, const float* h_means, const float* h_prec,
     const fe_batch::HostBand& hb = b->bands[j];
     cudaStream_t sj = (j & 1) ? b->s_comp : st;
     launch_blend_fwd_band(p.va, p.tile_w, p.tile_h, p.px, p.chunk, hb.t0, hb.t1, ctr + j,
-                          b->ks.trec, b->rs.ranges, p.beta2, p.beta3, dep_d, alp_d, nullptr,
-                          p.n_pix, b->rs.ctrl, sj);
+                          b->sorted, b->rs.recs, b->rs.ranges, p.beta2, p.beta3, dep_d, alp_d,
+                          nullptr, p.n_pix, sj);
     FE_CUDA(cudaGetLastError());
     FE_CUDA(cudaEventRecord(b->band_ev[j], sj));
   }
@@ -1320,11 +1329,17 @@ int fe_batch_bwd(fe_batch* b, const float* means, const float* prec, const float
   FE_CUDA(cudaMemsetAsync(glogw, 0, sizeof(float) * (size_t)b->n_gauss, st));
   if (b->keep_binning && b->binned && b->binned_for[0] == means && b->binned_for[1] == prec &&
       b->binned_for[2] == logw) {
-    // Reuse the forward's binning; only the blend's tile counter must start again at zero.
+    // Reuse the forward's binning; only the blend's tile counter must start again at zero, and
+    // the gathered tile records are built now if the forward did not need them.
     FE_CUDA(cudaMemsetAsync(&b->rs.ctrl->next_tile, 0, sizeof(uint32_t), st));
+    if (!b->trec_ready) {
+      launch_ranges_gather(p.va, b->sorted, b->rs.ctrl, b->cap, b->rs.recs, p.tile_w, p.tile_h,
+                           nullptr, b->ks.trec, st);
+      b->trec_ready = true;
+    }
   } else {
     b->binned = false;
-    int rc = batch_binning(b, p, st, nullptr);
+    int rc = batch_binning(b, p, true, st, nullptr);
     if (rc) return rc;
     note_binning(b, means, prec, logw);
   }
@@ -1370,14 +1385,14 @@ int fe_batch_fwd_timed(fe_batch* b, const float* means, const float* prec, const
   cudaEvent_t ev[7];
   for (auto& e : ev) FE_CUDA(cudaEventCreate(&e));
   b->binned = false;
-  int rc = batch_binning(b, p, st, ev);
+  int rc = batch_binning(b, p, false, st, ev);
   if (rc) {
     for (auto& e : ev) cudaEventDestroy(e);
     return rc;
   }
   note_binning(b, means, prec, logw);
-  launch_blend_fwd(p.va, p.tile_w, p.tile_h, p.px, p.chunk, p.n_tiles, b->ks.trec, b->rs.ranges,
-                   p.beta2, p.beta3, depth, alpha, stats, p.n_pix, b->rs.ctrl, st);
+  launch_blend_fwd(p.va, p.tile_w, p.tile_h, p.px, p.chunk, p.n_tiles, b->sorted, b->rs.recs,
+                   b->rs.ranges, p.beta2, p.beta3, depth, alpha, stats, p.n_pix, b->rs.ctrl, st);
   FE_CUDA(cudaEventRecord(ev[6], st));
   FE_CUDA(cudaEventSynchronize(ev[6]));
   for (int i = 0; i < 6; ++i) FE_CUDA(cudaEventElapsedTime(&stage_ms[i], ev[i], ev[i + 1]));
@@ -1501,22 +1516,20 @@ int fe_render_fwd_noalloc(const fe_render_desc* d, const float* means, const flo
   launch_preprocess(p.va, p.n_rec, p.means, p.prec, p.logw, p.quat, nullptr, p.trans, p.cull_mode,
                     p.cull_param, p.tile_w, p.tile_h, rs.recs, rs.rects, rs.touched, st);
   const RowPlan rp = p.radix ? RowPlan{} : row_plan(&p.va.one, 1);
+  uint64_t* sorted = ks.keys_a;
   if (rp.ok) {
     launch_tile_binning_count(p.va, rp.n_views, rp.max_gy, rs.rects, rs.row_tot, worst, rs.ctrl,
                               st);
     launch_tile_binning_emit(p.va, rp.n_views, rp.max_gy, rs.rects, rs.row_tot, rs.ctrl,
                              rs.ranges, ks.keys_a, st);
-    launch_ranges_gather(p.va, ks.keys_a, rs.ctrl, worst, rs.recs, p.tile_w, p.tile_h, nullptr,
-                         ks.trec, st);
   } else {
     launch_scan(rs.touched, rs.incl, p.n_rec, worst, rs.scan_tmp, rs.ctrl, st);
     launch_emit_keys(p.va, rs.incl, rs.rects, p.n_rec, rs.ctrl, ks.keys_a, worst, st);
-    uint64_t* sorted =
-        launch_sort(ks.keys_a, ks.keys_b, bits_for(p.n_tiles), rs.ctrl, worst, ks.hist, st);
+    sorted = launch_sort(ks.keys_a, ks.keys_b, bits_for(p.n_tiles), rs.ctrl, worst, ks.hist, st);
     launch_ranges_gather(p.va, sorted, rs.ctrl, worst, rs.recs, p.tile_w, p.tile_h, rs.ranges,
-                         ks.trec, st);
+                         nullptr, st);
   }
-  launch_blend_fwd(p.va, p.tile_w, p.tile_h, p.px, p.chunk, p.n_tiles, ks.trec, rs.ranges,
+  launch_blend_fwd(p.va, p.tile_w, p.tile_h, p.px, p.chunk, p.n_tiles, sorted, rs.recs, rs.ranges,
                    p.beta2, p.beta3, depth, alpha, stats, npix, rs.ctrl, st);
   if (device_error)
     FE_CUDA(cudaMemcpyAsync(device_error, &rs.ctrl->error, sizeof(uint32_t),

@@ -1,10 +1,13 @@
 // blend_fwd.cu -- per-tile forward blend: depth softmax and alpha in one pass.
 //
 // Persistent CTAs take screen tiles from a device-side work counter (one launch covers any number
-// of uneven renders); each thread owns PX pixels of one tile row. A tile's records
-// (pair-interleaved TilePairs, 160 B per two records, contiguous in key order) stream through a
-// two-stage shared-memory ring of CH pairs per stage filled by 1-D TMA bulk copies (cp.async.bulk ...
-// mbarrier::complete_tx; every wait bounded). Two records are evaluated together with packed
+// of uneven renders); each thread owns PX pixels of one tile row. A tile's keys are taken in
+// chunks of 2 CH: the chunk's Gaussian records (96 B each) are copied into shared memory with
+// cp.async while the previous chunk is evaluated, then each thread re-expands its records around
+// the tile centre into pair-interleaved TilePairs (two records per 160 B, field by field) in a
+// double-buffered shared-memory ring; the Gaussian ids of the chunk after are read one chunk
+// ahead of that. No record stream is written to or read from HBM for the forward. Two records
+// are evaluated together with packed
 // f32x2 arithmetic, so each 16-byte shared load yields two ready operands and every polynomial,
 // logit and accumulation step is one instruction for two evaluations. Per (pixel, Gaussian):
 //     vsv = V(du,dv)   psv = P(du,dv)   nq = N(du-cu, dv-cv)    (row-constant parts shared by
@@ -22,22 +25,21 @@
 #include <algorithm>
 
 #include "fe_kernels.cuh"
+#include "fe_tilerec.cuh"
 
 namespace fe {
 
 namespace {
 
-constexpr int kStages = 2;
-
 template <int CH>
 struct BlendSmem {
-  TilePair buf[kStages][CH];
-  uint64_t full[kStages];
+  TilePair buf[2][CH];      // record pairs: chunk c of a tile in buf[c & 1]
+  GaussRec src[2 * CH];     // source records of the next chunk (cp.async), record r at src[r]
   uint32_t tile;
 };
 
-// Make slot `sl` (0 = .x, 1 = .y) of a pair contribute nothing: vsv = 1, psv = 0 (z = 0, masked),
-// C = -inf (density 0).
+// Write a null record into slot `sl` (0 = .x, 1 = .y) of a pair: vsv = 1, psv = 0 (z = 0,
+// masked), C = -inf (density 0).
 __device__ __forceinline__ void null_slot(TilePair& p, int sl) {
 #pragma unroll
   for (int i = 0; i < kRecFields; ++i) {
@@ -46,14 +48,6 @@ __device__ __forceinline__ void null_slot(TilePair& p, int sl) {
     if (i == 15) v = -INFINITY;
     if (sl == 0) p.f[i].x = v; else p.f[i].y = v;
   }
-}
-
-template <int CH>
-__device__ __forceinline__ void issue_chunk(BlendSmem<CH>& sm, int stage, const TilePair* src,
-                                            int count) {
-  const uint32_t bytes = (uint32_t)count * (uint32_t)sizeof(TilePair);
-  mbar_arrive_expect_tx(&sm.full[stage], bytes);
-  tma_bulk_g2s(&sm.buf[stage][0], src, bytes, &sm.full[stage]);
 }
 
 // Threads per CTA for a tile of TW x TH pixels with PX pixels per thread (PX pixels of one row,
@@ -152,9 +146,10 @@ template <int TW, int TH, int PX, int CH>
 __global__ void __launch_bounds__(BlendShape<TW, TH, PX, CH>::NT,
                                   BlendShape<TW, TH, PX, CH>::MIN_CTAS) blend_fwd_kernel(
     ViewsArg va, uint32_t tile_begin, uint32_t tile_end, uint32_t* __restrict__ counter,
-    const TilePair* __restrict__ trec, const uint2* __restrict__ ranges, float nb2, float beta3,
+    const uint64_t* __restrict__ keys, const GaussRec* __restrict__ recs,
+    const uint2* __restrict__ ranges, float nb2, float beta3,
     float* __restrict__ depth, float* __restrict__ alpha, float* __restrict__ stats,
-    int64_t stats_stride, Control* __restrict__ ctrl) {
+    int64_t stats_stride) {
   using Sh = BlendShape<TW, TH, PX, CH>;
   constexpr int GP = Sh::GP;
   __shared__ __align__(128) BlendSmem<CH> sm;
@@ -172,12 +167,9 @@ __global__ void __launch_bounds__(BlendShape<TW, TH, PX, CH>::NT,
   }
   const f2_t ZERO2 = f2_pack(0.f, 0.f);
 
-  if (tid == 0) {
-#pragma unroll
-    for (int s = 0; s < kStages; ++s) mbar_init(&sm.full[s], 1);
-    fence_mbar_init();
-  }
-  uint32_t phase = 0;  // bit s: parity of the next completion to wait for on stage s
+  constexpr int RC = 2 * CH;                     // records per chunk
+  constexpr int RPT = (RC + Sh::NT - 1) / Sh::NT;  // records each thread stages and builds
+  const float hw = 0.5f * (TW - 1), hh = 0.5f * (TH - 1);
 
   while (true) {
     if (tid == 0) sm.tile = tile_begin + atomicAdd(counter, 1u);
@@ -188,6 +180,8 @@ __global__ void __launch_bounds__(BlendShape<TW, TH, PX, CH>::NT,
     const int gx = view_at(va, vi).gx;
     const int lt = (int)(tile - view_at(va, vi).tile_base);
     const int tx = lt % gx, ty = lt / gx;
+    const GaussRec* vrec = recs + view_at(va, vi).rec_base;
+    const float tcu = tx * TW + hw, tcv = ty * TH + hh;  // tile centre (pixels)
 
     const uint2 rg = ranges[tile];
     // m starts finite (kNoLogit) so that logit - m is never (-inf) - (-inf); masked logits are
@@ -199,68 +193,101 @@ __global__ void __launch_bounds__(BlendShape<TW, TH, PX, CH>::NT,
       A2[k] = ZERO2; W2[k] = ZERO2; Z2[k] = ZERO2;
       m[k] = kNoLogit;
     }
-    bool failed = false;
-
     if (rg.y > rg.x) {
-      const uint32_t p0 = rg.x >> 1, p1 = (rg.y + 1) >> 1;
-      const int np = (int)(p1 - p0);
-      const bool first_odd = (rg.x & 1u) != 0, last_odd = (rg.y & 1u) != 0;
-      const int nchunks = (np + CH - 1) / CH;
-      const TilePair* src = trec + p0;
-      if (tid == 0) {
-        for (int c = 0; c < kStages && c < nchunks; ++c)
-          issue_chunk(sm, c, src + c * CH, min(CH, np - c * CH));
+      const int nk = (int)(rg.y - rg.x);
+      const int nchunks = (nk + RC - 1) / RC;
+      const uint64_t* tkeys = keys + rg.x;
+      // Chunk c holds the tile's keys [c RC, c RC + RC); thread t stages and builds records
+      // t, t + NT, ... of a chunk. Source records of chunk c + 1 are copied (cp.async) while chunk
+      // c is evaluated; the Gaussian ids of chunk c + 2 are read one chunk ahead of that.
+      uint32_t gid_next[RPT];
+      auto stage = [&](int c, const uint32_t (&gid)[RPT]) {
+#pragma unroll
+        for (int q = 0; q < RPT; ++q) {
+          const int r = tid + q * Sh::NT;
+          if (r < RC && c * RC + r < nk) {
+            const char* g = reinterpret_cast<const char*>(vrec + gid[q]);
+            char* d = reinterpret_cast<char*>(&sm.src[r]);
+#pragma unroll
+            for (int b16 = 0; b16 < (int)(sizeof(GaussRec) / 16); ++b16)
+              cp_async16(d + 16 * b16, g + 16 * b16);
+          }
+        }
+        cp_async_commit();
+      };
+      auto load_gids = [&](int c, uint32_t (&gid)[RPT]) {
+#pragma unroll
+        for (int q = 0; q < RPT; ++q) {
+          const int r = tid + q * Sh::NT;
+          gid[q] = (r < RC && c * RC + r < nk) ? (uint32_t)tkeys[c * RC + r] : 0u;
+        }
+      };
+      // Build chunk c's record pairs from the staged source records (this thread's own records,
+      // so no barrier is needed before it) and null the slots past the tile's keys up to a whole
+      // group of pairs.
+      auto build = [&](int c) {
+        TilePair* pb = sm.buf[c & 1];
+        const int cnt = min(RC, nk - c * RC);
+        const int padded = (cnt + 2 * GP - 1) / (2 * GP) * (2 * GP);
+#pragma unroll
+        for (int q = 0; q < RPT; ++q) {
+          const int r = tid + q * Sh::NT;
+          if (r < cnt) {
+            const GaussRec& g = sm.src[r];
+            TileRec t;
+            tile_record(g, tcu - g.uc, tcv - g.vc, hw, hh, t);
+            const float* f = reinterpret_cast<const float*>(&t);
+            float* dst = reinterpret_cast<float*>(&pb[r >> 1]) + (r & 1);
+#pragma unroll
+            for (int i = 0; i < kRecFields; ++i) dst[2 * i] = f[i];
+          } else if (r < padded) {
+            null_slot(pb[r >> 1], r & 1);
+          }
+        }
+      };
+      {
+        // One staging buffer: chunk 1 is copied only once chunk 0 has been built from it.
+        uint32_t g0[RPT];
+        load_gids(0, g0);
+        stage(0, g0);
+        load_gids(1, g0);
+        cp_async_wait<0>();
+        build(0);
+        stage(1, g0);
+        load_gids(2, gid_next);
+        __syncthreads();
       }
       for (int c = 0; c < nchunks; ++c) {
-        const int stage = c % kStages;
-        const uint32_t parity = (phase >> stage) & 1u;
-        phase ^= 1u << stage;
-        const int cnt = min(CH, np - c * CH);
-        const int padded = (cnt + GP - 1) / GP * GP;
-        // Pad to whole groups with pairs that contribute nothing (disjoint from the copy's bytes).
-        if (tid < padded - cnt) {
-          null_slot(sm.buf[stage][cnt + tid], 0);
-          null_slot(sm.buf[stage][cnt + tid], 1);
-        }
-        const bool ok = mbar_wait_bounded(&sm.full[stage], parity);
-        // The first and last pairs may carry a neighbouring tile's record in one slot.
-        if (ok && tid == 0) {
-          if (c == 0 && first_odd) null_slot(sm.buf[stage][0], 0);
-          if (c == nchunks - 1 && last_odd) null_slot(sm.buf[stage][cnt - 1], 1);
-        }
-        if (__syncthreads_or(!ok)) {
-          // A copy did not land in time: flag it, let every outstanding copy finish (bounded)
-          // and stop this CTA; the tile's outputs are left unwritten.
-          if (tid == 0) {
-            atomicOr(&ctrl->error, FE_DEVERR_TIMEOUT);
-            for (int cc = c; cc < nchunks && cc < c + kStages; ++cc)
-              (void)mbar_wait_bounded(&sm.full[cc % kStages],
-                                      cc == c ? parity : (phase >> (cc % kStages)) & 1u);
-          }
-          failed = true;
-          break;
-        }
+        const int cnt = min(RC, nk - c * RC);
+        const int padded = (cnt + 2 * GP - 1) / (2 * GP) * (2 * GP) / 2;  // pairs, whole groups
+        const TilePair* pb = sm.buf[c & 1];
         for (int j = 0; j < padded; j += GP) {
           // Uniform over the CTA: the z > 0 mask is only evaluated for groups holding a record
           // whose psv is not positive over the whole tile (null slots included).
           bool need_mask = false;
 #pragma unroll
           for (int q = 0; q < GP; ++q) {
-            const float2 fr = sm.buf[stage][j + q].f[18];
+            const float2 fr = pb[j + q].f[18];
             need_mask |= !(fr.x != 0.f && fr.y != 0.f);
           }
           if (need_mask)
-            blend_group<PX, GP, true>(&sm.buf[stage][j], DU, DV, DVSQ, B3, NB2, A2, W2, Z2, m);
+            blend_group<PX, GP, true>(&pb[j], DU, DV, DVSQ, B3, NB2, A2, W2, Z2, m);
           else
-            blend_group<PX, GP, false>(&sm.buf[stage][j], DU, DV, DVSQ, B3, NB2, A2, W2, Z2, m);
+            blend_group<PX, GP, false>(&pb[j], DU, DV, DVSQ, B3, NB2, A2, W2, Z2, m);
         }
-        fence_proxy_async_smem();
-        __syncthreads();
-        if (tid == 0 && c + kStages < nchunks)
-          issue_chunk(sm, stage, src + (c + kStages) * CH, min(CH, np - (c + kStages) * CH));
+        if (c + 1 < nchunks) {
+          // Chunk c + 1: its source records have landed (this thread's copies; the barrier
+          // below publishes the built pairs). buf[(c + 1) & 1] was last read in chunk c - 1.
+          cp_async_wait<0>();
+          build(c + 1);
+          if (c + 2 < nchunks) {
+            stage(c + 2, gid_next);
+            load_gids(c + 3, gid_next);
+          }
+          __syncthreads();
+        }
       }
     }
-    if (failed) break;
 
     const ViewDev& V = view_at(va, vi);
     const int v = ty * TH + ly;
@@ -289,30 +316,30 @@ __global__ void __launch_bounds__(BlendShape<TW, TH, PX, CH>::NT,
 
 template <int TW, int TH, int PX, int CH>
 void launch_tiles(const ViewsArg& va, int64_t tile_begin, int64_t tile_end, uint32_t* counter,
-                  const TilePair* trec, const uint2* ranges, float nb2, float beta3, float* depth,
-                  float* alpha, float* stats, int64_t stats_stride, Control* ctrl,
+                  const uint64_t* keys, const GaussRec* recs, const uint2* ranges, float nb2,
+                  float beta3, float* depth, float* alpha, float* stats, int64_t stats_stride,
                   cudaStream_t st) {
   constexpr int NT = BlendShape<TW, TH, PX, CH>::NT;
   constexpr auto kern = blend_fwd_kernel<TW, TH, PX, CH>;
   const int64_t grid = std::min<int64_t>(tile_end - tile_begin, resident_ctas<kern>(NT));
-  kern<<<(unsigned)grid, NT, 0, st>>>(va, (uint32_t)tile_begin, (uint32_t)tile_end, counter, trec,
-                                      ranges, nb2, beta3, depth, alpha, stats, stats_stride, ctrl);
+  kern<<<(unsigned)grid, NT, 0, st>>>(va, (uint32_t)tile_begin, (uint32_t)tile_end, counter, keys,
+                                      recs, ranges, nb2, beta3, depth, alpha, stats, stats_stride);
 }
 
 template <int TW, int TH, int PX>
 void launch_chunk(int chunk, const ViewsArg& va, int64_t tile_begin, int64_t tile_end,
-                  uint32_t* counter, const TilePair* trec, const uint2* ranges, float nb2,
-                  float beta3, float* depth, float* alpha, float* stats, int64_t stats_stride,
-                  Control* ctrl, cudaStream_t st) {
+                  uint32_t* counter, const uint64_t* keys, const GaussRec* recs,
+                  const uint2* ranges, float nb2, float beta3, float* depth, float* alpha,
+                  float* stats, int64_t stats_stride, cudaStream_t st) {
   if (chunk == 8)
-    launch_tiles<TW, TH, PX, 8>(va, tile_begin, tile_end, counter, trec, ranges, nb2, beta3, depth,
-                                alpha, stats, stats_stride, ctrl, st);
+    launch_tiles<TW, TH, PX, 8>(va, tile_begin, tile_end, counter, keys, recs, ranges, nb2, beta3,
+                                depth, alpha, stats, stats_stride, st);
   else if (chunk == 32)
-    launch_tiles<TW, TH, PX, 32>(va, tile_begin, tile_end, counter, trec, ranges, nb2, beta3,
-                                 depth, alpha, stats, stats_stride, ctrl, st);
+    launch_tiles<TW, TH, PX, 32>(va, tile_begin, tile_end, counter, keys, recs, ranges, nb2,
+                                 beta3, depth, alpha, stats, stats_stride, st);
   else
-    launch_tiles<TW, TH, PX, 16>(va, tile_begin, tile_end, counter, trec, ranges, nb2, beta3,
-                                 depth, alpha, stats, stats_stride, ctrl, st);
+    launch_tiles<TW, TH, PX, 16>(va, tile_begin, tile_end, counter, keys, recs, ranges, nb2,
+                                 beta3, depth, alpha, stats, stats_stride, st);
 }
 
 }  // namespace
@@ -321,14 +348,14 @@ void launch_chunk(int chunk, const ViewsArg& va, int64_t tile_begin, int64_t til
 // Chunk: record pairs per shared-memory stage, 8, 16 or 32; 0 selects 16.
 void launch_blend_fwd_band(const ViewsArg& va, int tile_w, int tile_h, int px, int chunk,
                            int64_t tile_begin, int64_t tile_end, uint32_t* counter,
-                           const TilePair* trec, const uint2* ranges, float beta2, float beta3,
-                           float* depth, float* alpha, float* stats, int64_t stats_stride,
-                           Control* ctrl, cudaStream_t st) {
+                           const uint64_t* keys, const GaussRec* recs, const uint2* ranges,
+                           float beta2, float beta3, float* depth, float* alpha, float* stats,
+                           int64_t stats_stride, cudaStream_t st) {
   if (tile_end <= tile_begin) return;
   const float nb2 = -beta2 * kLog2e;
 #define FE_BLEND(TW_, TH_, PX_)                                                                 \
-  launch_chunk<TW_, TH_, PX_>(chunk, va, tile_begin, tile_end, counter, trec, ranges, nb2, beta3, \
-                              depth, alpha, stats, stats_stride, ctrl, st)
+  launch_chunk<TW_, TH_, PX_>(chunk, va, tile_begin, tile_end, counter, keys, recs, ranges, nb2,  \
+                              beta3, depth, alpha, stats, stats_stride, st)
   if (tile_w == 8 && tile_h == 8) {
     if (px == 1) FE_BLEND(8, 8, 1); else FE_BLEND(8, 8, 2);
   } else if (tile_w == 32 && tile_h == 8) {
@@ -340,11 +367,11 @@ void launch_blend_fwd_band(const ViewsArg& va, int tile_w, int tile_h, int px, i
 }
 
 void launch_blend_fwd(const ViewsArg& va, int tile_w, int tile_h, int px, int chunk,
-                      int64_t n_tiles, const TilePair* trec, const uint2* ranges, float beta2,
-                      float beta3, float* depth, float* alpha, float* stats,
-                      int64_t stats_stride, Control* ctrl, cudaStream_t st) {
-  launch_blend_fwd_band(va, tile_w, tile_h, px, chunk, 0, n_tiles, &ctrl->next_tile, trec, ranges,
-                        beta2, beta3, depth, alpha, stats, stats_stride, ctrl, st);
+                      int64_t n_tiles, const uint64_t* keys, const GaussRec* recs,
+                      const uint2* ranges, float beta2, float beta3, float* depth, float* alpha,
+                      float* stats, int64_t stats_stride, Control* ctrl, cudaStream_t st) {
+  launch_blend_fwd_band(va, tile_w, tile_h, px, chunk, 0, n_tiles, &ctrl->next_tile, keys, recs,
+                        ranges, beta2, beta3, depth, alpha, stats, stats_stride, st);
 }
 
 }  // namespace fe

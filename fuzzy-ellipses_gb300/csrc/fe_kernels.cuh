@@ -60,18 +60,20 @@ void launch_ranges(const uint64_t* keys, const Control* ctrl, int64_t capacity, 
 
 // blend_fwd.cu
 // px: pixels per thread (1, 2 or 4; 0 = default for the tile shape); chunk: record pairs per
-// shared-memory stage (8, 16 or 32; 0 = 16). Persistent: ctrl->next_tile must be zero.
+// shared-memory stage (8, 16 or 32; 0 = 16). The blend builds each key's tile record itself from
+// the sorted keys and the Gaussian records (no gathered record stream). Persistent:
+// ctrl->next_tile must be zero.
 void launch_blend_fwd(const ViewsArg& va, int tile_w, int tile_h, int px, int chunk, int64_t n_tiles,
-                      const TilePair* trec, const uint2* ranges, float beta2, float beta3,
-                      float* depth, float* alpha, float* stats, int64_t stats_stride,
+                      const uint64_t* keys, const GaussRec* recs, const uint2* ranges, float beta2,
+                      float beta3, float* depth, float* alpha, float* stats, int64_t stats_stride,
                       Control* ctrl, cudaStream_t st);
 // The blend over global tiles [tile_begin, tile_end) only, taking tiles from `counter` (zero at
 // launch); bands with their own counters may run concurrently on different streams.
 void launch_blend_fwd_band(const ViewsArg& va, int tile_w, int tile_h, int px, int chunk,
                            int64_t tile_begin, int64_t tile_end, uint32_t* counter,
-                           const TilePair* trec, const uint2* ranges, float beta2, float beta3,
-                           float* depth, float* alpha, float* stats, int64_t stats_stride,
-                           Control* ctrl, cudaStream_t st);
+                           const uint64_t* keys, const GaussRec* recs, const uint2* ranges,
+                           float beta2, float beta3, float* depth, float* alpha, float* stats,
+                           int64_t stats_stride, cudaStream_t st);
 
 // blend_bwd.cu
 void launch_pixel_prep(const ViewsArg& va, int64_t n_pix, const float* depth, const float* stats,
