@@ -110,7 +110,7 @@ struct RecSpace {
   uint32_t* incl;
   unsigned long long* scan_tmp;
   uint2* ranges;
-  unsigned long long* row_tot;  // tile-major binning: keys per tile row (row slots)
+  unsigned long long* row_tot;  // tile-major binning: row key-count differences per view
   float4* pix;     // backward only
   RecGrad* rgrad;  // backward only
 };
@@ -134,7 +134,7 @@ size_t carve_rec(char* base, int64_t n_rec, int64_t n_tiles, int64_t n_pix, bool
   s.incl = c.take<uint32_t>(n_rec);
   s.scan_tmp = c.take<unsigned long long>(scan_grid(std::max(n_rec, n_tiles)));
   s.ranges = c.take<uint2>(n_tiles);
-  s.row_tot = c.take<unsigned long long>(n_tiles);
+  s.row_tot = c.take<unsigned long long>(n_tiles + 1);
   s.pix = bwd ? c.take<float4>(n_pix) : nullptr;
   s.rgrad = bwd ? c.take<RecGrad>(n_rec) : nullptr;
   out(s);
@@ -260,23 +260,20 @@ int run_binning(const Pipeline& p, int64_t worst, DevBuf& recbuf, DevBuf& keybuf
   // `worst`: every record touching every tile of its view.
   const bool exact = worst > 0 && (size_t)worst * kBytesPerKey <= key_budget_bytes();
 
-  FE_CUDA(cudaMemsetAsync(rs.ctrl, 0, sizeof(Control), st));
-  FE_CUDA(cudaMemsetAsync(rs.ranges, 0, sizeof(uint2) * (size_t)p.n_tiles, st));
-  launch_preprocess(p.va, p.n_rec, p.means, p.prec, p.logw, p.quat, nullptr, p.trans, p.cull_mode,
-                    p.cull_param, p.tile_w, p.tile_h, rs.recs, rs.rects, rs.touched, st);
   // The single-view pipelines describe their view on the host (va.one).
   const RowPlan rp = (p.va.table || p.radix) ? RowPlan{} : row_plan(&p.va.one, 1);
+  FE_CUDA(cudaMemsetAsync(rs.ctrl, 0, sizeof(Control), st));
+  FE_CUDA(cudaMemsetAsync(rs.ranges, 0, sizeof(uint2) * (size_t)p.n_tiles, st));
+  if (rp.ok)
+    FE_CUDA(cudaMemsetAsync(rs.row_tot, 0, sizeof(unsigned long long) * (rp.max_gy + 1), st));
+  launch_preprocess(p.va, p.n_rec, p.means, p.prec, p.logw, p.quat, nullptr, p.trans, p.cull_mode,
+                    p.cull_param, p.tile_w, p.tile_h, rs.recs, rs.rects, rs.touched,
+                    rp.ok ? rs.row_tot : nullptr, rp.max_gy, rs.ctrl, st);
   if (exact) {
     cap = worst;
-    if (rp.ok)
-      launch_tile_binning_count(p.va, rp.n_views, rp.max_gy, rs.rects, rs.row_tot, cap, rs.ctrl,
-                                st);
   } else {
     // Count with an unbounded capacity first, read the count back, then size the keys.
-    if (rp.ok)
-      launch_tile_binning_count(p.va, rp.n_views, rp.max_gy, rs.rects, rs.row_tot,
-                                INT64_C(0xffffffff), rs.ctrl, st);
-    else
+    if (!rp.ok)
       launch_scan(rs.touched, rs.incl, p.n_rec, INT64_C(0xffffffff), rs.scan_tmp, rs.ctrl, st);
     FE_CUDA(cudaMemcpyAsync(h_pinned, &rs.ctrl->want_keys, sizeof(unsigned long long),
                             cudaMemcpyDeviceToHost, st));
@@ -290,7 +287,7 @@ int run_binning(const Pipeline& p, int64_t worst, DevBuf& recbuf, DevBuf& keybuf
   carve_keys(keybuf.ptr, cap, [&](const KeySpace& s) { ks = s; });
   if (exact && !rp.ok) launch_scan(rs.touched, rs.incl, p.n_rec, cap, rs.scan_tmp, rs.ctrl, st);
   if (rp.ok) {
-    launch_tile_binning_emit(p.va, rp.n_views, rp.max_gy, rs.rects, rs.row_tot, rs.ctrl,
+    launch_tile_binning_emit(p.va, rp.n_views, rp.max_gy, rs.rects, rs.row_tot, cap, rs.ctrl,
                              rs.ranges, ks.keys_a, st);
     sorted = ks.keys_a;
     if (need_trec)
@@ -1008,7 +1005,7 @@ int commit_batch(fe_batch* b, cudaStream_t st) {
                           cudaMemcpyHostToDevice, st));
   // (ranges and row totals: sized for the tiles and for the tile-major binning's row slots)
   const int64_t tile_slots =
-      std::max<int64_t>(b->n_tiles, (int64_t)b->rows.n_views * b->rows.max_gy);
+      std::max<int64_t>(b->n_tiles, (int64_t)b->rows.n_views * (b->rows.max_gy + 1));
   const size_t rb = carve_rec(nullptr, b->n_rec, tile_slots, b->n_pix, true, [](const RecSpace&) {});
   rc = b->rec.reserve(rb, st);
   if (rc) return rc;
@@ -1138,18 +1135,20 @@ static Pipeline batch_pipeline(fe_batch* b, const float* means, const float* pre
 static int batch_binning(fe_batch* b, const Pipeline& p, bool need_trec, cudaStream_t st,
                          cudaEvent_t* ev) {
   const RecSpace& rs = b->rs;
+  const RowPlan rp = p.radix ? RowPlan{} : b->rows;
   FE_CUDA(cudaMemsetAsync(rs.ctrl, 0, sizeof(Control), st));
   FE_CUDA(cudaMemsetAsync(rs.ranges, 0, sizeof(uint2) * (size_t)p.n_tiles, st));
+  if (rp.ok)
+    FE_CUDA(cudaMemsetAsync(rs.row_tot, 0,
+                            sizeof(unsigned long long) * (size_t)rp.n_views * (rp.max_gy + 1),
+                            st));
   if (ev) FE_CUDA(cudaEventRecord(ev[0], st));
   launch_preprocess(p.va, p.n_rec, p.means, p.prec, p.logw, p.quat, nullptr, p.trans, p.cull_mode,
-                    p.cull_param, p.tile_w, p.tile_h, rs.recs, rs.rects, rs.touched, st);
+                    p.cull_param, p.tile_w, p.tile_h, rs.recs, rs.rects, rs.touched,
+                    rp.ok ? rs.row_tot : nullptr, rp.max_gy, rs.ctrl, st);
   if (ev) FE_CUDA(cudaEventRecord(ev[1], st));
-  const RowPlan rp = p.radix ? RowPlan{} : b->rows;
   if (b->exact) {
-    if (rp.ok)
-      launch_tile_binning_count(p.va, rp.n_views, rp.max_gy, rs.rects, rs.row_tot,
-                                INT64_C(0xffffffff), rs.ctrl, st);
-    else
+    if (!rp.ok)
       launch_scan(rs.touched, rs.incl, p.n_rec, INT64_C(0xffffffff), rs.scan_tmp, rs.ctrl, st);
     FE_CUDA(cudaMemcpyAsync(b->h_pinned, &rs.ctrl->want_keys, sizeof(unsigned long long),
                             cudaMemcpyDeviceToHost, st));
@@ -1162,16 +1161,13 @@ static int batch_binning(fe_batch* b, const Pipeline& p, bool need_trec, cudaStr
       b->cap = K + K / 4;
       carve_keys(b->keys.ptr, b->cap, [&](const KeySpace& s_) { b->ks = s_; });
     }
-  } else if (rp.ok) {
-    launch_tile_binning_count(p.va, rp.n_views, rp.max_gy, rs.rects, rs.row_tot, b->cap, rs.ctrl,
-                              st);
-  } else {
+  } else if (!rp.ok) {
     launch_scan(rs.touched, rs.incl, p.n_rec, b->cap, rs.scan_tmp, rs.ctrl, st);
   }
   if (ev) FE_CUDA(cudaEventRecord(ev[2], st));
   const KeySpace& ks = b->ks;
   if (rp.ok) {
-    launch_tile_binning_emit(p.va, rp.n_views, rp.max_gy, rs.rects, rs.row_tot, rs.ctrl,
+    launch_tile_binning_emit(p.va, rp.n_views, rp.max_gy, rs.rects, rs.row_tot, b->cap, rs.ctrl,
                              rs.ranges, ks.keys_a, st);
     if (ev) FE_CUDA(cudaEventRecord(ev[3], st));
     b->sorted = ks.keys_a;
@@ -1513,14 +1509,15 @@ int fe_render_fwd_noalloc(const fe_render_desc* d, const float* means, const flo
   // the blend's tile counter) and the tile ranges (tiles without keys keep an empty range).
   FE_CUDA(cudaMemsetAsync(rs.ctrl, 0, sizeof(Control), st));
   FE_CUDA(cudaMemsetAsync(rs.ranges, 0, sizeof(uint2) * (size_t)p.n_tiles, st));
-  launch_preprocess(p.va, p.n_rec, p.means, p.prec, p.logw, p.quat, nullptr, p.trans, p.cull_mode,
-                    p.cull_param, p.tile_w, p.tile_h, rs.recs, rs.rects, rs.touched, st);
   const RowPlan rp = p.radix ? RowPlan{} : row_plan(&p.va.one, 1);
+  if (rp.ok)
+    FE_CUDA(cudaMemsetAsync(rs.row_tot, 0, sizeof(unsigned long long) * (rp.max_gy + 1), st));
+  launch_preprocess(p.va, p.n_rec, p.means, p.prec, p.logw, p.quat, nullptr, p.trans, p.cull_mode,
+                    p.cull_param, p.tile_w, p.tile_h, rs.recs, rs.rects, rs.touched,
+                    rp.ok ? rs.row_tot : nullptr, rp.max_gy, rs.ctrl, st);
   uint64_t* sorted = ks.keys_a;
   if (rp.ok) {
-    launch_tile_binning_count(p.va, rp.n_views, rp.max_gy, rs.rects, rs.row_tot, worst, rs.ctrl,
-                              st);
-    launch_tile_binning_emit(p.va, rp.n_views, rp.max_gy, rs.rects, rs.row_tot, rs.ctrl,
+    launch_tile_binning_emit(p.va, rp.n_views, rp.max_gy, rs.rects, rs.row_tot, worst, rs.ctrl,
                              rs.ranges, ks.keys_a, st);
   } else {
     launch_scan(rs.touched, rs.incl, p.n_rec, worst, rs.scan_tmp, rs.ctrl, st);

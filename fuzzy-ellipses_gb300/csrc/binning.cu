@@ -442,16 +442,13 @@ __global__ void __launch_bounds__(kGatherThreads, 4) ranges_gather_kernel(
 
 // ---- Tile-major binning ---------------------------------------------------------------------
 // The keys of a tile are its Gaussians in ascending id: the order the stable sort of the
-// Gaussian-major key list produces. Both kernels run one block per (view, tile row):
-//  row_totals_kernel  the row's key count (sum of the widths of the footprint rectangles that
-//                     cover the row); the last block to finish adds the rows up into the run's
-//                     key count (clamped to the capacity, FE_DEVERR_CAPACITY past it)
-//  tile_emit_kernel   the row's base (the totals of the rows before it), per-tile counts from a
-//                     difference array over the covering rectangles, the tile ranges, and the
-//                     keys: the covering rectangles in id order (order-preserving compaction into
-//                     shared memory), a warp per tile walking them 32 at a time, a ballot giving
-//                     each covering rectangle its slot
-// Row slot = view * gridDim.x + row (gridDim.x = the largest row count of the views).
+// Gaussian-major key list produces. The preprocess has recorded every footprint rectangle's width
+// as a difference of the row key counts of its view (+w at its first row, -w past its last:
+// row_tot) and the total in ctrl->want_keys. One block per (view, tile row) then takes the row's
+// base (the keys of the rows before it, from those differences), per-tile
+// counts from a difference array over the covering rectangles, writes the tile ranges, and places
+// the keys: the covering rectangles in id order (order-preserving compaction into shared memory)
+// are walked 32 at a time by a warp per tile, a ballot giving each covering rectangle its slot.
 constexpr int kRowThreads = kScanThreads;  // block_exclusive_scan works on kScanThreads threads
 constexpr int kRowWarps = kRowThreads / 32;
 constexpr int kRowPer = 4;                          // rectangles per thread per filter segment
@@ -483,49 +480,6 @@ __device__ __forceinline__ unsigned long long block_sum_u64(unsigned long long v
   return t;
 }
 
-__global__ void __launch_bounds__(kRowThreads) row_totals_kernel(
-    ViewsArg va, const TileRect* __restrict__ rects, unsigned long long* __restrict__ row_tot,
-    int64_t capacity, Control* __restrict__ ctrl) {
-  __shared__ unsigned long long ws[kRowWarps];
-  __shared__ bool last;
-  const int tid = threadIdx.x;
-  const unsigned slots = gridDim.x * gridDim.y;
-  const unsigned slot = blockIdx.y * gridDim.x + blockIdx.x;
-  const ViewDev& V = view_at(va, blockIdx.y);
-  const int row = blockIdx.x;
-  unsigned long long sum = 0;
-  if (row < V.gy) {
-    if (V.gx > kMaxRowTiles) {  // the host plans this path only for narrower views
-      if (tid == 0) atomicOr(&ctrl->error, FE_DEVERR_CAPACITY);
-    } else {
-      const TileRect* vr = rects + V.rec_base;
-#pragma unroll 4
-      for (int i = tid; i < V.n; i += kRowThreads) {
-        const TileRect r = vr[i];
-        if (covers_row(r, row)) sum += (unsigned)(r.x1 - r.x0);
-      }
-    }
-  }
-  sum = block_sum_u64(sum, ws);
-  if (tid == 0) {
-    row_tot[slot] = sum;
-    __threadfence();
-    last = atomicAdd(&ctrl->rows_done, 1u) == slots - 1;
-  }
-  __syncthreads();
-  if (!last) return;
-  __threadfence();
-  unsigned long long tot = 0;
-  for (unsigned s = tid; s < slots; s += kRowThreads) tot += __ldcg(&row_tot[s]);
-  tot = block_sum_u64(tot, ws);
-  if (tid == 0) {
-    const unsigned long long cap = (unsigned long long)capacity;
-    ctrl->want_keys = tot;
-    ctrl->num_keys = tot < cap ? tot : cap;
-    if (tot > cap) atomicOr(&ctrl->error, FE_DEVERR_CAPACITY);
-  }
-}
-
 // Order-preserving compaction of the segment's rectangles that cover `row` into `list`
 // (thread t takes rectangles s0 + kRowPer t .. + kRowPer - 1); returns their number. Ends with a
 // barrier after the list is written.
@@ -554,7 +508,7 @@ __device__ __forceinline__ uint32_t filter_row(const TileRect* __restrict__ vr, 
 
 __global__ void __launch_bounds__(kRowThreads) tile_emit_kernel(
     ViewsArg va, const TileRect* __restrict__ rects,
-    const unsigned long long* __restrict__ row_tot, const Control* __restrict__ ctrl,
+    const unsigned long long* __restrict__ row_tot, int64_t capacity, Control* __restrict__ ctrl,
     uint2* __restrict__ ranges, uint64_t* __restrict__ keys) {
   __shared__ RowRect list[kRowSeg];
   __shared__ int diff[kMaxRowTiles + 1];         // +1 at x0, -1 at x1 of every covering rectangle
@@ -565,17 +519,36 @@ __global__ void __launch_bounds__(kRowThreads) tile_emit_kernel(
   const unsigned full = 0xffffffffu;
   const uint32_t lt_mask = (1u << lane) - 1u;
   const unsigned slot = blockIdx.y * gridDim.x + blockIdx.x;
+  const unsigned long long want = ctrl->want_keys, cap = (unsigned long long)capacity;
+  const unsigned long long K = want < cap ? want : cap;
+  if (slot == 0 && tid == 0) {
+    ctrl->num_keys = K;
+    if (want > cap) atomicOr(&ctrl->error, FE_DEVERR_CAPACITY);
+  }
   const ViewDev& V = view_at(va, blockIdx.y);
   const int row = blockIdx.x;
-  if (row >= V.gy || V.gx > kMaxRowTiles) return;  // (uniform over the block)
+  if (row >= V.gy) return;  // (uniform over the block)
+  if (V.gx > kMaxRowTiles) {  // the host plans this path only for narrower views
+    if (tid == 0) atomicOr(&ctrl->error, FE_DEVERR_CAPACITY);
+    return;
+  }
   const int gx = V.gx, n = V.n;
   const int64_t tile0 = V.tile_base + (int64_t)row * gx;
   const TileRect* vr = rects + V.rec_base;
-  const unsigned long long K = ctrl->num_keys;
 
-  unsigned long long b = 0;
-  for (unsigned s = tid; s < slot; s += kRowThreads) b += row_tot[s];
-  const unsigned long long row_base = block_sum_u64(b, wsu);
+  // row_tot holds, per view, the difference of the row key counts (stride max_gy + 1): the count
+  // of row r is the sum of entries 0..r, so the keys before row `row` of this view are
+  // sum_{r' < row} d[r'] (row - r'), and a whole earlier view holds sum_{r' < gy} d[r'] (gy - r').
+  const int stride = (int)gridDim.x + 1;
+  long long b = 0;
+  for (int idx = tid; idx < (int)blockIdx.y * stride; idx += kRowThreads) {
+    const int v2 = idx / stride, r2 = idx - v2 * stride;
+    const int gy2 = view_at(va, v2).gy;
+    if (r2 < gy2) b += (long long)row_tot[idx] * (gy2 - r2);
+  }
+  for (int r2 = tid; r2 < row; r2 += kRowThreads)
+    b += (long long)row_tot[(int64_t)blockIdx.y * stride + r2] * (row - r2);
+  const unsigned long long row_base = block_sum_u64((unsigned long long)b, wsu);
   // Keys of this row: slot p (relative to the row's base) for p < lim.
   uint64_t* row_keys = keys + row_base;
   const unsigned long long left = K > row_base ? K - row_base : 0ull;
@@ -734,20 +707,12 @@ void launch_ranges_gather(const ViewsArg& va, const uint64_t* keys, const Contro
                                                         ranges, trec);
 }
 
-void launch_tile_binning_count(const ViewsArg& va, int n_views, int max_gy,
-                               const TileRect* rects, unsigned long long* row_tot,
-                               int64_t capacity, Control* ctrl, cudaStream_t st) {
-  if (n_views <= 0 || max_gy <= 0) return;
-  row_totals_kernel<<<dim3((unsigned)max_gy, (unsigned)n_views), kRowThreads, 0, st>>>(
-      va, rects, row_tot, capacity, ctrl);
-}
-
 void launch_tile_binning_emit(const ViewsArg& va, int n_views, int max_gy, const TileRect* rects,
-                              const unsigned long long* row_tot, const Control* ctrl,
+                              const unsigned long long* row_tot, int64_t capacity, Control* ctrl,
                               uint2* ranges, uint64_t* keys, cudaStream_t st) {
   if (n_views <= 0 || max_gy <= 0) return;
   tile_emit_kernel<<<dim3((unsigned)max_gy, (unsigned)n_views), kRowThreads, 0, st>>>(
-      va, rects, row_tot, ctrl, ranges, keys);
+      va, rects, row_tot, capacity, ctrl, ranges, keys);
 }
 
 void launch_ranges(const uint64_t* keys, const Control* ctrl, int64_t capacity, uint2* ranges,

@@ -56,8 +56,8 @@ struct __align__(16) GaussRec {
 };
 static_assert(sizeof(GaussRec) == 96, "GaussRec layout");
 
-// Tile-local polynomial form of a record (what the blend streams with TMA bulk copies, stored
-// pair-interleaved: see TilePair).
+// Tile-local polynomial form of a record (what the forward blend builds in shared memory and the
+// backward reads as a gathered stream, stored pair-interleaved: see TilePair).
 // With (du,dv) the pixel offset from the tile centre and (eu,ev) = (du-cu, dv-cv) the offset from
 // the expansion centre (cu,cv) of the Mahalanobis term:
 //   vsv = V0 + V1 du + V2 dv + V3 du^2 + V4 du dv + V5 dv^2
@@ -110,8 +110,7 @@ struct Control {
   unsigned long long want_keys; // keys the run needed
   uint32_t error;               // FE_DEVERR_* bits
   uint32_t next_tile;           // work counter of the persistent blend
-  uint32_t rows_done;           // tile-major binning: row-total blocks finished
-  uint32_t pad[9];
+  uint32_t pad[10];
 };
 
 // View lookup: the plain single-render path passes its one view by value (so it needs no

@@ -10,7 +10,7 @@ void launch_preprocess(const ViewsArg& va, int64_t n_rec, const float* means, co
                        const float* logw, const float* quat, const float* rotm,
                        const float* trans, int cull_mode, float cull_param, int tile_w,
                        int tile_h, GaussRec* recs, TileRect* rects, uint32_t* touched,
-                       cudaStream_t st);
+                       unsigned long long* row_tot, int max_gy, Control* ctrl, cudaStream_t st);
 void launch_preprocess_reference(int P, float n_std, const float* means, const float* scales,
                                  const float* rots, const float* viewmatrix,
                                  const float* projmatrix, int W, int H, float tan_fovx,
@@ -41,18 +41,17 @@ uint64_t* launch_sort(uint64_t* a, uint64_t* b, int key_bits, const Control* ctr
 void launch_ranges_gather(const ViewsArg& va, const uint64_t* keys, const Control* ctrl,
                           int64_t capacity, const GaussRec* recs, int tile_w, int tile_h,
                           uint2* ranges, TilePair* trec, cudaStream_t st);
-// Tile-major binning for views at most kMaxRowTiles tiles wide (grids: one block per tile row
-// of every view; row_tot: n_views * max_gy entries). The count pass writes every row's key count
-// and the run's key count (clamped to capacity, as launch_scan does); the emit pass writes the
-// keys of every tile in ascending Gaussian id at their place in the sorted order (keys past
-// ctrl->num_keys dropped) and the non-empty tile ranges (ranges zeroed beforehand). Same keys and
-// ranges as emit + stable sort + ranges. ctrl->rows_done must be zero before the count pass.
+// Tile-major binning for views at most kMaxRowTiles tiles wide. launch_preprocess with row_tot
+// (n_views * (max_gy + 1) zeroed entries, view v's at v * (max_gy + 1)) records every rectangle's
+// width as a difference of its view's row key counts (+w at row y0, -w at row y1) and adds the
+// run's key count to ctrl->want_keys; the emit
+// pass (one block per tile row of every view) sets ctrl->num_keys = min(want_keys, capacity)
+// (FE_DEVERR_CAPACITY past it) and writes the keys of every tile in ascending Gaussian id at their
+// place in the sorted order (keys past num_keys dropped) and the non-empty tile ranges (ranges
+// zeroed beforehand). Same keys and ranges as emit + stable sort + ranges.
 constexpr int kMaxRowTiles = 1024;
-void launch_tile_binning_count(const ViewsArg& va, int n_views, int max_gy,
-                               const TileRect* rects, unsigned long long* row_tot,
-                               int64_t capacity, Control* ctrl, cudaStream_t st);
 void launch_tile_binning_emit(const ViewsArg& va, int n_views, int max_gy, const TileRect* rects,
-                              const unsigned long long* row_tot, const Control* ctrl,
+                              const unsigned long long* row_tot, int64_t capacity, Control* ctrl,
                               uint2* ranges, uint64_t* keys, cudaStream_t st);
 // Ranges only (reference-compatible binning).
 void launch_ranges(const uint64_t* keys, const Control* ctrl, int64_t capacity, uint2* ranges,

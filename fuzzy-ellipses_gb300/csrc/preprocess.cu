@@ -139,7 +139,9 @@ __global__ void __launch_bounds__(64) preprocess_kernel(
     ViewsArg va, int64_t n_rec, const float* __restrict__ means, const float* __restrict__ prec,
     const float* __restrict__ logw, const float* __restrict__ quat, const float* __restrict__ rotm,
     const float* __restrict__ trans, int cull_mode, float cull_param, int tile_w, int tile_h,
-    GaussRec* __restrict__ recs, TileRect* __restrict__ rects, uint32_t* __restrict__ touched) {
+    GaussRec* __restrict__ recs, TileRect* __restrict__ rects, uint32_t* __restrict__ touched,
+    unsigned long long* __restrict__ row_tot, int max_gy, Control* __restrict__ ctrl) {
+  unsigned long long keys = 0;  // this thread's keys (row_tot != NULL)
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n_rec;
        i += (int64_t)gridDim.x * blockDim.x) {
     const int vi = find_view<&ViewDev::rec_base>(va, i);
@@ -166,6 +168,20 @@ __global__ void __launch_bounds__(64) preprocess_kernel(
     recs[i] = rec;
     rects[i] = TileRect{(uint16_t)tx0, (uint16_t)ty0, (uint16_t)tx1, (uint16_t)ty1};
     touched[i] = (uint32_t)((tx1 - tx0) * (ty1 - ty0));
+    if (row_tot != nullptr && tx1 > tx0) {
+      // Tile-major binning: the rectangle adds its width to the key count of rows [ty0, ty1),
+      // recorded as a difference (+w at ty0, -w at ty1; the emit pass takes the prefix sums).
+      unsigned long long* rd = row_tot + (int64_t)vi * (max_gy + 1);
+      const unsigned long long w = (unsigned long long)(tx1 - tx0);
+      atomicAdd(&rd[ty0], w);
+      atomicAdd(&rd[ty1], 0ull - w);
+      keys += w * (unsigned long long)(ty1 - ty0);
+    }
+  }
+  if (row_tot != nullptr) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) keys += __shfl_xor_sync(0xffffffffu, keys, o);
+    if ((threadIdx.x & 31) == 0 && keys) atomicAdd(&ctrl->want_keys, keys);
   }
 }
 
@@ -376,14 +392,14 @@ void launch_preprocess(const ViewsArg& va, int64_t n_rec, const float* means, co
                        const float* logw, const float* quat, const float* rotm,
                        const float* trans, int cull_mode, float cull_param, int tile_w,
                        int tile_h, GaussRec* recs, TileRect* rects, uint32_t* touched,
-                       cudaStream_t st) {
+                       unsigned long long* row_tot, int max_gy, Control* ctrl, cudaStream_t st) {
   if (n_rec <= 0) return;
   const int threads = 64;
   const int64_t want = (n_rec + threads - 1) / threads;
   const int blocks = (int)(want < 65535 ? want : 65535);
   preprocess_kernel<<<blocks, threads, 0, st>>>(va, n_rec, means, prec, logw, quat, rotm, trans,
                                                 cull_mode, cull_param, tile_w, tile_h, recs,
-                                                rects, touched);
+                                                rects, touched, row_tot, max_gy, ctrl);
 }
 
 void launch_preprocess_reference(int P, float n_std, const float* means, const float* scales,
