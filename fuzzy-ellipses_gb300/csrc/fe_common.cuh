@@ -221,14 +221,6 @@ __device__ __forceinline__ void bulk_wait_group0() {
   asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
 }
 
-__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
-  asm volatile(
-      "{\n\t.reg .b64 st;\n\t"
-      "mbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n\t}" ::"r"(smem_addr(bar)),
-      "r"(bytes)
-      : "memory");
-}
-
 __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
   uint32_t done;
   asm volatile(
@@ -254,17 +246,6 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity
 }
 __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity) {
   return mbar_wait_bounded(bar, parity, kWaitLimitNs);
-}
-
-// 1-D TMA bulk copy global -> shared, completion counted on `bar` in bytes.
-// Requires 16-byte aligned addresses and a byte count that is a multiple of 16.
-__device__ __forceinline__ void tma_bulk_g2s(void* smem_dst, const void* gmem_src, uint32_t bytes,
-                                             uint64_t* bar) {
-  asm volatile(
-      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::
-          "r"(smem_addr(smem_dst)),
-      "l"(gmem_src), "r"(bytes), "r"(smem_addr(bar))
-      : "memory");
 }
 
 // Packed float32 pairs (Blackwell add/sub/mul/fma .f32x2): one instruction for two lanes of work.

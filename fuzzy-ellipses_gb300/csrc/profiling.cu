@@ -59,7 +59,7 @@ __global__ void __launch_bounds__(256) peak_fma2_kernel(float* out, int iters, f
 }
 
 // Failure-detection self-test: one block waits on an mbarrier that nothing ever arrives at,
-// through the same bounded wait the blend uses for its TMA copies. The wait must give up after
+// through the library's bounded mbarrier wait (globaltimer limit). The wait must give up after
 // limit_ns and report FE_DEVERR_TIMEOUT, leaving the context usable.
 __global__ void wait_selftest_kernel(unsigned long long limit_ns, uint32_t* status,
                                      unsigned long long* elapsed_ns) {

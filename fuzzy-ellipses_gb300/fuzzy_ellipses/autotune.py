@@ -3,11 +3,11 @@
 Three knobs change the work and its mapping onto the GPU:
 
 * ``tile``  -- screen tile of the binning and of one blend work item (8x8, 16x16 or 32x8):
-  smaller tiles cull more precisely (fewer evaluations) but produce more keys to sort and
-  gather;
+  smaller tiles cull more precisely (fewer evaluations) but produce more keys to emit and
+  more tile records to build;
 * ``px``    -- pixels of one tile row per thread (1, 2, 4): shares each record's shared-memory
   loads and row-constant polynomial terms across more evaluations, at the cost of registers;
-* ``chunk`` -- record pairs per shared-memory stage of the TMA ring (8, 16, 32).
+* ``chunk`` -- record pairs per shared-memory stage of the blend's record ring (8, 16, 32).
 
 ``Autotuner.tune`` times every candidate on the actual batch (median of per-stage CUDA-event
 timings of the whole pipeline, not just the blend) and caches the fastest per workload bucket

@@ -471,7 +471,7 @@ int fe_check_device_status(fe_stream_t stream, uint32_t *device_error);
 #define FE_DEVERR_TIMEOUT 2u  /* a bounded mbarrier wait gave up */
 
 /* Failure-detection self-test (no reference counterpart): one block waits on an mbarrier that
- * nothing arrives at, through the same bounded wait the blend uses for its TMA copies, with the
+ * nothing arrives at, through the library's bounded mbarrier wait (globaltimer limit), with the
  * limit limit_ns (1 us .. 1 s). Synchronises `stream`; *h_status receives FE_DEVERR_TIMEOUT when
  * the wait gave up (the expected outcome) and *h_elapsed_ns the time the wait took. The context
  * stays usable afterwards. */
