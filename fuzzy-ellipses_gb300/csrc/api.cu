@@ -1293,7 +1293,7 @@ int fe_batch_fwd_host(fe_batch* b, const float* h_means, const float* h_prec,
     cudaStream_t sj = (j & 1) ? b->s_comp : st;
     launch_blend_fwd_band(p.va, p.tile_w, p.tile_h, p.px, p.chunk, hb.t0, hb.t1, ctr + j,
                           b->sorted, b->rs.recs, b->rs.ranges, p.beta2, p.beta3, dep_d, alp_d,
-                          nullptr, p.n_pix, sj);
+                          nullptr, p.n_pix, b->rs.ctrl, sj);
     FE_CUDA(cudaGetLastError());
     FE_CUDA(cudaEventRecord(b->band_ev[j], sj));
   }

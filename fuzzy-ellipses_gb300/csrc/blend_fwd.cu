@@ -2,8 +2,9 @@
 //
 // Persistent CTAs take screen tiles from a device-side work counter (one launch covers any number
 // of uneven renders); each thread owns PX pixels of one tile row. A tile's keys are taken in
-// chunks of 2 CH: the chunk's Gaussian records (96 B each) are copied into shared memory with
-// cp.async while the previous chunk is evaluated, then each thread re-expands its records around
+// chunks of 2 CH: the chunk's Gaussian records (96 B each) are staged in shared memory by 1-D TMA
+// bulk copies (cp.async.bulk, one per record, completing on an mbarrier; every wait bounded)
+// while the previous chunk is evaluated, then each thread re-expands its records around
 // the tile centre into pair-interleaved TilePairs (two records per 160 B, field by field) in a
 // double-buffered shared-memory ring; the Gaussian ids of the chunk after are read one chunk
 // ahead of that. No record stream is written to or read from HBM for the forward. Two records
@@ -34,7 +35,8 @@ namespace {
 template <int CH>
 struct BlendSmem {
   TilePair buf[2][CH];      // record pairs: chunk c of a tile in buf[c & 1]
-  GaussRec src[2 * CH];     // source records of the next chunk (cp.async), record r at src[r]
+  GaussRec src[2 * CH];     // source records of the next chunk (TMA bulk copies), record r at src[r]
+  uint64_t bar;             // completion of the source-record copies, one phase per chunk
   uint32_t tile;
 };
 
@@ -149,7 +151,7 @@ __global__ void __launch_bounds__(BlendShape<TW, TH, PX, CH>::NT,
     const uint64_t* __restrict__ keys, const GaussRec* __restrict__ recs,
     const uint2* __restrict__ ranges, float nb2, float beta3,
     float* __restrict__ depth, float* __restrict__ alpha, float* __restrict__ stats,
-    int64_t stats_stride) {
+    int64_t stats_stride, Control* __restrict__ ctrl) {
   using Sh = BlendShape<TW, TH, PX, CH>;
   constexpr int GP = Sh::GP;
   __shared__ __align__(128) BlendSmem<CH> sm;
@@ -170,6 +172,11 @@ __global__ void __launch_bounds__(BlendShape<TW, TH, PX, CH>::NT,
   constexpr int RC = 2 * CH;                     // records per chunk
   constexpr int RPT = (RC + Sh::NT - 1) / Sh::NT;  // records each thread stages and builds
   const float hw = 0.5f * (TW - 1), hh = 0.5f * (TH - 1);
+  if (tid == 0) {
+    mbar_init(&sm.bar, 1);
+    fence_mbar_init();
+  }
+  uint32_t phase = 0;  // parity of the next completion of sm.bar
 
   while (true) {
     if (tid == 0) sm.tile = tile_begin + atomicAdd(counter, 1u);
@@ -198,22 +205,33 @@ __global__ void __launch_bounds__(BlendShape<TW, TH, PX, CH>::NT,
       const int nchunks = (nk + RC - 1) / RC;
       const uint64_t* tkeys = keys + rg.x;
       // Chunk c holds the tile's keys [c RC, c RC + RC); thread t stages and builds records
-      // t, t + NT, ... of a chunk. Source records of chunk c + 1 are copied (cp.async) while chunk
-      // c is evaluated; the Gaussian ids of chunk c + 2 are read one chunk ahead of that.
+      // t, t + NT, ... of a chunk. The source records of chunk c + 1 arrive by TMA bulk copies
+      // (96 B each, completing on sm.bar) while chunk c is evaluated; the Gaussian ids of chunk
+      // c + 2 are read one chunk ahead of that. Copies into the staging buffer are issued only
+      // after a barrier that every thread reaches after its wait for the previous chunk.
       uint32_t gid_next[RPT];
       auto stage = [&](int c, const uint32_t (&gid)[RPT]) {
+        const int cnt = min(RC, nk - c * RC);
+        fence_proxy_async_smem();  // this thread's reads of sm.src precede the copies into it
+        if (tid == 0) mbar_arrive_expect_tx(&sm.bar, (uint32_t)(cnt * (int)sizeof(GaussRec)));
 #pragma unroll
         for (int q = 0; q < RPT; ++q) {
           const int r = tid + q * Sh::NT;
-          if (r < RC && c * RC + r < nk) {
-            const char* g = reinterpret_cast<const char*>(vrec + gid[q]);
-            char* d = reinterpret_cast<char*>(&sm.src[r]);
-#pragma unroll
-            for (int b16 = 0; b16 < (int)(sizeof(GaussRec) / 16); ++b16)
-              cp_async16(d + 16 * b16, g + 16 * b16);
-          }
+          if (r < cnt) tma_bulk_g2s(&sm.src[r], vrec + gid[q], (uint32_t)sizeof(GaussRec), &sm.bar);
         }
-        cp_async_commit();
+      };
+      auto wait_src = [&]() {
+        const bool ok = mbar_wait_bounded(&sm.bar, phase);
+        phase ^= 1u;
+        return ok;
+      };
+      // A copy that did not land in time: flag it, give the outstanding copies one more bounded
+      // wait and stop this CTA; the tile's outputs are left unwritten.
+      auto give_up = [&]() {
+        if (tid == 0) {
+          atomicOr(&ctrl->error, FE_DEVERR_TIMEOUT);
+          (void)mbar_wait_bounded(&sm.bar, phase ^ 1u);
+        }
       };
       auto load_gids = [&](int c, uint32_t (&gid)[RPT]) {
 #pragma unroll
@@ -222,9 +240,9 @@ __global__ void __launch_bounds__(BlendShape<TW, TH, PX, CH>::NT,
           gid[q] = (r < RC && c * RC + r < nk) ? (uint32_t)tkeys[c * RC + r] : 0u;
         }
       };
-      // Build chunk c's record pairs from the staged source records (this thread's own records,
-      // so no barrier is needed before it) and null the slots past the tile's keys up to a whole
-      // group of pairs.
+      // Build chunk c's record pairs from the staged source records (after the wait every
+      // thread sees all of them; each builds its own) and null the slots past the tile's keys up
+      // to a whole group of pairs.
       auto build = [&](int c) {
         TilePair* pb = sm.buf[c & 1];
         const int cnt = min(RC, nk - c * RC);
@@ -251,11 +269,14 @@ __global__ void __launch_bounds__(BlendShape<TW, TH, PX, CH>::NT,
         load_gids(0, g0);
         stage(0, g0);
         load_gids(1, g0);
-        cp_async_wait<0>();
+        const bool ok = wait_src();
         build(0);
-        stage(1, g0);
+        if (__syncthreads_or(!ok)) {
+          give_up();
+          return;
+        }
+        if (nchunks > 1) stage(1, g0);
         load_gids(2, gid_next);
-        __syncthreads();
       }
       for (int c = 0; c < nchunks; ++c) {
         const int cnt = min(RC, nk - c * RC);
@@ -276,15 +297,18 @@ __global__ void __launch_bounds__(BlendShape<TW, TH, PX, CH>::NT,
             blend_group<PX, GP, false>(&pb[j], DU, DV, DVSQ, B3, NB2, A2, W2, Z2, m);
         }
         if (c + 1 < nchunks) {
-          // Chunk c + 1: its source records have landed (this thread's copies; the barrier
-          // below publishes the built pairs). buf[(c + 1) & 1] was last read in chunk c - 1.
-          cp_async_wait<0>();
+          // Chunk c + 1: wait for its source records, build its pairs (buf[(c + 1) & 1] was last
+          // read in chunk c - 1), publish them, then stage chunk c + 2.
+          const bool ok = wait_src();
           build(c + 1);
+          if (__syncthreads_or(!ok)) {
+            give_up();
+            return;
+          }
           if (c + 2 < nchunks) {
             stage(c + 2, gid_next);
             load_gids(c + 3, gid_next);
           }
-          __syncthreads();
         }
       }
     }
@@ -318,28 +342,29 @@ template <int TW, int TH, int PX, int CH>
 void launch_tiles(const ViewsArg& va, int64_t tile_begin, int64_t tile_end, uint32_t* counter,
                   const uint64_t* keys, const GaussRec* recs, const uint2* ranges, float nb2,
                   float beta3, float* depth, float* alpha, float* stats, int64_t stats_stride,
-                  cudaStream_t st) {
+                  Control* ctrl, cudaStream_t st) {
   constexpr int NT = BlendShape<TW, TH, PX, CH>::NT;
   constexpr auto kern = blend_fwd_kernel<TW, TH, PX, CH>;
   const int64_t grid = std::min<int64_t>(tile_end - tile_begin, resident_ctas<kern>(NT));
   kern<<<(unsigned)grid, NT, 0, st>>>(va, (uint32_t)tile_begin, (uint32_t)tile_end, counter, keys,
-                                      recs, ranges, nb2, beta3, depth, alpha, stats, stats_stride);
+                                      recs, ranges, nb2, beta3, depth, alpha, stats, stats_stride,
+                                      ctrl);
 }
 
 template <int TW, int TH, int PX>
 void launch_chunk(int chunk, const ViewsArg& va, int64_t tile_begin, int64_t tile_end,
                   uint32_t* counter, const uint64_t* keys, const GaussRec* recs,
                   const uint2* ranges, float nb2, float beta3, float* depth, float* alpha,
-                  float* stats, int64_t stats_stride, cudaStream_t st) {
+                  float* stats, int64_t stats_stride, Control* ctrl, cudaStream_t st) {
   if (chunk == 8)
     launch_tiles<TW, TH, PX, 8>(va, tile_begin, tile_end, counter, keys, recs, ranges, nb2, beta3,
-                                depth, alpha, stats, stats_stride, st);
+                                depth, alpha, stats, stats_stride, ctrl, st);
   else if (chunk == 32)
     launch_tiles<TW, TH, PX, 32>(va, tile_begin, tile_end, counter, keys, recs, ranges, nb2,
-                                 beta3, depth, alpha, stats, stats_stride, st);
+                                 beta3, depth, alpha, stats, stats_stride, ctrl, st);
   else
     launch_tiles<TW, TH, PX, 16>(va, tile_begin, tile_end, counter, keys, recs, ranges, nb2,
-                                 beta3, depth, alpha, stats, stats_stride, st);
+                                 beta3, depth, alpha, stats, stats_stride, ctrl, st);
 }
 
 }  // namespace
@@ -350,12 +375,12 @@ void launch_blend_fwd_band(const ViewsArg& va, int tile_w, int tile_h, int px, i
                            int64_t tile_begin, int64_t tile_end, uint32_t* counter,
                            const uint64_t* keys, const GaussRec* recs, const uint2* ranges,
                            float beta2, float beta3, float* depth, float* alpha, float* stats,
-                           int64_t stats_stride, cudaStream_t st) {
+                           int64_t stats_stride, Control* ctrl, cudaStream_t st) {
   if (tile_end <= tile_begin) return;
   const float nb2 = -beta2 * kLog2e;
 #define FE_BLEND(TW_, TH_, PX_)                                                                 \
   launch_chunk<TW_, TH_, PX_>(chunk, va, tile_begin, tile_end, counter, keys, recs, ranges, nb2,  \
-                              beta3, depth, alpha, stats, stats_stride, st)
+                              beta3, depth, alpha, stats, stats_stride, ctrl, st)
   if (tile_w == 8 && tile_h == 8) {
     if (px == 1) FE_BLEND(8, 8, 1); else FE_BLEND(8, 8, 2);
   } else if (tile_w == 32 && tile_h == 8) {
@@ -371,7 +396,7 @@ void launch_blend_fwd(const ViewsArg& va, int tile_w, int tile_h, int px, int ch
                       const uint2* ranges, float beta2, float beta3, float* depth, float* alpha,
                       float* stats, int64_t stats_stride, Control* ctrl, cudaStream_t st) {
   launch_blend_fwd_band(va, tile_w, tile_h, px, chunk, 0, n_tiles, &ctrl->next_tile, keys, recs,
-                        ranges, beta2, beta3, depth, alpha, stats, stats_stride, st);
+                        ranges, beta2, beta3, depth, alpha, stats, stats_stride, ctrl, st);
 }
 
 }  // namespace fe

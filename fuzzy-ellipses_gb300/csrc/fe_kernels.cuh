@@ -72,7 +72,7 @@ void launch_blend_fwd_band(const ViewsArg& va, int tile_w, int tile_h, int px, i
                            int64_t tile_begin, int64_t tile_end, uint32_t* counter,
                            const uint64_t* keys, const GaussRec* recs, const uint2* ranges,
                            float beta2, float beta3, float* depth, float* alpha, float* stats,
-                           int64_t stats_stride, cudaStream_t st);
+                           int64_t stats_stride, Control* ctrl, cudaStream_t st);
 
 // blend_bwd.cu
 void launch_pixel_prep(const ViewsArg& va, int64_t n_pix, const float* depth, const float* stats,
