@@ -206,22 +206,6 @@ __device__ __forceinline__ void fence_proxy_async_smem() {
   asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
 }
 
-// 16-byte asynchronous copy global -> shared (both addresses 16-byte aligned), grouped per thread
-// by cp_async_commit and waited for by cp_async_wait<N> (at most N of the thread's groups still
-// in flight); a barrier then makes the data visible to the other threads.
-__device__ __forceinline__ void cp_async16(void* smem_dst, const void* gmem_src) {
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_addr(smem_dst)),
-               "l"(gmem_src)
-               : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() {
-  asm volatile("cp.async.commit_group;" ::: "memory");
-}
-template <int N>
-__device__ __forceinline__ void cp_async_wait() {
-  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
-}
-
 // 1-D TMA bulk store shared -> global (16-byte aligned addresses, size a multiple of 16), tracked
 // by the issuing thread's bulk async-groups.
 __device__ __forceinline__ void bulk_store_s2g(void* gmem_dst, const void* smem_src,
