@@ -56,7 +56,7 @@ size_t key_budget_bytes() {
 }
 
 // Bytes of key-proportional scratch per key: two key buffers and one tile record.
-constexpr size_t kBytesPerKey = 2 * sizeof(uint64_t) + sizeof(TilePair) / 2;
+constexpr size_t kBytesPerKey = 2 * sizeof(uint64_t);
 
 int bits_for(int64_t n) {
   int b = 0;
@@ -120,7 +120,6 @@ struct KeySpace {
   uint64_t* keys_a;
   uint64_t* keys_b;
   uint32_t* hist;
-  TilePair* trec;  // key k at trec[k/2], slot k%2
 };
 
 template <class F>
@@ -148,7 +147,6 @@ size_t carve_keys(char* base, int64_t cap, F&& out) {
   s.keys_a = c.take<uint64_t>(cap);
   s.keys_b = c.take<uint64_t>(cap);
   s.hist = c.take<uint32_t>(int64_t(sort_grid(cap) + 1) * 256);
-  s.trec = c.take<TilePair>((cap + 1) / 2);
   out(s);
   return c.off;
 }
@@ -247,11 +245,9 @@ RowPlan row_plan(const ViewDev* views, int n_views) {
   return r;
 }
 
-// need_trec: also build the gathered tile-record stream (the backward and the feature pass read
-// it; the forward blend builds its records itself).
 int run_binning(const Pipeline& p, int64_t worst, DevBuf& recbuf, DevBuf& keybuf,
-                unsigned long long* h_pinned, bool bwd, bool need_trec, cudaStream_t st,
-                RecSpace& rs, KeySpace& ks, int64_t& cap, uint64_t*& sorted) {
+                unsigned long long* h_pinned, bool bwd, cudaStream_t st, RecSpace& rs,
+                KeySpace& ks, int64_t& cap, uint64_t*& sorted) {
   size_t rec_bytes = carve_rec(nullptr, p.n_rec, p.n_tiles, p.n_pix, bwd, [](const RecSpace&) {});
   int rc = recbuf.reserve(rec_bytes, st);
   if (rc) return rc;
@@ -290,14 +286,10 @@ int run_binning(const Pipeline& p, int64_t worst, DevBuf& recbuf, DevBuf& keybuf
     launch_tile_binning_emit(p.va, rp.n_views, rp.max_gy, rs.rects, rs.row_tot, cap, rs.ctrl,
                              rs.ranges, ks.keys_a, st);
     sorted = ks.keys_a;
-    if (need_trec)
-      launch_ranges_gather(p.va, sorted, rs.ctrl, cap, rs.recs, p.tile_w, p.tile_h, nullptr,
-                           ks.trec, st);
   } else {
     launch_emit_keys(p.va, rs.incl, rs.rects, p.n_rec, rs.ctrl, ks.keys_a, cap, st);
     sorted = launch_sort(ks.keys_a, ks.keys_b, bits_for(p.n_tiles), rs.ctrl, cap, ks.hist, st);
-    launch_ranges_gather(p.va, sorted, rs.ctrl, cap, rs.recs, p.tile_w, p.tile_h, rs.ranges,
-                         need_trec ? ks.trec : nullptr, st);
+    launch_ranges(sorted, rs.ctrl, cap, rs.ranges, st);
   }
   return FE_OK;
 }
@@ -403,7 +395,7 @@ int fe_render_fwd(const fe_render_desc* d, const float* means, const float* prec
   KeySpace ks;
   int64_t cap = 0;
   uint64_t* sorted = nullptr;
-  rc = run_binning(p, p.n_rec * p.n_tiles, a->rec, a->keys, a->h_pinned, false, false, st, rs, ks, cap,
+  rc = run_binning(p, p.n_rec * p.n_tiles, a->rec, a->keys, a->h_pinned, false, st, rs, ks, cap,
                    sorted);
   if (rc) return rc;
   launch_blend_fwd(p.va, p.tile_w, p.tile_h, p.px, p.chunk, p.n_tiles, sorted, rs.recs, rs.ranges, p.beta2, p.beta3,
@@ -437,12 +429,12 @@ int fe_render_bwd(const fe_render_desc* d, const float* means, const float* prec
   KeySpace ks;
   int64_t cap = 0;
   uint64_t* sorted = nullptr;
-  rc = run_binning(p, p.n_rec * p.n_tiles, a->rec, a->keys, a->h_pinned, true, true, st, rs, ks, cap,
+  rc = run_binning(p, p.n_rec * p.n_tiles, a->rec, a->keys, a->h_pinned, true, st, rs, ks, cap,
                    sorted);
   if (rc) return rc;
   FE_CUDA(cudaMemsetAsync(rs.rgrad, 0, sizeof(RecGrad) * (size_t)p.n_rec, st));
   launch_pixel_prep(p.va, p.n_pix, depth, stats, p.n_pix, gdepth, galpha, rs.pix, st);
-  launch_blend_bwd(p.va, p.tile_w, p.tile_h, p.n_tiles, sorted, rs.ranges, ks.trec, rs.recs,
+  launch_blend_bwd(p.va, p.tile_w, p.tile_h, p.n_tiles, sorted, rs.ranges, rs.recs,
                    rs.pix, p.beta2, p.beta3, rs.rgrad, rs.ctrl, st);
   launch_record_vjp(p.va, p.n_rec, means, prec, quat, trans, rs.recs, rs.rgrad, gmeans, gprec,
                     glogw, st);
@@ -474,10 +466,10 @@ int fe_render_features(const fe_render_desc* d, const float* means, const float*
   KeySpace ks;
   int64_t cap = 0;
   uint64_t* sorted = nullptr;
-  rc = run_binning(p, p.n_rec * p.n_tiles, a->rec, a->keys, a->h_pinned, false, true, st, rs, ks, cap,
+  rc = run_binning(p, p.n_rec * p.n_tiles, a->rec, a->keys, a->h_pinned, false, st, rs, ks, cap,
                    sorted);
   if (rc) return rc;
-  launch_features(p.va, p.tile_w, p.tile_h, p.n_tiles, sorted, rs.ranges, ks.trec, stats, npix,
+  launch_features(p.va, p.tile_w, p.tile_h, p.n_tiles, sorted, rs.ranges, rs.recs, stats, npix,
                   p.beta2, p.beta3, features, n_features, out, rs.ctrl, st);
   FE_CUDA(cudaGetLastError());
   return FE_OK;
@@ -504,7 +496,7 @@ int fe_render_binning(const fe_render_desc* d, const float* means, const float* 
   KeySpace ks;
   int64_t cap = 0;
   uint64_t* sorted = nullptr;
-  rc = run_binning(p, p.n_rec * p.n_tiles, a->rec, a->keys, a->h_pinned, false, false, st, rs, ks, cap,
+  rc = run_binning(p, p.n_rec * p.n_tiles, a->rec, a->keys, a->h_pinned, false, st, rs, ks, cap,
                    sorted);
   if (rc) return rc;
   FE_CUDA(cudaMemcpyAsync(a->h_pinned, &rs.ctrl->num_keys, sizeof(unsigned long long),
@@ -832,7 +824,7 @@ int fe_rasterize_legacy(const fe_legacy_desc* d, const float* means, const float
   carve_keys(a->keys.ptr, cap, [&](const KeySpace& s_) { ks = s_; });
   launch_emit_keys(va, rs.incl, rs.rects, P, rs.ctrl, ks.keys_a, cap, st);
   uint64_t* sorted = launch_sort(ks.keys_a, ks.keys_b, bits_for(T), rs.ctrl, cap, ks.hist, st);
-  launch_ranges_gather(va, sorted, rs.ctrl, cap, rs.recs, 8, 8, rs.ranges, nullptr, st);
+  launch_ranges(sorted, rs.ctrl, cap, rs.ranges, st);
   launch_blend_fwd(va, 8, 8, 0, 0, T, sorted, rs.recs, rs.ranges, 21.4f, 2.66f, out_z, out_alpha, nullptr, 0,
                    rs.ctrl, st);
   FE_CUDA(cudaGetLastError());
@@ -930,7 +922,6 @@ struct fe_batch {
   cudaEvent_t ev_bin = nullptr, ev_copy = nullptr;
   std::vector<cudaEvent_t> band_ev;
   RowPlan rows;  // tile-major binning plan (rows.ok) or the emit + sort path
-  bool trec_ready = false;  // the binning's gathered tile records are built (the backward's input)
 };
 
 namespace {
@@ -1130,10 +1121,7 @@ static Pipeline batch_pipeline(fe_batch* b, const float* means, const float* pre
 
 // Binning of a batch. With exact key sizing the key count is read back after the scan (one
 // 8-byte copy and a stream synchronisation) and the key scratch grows to fit it.
-// need_trec: also build the gathered tile-record stream (the backward reads it; the forward blend
-// builds its records itself).
-static int batch_binning(fe_batch* b, const Pipeline& p, bool need_trec, cudaStream_t st,
-                         cudaEvent_t* ev) {
+static int batch_binning(fe_batch* b, const Pipeline& p, cudaStream_t st, cudaEvent_t* ev) {
   const RecSpace& rs = b->rs;
   const RowPlan rp = p.radix ? RowPlan{} : b->rows;
   FE_CUDA(cudaMemsetAsync(rs.ctrl, 0, sizeof(Control), st));
@@ -1172,18 +1160,13 @@ static int batch_binning(fe_batch* b, const Pipeline& p, bool need_trec, cudaStr
     if (ev) FE_CUDA(cudaEventRecord(ev[3], st));
     b->sorted = ks.keys_a;
     if (ev) FE_CUDA(cudaEventRecord(ev[4], st));
-    if (need_trec)
-      launch_ranges_gather(p.va, b->sorted, rs.ctrl, b->cap, rs.recs, p.tile_w, p.tile_h, nullptr,
-                           ks.trec, st);
   } else {
     launch_emit_keys(p.va, rs.incl, rs.rects, p.n_rec, rs.ctrl, ks.keys_a, b->cap, st);
     if (ev) FE_CUDA(cudaEventRecord(ev[3], st));
     b->sorted = launch_sort(ks.keys_a, ks.keys_b, bits_for(p.n_tiles), rs.ctrl, b->cap, ks.hist, st);
     if (ev) FE_CUDA(cudaEventRecord(ev[4], st));
-    launch_ranges_gather(p.va, b->sorted, rs.ctrl, b->cap, rs.recs, p.tile_w, p.tile_h, rs.ranges,
-                         need_trec ? ks.trec : nullptr, st);
+    launch_ranges(b->sorted, rs.ctrl, b->cap, rs.ranges, st);
   }
-  b->trec_ready = need_trec;
   if (ev) FE_CUDA(cudaEventRecord(ev[5], st));
   return FE_OK;
 }
@@ -1230,7 +1213,7 @@ int fe_batch_fwd(fe_batch* b, const float* means, const float* prec, const float
   if (p.n_rec > 0 && (!means || !prec || !logw))
     return fail(FE_ERR_INVALID_ARGUMENT, "NULL Gaussian pointer");
   b->binned = false;
-  int rc = batch_binning(b, p, false, st, nullptr);
+  int rc = batch_binning(b, p, st, nullptr);
   if (rc) return rc;
   note_binning(b, means, prec, logw);
   launch_blend_fwd(p.va, p.tile_w, p.tile_h, p.px, p.chunk, p.n_tiles, b->sorted, b->rs.recs,
@@ -1280,7 +1263,7 @@ int fe_batch_fwd_host(fe_batch* b, const float* h_means, const float* h_prec,
   }
   Pipeline p = batch_pipeline(b, m_d, p_d, w_d);
   b->binned = false;
-  rc = batch_binning(b, p, false, st, nullptr);
+  rc = batch_binning(b, p, st, nullptr);
   if (rc) return rc;
   note_binning(b, m_d, p_d, w_d);
   FE_CUDA(cudaMemsetAsync(ctr, 0, sizeof(uint32_t) * nb, st));
@@ -1325,23 +1308,17 @@ int fe_batch_bwd(fe_batch* b, const float* means, const float* prec, const float
   FE_CUDA(cudaMemsetAsync(glogw, 0, sizeof(float) * (size_t)b->n_gauss, st));
   if (b->keep_binning && b->binned && b->binned_for[0] == means && b->binned_for[1] == prec &&
       b->binned_for[2] == logw) {
-    // Reuse the forward's binning; only the blend's tile counter must start again at zero, and
-    // the gathered tile records are built now if the forward did not need them.
+    // Reuse the forward's binning; only the blend's tile counter must start again at zero.
     FE_CUDA(cudaMemsetAsync(&b->rs.ctrl->next_tile, 0, sizeof(uint32_t), st));
-    if (!b->trec_ready) {
-      launch_ranges_gather(p.va, b->sorted, b->rs.ctrl, b->cap, b->rs.recs, p.tile_w, p.tile_h,
-                           nullptr, b->ks.trec, st);
-      b->trec_ready = true;
-    }
   } else {
     b->binned = false;
-    int rc = batch_binning(b, p, true, st, nullptr);
+    int rc = batch_binning(b, p, st, nullptr);
     if (rc) return rc;
     note_binning(b, means, prec, logw);
   }
   FE_CUDA(cudaMemsetAsync(b->rs.rgrad, 0, sizeof(RecGrad) * (size_t)p.n_rec, st));
   launch_pixel_prep(p.va, p.n_pix, depth, stats, p.n_pix, gdepth, galpha, b->rs.pix, st);
-  launch_blend_bwd(p.va, p.tile_w, p.tile_h, p.n_tiles, b->sorted, b->rs.ranges, b->ks.trec,
+  launch_blend_bwd(p.va, p.tile_w, p.tile_h, p.n_tiles, b->sorted, b->rs.ranges,
                    b->rs.recs, b->rs.pix, p.beta2, p.beta3, b->rs.rgrad, b->rs.ctrl, st);
   launch_record_vjp(p.va, p.n_rec, means, prec, p.quat, p.trans, b->rs.recs, b->rs.rgrad, gmeans,
                     gprec, glogw, st);
@@ -1381,7 +1358,7 @@ int fe_batch_fwd_timed(fe_batch* b, const float* means, const float* prec, const
   cudaEvent_t ev[7];
   for (auto& e : ev) FE_CUDA(cudaEventCreate(&e));
   b->binned = false;
-  int rc = batch_binning(b, p, false, st, ev);
+  int rc = batch_binning(b, p, st, ev);
   if (rc) {
     for (auto& e : ev) cudaEventDestroy(e);
     return rc;
@@ -1523,8 +1500,7 @@ int fe_render_fwd_noalloc(const fe_render_desc* d, const float* means, const flo
     launch_scan(rs.touched, rs.incl, p.n_rec, worst, rs.scan_tmp, rs.ctrl, st);
     launch_emit_keys(p.va, rs.incl, rs.rects, p.n_rec, rs.ctrl, ks.keys_a, worst, st);
     sorted = launch_sort(ks.keys_a, ks.keys_b, bits_for(p.n_tiles), rs.ctrl, worst, ks.hist, st);
-    launch_ranges_gather(p.va, sorted, rs.ctrl, worst, rs.recs, p.tile_w, p.tile_h, rs.ranges,
-                         nullptr, st);
+    launch_ranges(sorted, rs.ctrl, worst, rs.ranges, st);
   }
   launch_blend_fwd(p.va, p.tile_w, p.tile_h, p.px, p.chunk, p.n_tiles, sorted, rs.recs, rs.ranges,
                    p.beta2, p.beta3, depth, alpha, stats, npix, rs.ctrl, st);

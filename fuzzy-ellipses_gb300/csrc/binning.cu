@@ -10,13 +10,12 @@
 //            (rasterizer_impl.cu:287)
 //  ranges    [first, last+1) of every non-empty tile; empty tiles keep {0,0}
 //            (reference: getPerTileRanges, rasterizer_impl.cu:127-152)
-//  gather    re-expands each key's record around its tile into the contiguous, pair-interleaved
-//            tile-record stream the blend reads with TMA bulk copies
+//  tile-major binning (the default where it applies): the keys written directly in sorted order
+//            with their ranges, no scan, emission pass or sort
 //
 // Every kernel reads the key count from device memory and uses a fixed grid, so the sequence
 // needs no host synchronisation and can be captured in a CUDA graph.
 #include "fe_kernels.cuh"
-#include "fe_tilerec.cuh"
 
 namespace fe {
 
@@ -325,119 +324,31 @@ __global__ void sort_scatter_kernel(const uint64_t* __restrict__ in, uint64_t* _
   }
 }
 
-// Gather: each warp takes 32 consecutive sorted keys (16 TilePairs) at a time and works on its
-// own slice of shared memory, so the only barriers are warp barriers.
-constexpr int kGatherWarps = 8;
-constexpr int kGatherThreads = 32 * kGatherWarps;
-constexpr int kGatherParts = (int)(sizeof(GaussRec) / 16);  // 16-byte parts of a GaussRec (6)
-constexpr int kRecWords = 28;  // GaussRec stride in shared memory (96 B + 16 B: conflict-free)
-constexpr int kLoadRecs = 32 / kGatherParts;  // records fetched per cooperative load (5)
+// Tile ranges of a sorted key list, one key per thread: a key whose tile differs from its
+// predecessor's starts its tile's range, one whose tile differs from its successor's ends it.
+// Empty tiles keep their zeroed range.
+constexpr int kRangeThreads = 256;
 
-struct GatherWarpSmem {
-  union {
-    float rec[32 * kRecWords];  // the warp's 32 source records (3.5 KB)
-    TilePair out[16];           // the warp's 16 output pairs (2.5 KB)
-  } u;
-};
-
-// Tile ranges, and every key's tile record, written pair-interleaved. Per 32 keys a warp
-//  - reads the keys (coalesced) and writes the range ends found among them,
-//  - fetches the 32 source records cooperatively: in each round lanes 0..29 read the six
-//    16-byte parts of five records, so a load instruction touches 5 records instead of 32,
-//  - expands each lane's record around its tile and stores it into its slot of the pair,
-//  - writes its 16 pairs (2.5 KB) with one TMA bulk store, which runs while the warp goes on.
-// trec == nullptr computes the ranges only.
-__global__ void __launch_bounds__(kGatherThreads, 4) ranges_gather_kernel(
-    ViewsArg va, const uint64_t* __restrict__ keys, const Control* __restrict__ ctrl,
-    const GaussRec* __restrict__ recs, int tile_w, int tile_h, uint2* __restrict__ ranges,
-    TilePair* __restrict__ trec) {
-  __shared__ __align__(128) GatherWarpSmem wsm[kGatherWarps];
+__global__ void __launch_bounds__(kRangeThreads) ranges_kernel(const uint64_t* __restrict__ keys,
+                                                               const Control* __restrict__ ctrl,
+                                                               uint2* __restrict__ ranges) {
   const unsigned full = 0xffffffffu;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  GatherWarpSmem& sm = wsm[warp];
-  const int sub = lane / kGatherParts, part = lane - sub * kGatherParts;
+  const int lane = threadIdx.x & 31;
   const int64_t K = (int64_t)ctrl->num_keys;
-  const int64_t npairs = (K + 1) >> 1;
-  const float hw = 0.5f * (tile_w - 1), hh = 0.5f * (tile_h - 1);
-  for (int64_t p0 = ((int64_t)blockIdx.x * kGatherWarps + warp) * 16; p0 < npairs;
-       p0 += (int64_t)gridDim.x * kGatherWarps * 16) {
-    const int64_t k = 2 * p0 + lane;  // lane 0's key always exists (2 p0 < K)
+  for (int64_t base = (int64_t)blockIdx.x * kRangeThreads; base < K;
+       base += (int64_t)gridDim.x * kRangeThreads) {
+    const int64_t k = base + threadIdx.x;
     const bool valid = k < K;
-    const uint64_t key = valid ? keys[k] : 0ull;
-    const uint32_t tile = (uint32_t)(key >> 32);
+    const uint32_t tile = valid ? (uint32_t)(keys[k] >> 32) : 0u;
     uint32_t prev = __shfl_up_sync(full, tile, 1);
     uint32_t next = __shfl_down_sync(full, tile, 1);
-    if (valid && ranges != nullptr) {
+    if (valid) {
       if (lane == 0 && k > 0) prev = (uint32_t)(keys[k - 1] >> 32);
       if (lane == 31 && k + 1 < K) next = (uint32_t)(keys[k + 1] >> 32);
       if (k == 0 || prev != tile) ranges[tile].x = (uint32_t)k;
       if (k == K - 1 || next != tile) ranges[tile].y = (uint32_t)(k + 1);
     }
-    if (trec == nullptr) continue;
-
-    // View of each key: the keys are sorted by tile, so the warp's keys almost always share
-    // lane 0's view; lanes past its last tile search for their own.
-    int v0 = 0;
-    if (lane == 0) v0 = find_view<&ViewDev::tile_base>(va, tile);
-    v0 = __shfl_sync(full, v0, 0);
-    int vi = v0;
-    if (va.table != nullptr && v0 + 1 < va.count && valid &&
-        (int64_t)tile >= va.table[v0 + 1].tile_base)
-      vi = find_view<&ViewDev::tile_base>(va, tile);
-    const ViewDev& V = view_at(va, vi);
-    // Tile row and column: a float estimate of lt / gx, corrected by one step (exact while
-    // lt / gx < 2^22).
-    const int lt = (int)(tile - V.tile_base);
-    int ty = (int)((float)lt * rcp_approx((float)V.gx));
-    int tx = lt - ty * V.gx;
-    if (tx < 0) {
-      --ty;
-      tx += V.gx;
-    } else if (tx >= V.gx) {
-      ++ty;
-      tx -= V.gx;
-    }
-    const int64_t src = valid ? V.rec_base + (int64_t)(uint32_t)key : -1;
-
-    if (lane == 0) bulk_wait_group_read0();  // the previous store has read u.out (aliases u.rec)
-    __syncwarp();
-#pragma unroll
-    for (int it = 0; it < (32 + kLoadRecs - 1) / kLoadRecs; ++it) {
-      const int r = kLoadRecs * it + sub;
-      const int64_t s = __shfl_sync(full, src, r & 31);
-      if (lane < kLoadRecs * kGatherParts && r < 32 && s >= 0)
-        *reinterpret_cast<float4*>(&sm.u.rec[r * kRecWords + 4 * part]) =
-            reinterpret_cast<const float4*>(recs + s)[part];
-    }
-    __syncwarp();
-    GaussRec g;
-    if (valid) {
-      float4* gd = reinterpret_cast<float4*>(&g);
-#pragma unroll
-      for (int q = 0; q < kGatherParts; ++q)
-        gd[q] = *reinterpret_cast<const float4*>(&sm.u.rec[lane * kRecWords + 4 * q]);
-    }
-    __syncwarp();  // every record read before u.out (aliased) is written
-
-    TileRec t;
-    if (valid)
-      tile_record(g, tx * tile_w + hw - g.uc, ty * tile_h + hh - g.vc, hw, hh, t);
-    else
-      null_tile_record(t);
-    // Field i of the even lane's record is f[i].x of pair lane/2, of the odd lane's f[i].y.
-    const float* mine = reinterpret_cast<const float*>(&t);
-    float* dst = reinterpret_cast<float*>(&sm.u.out[lane >> 1]) + (lane & 1);
-#pragma unroll
-    for (int i = 0; i < kRecFields; ++i) dst[2 * i] = mine[i];
-    fence_proxy_async_smem();
-    __syncwarp();
-    if (lane == 0) {
-      const int64_t np = min((int64_t)16, npairs - p0);
-      bulk_store_s2g(trec + p0, sm.u.out, (uint32_t)(np * sizeof(TilePair)));
-      bulk_commit_group();
-    }
   }
-  if (trec != nullptr && lane == 0) bulk_wait_group0();
 }
 
 // ---- Tile-major binning ---------------------------------------------------------------------
@@ -698,14 +609,6 @@ uint64_t* launch_sort(uint64_t* a, uint64_t* b, int key_bits, const Control* ctr
   return src;
 }
 
-void launch_ranges_gather(const ViewsArg& va, const uint64_t* keys, const Control* ctrl,
-                          int64_t capacity, const GaussRec* recs, int tile_w, int tile_h,
-                          uint2* ranges, TilePair* trec, cudaStream_t st) {
-  const int grid = grid_for((capacity + 1) / 2, 16 * kGatherWarps,
-                            resident_ctas<ranges_gather_kernel>(kGatherThreads));
-  ranges_gather_kernel<<<grid, kGatherThreads, 0, st>>>(va, keys, ctrl, recs, tile_w, tile_h,
-                                                        ranges, trec);
-}
 
 void launch_tile_binning_emit(const ViewsArg& va, int n_views, int max_gy, const TileRect* rects,
                               const unsigned long long* row_tot, int64_t capacity, Control* ctrl,
@@ -717,11 +620,8 @@ void launch_tile_binning_emit(const ViewsArg& va, int n_views, int max_gy, const
 
 void launch_ranges(const uint64_t* keys, const Control* ctrl, int64_t capacity, uint2* ranges,
                    cudaStream_t st) {
-  ViewsArg va{};
-  const int grid = grid_for((capacity + 1) / 2, 16 * kGatherWarps,
-                            resident_ctas<ranges_gather_kernel>(kGatherThreads));
-  ranges_gather_kernel<<<grid, kGatherThreads, 0, st>>>(va, keys, ctrl, nullptr, 8, 8, ranges,
-                                                        nullptr);
+  ranges_kernel<<<grid_for(capacity, kRangeThreads, 152 * 8), kRangeThreads, 0, st>>>(keys, ctrl,
+                                                                                   ranges);
 }
 
 }  // namespace fe

@@ -20,6 +20,7 @@
 #include <algorithm>
 
 #include "fe_kernels.cuh"
+#include "fe_tilerec.cuh"
 
 namespace fe {
 
@@ -65,8 +66,8 @@ struct alignas(16) BwdSlice {
 template <int TW, int TH>
 __global__ void __launch_bounds__(32 * kBwdWarps) blend_bwd_kernel(
     ViewsArg va, uint32_t n_tiles, const uint64_t* __restrict__ keys,
-    const uint2* __restrict__ ranges, const TilePair* __restrict__ trec,
-    const GaussRec* __restrict__ recs, const float4* __restrict__ pix, float nb2, float beta3,
+    const uint2* __restrict__ ranges, const GaussRec* __restrict__ recs,
+    const float4* __restrict__ pix, float nb2, float beta3,
     float beta2, RecGrad* __restrict__ rgrad, Control* ctrl) {
   using Slice = BwdSlice<TW, TH>;
   __shared__ Slice slices[kBwdWarps];
@@ -120,13 +121,18 @@ __global__ void __launch_bounds__(32 * kBwdWarps) blend_bwd_kernel(
       // S* = sum h du^k with h = -dL/dvsv, Q* = sum dL/dpsv du^k, T* = sum dL/dnq eu^k; the row
       // end maps them onto the basis.
       float gV[6] = {0, 0, 0, 0, 0, 0}, gP[3] = {0, 0, 0}, gN[6] = {0, 0, 0, 0, 0, 0}, gC = 0.f;
-      // Record k lives in slot k%2 of pair k/2 (field i at float offset 2*i + slot).
-      const float* tf = reinterpret_cast<const float*>(trec + (k >> 1)) + (k & 1);
       if (active) {
-        const float V0 = tf[0], V1 = tf[2], V2 = tf[4], V3 = tf[6], V4 = tf[8], V5 = tf[10];
-        const float P0 = tf[12], P1 = tf[14], P2 = tf[16];
-        const float N0 = tf[18], N1 = tf[20], N2 = tf[22], N3 = tf[24], N4 = tf[26], N5 = tf[28];
-        const float C = tf[30], cu = tf[32], cvv = tf[34];
+        // The key's tile record, built from its Gaussian record as the forward blend builds it.
+        TileRec t;
+        {
+          const GaussRec g = recs[V.rec_base + (uint32_t)keys[k]];
+          const float hw = 0.5f * (TW - 1), hh = 0.5f * (TH - 1);
+          tile_record(g, tx * TW + hw - g.uc, ty * TH + hh - g.vc, hw, hh, t);
+        }
+        const float V0 = t.V[0], V1 = t.V[1], V2 = t.V[2], V3 = t.V[3], V4 = t.V[4], V5 = t.V[5];
+        const float P0 = t.P[0], P1 = t.P[1], P2 = t.P[2];
+        const float N0 = t.N[0], N1 = t.N[1], N2 = t.N[2], N3 = t.N[3], N4 = t.N[4], N5 = t.N[5];
+        const float C = t.C, cu = t.cu, cvv = t.cv;
         const f2_t V3p = f2_pack(V3, V3), P1p = f2_pack(P1, P1), N3p = f2_pack(N3, N3);
         const f2_t Cp = f2_pack(C, C), CUp = f2_pack(cu, cu);
         for (int ly = sub; ly < ys; ly += s) {
@@ -243,11 +249,11 @@ __global__ void __launch_bounds__(32 * kBwdWarps) blend_bwd_kernel(
       if (!active || sub != 0) continue;
       const uint32_t gid = (uint32_t)keys[k];
 
-      // Back through the tile re-expansion (binning.cu tile_record) to record space.
+      // Back through the tile re-expansion (fe_tilerec.cuh tile_record) to record space.
       const GaussRec g = recs[V.rec_base + gid];
       const float tcx = tx * TW + 0.5f * (TW - 1), tcy = ty * TH + 0.5f * (TH - 1);
       const float du = tcx - g.uc, dv = tcy - g.vc;
-      // Same choice of expansion centre as the gather (binning.cu tile_record).
+      // Same choice of expansion centre as tile_record.
       const bool near = fabsf(du) <= kNearCentre && fabsf(dv) <= kNearCentre;
       const float kn = -0.5f * kLog2e;
       float a0[3], y0[3];
@@ -383,15 +389,13 @@ __global__ void record_vjp_kernel(ViewsArg va, int64_t n_rec, const float* __res
 
 template <int TW, int TH>
 void launch_bwd_tiles(const ViewsArg& va, int64_t n_tiles, const uint64_t* keys,
-                      const uint2* ranges, const TilePair* trec, const GaussRec* recs,
-                      const float4* pix, float beta2, float beta3, RecGrad* rgrad, Control* ctrl,
-                      cudaStream_t st) {
+                      const uint2* ranges, const GaussRec* recs, const float4* pix, float beta2,
+                      float beta3, RecGrad* rgrad, Control* ctrl, cudaStream_t st) {
   constexpr auto kern = blend_bwd_kernel<TW, TH>;
   const int resident = resident_ctas<kern>(32 * kBwdWarps);
   const int64_t grid =
       std::max<int64_t>(1, std::min<int64_t>((n_tiles + kBwdWarps - 1) / kBwdWarps, resident));
-  kern<<<(unsigned)grid, 32 * kBwdWarps, 0, st>>>(va, (uint32_t)n_tiles, keys, ranges, trec, recs,
-                                                  pix, -beta2 * kLog2e, beta3, beta2, rgrad, ctrl);
+  kern<<<(unsigned)grid, 32 * kBwdWarps, 0, st>>>(va, (uint32_t)n_tiles, keys, ranges, recs, pix, -beta2 * kLog2e, beta3, beta2, rgrad, ctrl);
 }
 
 }  // namespace
@@ -407,16 +411,16 @@ void launch_pixel_prep(const ViewsArg& va, int64_t n_pix, const float* depth, co
 }
 
 void launch_blend_bwd(const ViewsArg& va, int tile_w, int tile_h, int64_t n_tiles,
-                      const uint64_t* keys, const uint2* ranges, const TilePair* trec,
-                      const GaussRec* recs, const float4* pix, float beta2, float beta3,
-                      RecGrad* rgrad, Control* ctrl, cudaStream_t st) {
+                      const uint64_t* keys, const uint2* ranges, const GaussRec* recs,
+                      const float4* pix, float beta2, float beta3, RecGrad* rgrad, Control* ctrl,
+                      cudaStream_t st) {
   if (n_tiles <= 0) return;
   if (tile_w == 8 && tile_h == 8)
-    launch_bwd_tiles<8, 8>(va, n_tiles, keys, ranges, trec, recs, pix, beta2, beta3, rgrad, ctrl, st);
+    launch_bwd_tiles<8, 8>(va, n_tiles, keys, ranges, recs, pix, beta2, beta3, rgrad, ctrl, st);
   else if (tile_w == 32 && tile_h == 8)
-    launch_bwd_tiles<32, 8>(va, n_tiles, keys, ranges, trec, recs, pix, beta2, beta3, rgrad, ctrl, st);
+    launch_bwd_tiles<32, 8>(va, n_tiles, keys, ranges, recs, pix, beta2, beta3, rgrad, ctrl, st);
   else
-    launch_bwd_tiles<16, 16>(va, n_tiles, keys, ranges, trec, recs, pix, beta2, beta3, rgrad, ctrl, st);
+    launch_bwd_tiles<16, 16>(va, n_tiles, keys, ranges, recs, pix, beta2, beta3, rgrad, ctrl, st);
 }
 
 void launch_record_vjp(const ViewsArg& va, int64_t n_rec, const float* means, const float* prec,

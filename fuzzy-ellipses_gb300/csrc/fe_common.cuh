@@ -206,26 +206,6 @@ __device__ __forceinline__ void fence_proxy_async_smem() {
   asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
 }
 
-// 1-D TMA bulk store shared -> global (16-byte aligned addresses, size a multiple of 16), tracked
-// by the issuing thread's bulk async-groups.
-__device__ __forceinline__ void bulk_store_s2g(void* gmem_dst, const void* smem_src,
-                                               uint32_t bytes) {
-  asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(gmem_dst),
-               "r"(smem_addr(smem_src)), "r"(bytes)
-               : "memory");
-}
-__device__ __forceinline__ void bulk_commit_group() {
-  asm volatile("cp.async.bulk.commit_group;" ::: "memory");
-}
-// Wait until every committed bulk store has finished reading its shared-memory source.
-__device__ __forceinline__ void bulk_wait_group_read0() {
-  asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
-}
-// Wait until every committed bulk store has completed.
-__device__ __forceinline__ void bulk_wait_group0() {
-  asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
-}
-
 __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
   uint32_t done;
   asm volatile(

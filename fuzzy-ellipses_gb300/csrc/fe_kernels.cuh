@@ -36,11 +36,6 @@ void launch_emit_keys(const ViewsArg& va, const uint32_t* incl, const TileRect* 
 // result (a or b). hist: 256 * (sort_grid(capacity) + 1) uint32.
 uint64_t* launch_sort(uint64_t* a, uint64_t* b, int key_bits, const Control* ctrl,
                       int64_t capacity, uint32_t* hist, cudaStream_t st);
-// Tile ranges (ranges must be zeroed beforehand; NULL skips them) and the tile-local record
-// stream, key k at trec[k/2] slot k%2 (capacity/2 rounded up pairs).
-void launch_ranges_gather(const ViewsArg& va, const uint64_t* keys, const Control* ctrl,
-                          int64_t capacity, const GaussRec* recs, int tile_w, int tile_h,
-                          uint2* ranges, TilePair* trec, cudaStream_t st);
 // Tile-major binning for views at most kMaxRowTiles tiles wide. launch_preprocess with row_tot
 // (n_views * (max_gy + 1) zeroed entries, view v's at v * (max_gy + 1)) records every rectangle's
 // width as a difference of its view's row key counts (+w at row y0, -w at row y1) and adds the
@@ -53,7 +48,7 @@ constexpr int kMaxRowTiles = 1024;
 void launch_tile_binning_emit(const ViewsArg& va, int n_views, int max_gy, const TileRect* rects,
                               const unsigned long long* row_tot, int64_t capacity, Control* ctrl,
                               uint2* ranges, uint64_t* keys, cudaStream_t st);
-// Ranges only (reference-compatible binning).
+// Tile ranges of the sorted keys (ranges zeroed beforehand; empty tiles keep {0,0}).
 void launch_ranges(const uint64_t* keys, const Control* ctrl, int64_t capacity, uint2* ranges,
                    cudaStream_t st);
 
@@ -78,10 +73,11 @@ void launch_blend_fwd_band(const ViewsArg& va, int tile_w, int tile_h, int px, i
 void launch_pixel_prep(const ViewsArg& va, int64_t n_pix, const float* depth, const float* stats,
                        int64_t stats_stride, const float* grad_depth, const float* grad_alpha,
                        float4* pix, cudaStream_t st);
+// Tile records are built per key from the Gaussian records (fe_tilerec.cuh), as in the forward.
 void launch_blend_bwd(const ViewsArg& va, int tile_w, int tile_h, int64_t n_tiles,
-                      const uint64_t* keys, const uint2* ranges, const TilePair* trec,
-                      const GaussRec* recs, const float4* pix, float beta2, float beta3,
-                      RecGrad* rgrad, Control* ctrl, cudaStream_t st);
+                      const uint64_t* keys, const uint2* ranges, const GaussRec* recs,
+                      const float4* pix, float beta2, float beta3, RecGrad* rgrad, Control* ctrl,
+                      cudaStream_t st);
 // Gradients are accumulated (atomically) into gmeans/gprec/glogw, which must be zeroed first.
 void launch_record_vjp(const ViewsArg& va, int64_t n_rec, const float* means, const float* prec,
                        const float* quat, const float* trans, const GaussRec* recs,
@@ -137,7 +133,7 @@ void launch_render_pixels(int n, int n_poses, const float* means, const float* p
 // features.cu
 // Softmax-weighted features (nf per Gaussian) of an image render from the forward's statistics.
 void launch_features(const ViewsArg& va, int tile_w, int tile_h, int64_t n_tiles,
-                     const uint64_t* keys, const uint2* ranges, const TilePair* trec,
+                     const uint64_t* keys, const uint2* ranges, const GaussRec* recs,
                      const float* stats, int64_t stats_stride, float beta2, float beta3,
                      const float* feats, int nf, float* out, Control* ctrl, cudaStream_t st);
 

@@ -7,10 +7,12 @@
 // (softmax maximum m and normaliser W, base 2), so w_i = 2^(l_i - m) / W for the tile's front
 // Gaussians. Persistent warps take tiles from the device counter; each lane owns TW*TH/32 pixels
 // of the tile, re-evaluates every key's logit there and accumulates four features at a time
-// (the Gaussian index comes from the sorted key, the feature row from global memory).
+// (the Gaussian index comes from the sorted key, the feature row from global memory). The keys'
+// tile records are built 32 at a time, one per lane, into the warp's shared memory.
 #include <algorithm>
 
 #include "fe_kernels.cuh"
+#include "fe_tilerec.cuh"
 
 namespace fe {
 namespace {
@@ -21,12 +23,16 @@ constexpr int kFeatChunk = 4;
 template <int TW, int TH>
 __global__ void __launch_bounds__(32 * kFeatWarps) features_kernel(
     ViewsArg va, uint32_t n_tiles, const uint64_t* __restrict__ keys,
-    const uint2* __restrict__ ranges, const TilePair* __restrict__ trec,
+    const uint2* __restrict__ ranges, const GaussRec* __restrict__ recs,
     const float* __restrict__ stats, int64_t stride, float nb2, float beta3,
     const float* __restrict__ feats, int nf, float* __restrict__ out, Control* ctrl) {
   constexpr int NPX = TW * TH / 32;  // pixels per lane
+  __shared__ TileRec rec_buf[kFeatWarps][32];
+  __shared__ uint32_t gid_buf[kFeatWarps][32];
   const unsigned full = 0xffffffffu;
   const int lane = threadIdx.x & 31;
+  TileRec* wrec = rec_buf[threadIdx.x >> 5];
+  uint32_t* wgid = gid_buf[threadIdx.x >> 5];
   for (;;) {
     uint32_t tile = 0;
     if (lane == 0) tile = atomicAdd(&ctrl->next_tile, 1u);
@@ -61,33 +67,44 @@ __global__ void __launch_bounds__(32 * kFeatWarps) features_kernel(
       for (int i = 0; i < NPX; ++i)
 #pragma unroll
         for (int j = 0; j < kFeatChunk; ++j) acc[i][j] = 0.f;
-      for (uint32_t k = range.x; k < range.y; ++k) {
-        // Record k lives in slot k%2 of pair k/2 (field i at float offset 2*i + slot).
-        const float* tf = reinterpret_cast<const float*>(trec + (k >> 1)) + (k & 1);
-        const float V0 = tf[0], V1 = tf[2], V2 = tf[4], V3 = tf[6], V4 = tf[8], V5 = tf[10];
-        const float P0 = tf[12], P1 = tf[14], P2 = tf[16];
-        const float N0 = tf[18], N1 = tf[20], N2 = tf[22], N3 = tf[24], N4 = tf[26], N5 = tf[28];
-        const float C = tf[30], cu = tf[32], cv = tf[34];
-        const uint32_t gid = (uint32_t)keys[k];
-        const float* fr = feats + (int64_t)gid * nf + c0;
-        float f[kFeatChunk];
+      for (uint32_t k0 = range.x; k0 < range.y; k0 += 32) {
+        const int nk = (int)min(32u, range.y - k0);
+        __syncwarp();  // the previous keys' records are no longer read
+        if (lane < nk) {
+          const uint32_t g_id = (uint32_t)keys[k0 + lane];
+          const GaussRec g = recs[V.rec_base + g_id];
+          const float hw = 0.5f * (TW - 1), hh = 0.5f * (TH - 1);
+          tile_record(g, tx * TW + hw - g.uc, ty * TH + hh - g.vc, hw, hh, wrec[lane]);
+          wgid[lane] = g_id;
+        }
+        __syncwarp();
+        for (int kj = 0; kj < nk; ++kj) {
+          const TileRec& tr = wrec[kj];
+          const float V0 = tr.V[0], V1 = tr.V[1], V2 = tr.V[2], V3 = tr.V[3], V4 = tr.V[4];
+          const float V5 = tr.V[5], P0 = tr.P[0], P1 = tr.P[1], P2 = tr.P[2];
+          const float N0 = tr.N[0], N1 = tr.N[1], N2 = tr.N[2], N3 = tr.N[3], N4 = tr.N[4];
+          const float N5 = tr.N[5], C = tr.C, cu = tr.cu, cv = tr.cv;
+          const uint32_t gid = wgid[kj];
+          const float* fr = feats + (int64_t)gid * nf + c0;
+          float f[kFeatChunk];
 #pragma unroll
-        for (int j = 0; j < kFeatChunk; ++j) f[j] = j < cn ? fr[j] : 0.f;
+          for (int j = 0; j < kFeatChunk; ++j) f[j] = j < cn ? fr[j] : 0.f;
 #pragma unroll
-        for (int i = 0; i < NPX; ++i) {
-          const float u = du[i], v = dv[i];
-          const float vsv = fmaf(fmaf(V3, u, fmaf(V4, v, V1)), u, fmaf(fmaf(V5, v, V2), v, V0));
-          const float psv = fmaf(P1, u, fmaf(P2, v, P0));
-          const float eu = u - cu, ev = v - cv;
-          const float nq = fmaf(fmaf(N3, eu, fmaf(N4, ev, N1)), eu, fmaf(fmaf(N5, ev, N2), ev, N0));
-          const float qi = rcp_approx(vsv);
-          const float z = psv * qi;
-          const float s2 = fmaf(nq, qi, C);
-          const float l = fmaf(beta3, s2, nb2 * z);
-          // (a pixel without front Gaussians has W = 0 and m at the forward's sentinel)
-          const float e = (z > 0.f && iw[i] > 0.f) ? ex2_approx(l - m[i]) * iw[i] : 0.f;
+          for (int i = 0; i < NPX; ++i) {
+            const float u = du[i], v = dv[i];
+            const float vsv = fmaf(fmaf(V3, u, fmaf(V4, v, V1)), u, fmaf(fmaf(V5, v, V2), v, V0));
+            const float psv = fmaf(P1, u, fmaf(P2, v, P0));
+            const float eu = u - cu, ev = v - cv;
+            const float nq = fmaf(fmaf(N3, eu, fmaf(N4, ev, N1)), eu, fmaf(fmaf(N5, ev, N2), ev, N0));
+            const float qi = rcp_approx(vsv);
+            const float z = psv * qi;
+            const float s2 = fmaf(nq, qi, C);
+            const float l = fmaf(beta3, s2, nb2 * z);
+            // (a pixel without front Gaussians has W = 0 and m at the forward's sentinel)
+            const float e = (z > 0.f && iw[i] > 0.f) ? ex2_approx(l - m[i]) * iw[i] : 0.f;
 #pragma unroll
-          for (int j = 0; j < kFeatChunk; ++j) acc[i][j] = fmaf(e, f[j], acc[i][j]);
+            for (int j = 0; j < kFeatChunk; ++j) acc[i][j] = fmaf(e, f[j], acc[i][j]);
+          }
         }
       }
 #pragma unroll
@@ -100,14 +117,14 @@ __global__ void __launch_bounds__(32 * kFeatWarps) features_kernel(
 
 template <int TW, int TH>
 void launch_tiles(const ViewsArg& va, int64_t n_tiles, const uint64_t* keys, const uint2* ranges,
-                  const TilePair* trec, const float* stats, int64_t stride, float beta2,
+                  const GaussRec* recs, const float* stats, int64_t stride, float beta2,
                   float beta3, const float* feats, int nf, float* out, Control* ctrl,
                   cudaStream_t st) {
   constexpr auto kern = features_kernel<TW, TH>;
   const int resident = resident_ctas<kern>(32 * kFeatWarps);
   const int64_t grid =
       std::max<int64_t>(1, std::min<int64_t>((n_tiles + kFeatWarps - 1) / kFeatWarps, resident));
-  kern<<<(unsigned)grid, 32 * kFeatWarps, 0, st>>>(va, (uint32_t)n_tiles, keys, ranges, trec,
+  kern<<<(unsigned)grid, 32 * kFeatWarps, 0, st>>>(va, (uint32_t)n_tiles, keys, ranges, recs,
                                                    stats, stride, -beta2 * kLog2e, beta3, feats,
                                                    nf, out, ctrl);
 }
@@ -115,18 +132,18 @@ void launch_tiles(const ViewsArg& va, int64_t n_tiles, const uint64_t* keys, con
 }  // namespace
 
 void launch_features(const ViewsArg& va, int tile_w, int tile_h, int64_t n_tiles,
-                     const uint64_t* keys, const uint2* ranges, const TilePair* trec,
+                     const uint64_t* keys, const uint2* ranges, const GaussRec* recs,
                      const float* stats, int64_t stats_stride, float beta2, float beta3,
                      const float* feats, int nf, float* out, Control* ctrl, cudaStream_t st) {
   if (n_tiles <= 0 || nf <= 0) return;
   if (tile_w == 8 && tile_h == 8)
-    launch_tiles<8, 8>(va, n_tiles, keys, ranges, trec, stats, stats_stride, beta2, beta3, feats,
+    launch_tiles<8, 8>(va, n_tiles, keys, ranges, recs, stats, stats_stride, beta2, beta3, feats,
                        nf, out, ctrl, st);
   else if (tile_w == 32 && tile_h == 8)
-    launch_tiles<32, 8>(va, n_tiles, keys, ranges, trec, stats, stats_stride, beta2, beta3,
+    launch_tiles<32, 8>(va, n_tiles, keys, ranges, recs, stats, stats_stride, beta2, beta3,
                         feats, nf, out, ctrl, st);
   else
-    launch_tiles<16, 16>(va, n_tiles, keys, ranges, trec, stats, stats_stride, beta2, beta3,
+    launch_tiles<16, 16>(va, n_tiles, keys, ranges, recs, stats, stats_stride, beta2, beta3,
                          feats, nf, out, ctrl, st);
 }
 

@@ -367,9 +367,10 @@ int fe_bench_peak(int kind, int iters, double *ops_per_second, fe_stream_t strea
  * rasterizer_impl.cu:47-79). For callers that cannot allocate during a call, e.g. an XLA custom
  * call under XLA's preallocating allocator.
  *   Limit: requests whose worst-case scratch (n_gaussians x tiles keys) exceeds
- *     FE_NOALLOC_SCRATCH_BYTES return FE_ERR_SCRATCH_LIMIT before any device work (96 bytes
- *     per Gaussian-tile pair, about 1.39M pairs: 1000 Gaussians on a 640x480 image with 16x16
- *     tiles fit, 1200 do not).
+ *     FE_NOALLOC_SCRATCH_BYTES return FE_ERR_SCRATCH_LIMIT before any device work (16 bytes
+ *     per Gaussian-tile pair -- the key and its radix-sort twin -- plus small per-Gaussian and
+ *     per-tile terms, about 8.3M pairs: 6000 Gaussians on a 640x480 image with 16x16 tiles fit,
+ *     7000 do not).
  *   Set-up: the first call on a device resolves the array's address (cudaGetSymbolAddress) and
  *     loads the library's kernels; make it during set-up, before any stream capture begins.
  *   Concurrency: one scratch per device, so calls on one device must not overlap -- issue them

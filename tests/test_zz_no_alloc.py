@@ -101,14 +101,14 @@ def test_noalloc_smaller_request_then_larger_again(cuda_device):
 
 def test_noalloc_rejects_requests_beyond_the_fixed_scratch(cuda_device):
     rng = np.random.default_rng(12)
-    scene = S.random_gaussians(1200, 0.1, rng)  # 1200 x 1200 tiles: over the fixed scratch
+    scene = S.random_gaussians(7000, 0.1, rng)  # 7000 x 1200 tiles: over the fixed scratch
     cam = S.config1(seed=0)[1][0]
     sd = scene_to_dev(scene, cuda_device)
     outs = _outputs(cam.height, cam.width, cuda_device)
     rc = _call("fe_render_fwd_noalloc", sd, cam, _desc(scene, cam), outs)
     assert rc == FE_ERR_SCRATCH_LIMIT
     msg = N.load().fe_last_error_message().decode()
-    assert "1200 Gaussians" in msg and str(128 << 20) in msg
+    assert "7000 Gaussians" in msg and str(128 << 20) in msg
     assert torch.isnan(outs[1]).all()  # nothing was launched
     # The same request through the arena entry still works.
     assert _call("fe_render_fwd", sd, cam, _desc(scene, cam), outs) == 0
