@@ -64,6 +64,9 @@ def parse():
                     help="build the workload, warm up, run one batched forward step, then one "
                          "forward with statistics and its backward, and exit (the command the "
                          "committed ncu summaries capture)")
+    ap.add_argument("--binning", choices=["tiles", "radix"], default="tiles",
+                    help="binning of the batched step: tile-major (default) or key emission + "
+                         "radix sort (to profile the sort path)")
     return ap.parse_args()
 
 
@@ -292,7 +295,7 @@ def main():
         tuned = tuner.tune([(0, scene.n)], views, m, p, w, reps=3)
         cfg = {k: tuned[k] for k in ("tile", "px", "chunk")}
     batch = fe.Batch([(0, scene.n)], views, tile=cfg["tile"], px=cfg["px"], chunk=cfg["chunk"],
-                     keep_binning=True)
+                     keep_binning=True, binning=args.binning)
     per_cam_evals = count_evals(fe, cams, mpw) if not args.profile_step else [0] * len(cams)
     e_step = float(sum(per_cam_evals))
     depth = torch.empty(batch.n_pixels, device=dev)
@@ -522,6 +525,8 @@ def main():
         "config": {"workload": WORKLOAD, "step": "batched forward of all 16 cameras",
                    "tile": f"{cfg['tile'][0]}x{cfg['tile'][1]}", "px_per_thread": cfg["px"],
                    "chunk_pairs": cfg["chunk"], "autotuned": tuned is not None,
+                   "binning": "tile-major (keys emitted in sorted order)" if args.binning == "tiles"
+                   else "key emission + radix sort",
                    "launch": "CUDA graph replay of the batched forward (captured once)",
                    "eager_ms_per_step": eager_ms,
                    "l2": "flushed between steps (256 MiB write outside the per-step CUDA "
