@@ -55,7 +55,7 @@ size_t key_budget_bytes() {
   return v;
 }
 
-// Bytes of key-proportional scratch per key: two key buffers and one tile record.
+// Bytes of key-proportional scratch per key: the key and its radix-sort twin.
 constexpr size_t kBytesPerKey = 2 * sizeof(uint64_t);
 
 int bits_for(int64_t n) {

@@ -171,3 +171,48 @@ def test_forward_host_bands_within_and_across_views(cuda_device):
     rev = [dict(v, pixel_offset=int(o)) for v, o in zip(views[:5], offs)]
     b2 = fe.Batch([(0, scene.n)], rev, tile=(32, 8))
     _host_forward_matches(b2, m, p, w)
+
+
+_OVERFLOW_CHILD = r"""
+import sys, json
+sys.path[:0] = sys.argv[1:3]
+import numpy as np, torch
+import fuzzy_ellipses as fe
+from fuzzy_ellipses import synthetic as S
+scene, cams = S.config1(seed=0)
+dev = torch.device("cuda")
+m, p, w = [torch.from_numpy(x).to(dev) for x in (scene.means, scene.prec, scene.logw)]
+views = [dict(scene=0, height=c.height, width=c.width, fx=c.fx, fy=c.fy, cx=c.cx, cy=c.cy,
+              quat=c.quat, trans=c.trans) for c in cams[:4]]
+out = {}
+for binning in ("tiles", "radix"):
+    b = fe.Batch([(0, scene.n)], views, binning=binning)
+    d, a = b.forward(m, p, w)
+    torch.cuda.synchronize()
+    st = b.status()
+    out[binning] = dict(st, finite=bool(torch.isfinite(d).all() and torch.isfinite(a).all()))
+print(json.dumps(out))
+"""
+
+
+def test_key_overflow_is_flagged_on_both_binning_paths(cuda_device):
+    """With a key budget far below the keys a batch needs (FE_KEY_BUDGET_BYTES, read once per
+    process, so in a child process), both binnings keep the first keys that fit, set the
+    capacity error bit, report the needed count, and render without faulting."""
+    import json
+    import os
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    env = dict(os.environ, FE_KEY_BUDGET_BYTES=str(1 << 20))  # 65,536 keys of 16 B
+    r = subprocess.run([sys.executable, "-c", _OVERFLOW_CHILD, root,
+                        os.path.join(root, "fuzzy-ellipses_gb300")],
+                       env=env, capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr[-2000:]
+    out = json.loads(r.stdout.strip().splitlines()[-1])
+    for binning, st in out.items():
+        assert st["num_keys"] == 1 << 16, (binning, st)
+        assert st["want_keys"] > st["num_keys"], (binning, st)
+        assert st["device_error"] & 1, (binning, st)  # FE_DEVERR_CAPACITY
+        assert st["finite"], (binning, st)
+    assert out["tiles"]["want_keys"] == out["radix"]["want_keys"]
