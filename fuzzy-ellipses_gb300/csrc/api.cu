@@ -1386,6 +1386,10 @@ int fe_batch_fwd_timed(fe_batch* b, const float* means, const float* prec, const
 
 int fe_batch_launch_count(const fe_batch* b) {
   if (!b) return 0;
+  const bool radix = (b->desc.flags & FE_FLAG_RADIX_BINNING) != 0;
+  // Tile-major binning: preprocess, emission, blend.
+  if (b->rows.ok && !radix) return 3;
+  // Emit + sort: preprocess, scan, emission, three kernels per radix pass, ranges, blend.
   const int passes = (bits_for(b->n_tiles) + 7) / 8;
   const int scan = b->n_rec <= 65536 ? 1 : 3;
   return 1 + scan + 1 + 3 * passes + 1 + 1;
