@@ -111,7 +111,6 @@ struct RecSpace {
   unsigned long long* scan_tmp;
   uint2* ranges;
   unsigned long long* row_tot;  // tile-major binning: row key-count differences per view
-  float4* pix;     // backward only
   RecGrad* rgrad;  // backward only
 };
 
@@ -134,7 +133,6 @@ size_t carve_rec(char* base, int64_t n_rec, int64_t n_tiles, int64_t n_pix, bool
   s.scan_tmp = c.take<unsigned long long>(scan_grid(std::max(n_rec, n_tiles)));
   s.ranges = c.take<uint2>(n_tiles);
   s.row_tot = c.take<unsigned long long>(n_tiles + 1);
-  s.pix = bwd ? c.take<float4>(n_pix) : nullptr;
   s.rgrad = bwd ? c.take<RecGrad>(n_rec) : nullptr;
   out(s);
   return c.off;
@@ -443,9 +441,8 @@ int fe_render_bwd(const fe_render_desc* d, const float* means, const float* prec
                    sorted);
   if (rc) return rc;
   FE_CUDA(cudaMemsetAsync(rs.rgrad, 0, sizeof(RecGrad) * (size_t)p.n_rec, st));
-  launch_pixel_prep(p.va, p.n_pix, depth, stats, p.n_pix, gdepth, galpha, rs.pix, st);
-  launch_blend_bwd(p.va, p.tile_w, p.tile_h, p.n_tiles, sorted, rs.ranges, rs.recs,
-                   rs.pix, p.beta2, p.beta3, rs.rgrad, rs.ctrl, st);
+  launch_blend_bwd(p.va, p.tile_w, p.tile_h, p.n_tiles, sorted, rs.ranges, rs.recs, depth,
+                   stats, p.n_pix, gdepth, galpha, p.beta2, p.beta3, rs.rgrad, rs.ctrl, st);
   launch_record_vjp(p.va, p.n_rec, means, prec, quat, trans, rs.recs, rs.rgrad, gmeans, gprec,
                     glogw, st);
   FE_CUDA(cudaGetLastError());
@@ -1327,9 +1324,9 @@ int fe_batch_bwd(fe_batch* b, const float* means, const float* prec, const float
     note_binning(b, means, prec, logw);
   }
   FE_CUDA(cudaMemsetAsync(b->rs.rgrad, 0, sizeof(RecGrad) * (size_t)p.n_rec, st));
-  launch_pixel_prep(p.va, p.n_pix, depth, stats, p.n_pix, gdepth, galpha, b->rs.pix, st);
-  launch_blend_bwd(p.va, p.tile_w, p.tile_h, p.n_tiles, b->sorted, b->rs.ranges,
-                   b->rs.recs, b->rs.pix, p.beta2, p.beta3, b->rs.rgrad, b->rs.ctrl, st);
+  launch_blend_bwd(p.va, p.tile_w, p.tile_h, p.n_tiles, b->sorted, b->rs.ranges, b->rs.recs,
+                   depth, stats, p.n_pix, gdepth, galpha, p.beta2, p.beta3, b->rs.rgrad,
+                   b->rs.ctrl, st);
   launch_record_vjp(p.va, p.n_rec, means, prec, p.quat, p.trans, b->rs.recs, b->rs.rgrad, gmeans,
                     gprec, glogw, st);
   FE_CUDA(cudaGetLastError());

@@ -26,19 +26,6 @@ namespace fe {
 
 namespace {
 
-__global__ void pixel_prep_kernel(ViewsArg va, int64_t n_pix, const float* __restrict__ depth,
-                                  const float* __restrict__ stats, int64_t stride,
-                                  const float* __restrict__ gdepth,
-                                  const float* __restrict__ galpha, float4* __restrict__ pix) {
-  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < n_pix;
-       p += (int64_t)gridDim.x * blockDim.x) {
-    const float m = stats[p], W = stats[stride + p], A = stats[2 * stride + p];
-    const float gD = gdepth ? gdepth[p] : 0.f;
-    const float gA = galpha ? galpha[p] : 0.f;
-    pix[p] = make_float4(depth[p], m, W > 0.f ? gD / W : 0.f, gA * expf(-A));
-  }
-}
-
 __device__ __forceinline__ void red_add_v4(float* addr, float a, float b, float c, float d) {
   asm volatile("red.global.add.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(addr), "f"(a), "f"(b),
                "f"(c), "f"(d)
@@ -67,7 +54,8 @@ template <int TW, int TH>
 __global__ void __launch_bounds__(32 * kBwdWarps) blend_bwd_kernel(
     ViewsArg va, uint32_t n_tiles, const uint64_t* __restrict__ keys,
     const uint2* __restrict__ ranges, const GaussRec* __restrict__ recs,
-    const float4* __restrict__ pix, float nb2, float beta3,
+    const float* __restrict__ depth, const float* __restrict__ stats, int64_t stride,
+    const float* __restrict__ gdepth, const float* __restrict__ galpha, float nb2, float beta3,
     float beta2, RecGrad* __restrict__ rgrad, Control* ctrl) {
   using Slice = BwdSlice<TW, TH>;
   __shared__ Slice slices[kBwdWarps];
@@ -92,15 +80,20 @@ __global__ void __launch_bounds__(32 * kBwdWarps) blend_bwd_kernel(
     const int xs = min(TW, V.W - tx * TW), ys = min(TH, V.H - ty * TH);
 
     __syncwarp();  // the previous tile's readers are done with the slice
+    // The tile's per-pixel data from the forward's outputs and statistics and the cotangents:
+    // depth, softmax max m, dL/ddepth / W, dL/dalpha (1 - alpha) with 1 - alpha = exp(-A).
     for (int q = lane; q < TW * TH; q += 32) {
       const int ly = q / TW, lx = q - ly * TW;
       if (lx < xs && ly < ys) {
-        const float4 v = pix[V.pix_base + (int64_t)(ty * TH + ly) * V.W + tx * TW + lx];
+        const int64_t pi = V.pix_base + (int64_t)(ty * TH + ly) * V.W + tx * TW + lx;
+        const float m = stats[pi], W = stats[stride + pi], A = stats[2 * stride + pi];
+        const float gD = gdepth ? gdepth[pi] : 0.f;
+        const float gA = galpha ? galpha[pi] : 0.f;
         const int o = ly * Slice::ROW + lx;
-        sl.plane[0][o] = v.x;
-        sl.plane[1][o] = v.y;
-        sl.plane[2][o] = v.z;
-        sl.plane[3][o] = v.w;
+        sl.plane[0][o] = depth[pi];
+        sl.plane[1][o] = m;
+        sl.plane[2][o] = W > 0.f ? gD / W : 0.f;
+        sl.plane[3][o] = gA * expf(-A);
       }
     }
     __syncwarp();
@@ -389,38 +382,38 @@ __global__ void record_vjp_kernel(ViewsArg va, int64_t n_rec, const float* __res
 
 template <int TW, int TH>
 void launch_bwd_tiles(const ViewsArg& va, int64_t n_tiles, const uint64_t* keys,
-                      const uint2* ranges, const GaussRec* recs, const float4* pix, float beta2,
-                      float beta3, RecGrad* rgrad, Control* ctrl, cudaStream_t st) {
+                      const uint2* ranges, const GaussRec* recs, const float* depth,
+                      const float* stats, int64_t stride, const float* gdepth,
+                      const float* galpha, float beta2, float beta3, RecGrad* rgrad,
+                      Control* ctrl, cudaStream_t st) {
   constexpr auto kern = blend_bwd_kernel<TW, TH>;
   const int resident = resident_ctas<kern>(32 * kBwdWarps);
   const int64_t grid =
       std::max<int64_t>(1, std::min<int64_t>((n_tiles + kBwdWarps - 1) / kBwdWarps, resident));
-  kern<<<(unsigned)grid, 32 * kBwdWarps, 0, st>>>(va, (uint32_t)n_tiles, keys, ranges, recs, pix, -beta2 * kLog2e, beta3, beta2, rgrad, ctrl);
+  kern<<<(unsigned)grid, 32 * kBwdWarps, 0, st>>>(va, (uint32_t)n_tiles, keys, ranges, recs, depth,
+                                                  stats, stride, gdepth, galpha, -beta2 * kLog2e,
+                                                  beta3, beta2, rgrad, ctrl);
 }
 
 }  // namespace
 
-void launch_pixel_prep(const ViewsArg& va, int64_t n_pix, const float* depth, const float* stats,
-                       int64_t stats_stride, const float* grad_depth, const float* grad_alpha,
-                       float4* pix, cudaStream_t st) {
-  (void)va;
-  if (n_pix <= 0) return;
-  const int64_t want = (n_pix + 255) / 256;
-  pixel_prep_kernel<<<(int)(want < 8192 ? want : 8192), 256, 0, st>>>(
-      va, n_pix, depth, stats, stats_stride, grad_depth, grad_alpha, pix);
-}
 
 void launch_blend_bwd(const ViewsArg& va, int tile_w, int tile_h, int64_t n_tiles,
                       const uint64_t* keys, const uint2* ranges, const GaussRec* recs,
-                      const float4* pix, float beta2, float beta3, RecGrad* rgrad, Control* ctrl,
-                      cudaStream_t st) {
+                      const float* depth, const float* stats, int64_t stats_stride,
+                      const float* grad_depth, const float* grad_alpha, float beta2, float beta3,
+                      RecGrad* rgrad, Control* ctrl, cudaStream_t st) {
   if (n_tiles <= 0) return;
+#define FE_BWD(TW_, TH_)                                                                       \
+  launch_bwd_tiles<TW_, TH_>(va, n_tiles, keys, ranges, recs, depth, stats, stats_stride,     \
+                             grad_depth, grad_alpha, beta2, beta3, rgrad, ctrl, st)
   if (tile_w == 8 && tile_h == 8)
-    launch_bwd_tiles<8, 8>(va, n_tiles, keys, ranges, recs, pix, beta2, beta3, rgrad, ctrl, st);
+    FE_BWD(8, 8);
   else if (tile_w == 32 && tile_h == 8)
-    launch_bwd_tiles<32, 8>(va, n_tiles, keys, ranges, recs, pix, beta2, beta3, rgrad, ctrl, st);
+    FE_BWD(32, 8);
   else
-    launch_bwd_tiles<16, 16>(va, n_tiles, keys, ranges, recs, pix, beta2, beta3, rgrad, ctrl, st);
+    FE_BWD(16, 16);
+#undef FE_BWD
 }
 
 void launch_record_vjp(const ViewsArg& va, int64_t n_rec, const float* means, const float* prec,

@@ -70,14 +70,14 @@ void launch_blend_fwd_band(const ViewsArg& va, int tile_w, int tile_h, int px, i
                            int64_t stats_stride, Control* ctrl, cudaStream_t st);
 
 // blend_bwd.cu
-void launch_pixel_prep(const ViewsArg& va, int64_t n_pix, const float* depth, const float* stats,
-                       int64_t stats_stride, const float* grad_depth, const float* grad_alpha,
-                       float4* pix, cudaStream_t st);
-// Tile records are built per key from the Gaussian records (fe_tilerec.cuh), as in the forward.
+// Tile records are built per key from the Gaussian records (fe_tilerec.cuh), as in the forward;
+// each tile's per-pixel terms are formed from depth, the forward's statistics (stats, stride) and
+// the cotangents (NULL = zero) when the tile is staged.
 void launch_blend_bwd(const ViewsArg& va, int tile_w, int tile_h, int64_t n_tiles,
                       const uint64_t* keys, const uint2* ranges, const GaussRec* recs,
-                      const float4* pix, float beta2, float beta3, RecGrad* rgrad, Control* ctrl,
-                      cudaStream_t st);
+                      const float* depth, const float* stats, int64_t stats_stride,
+                      const float* grad_depth, const float* grad_alpha, float beta2, float beta3,
+                      RecGrad* rgrad, Control* ctrl, cudaStream_t st);
 // Gradients are accumulated (atomically) into gmeans/gprec/glogw, which must be zeroed first.
 void launch_record_vjp(const ViewsArg& va, int64_t n_rec, const float* means, const float* prec,
                        const float* quat, const float* trans, const GaussRec* recs,
