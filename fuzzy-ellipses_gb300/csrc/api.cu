@@ -1184,10 +1184,29 @@ static int batch_binning(fe_batch* b, const Pipeline& p, cudaStream_t st, cudaEv
 constexpr int64_t kHostBandPixels = INT64_C(1) << 19;
 constexpr int64_t kMaxHostBands = 8;
 
+// Tuning knobs of the host-to-host forward, read once: FE_HOST_BANDS (most bands, default 8) and
+// FE_HOST_BAND_STREAMS (1: all bands on the caller's stream; 2, the default: alternate with the
+// batch's second stream so one band's tail overlaps the next band's start).
+static int64_t host_band_limit() {
+  static const int64_t v = [] {
+    const char* s = std::getenv("FE_HOST_BANDS");
+    const long long x = s ? std::strtoll(s, nullptr, 10) : kMaxHostBands;
+    return (int64_t)std::min<long long>(64, std::max<long long>(1, x));
+  }();
+  return v;
+}
+static int host_band_streams() {
+  static const int v = [] {
+    const char* s = std::getenv("FE_HOST_BAND_STREAMS");
+    return (s && std::atoi(s) == 1) ? 1 : 2;
+  }();
+  return v;
+}
+
 static void plan_host_bands(fe_batch* b) {
   b->bands.clear();
   const int64_t k =
-      std::min(kMaxHostBands, std::max<int64_t>(1, (b->n_pix + kHostBandPixels - 1) / kHostBandPixels));
+      std::min(host_band_limit(), std::max<int64_t>(1, (b->n_pix + kHostBandPixels - 1) / kHostBandPixels));
   const int64_t target = std::max<int64_t>(1, (b->n_tiles + k - 1) / k);
   fe_batch::HostBand cur{0, 0, 0, 0};
   bool open = false;
@@ -1280,7 +1299,7 @@ int fe_batch_fwd_host(fe_batch* b, const float* h_means, const float* h_prec,
   // the calling thread) cannot delay the renders.
   for (int j = 0; j < nb; ++j) {
     const fe_batch::HostBand& hb = b->bands[j];
-    cudaStream_t sj = (j & 1) ? b->s_comp : st;
+    cudaStream_t sj = (host_band_streams() == 2 && (j & 1)) ? b->s_comp : st;
     launch_blend_fwd_band(p.va, p.tile_w, p.tile_h, p.px, p.chunk, hb.t0, hb.t1, ctr + j,
                           b->sorted, b->rs.recs, b->rs.ranges, p.beta2, p.beta3, dep_d, alp_d,
                           nullptr, p.n_pix, b->rs.ctrl, sj);
