@@ -513,21 +513,26 @@ class Batch:
         copied in, the blend runs in bands whose outputs are copied back while the next bands
         render. Outputs default to new pinned tensors; returns after the copies have landed."""
         lib = N.load()
-        host = [t.detach().contiguous().float() for t in (means, prec, logw)]
-        for t in host:
+        host = []  # keeps converted copies alive until the call returns
+        for t in (means, prec, logw):
             if t.is_cuda:
                 raise ValueError("forward_host takes host (CPU) tensors")
+            if t.dtype is not torch.float32 or not t.is_contiguous():
+                t = t.detach().contiguous().float()
+            host.append(t)
         if depth is None:
             depth = torch.empty(self.n_pixels, dtype=torch.float32).pin_memory()
         if alpha is None:
             alpha = torch.empty(self.n_pixels, dtype=torch.float32).pin_memory()
         for t in (depth, alpha):
-            if t.is_cuda or t.dtype != torch.float32 or not t.is_contiguous() or \
+            if t.is_cuda or t.dtype is not torch.float32 or not t.is_contiguous() or \
                     t.numel() < self.n_pixels:
                 raise ValueError("outputs must be contiguous float32 host tensors of n_pixels")
-        N.check(lib.fe_batch_fwd_host(self._h, _ptr(host[0]), _ptr(host[1]), _ptr(host[2]),
-                                      _ptr(depth), _ptr(alpha), _stream()))
-        torch.cuda.current_stream().synchronize()
+        st = torch.cuda.current_stream()
+        N.check(lib.fe_batch_fwd_host(self._h, host[0].data_ptr(), host[1].data_ptr(),
+                                      host[2].data_ptr(), depth.data_ptr(), alpha.data_ptr(),
+                                      st.cuda_stream))
+        st.synchronize()
         return depth, alpha
 
     def backward(self, means, prec, logw, depth, alpha, stats, gdepth, galpha):
