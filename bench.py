@@ -41,11 +41,11 @@ WORKLOAD = ("N=1000 Gaussians (means U[-0.3,0.3]^3 m, scales logU[0.005,0.03] m,
 # the logit and the three accumulations) and 3 MUFU operations (rcp and two ex2).
 PER_EVAL_FMA = 22
 PER_EVAL_MUFU = 3
-# Backward, counted from blend_bwd_kernel's per-pixel loop: 37 FMA-pipe operations (pixel
-# offsets 2, the three row-folded polynomials 5, peak and logits 5, chain rule 14, row moments
-# of the coefficient gradients 11) and 3 MUFU (rcp, ex2 of the density, ex2 of the softmax
+# Backward, counted from blend_bwd_kernel's per-pixel loop: 32 FMA-pipe operations (pixel
+# offsets 2, the three row-folded polynomials 5, peak and logit 4, chain rule 12, running sums
+# of the coefficient gradients 9) and 3 MUFU (rcp, ex2 of the density, ex2 of the softmax
 # weight).
-PER_EVAL_BWD_FMA = 37
+PER_EVAL_BWD_FMA = 32
 PER_EVAL_BWD_MUFU = 3
 
 
@@ -494,9 +494,9 @@ def main():
                              "peak": bwd_peak / 1e9, "unit": "Gevals/s",
                              "frac": bwd_evals_s / bwd_peak,
                              "per_eval": {"fma_pipe": PER_EVAL_BWD_FMA, "mufu": PER_EVAL_BWD_MUFU},
-                             "scope": "whole backward (pixel prep, per-key recompute and "
-                                      "coefficient gradients, record VJP) of the 16-view step, "
-                                      "reusing the forward's binning"}}
+                             "scope": "whole backward (per-key recompute and coefficient "
+                                      "gradients, record VJP) of the 16-view step, reusing the "
+                                      "forward's binning"}}
 
     # ---- the kernels beyond the render path ------------------------------------------------
     next_rows = None if args.no_next else next_rows_bench(fe, dev, scene, cams, fma_ops, ex2_ops,

@@ -34,10 +34,11 @@ __device__ __forceinline__ void red_add_v4(float* addr, float a, float b, float 
 
 constexpr int kBwdWarps = 4;
 
-// Per-warp shared-memory slice: the tile's per-pixel data as four planes (depth, softmax max m,
-// dL/ddepth / W, dL/dalpha (1-alpha)), so that one 64-bit load gives the same field of two
-// adjacent pixels for the packed arithmetic. Rows are padded to TW + 2 floats (8-byte aligned
-// pairs; lanes of one key reading different rows of the same columns hit different banks).
+// Per-warp shared-memory slice: the tile's per-pixel data as four planes (depth, -m for the
+// softmax max m, dL/ddepth / W, dL/dalpha (1-alpha) ln 2), so that one 64-bit load gives the
+// same field of two adjacent pixels for the packed arithmetic. Rows are padded to TW + 2 floats
+// (8-byte aligned pairs; lanes of one key reading different rows of the same columns hit
+// different banks).
 template <int TW, int TH>
 struct alignas(16) BwdSlice {
   static constexpr int ROW = TW + 2;
@@ -63,8 +64,8 @@ __global__ void __launch_bounds__(32 * kBwdWarps) blend_bwd_kernel(
   const int lane = threadIdx.x & 31;
   Slice& sl = slices[threadIdx.x >> 5];
   const f2_t B3 = f2_pack(beta3, beta3), NB2 = f2_pack(nb2, nb2);
-  const f2_t NEGB2 = f2_pack(-beta2, -beta2), ONE = f2_pack(1.f, 1.f), TWO = f2_pack(2.f, 2.f);
-  const f2_t LN2 = f2_pack(kLn2, kLn2);
+  const f2_t NEGB2 = f2_pack(-beta2, -beta2), TWO = f2_pack(2.f, 2.f);
+  const f2_t B3L = f2_pack(beta3 * kLn2, beta3 * kLn2), FOUR = f2_pack(4.f, 4.f);
   for (;;) {
     uint32_t tile = 0;
     if (lane == 0) tile = atomicAdd(&ctrl->next_tile, 1u);
@@ -81,7 +82,7 @@ __global__ void __launch_bounds__(32 * kBwdWarps) blend_bwd_kernel(
 
     __syncwarp();  // the previous tile's readers are done with the slice
     // The tile's per-pixel data from the forward's outputs and statistics and the cotangents:
-    // depth, softmax max m, dL/ddepth / W, dL/dalpha (1 - alpha) with 1 - alpha = exp(-A).
+    // depth, -m (softmax max), dL/ddepth / W, dL/dalpha (1 - alpha) ln 2 with 1 - alpha = exp(-A).
     for (int q = lane; q < TW * TH; q += 32) {
       const int ly = q / TW, lx = q - ly * TW;
       if (lx < xs && ly < ys) {
@@ -91,9 +92,9 @@ __global__ void __launch_bounds__(32 * kBwdWarps) blend_bwd_kernel(
         const float gA = galpha ? galpha[pi] : 0.f;
         const int o = ly * Slice::ROW + lx;
         sl.plane[0][o] = depth[pi];
-        sl.plane[1][o] = m;
+        sl.plane[1][o] = -m;
         sl.plane[2][o] = W > 0.f ? gD / W : 0.f;
-        sl.plane[3][o] = gA * expf(-A);
+        sl.plane[3][o] = gA * expf(-A) * kLn2;
       }
     }
     __syncwarp();
@@ -110,10 +111,19 @@ __global__ void __launch_bounds__(32 * kBwdWarps) blend_bwd_kernel(
       // Coefficient gradients: gV over the basis [1, du, dv, du^2, du dv, dv^2] of vsv, gP over
       // [1, du, dv] of psv, gN over [1, eu, ev, eu^2, eu ev, ev^2] of nq (eu = du - cu,
       // ev = dv - cv). Within a row dv and ev are constant, so the row's polynomials are folded
-      // to quadratics in du / eu and the pixel loop only accumulates the row moments
-      // S* = sum h du^k with h = -dL/dvsv, Q* = sum dL/dpsv du^k, T* = sum dL/dnq eu^k; the row
-      // end maps them onto the basis.
-      float gV[6] = {0, 0, 0, 0, 0, 0}, gP[3] = {0, 0, 0}, gN[6] = {0, 0, 0, 0, 0, 0}, gC = 0.f;
+      // to quadratics in du / eu. Each lane of a pixel pair visits the row's columns
+      // du = D0 + 2 i (i = 0 .. n-1, D0 = (du0, du0 + 1)); instead of the moments sum h du^k
+      // the pixel loop keeps running sums (S0 = sum h, C1 = sum of S0, C2 = sum of C1), which
+      // give sum i h = n S0 - C1 and sum i^2 h = n^2 S0 - (2n+1) C1 + 2 C2. These are linear
+      // with coefficients that are the same for every row of the tile, so the rows only add
+      // them up (weighted by 1, dv, dv^2 or ev, ev^2) and the basis is formed once per key.
+      // h = -dL/dvsv (S), dL/dpsv (Q), dL/dnq (T).
+      const int n = (xs + 1) >> 1;  // pair steps per row; for odd xs lane b of the last is off
+      f2_t aS0 = 0, aC1 = 0, aC2 = 0, bS0 = 0, bC1 = 0, dS0 = 0;
+      f2_t aQ0 = 0, aQ1 = 0, bQ0 = 0;
+      f2_t aT0 = 0, aT1 = 0, aT2 = 0, bT0 = 0, bT1 = 0, dT0 = 0;
+      f2_t G = 0;
+      float cu = 0.f;
       if (active) {
         // The key's tile record, built from its Gaussian record as the forward blend builds it.
         TileRec t;
@@ -125,7 +135,8 @@ __global__ void __launch_bounds__(32 * kBwdWarps) blend_bwd_kernel(
         const float V0 = t.V[0], V1 = t.V[1], V2 = t.V[2], V3 = t.V[3], V4 = t.V[4], V5 = t.V[5];
         const float P0 = t.P[0], P1 = t.P[1], P2 = t.P[2];
         const float N0 = t.N[0], N1 = t.N[1], N2 = t.N[2], N3 = t.N[3], N4 = t.N[4], N5 = t.N[5];
-        const float C = t.C, cu = t.cu, cvv = t.cv;
+        const float C = t.C, cvv = t.cv;
+        cu = t.cu;
         const f2_t V3p = f2_pack(V3, V3), P1p = f2_pack(P1, P1), N3p = f2_pack(N3, N3);
         const f2_t Cp = f2_pack(C, C), CUp = f2_pack(cu, cu);
         for (int ly = sub; ly < ys; ly += s) {
@@ -136,17 +147,17 @@ __global__ void __launch_bounds__(32 * kBwdWarps) blend_bwd_kernel(
           const float rn0 = fmaf(N5, ev2, fmaf(N2, ev, N0)), rn1 = fmaf(N4, ev, N1);
           const f2_t RV0 = f2_pack(rv0, rv0), RV1 = f2_pack(rv1, rv1), RP0 = f2_pack(rp0, rp0);
           const f2_t RN0 = f2_pack(rn0, rn0), RN1 = f2_pack(rn1, rn1);
-          f2_t S0 = 0, S1 = 0, S2 = 0, Q0 = 0, Q1 = 0, T0 = 0, T1 = 0, T2 = 0, G = 0;
+          f2_t S0 = 0, C1 = 0, C2 = 0, Q0 = 0, Q1 = 0, T0 = 0, T1 = 0, T2 = 0;
           const int o = ly * Slice::ROW;
           const f2_t* pd = reinterpret_cast<const f2_t*>(&sl.plane[0][o]);
           const f2_t* pm = reinterpret_cast<const f2_t*>(&sl.plane[1][o]);
           const f2_t* pz = reinterpret_cast<const f2_t*>(&sl.plane[2][o]);
           const f2_t* pa = reinterpret_cast<const f2_t*>(&sl.plane[3][o]);
           f2_t du = f2_pack(-0.5f * (TW - 1), 1.f - 0.5f * (TW - 1));
-          const int pairs = xs >> 1;
-#pragma unroll 2
-          for (int j = 0; j < pairs; ++j, du = add2(du, TWO)) {
-            const f2_t D = pd[j], M = pm[j], GDW = pz[j], GA = pa[j];
+          // One pixel pair. With lane_b_off the pair's second pixel lies past the tile's last
+          // column (its plane entries are stale): its four results are replaced by zeros.
+          auto step = [&](int j, bool lane_b_off) {
+            const f2_t D = pd[j], NM = pm[j], GDW = pz[j], GA = pa[j];
             const f2_t eu = sub2(du, CUp);
             const f2_t vsv = fma2(fma2(V3p, du, RV1), du, RV0);
             const f2_t psv = fma2(P1p, du, RP0);
@@ -159,75 +170,85 @@ __global__ void __launch_bounds__(32 * kBwdWarps) blend_bwd_kernel(
             float sa, sb;
             f2_unpack(s2, sa, sb);
             const f2_t eA = f2_pack(ex2_approx(sa), ex2_approx(sb));
-            const f2_t lm = sub2(fma2(B3, s2, mul2(NB2, z)), M);
+            const f2_t lm = fma2(B3, s2, fma2(NB2, z, NM));          // logit - m
             float la, lb, za, zb;
             f2_unpack(lm, la, lb);
             f2_unpack(z, za, zb);
             const f2_t e = f2_pack(za > 0.f ? ex2_approx(la) : 0.f, zb > 0.f ? ex2_approx(lb) : 0.f);
             const f2_t we = mul2(GDW, e);                            // dL/ddepth * weight
-            const f2_t zd = sub2(z, D);
-            const f2_t gs = fma2(GA, eA, mul2(mul2(B3, we), zd));    // dL/ds (natural)
-            const f2_t gz = mul2(we, fma2(NEGB2, zd, ONE));           // dL/dz
-            const f2_t gs2 = mul2(gs, LN2);                           // dL/ds2
-            const f2_t gnq = mul2(gs2, qi);
+            const f2_t u = mul2(we, sub2(z, D));
+            f2_t gs2 = fma2(B3L, u, mul2(GA, eA));                   // dL/ds2
+            const f2_t gz = fma2(NEGB2, u, we);                      // dL/dz
+            f2_t gnq = mul2(gs2, qi);
             const f2_t gq = fma2(gs2, nq, mul2(gz, psv));
-            const f2_t gpsv = mul2(gz, qi);
-            const f2_t h = mul2(mul2(gq, qi), qi);                    // -dL/dvsv
+            f2_t gpsv = mul2(gz, qi);
+            f2_t h = mul2(mul2(gq, qi), qi);                         // -dL/dvsv
+            if (lane_b_off) {
+              float a0, b0;
+              f2_unpack(gs2, a0, b0); gs2 = f2_pack(a0, 0.f);
+              f2_unpack(gnq, a0, b0); gnq = f2_pack(a0, 0.f);
+              f2_unpack(gpsv, a0, b0); gpsv = f2_pack(a0, 0.f);
+              f2_unpack(h, a0, b0); h = f2_pack(a0, 0.f);
+            }
             G = add2(G, gs2);
-            const f2_t tv = mul2(h, du), tn = mul2(gnq, eu);
-            S0 = add2(S0, h); S1 = add2(S1, tv); S2 = fma2(tv, du, S2);
-            Q0 = add2(Q0, gpsv); Q1 = fma2(gpsv, du, Q1);
-            T0 = add2(T0, gnq); T1 = add2(T1, tn); T2 = fma2(tn, eu, T2);
-          }
-          float s0, s1, s2v, q0, q1, t0, t1, t2, gc;
-          {
-            float a, b;
-            f2_unpack(S0, a, b); s0 = a + b;
-            f2_unpack(S1, a, b); s1 = a + b;
-            f2_unpack(S2, a, b); s2v = a + b;
-            f2_unpack(Q0, a, b); q0 = a + b;
-            f2_unpack(Q1, a, b); q1 = a + b;
-            f2_unpack(T0, a, b); t0 = a + b;
-            f2_unpack(T1, a, b); t1 = a + b;
-            f2_unpack(T2, a, b); t2 = a + b;
-            f2_unpack(G, a, b); gc = a + b;
-          }
-          if (xs & 1) {  // the odd last column
-            const int lx = xs - 1;
-            const float du1 = lx - 0.5f * (TW - 1), eu = du1 - cu;
-            const float D = sl.plane[0][o + lx], M = sl.plane[1][o + lx];
-            const float GDW = sl.plane[2][o + lx], GA = sl.plane[3][o + lx];
-            const float vsv = fmaf(fmaf(V3, du1, rv1), du1, rv0);
-            const float psv = fmaf(P1, du1, rp0);
-            const float nq = fmaf(fmaf(N3, eu, rn1), eu, rn0);
-            const float qi = rcp_approx(vsv);
-            const float z = psv * qi;
-            const float s2 = fmaf(nq, qi, C);
-            const float eA = ex2_approx(s2);
-            const float l = fmaf(beta3, s2, nb2 * z);
-            const float e = z > 0.f ? ex2_approx(l - M) : 0.f;
-            const float we = GDW * e;
-            const float zd = z - D;
-            const float gs = fmaf(GA, eA, beta3 * we * zd);
-            const float gz = we * fmaf(-beta2, zd, 1.f);
-            const float gs2 = gs * kLn2;
-            const float gnq = gs2 * qi;
-            const float gq = fmaf(gs2, nq, gz * psv);
-            const float gpsv = gz * qi;
-            const float h = gq * qi * qi;
-            gc += gs2;
-            const float tv = h * du1, tn = gnq * eu;
-            s0 += h; s1 += tv; s2v = fmaf(tv, du1, s2v);
-            q0 += gpsv; q1 = fmaf(gpsv, du1, q1);
-            t0 += gnq; t1 += tn; t2 = fmaf(tn, eu, t2);
-          }
-          gC += gc;
-          gV[0] -= s0; gV[1] -= s1; gV[2] = fmaf(-dv, s0, gV[2]);
-          gV[3] -= s2v; gV[4] = fmaf(-dv, s1, gV[4]); gV[5] = fmaf(-dv2, s0, gV[5]);
-          gP[0] += q0; gP[1] += q1; gP[2] = fmaf(dv, q0, gP[2]);
-          gN[0] += t0; gN[1] += t1; gN[2] = fmaf(ev, t0, gN[2]);
-          gN[3] += t2; gN[4] = fmaf(ev, t1, gN[4]); gN[5] = fmaf(ev2, t0, gN[5]);
+            S0 = add2(S0, h); C1 = add2(C1, S0); C2 = add2(C2, C1);
+            Q0 = add2(Q0, gpsv); Q1 = add2(Q1, Q0);
+            T0 = add2(T0, gnq); T1 = add2(T1, T0); T2 = add2(T2, T1);
+          };
+          const int pairs = xs >> 1;
+#pragma unroll 2
+          for (int j = 0; j < pairs; ++j, du = add2(du, TWO)) step(j, false);
+          if (xs & 1) step(pairs, true);
+          const f2_t DV = f2_pack(dv, dv), DV2 = f2_pack(dv2, dv2);
+          const f2_t EV = f2_pack(ev, ev), EV2 = f2_pack(ev2, ev2);
+          aS0 = add2(aS0, S0); aC1 = add2(aC1, C1); aC2 = add2(aC2, C2);
+          bS0 = fma2(DV, S0, bS0); bC1 = fma2(DV, C1, bC1); dS0 = fma2(DV2, S0, dS0);
+          aQ0 = add2(aQ0, Q0); aQ1 = add2(aQ1, Q1); bQ0 = fma2(DV, Q0, bQ0);
+          aT0 = add2(aT0, T0); aT1 = add2(aT1, T1); aT2 = add2(aT2, T2);
+          bT0 = fma2(EV, T0, bT0); bT1 = fma2(EV, T1, bT1); dT0 = fma2(EV2, T0, dT0);
         }
+      }
+      // The basis, per lane of the pair, then summed over the pair: with I1 = sum i x and
+      // I2 = sum i^2 x, sum x du = D0 x + 2 I1 and sum x du^2 = D0^2 x + 4 D0 I1 + 4 I2
+      // (E0 = D0 - cu in place of D0 for eu).
+      float gV[6], gP[3], gN[6], gC;
+      {
+        const float nf = (float)n;
+        const f2_t NF = f2_pack(nf, nf), NN = f2_pack(nf * nf, nf * nf);
+        const f2_t N21 = f2_pack(2.f * nf + 1.f, 2.f * nf + 1.f);
+        const f2_t D0 = f2_pack(-0.5f * (TW - 1), 1.f - 0.5f * (TW - 1));
+        const f2_t E0 = sub2(D0, f2_pack(cu, cu));
+        auto first = [&](f2_t X0, f2_t X1) { return sub2(mul2(NF, X0), X1); };
+        auto second = [&](f2_t X0, f2_t X1, f2_t X2) {
+          return fma2(TWO, X2, fma2(NN, X0, mul2(N21, sub2(f2_pack(0.f, 0.f), X1))));
+        };
+        auto lin = [&](f2_t O, f2_t X0, f2_t I1) { return fma2(O, X0, mul2(TWO, I1)); };
+        auto quad = [&](f2_t O, f2_t X0, f2_t I1, f2_t I2) {
+          return fma2(O, fma2(O, X0, mul2(FOUR, I1)), mul2(FOUR, I2));
+        };
+        auto hsum = [](f2_t x) {
+          float a, b;
+          f2_unpack(x, a, b);
+          return a + b;
+        };
+        const f2_t iS = first(aS0, aC1), iiS = second(aS0, aC1, aC2);
+        gV[0] = -hsum(aS0);
+        gV[1] = -hsum(lin(D0, aS0, iS));
+        gV[2] = -hsum(bS0);
+        gV[3] = -hsum(quad(D0, aS0, iS, iiS));
+        gV[4] = -hsum(lin(D0, bS0, first(bS0, bC1)));
+        gV[5] = -hsum(dS0);
+        gP[0] = hsum(aQ0);
+        gP[1] = hsum(lin(D0, aQ0, first(aQ0, aQ1)));
+        gP[2] = hsum(bQ0);
+        const f2_t iT = first(aT0, aT1), iiT = second(aT0, aT1, aT2);
+        gN[0] = hsum(aT0);
+        gN[1] = hsum(lin(E0, aT0, iT));
+        gN[2] = hsum(bT0);
+        gN[3] = hsum(quad(E0, aT0, iT, iiT));
+        gN[4] = hsum(lin(E0, bT0, first(bT0, bT1)));
+        gN[5] = hsum(dT0);
+        gC = hsum(G);
       }
       // Combine the s lanes of each key (all lanes take part; idle lanes hold zeros).
       for (int o = 1; o < s; o <<= 1) {
