@@ -82,7 +82,7 @@ __global__ void __launch_bounds__(32 * kBwdWarps) blend_bwd_kernel(
 
     __syncwarp();  // the previous tile's readers are done with the slice
     // The tile's per-pixel data from the forward's outputs and statistics and the cotangents:
-    // depth, -m (softmax max), dL/ddepth / W, dL/dalpha (1 - alpha) ln 2 with 1 - alpha = exp(-A).
+    // depth, -m (softmax max), dL/ddepth / W, dL/dalpha (1 - alpha) ln 2, 1 - alpha = exp(-A).
     for (int q = lane; q < TW * TH; q += 32) {
       const int ly = q / TW, lx = q - ly * TW;
       if (lx < xs && ly < ys) {
