@@ -56,8 +56,9 @@ struct __align__(16) GaussRec {
 };
 static_assert(sizeof(GaussRec) == 96, "GaussRec layout");
 
-// Tile-local polynomial form of a record (what the forward blend builds in shared memory and the
-// backward reads as a gathered stream, stored pair-interleaved: see TilePair).
+// Tile-local polynomial form of a record, built per key by the kernels that evaluate it (the
+// forward blend stores it pair-interleaved in shared memory, see TilePair; the backward keeps it
+// in registers).
 // With (du,dv) the pixel offset from the tile centre and (eu,ev) = (du-cu, dv-cv) the offset from
 // the expansion centre (cu,cv) of the Mahalanobis term:
 //   vsv = V0 + V1 du + V2 dv + V3 du^2 + V4 du dv + V5 dv^2
