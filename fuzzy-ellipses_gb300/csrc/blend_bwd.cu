@@ -195,10 +195,17 @@ __global__ void __launch_bounds__(32 * kBwdWarps) blend_bwd_kernel(
             Q0 = add2(Q0, gpsv); Q1 = add2(Q1, Q0);
             T0 = add2(T0, gnq); T1 = add2(T1, T0); T2 = add2(T2, T1);
           };
-          const int pairs = xs >> 1;
+          // A full-width row is unrolled completely: its pixel pairs are independent but for the
+          // running sums, so the scheduler can interleave them (the loop dominates the kernel).
+          if (xs == TW) {
+#pragma unroll
+            for (int j = 0; j < TW / 2; ++j, du = add2(du, TWO)) step(j, false);
+          } else {
+            const int pairs = xs >> 1;
 #pragma unroll 2
-          for (int j = 0; j < pairs; ++j, du = add2(du, TWO)) step(j, false);
-          if (xs & 1) step(pairs, true);
+            for (int j = 0; j < pairs; ++j, du = add2(du, TWO)) step(j, false);
+            if (xs & 1) step(pairs, true);
+          }
           const f2_t DV = f2_pack(dv, dv), DV2 = f2_pack(dv2, dv2);
           const f2_t EV = f2_pack(ev, ev), EV2 = f2_pack(ev2, ev2);
           aS0 = add2(aS0, S0); aC1 = add2(aC1, C1); aC2 = add2(aC2, C2);
