@@ -311,7 +311,10 @@ __global__ void __launch_bounds__(32 * kBwdWarps) blend_bwd_kernel(
   }
 }
 
-// Chain rule of the record builder (preprocess.cu build_camera_terms / write_record), in double.
+// Chain rule of the record builder (preprocess.cu build_camera_terms / write_record), in T:
+// float, the precision of the preprocess it differentiates (in double the kernel is FP64-bound
+// and adds 4% to a 16-view backward; both pass the float64 and finite-difference gradient tests).
+template <typename T>
 __global__ void record_vjp_kernel(ViewsArg va, int64_t n_rec, const float* __restrict__ means,
                                   const float* __restrict__ prec, const float* __restrict__ quat,
                                   const float* __restrict__ trans, const GaussRec* __restrict__ recs,
@@ -325,64 +328,64 @@ __global__ void record_vjp_kernel(ViewsArg va, int64_t n_rec, const float* __res
     const int64_t gi = V.gauss_base + (i - V.rec_base);
     const RecGrad rg = rgrad[i];
 
-    double U[9], R[9];
-    for (int k = 0; k < 9; ++k) U[k] = (k == 3 || k == 6 || k == 7) ? 0.0 : prec[9 * gi + k];
-    quat_to_rot<double>(quat + 4 * V.pose, R);
-    const double t[3] = {trans[3 * V.pose], trans[3 * V.pose + 1], trans[3 * V.pose + 2]};
-    const V3<double> p = v3(means[3 * gi] - t[0], means[3 * gi + 1] - t[1], means[3 * gi + 2] - t[2]);
-    const V3<double> pc = matvec(R, p);
-    double M[9], Y[9];
+    T U[9], R[9];
+    for (int k = 0; k < 9; ++k) U[k] = (k == 3 || k == 6 || k == 7) ? T(0) : (T)prec[9 * gi + k];
+    quat_to_rot<T>(quat + 4 * V.pose, R);
+    const T t[3] = {trans[3 * V.pose], trans[3 * V.pose + 1], trans[3 * V.pose + 2]};
+    const V3<T> p = v3<T>(means[3 * gi] - t[0], means[3 * gi + 1] - t[1], means[3 * gi + 2] - t[2]);
+    const V3<T> pc = matvec(R, p);
+    T M[9], Y[9];
     for (int a = 0; a < 3; ++a)
       for (int b = 0; b < 3; ++b) {
-        double s = 0.0;
+        T s = T(0);
         for (int k = 0; k <= a; ++k) s += U[k * 3 + a] * R[b * 3 + k];
         M[a * 3 + b] = s;
       }
     cofactor3(M, Y);
-    const double fx = V.fx, fy = V.fy;
-    const V3<double> r0 = v3(((double)recs[i].uc - V.cx) / fx, ((double)recs[i].vc - V.cy) / fy, 1.0);
-    const V3<double> c0 = cross(r0, pc);
-    const V3<double> cxv = v3(0.0, -pc.z / fx, pc.y / fx);
-    const V3<double> cyv = v3(pc.z / fy, 0.0, -pc.x / fy);
+    const T fx = V.fx, fy = V.fy;
+    const V3<T> r0 = v3<T>(((T)recs[i].uc - V.cx) / fx, ((T)recs[i].vc - V.cy) / fy, T(1));
+    const V3<T> c0 = cross(r0, pc);
+    const V3<T> cxv = v3<T>(T(0), -pc.z / fx, pc.y / fx);
+    const V3<T> cyv = v3<T>(pc.z / fy, T(0), -pc.x / fy);
 
-    const V3<double> ga0 = v3<double>(rg.a0[0], rg.a0[1], rg.a0[2]);
-    const V3<double> ga1 = v3<double>(rg.a1[0], rg.a1[1], rg.a1[2]);
-    const V3<double> ga2 = v3<double>(rg.a2[0], rg.a2[1], rg.a2[2]);
-    const V3<double> gb = v3<double>(rg.b[0], rg.b[1], rg.b[2]);
-    const V3<double> gy0 = v3<double>(rg.y0[0], rg.y0[1], rg.y0[2]);
-    const V3<double> gy1 = v3<double>(rg.y1[0], rg.y1[1], rg.y1[2]);
-    const V3<double> gy2 = v3<double>(rg.y2[0], rg.y2[1], rg.y2[2]);
+    const V3<T> ga0 = v3<T>(rg.a0[0], rg.a0[1], rg.a0[2]);
+    const V3<T> ga1 = v3<T>(rg.a1[0], rg.a1[1], rg.a1[2]);
+    const V3<T> ga2 = v3<T>(rg.a2[0], rg.a2[1], rg.a2[2]);
+    const V3<T> gb = v3<T>(rg.b[0], rg.b[1], rg.b[2]);
+    const V3<T> gy0 = v3<T>(rg.y0[0], rg.y0[1], rg.y0[2]);
+    const V3<T> gy1 = v3<T>(rg.y1[0], rg.y1[1], rg.y1[2]);
+    const V3<T> gy2 = v3<T>(rg.y2[0], rg.y2[1], rg.y2[2]);
 
     // a0 = M r0, a1 = M e_x / fx, a2 = M e_y / fy, b = M pc.
-    double gM[9];
-    const double ga0a[3] = {ga0.x, ga0.y, ga0.z}, ga1a[3] = {ga1.x, ga1.y, ga1.z};
-    const double ga2a[3] = {ga2.x, ga2.y, ga2.z}, gba[3] = {gb.x, gb.y, gb.z};
-    const double r0a[3] = {r0.x, r0.y, r0.z}, pca[3] = {pc.x, pc.y, pc.z};
+    T gM[9];
+    const T ga0a[3] = {ga0.x, ga0.y, ga0.z}, ga1a[3] = {ga1.x, ga1.y, ga1.z};
+    const T ga2a[3] = {ga2.x, ga2.y, ga2.z}, gba[3] = {gb.x, gb.y, gb.z};
+    const T r0a[3] = {r0.x, r0.y, r0.z}, pca[3] = {pc.x, pc.y, pc.z};
     for (int a = 0; a < 3; ++a)
       for (int b = 0; b < 3; ++b) gM[a * 3 + b] = ga0a[a] * r0a[b] + gba[a] * pca[b];
     for (int a = 0; a < 3; ++a) {
       gM[a * 3 + 0] += ga1a[a] / fx;
       gM[a * 3 + 1] += ga2a[a] / fy;
     }
-    V3<double> gpc = matTvec(M, gb);
+    V3<T> gpc = matTvec(M, gb);
     // y0 = Y c0, y1 = Y cxv, y2 = Y cyv.
-    double gY[9];
-    const double gy0a[3] = {gy0.x, gy0.y, gy0.z}, gy1a[3] = {gy1.x, gy1.y, gy1.z};
-    const double gy2a[3] = {gy2.x, gy2.y, gy2.z};
-    const double c0a[3] = {c0.x, c0.y, c0.z}, cxa[3] = {cxv.x, cxv.y, cxv.z};
-    const double cya[3] = {cyv.x, cyv.y, cyv.z};
+    T gY[9];
+    const T gy0a[3] = {gy0.x, gy0.y, gy0.z}, gy1a[3] = {gy1.x, gy1.y, gy1.z};
+    const T gy2a[3] = {gy2.x, gy2.y, gy2.z};
+    const T c0a[3] = {c0.x, c0.y, c0.z}, cxa[3] = {cxv.x, cxv.y, cxv.z};
+    const T cya[3] = {cyv.x, cyv.y, cyv.z};
     for (int a = 0; a < 3; ++a)
       for (int b = 0; b < 3; ++b)
         gY[a * 3 + b] = gy0a[a] * c0a[b] + gy1a[a] * cxa[b] + gy2a[a] * cya[b];
-    const V3<double> gc0 = matTvec(Y, gy0), gcx = matTvec(Y, gy1), gcy = matTvec(Y, gy2);
+    const V3<T> gc0 = matTvec(Y, gy0), gcx = matTvec(Y, gy1), gcy = matTvec(Y, gy2);
     gpc = gpc + cross(gc0, r0);                  // c0 = r0 x pc
     gpc.y += gcx.z / fx;                         // cxv = (0, -pc.z, pc.y) / fx
     gpc.z -= gcx.y / fx;
     gpc.x -= gcy.z / fy;                         // cyv = (pc.z, 0, -pc.x) / fy
     gpc.z += gcy.x / fy;
     // Y = cof(M).
-    const double* m = M;
-    const double* gc = gY;
+    const T* m = M;
+    const T* gc = gY;
     gM[4] += gc[0] * m[8]; gM[8] += gc[0] * m[4]; gM[5] -= gc[0] * m[7]; gM[7] -= gc[0] * m[5];
     gM[5] += gc[1] * m[6]; gM[6] += gc[1] * m[5]; gM[3] -= gc[1] * m[8]; gM[8] -= gc[1] * m[3];
     gM[3] += gc[2] * m[7]; gM[7] += gc[2] * m[3]; gM[4] -= gc[2] * m[6]; gM[6] -= gc[2] * m[4];
@@ -395,16 +398,16 @@ __global__ void record_vjp_kernel(ViewsArg va, int64_t n_rec, const float* __res
     // M[a][b] = sum_k U[k][a] R[b][k]  ->  dL/dU[k][a] = sum_b gM[a][b] R[b][k]  (k <= a).
     for (int a = 0; a < 3; ++a)
       for (int k = 0; k <= a; ++k) {
-        double s = 0.0;
+        T s = T(0);
         for (int b = 0; b < 3; ++b) s += gM[a * 3 + b] * R[b * 3 + k];
         atomicAdd(&gprec[9 * gi + k * 3 + a], (float)s);
       }
     // pc = R (m - t).
-    const V3<double> gm = matTvec(R, gpc);
+    const V3<T> gm = matTvec(R, gpc);
     atomicAdd(&gmeans[3 * gi + 0], (float)gm.x);
     atomicAdd(&gmeans[3 * gi + 1], (float)gm.y);
     atomicAdd(&gmeans[3 * gi + 2], (float)gm.z);
-    atomicAdd(&glogw[gi], (float)((double)rg.w * kLog2eD));
+    atomicAdd(&glogw[gi], rg.w * kLog2e);
   }
 }
 
@@ -450,7 +453,7 @@ void launch_record_vjp(const ViewsArg& va, int64_t n_rec, const float* means, co
                        cudaStream_t st) {
   if (n_rec <= 0) return;
   const int64_t want = (n_rec + 127) / 128;
-  record_vjp_kernel<<<(int)(want < 65535 ? want : 65535), 128, 0, st>>>(
+  record_vjp_kernel<float><<<(int)(want < 65535 ? want : 65535), 128, 0, st>>>(
       va, n_rec, means, prec, quat, trans, recs, rgrad, gmeans, gprec, glogw);
 }
 
