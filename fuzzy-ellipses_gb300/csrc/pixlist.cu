@@ -108,9 +108,7 @@ __global__ void __launch_bounds__(128) pixlist_kernel(
     float F[kMaxF];
 #pragma unroll
     for (int q = 0; q < kMaxF; ++q) F[q] = 0.f;
-    for (int i = 0; i < n; ++i) {
-      const float4 bnd = *reinterpret_cast<const float4*>(pr + i);
-      if (!(u >= bnd.x && u <= bnd.y && v >= bnd.z && v <= bnd.w)) continue;
+    auto eval = [&](int i) {
       const GaussRec& g = pr[i].g;
       const float du = u - g.uc, dv = v - g.vc;
       float a[3], y[3];
@@ -139,6 +137,28 @@ __global__ void __launch_bounds__(128) pixlist_kernel(
         Z = fmaf(e, z, Z);
         for (int q = 0; q < nf && q < kMaxF; ++q) F[q] = fmaf(e, feats[(int64_t)i * nf + q], F[q]);
       }
+    };
+    // The screen bounds of kBatch Gaussians are loaded together (independent loads in flight),
+    // then the Gaussians whose bounds hold the ray are evaluated in index order.
+    constexpr int kBatch = 8;
+    int i0 = 0;
+    for (; i0 + kBatch <= n; i0 += kBatch) {
+      float4 bnd[kBatch];
+#pragma unroll
+      for (int t = 0; t < kBatch; ++t) bnd[t] = *reinterpret_cast<const float4*>(pr + i0 + t);
+      unsigned hit = 0;
+#pragma unroll
+      for (int t = 0; t < kBatch; ++t)
+        hit |= (u >= bnd[t].x && u <= bnd[t].y && v >= bnd[t].z && v <= bnd[t].w) ? 1u << t : 0u;
+      while (hit) {
+        const int t = __ffs(hit) - 1;
+        hit &= hit - 1;
+        eval(i0 + t);
+      }
+    }
+    for (int i = i0; i < n; ++i) {
+      const float4 bnd = *reinterpret_cast<const float4*>(pr + i);
+      if (u >= bnd.x && u <= bnd.y && v >= bnd.z && v <= bnd.w) eval(i);
     }
     const float iw = W > 0.f ? 1.f / W : 0.f;
     const float zd = Z * iw;  // parameter of the ray (x inv_f, y inv_f, c)
