@@ -361,18 +361,18 @@ void launch_chunk(int chunk, const ViewsArg& va, int64_t tile_begin, int64_t til
   if (chunk == 8)
     launch_tiles<TW, TH, PX, 8>(va, tile_begin, tile_end, counter, keys, recs, ranges, nb2, beta3,
                                 depth, alpha, stats, stats_stride, ctrl, st);
-  else if (chunk == 32)
-    launch_tiles<TW, TH, PX, 32>(va, tile_begin, tile_end, counter, keys, recs, ranges, nb2,
+  else if (chunk == 16)
+    launch_tiles<TW, TH, PX, 16>(va, tile_begin, tile_end, counter, keys, recs, ranges, nb2,
                                  beta3, depth, alpha, stats, stats_stride, ctrl, st);
   else
-    launch_tiles<TW, TH, PX, 16>(va, tile_begin, tile_end, counter, keys, recs, ranges, nb2,
+    launch_tiles<TW, TH, PX, 32>(va, tile_begin, tile_end, counter, keys, recs, ranges, nb2,
                                  beta3, depth, alpha, stats, stats_stride, ctrl, st);
 }
 
 }  // namespace
 
 // Pixels per thread: px in {1, 2, 4} (8x8 tiles: 1, 2); 0 selects the default for the tile.
-// Chunk: record pairs per shared-memory stage, 8, 16 or 32; 0 selects 16.
+// Chunk: record pairs per shared-memory stage, 8, 16 or 32; 0 selects 32.
 void launch_blend_fwd_band(const ViewsArg& va, int tile_w, int tile_h, int px, int chunk,
                            int64_t tile_begin, int64_t tile_end, uint32_t* counter,
                            const uint64_t* keys, const GaussRec* recs, const uint2* ranges,

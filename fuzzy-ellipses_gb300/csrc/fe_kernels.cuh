@@ -54,7 +54,7 @@ void launch_ranges(const uint64_t* keys, const Control* ctrl, int64_t capacity, 
 
 // blend_fwd.cu
 // px: pixels per thread (1, 2 or 4; 0 = default for the tile shape); chunk: record pairs per
-// shared-memory stage (8, 16 or 32; 0 = 16). The blend builds each key's tile record itself from
+// shared-memory stage (8, 16 or 32; 0 = 32). The blend builds each key's tile record itself from
 // the sorted keys and the Gaussian records (no gathered record stream). Persistent:
 // ctrl->next_tile must be zero.
 void launch_blend_fwd(const ViewsArg& va, int tile_w, int tile_h, int px, int chunk, int64_t n_tiles,

@@ -60,7 +60,7 @@ typedef enum fe_cull_mode {
 
 /* Flags for fe_render_desc.flags */
 #define FE_FLAG_SAVE_STATS 1u /* write per-pixel softmax statistics needed by the backward */
-/* Bits 8..15 of flags: record pairs per shared-memory stage of the blend (8, 16 or 32; 0 = 16). */
+/* Bits 8..15 of flags: record pairs per shared-memory stage of the blend (8, 16 or 32; 0 = 32). */
 #define FE_FLAG_CHUNK(pairs) (((uint32_t)(pairs) & 0xffu) << 8)
 /* Batches only: size the key scratch from the device-side key count (one 8-byte readback and a
  * stream synchronisation per run) instead of the worst case (views x Gaussians x tiles). */
@@ -91,7 +91,8 @@ typedef struct fe_render_desc {
   int32_t tile_w;      /* screen tile width/height in pixels: 8x8, 16x16 or 32x8; 0 = 16x16 */
   int32_t tile_h;
   uint32_t flags;      /* FE_FLAG_* */
-  int32_t px_per_thread; /* blend pixels per thread: 1, 2 or 4 (8x8 tiles: 1 or 2); 0 = default */
+  int32_t px_per_thread; /* blend pixels per thread: 1, 2 or 4 (8x8 tiles: 1 or 2); 0 = default:
+                          * 2 for 8x8 tiles and for single views of fewer than 3000 tiles, else 4 */
 } fe_render_desc;
 
 /* Fill d with defaults for an HxW image of n Gaussians. */
