@@ -385,10 +385,11 @@ def main():
         "preprocess": (52 * scene.n + len(cams) * scene.n * (96 + 8 + 4)) / (stages["preprocess"] * 1e-3) / 1e9,
         "emit": (8 * nk) / (stages["emit"] * 1e-3) / 1e9,
     }
-    # The forward blend builds its tile records itself; a separate gather runs only on the emit +
-    # radix sort path's forward and for the backward.
-    if stages["gather"] > 1e-3:
-        hbm["gather"] = (8 * nk + 64 * nk) / (stages["gather"] * 1e-3) / 1e9
+    # The tile-major binning writes the ranges with the keys; the emit + radix sort path reads the
+    # sorted keys once more for them (8 B per key, 8 B per tile written).
+    if stages["ranges"] > 1e-3:
+        rbytes = 8 * nk + 8 * batch_tiles(cams, *cfg["tile"])
+        hbm["ranges"] = rbytes / (stages["ranges"] * 1e-3) / 1e9
     # The tile-major binning writes the keys in order (its "sort" stage is empty); the emit +
     # radix sort path moves 16 B per key per pass.
     if stages["sort"] > 1e-3:

@@ -543,7 +543,7 @@ class Batch:
                                  _ptr(gp), _ptr(gw), _stream()))
         return gm, gp, gw
 
-    STAGES = ("preprocess", "scan", "emit", "sort", "gather", "blend")
+    STAGES = ("preprocess", "scan", "emit", "sort", "ranges", "blend")
 
     def forward_timed(self, means, prec, logw, depth=None, alpha=None, stats=None):
         """forward() with per-stage CUDA-event timings (ms); synchronises."""

@@ -271,8 +271,9 @@ int fe_batch_status(fe_batch *b, fe_stream_t stream, int64_t *num_keys, int64_t 
  * --------------------------------------------------------------------------------------------- */
 
 /* fe_batch_fwd with a CUDA event recorded between stages on `stream`; synchronises and writes the
- * six stage durations in milliseconds to stage_ms: preprocess, scan, key emission, sort,
- * ranges+tile-record gather, blend. The reference times only its blend, with events
+ * six stage durations in milliseconds to stage_ms: preprocess, scan, key emission, sort, tile
+ * ranges, blend (the tile-major binning emits keys and ranges in one kernel: its scan, sort and
+ * ranges stages are empty). The reference times only its blend, with events
  * (cuda_rasterizer/rasterizer_impl.cu:314-341). */
 int fe_batch_fwd_timed(fe_batch *b, const float *d_means, const float *d_prec, const float *d_logw,
                        float *d_depth, float *d_alpha, float *d_stats, float *stage_ms,
