@@ -453,9 +453,19 @@ def main():
         out_b[batch.n_pixels:].copy_(alp_b, non_blocking=True)
         torch.cuda.current_stream().synchronize()
 
-    # fe_batch_fwd_host: host Gaussians in, banded blend, each band's images copied back while the
-    # next bands render; the call returns once the last copy has landed.
+    # fe_batch_fwd_host, the C-ABI call: host Gaussians in, banded blend, each band's images
+    # copied back while the next bands render; then the stream is synchronised. The same call
+    # through the Python wrapper (Batch.forward_host, argument checks included) is timed beside.
+    lib = fe._native.load()
+    host_args = (batch._h, m_h.data_ptr(), p_h.data_ptr(), w_h.data_ptr(), out_b.data_ptr(),
+                 out_b.data_ptr() + 4 * batch.n_pixels)
+
     def e2e_batch_step():
+        cs = torch.cuda.current_stream()
+        fe._native.check(lib.fe_batch_fwd_host(*host_args, cs.cuda_stream))
+        cs.synchronize()
+
+    def e2e_wrapper_step():
         batch.forward_host(m_h, p_h, w_h, out_b[:batch.n_pixels], out_b[batch.n_pixels:])
 
     def timed_host(step):
@@ -468,6 +478,7 @@ def main():
 
     e2e_serial_s = timed_host(e2e_serial_step)
     e2e_s = timed_host(e2e_batch_step)
+    e2e_wrapper_s = timed_host(e2e_wrapper_step)
     e2e_value = e_step / e2e_s / 1e6
     h2d_batch = sum(x.numel() * 4 for x in (m_h, p_h, w_h))
 
@@ -539,11 +550,15 @@ def main():
                            "mevals_per_s": e_step / plain_s / 1e6},
         "e2e": {"value": e2e_value, "unit": "Mevals/s", "h2d_bytes_per_step": h2d_batch,
                 "d2h_bytes_per_step": out_b.numel() * 4,
-                "path": "fe_batch_fwd_host over the 16 cameras: pinned host Gaussians in, depth "
-                        "and alpha out to pinned host buffers, the blend in bands of tile rows "
-                        "whose images are copied back while the next bands render; poses part "
-                        "of the batch plan; wall clock per call including the final sync",
+                "path": "fe_batch_fwd_host C-ABI call (ctypes) over the 16 cameras: pinned "
+                        "host Gaussians in, depth and alpha out to pinned host buffers, the "
+                        "blend in bands of tile rows whose images are copied back while the next "
+                        "bands render; poses part of the batch plan; wall clock per call "
+                        "including the final sync",
                 "ms_per_step": 1e3 * e2e_s,
+                "python_wrapper": {"value": e_step / e2e_wrapper_s / 1e6,
+                                   "ms_per_step": 1e3 * e2e_wrapper_s,
+                                   "path": "the same call through Batch.forward_host"},
                 "serial": {"value": e_step / e2e_serial_s / 1e6, "ms_per_step": 1e3 * e2e_serial_s,
                            "path": "copy in, fe_batch_fwd, then copy depth and alpha out"}},
         "e2e_per_call": {"value": e_step / e2e_call_s / 1e6, "unit": "Mevals/s",
