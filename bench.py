@@ -381,19 +381,19 @@ def main():
     peaks, peak_kind = measured_peaks()
     nk = batch.status()["num_keys"]
     passes = (max(1, int(np.ceil(np.log2(batch_tiles(cams, *cfg["tile"]))))) + 7) // 8
+    # The tile-major binning (three launches per forward) writes the keys in order and the tile
+    # ranges with them: its scan, sort and ranges stages are empty (event gaps only). The emit +
+    # radix sort path moves 16 B per key per sort pass and reads the sorted keys once more for the
+    # ranges (8 B per key, 8 B per tile written).
+    radix_path = batch.launches_per_forward > 3
+    n_tiles_b = batch_tiles(cams, *cfg["tile"])
     hbm = {
         "preprocess": (52 * scene.n + len(cams) * scene.n * (96 + 8 + 4)) / (stages["preprocess"] * 1e-3) / 1e9,
-        "emit": (8 * nk) / (stages["emit"] * 1e-3) / 1e9,
+        "emit": (8 * nk + (0 if radix_path else 8 * n_tiles_b)) / (stages["emit"] * 1e-3) / 1e9,
     }
-    # The tile-major binning writes the ranges with the keys; the emit + radix sort path reads the
-    # sorted keys once more for them (8 B per key, 8 B per tile written).
-    if stages["ranges"] > 1e-3:
-        rbytes = 8 * nk + 8 * batch_tiles(cams, *cfg["tile"])
-        hbm["ranges"] = rbytes / (stages["ranges"] * 1e-3) / 1e9
-    # The tile-major binning writes the keys in order (its "sort" stage is empty); the emit +
-    # radix sort path moves 16 B per key per pass.
-    if stages["sort"] > 1e-3:
+    if radix_path:
         hbm["sort"] = (16 * nk * passes) / (stages["sort"] * 1e-3) / 1e9
+        hbm["ranges"] = (8 * nk + 8 * n_tiles_b) / (stages["ranges"] * 1e-3) / 1e9
 
     # ---- plain per-call drop-in on device-resident inputs ----------------------------------
     outs = [(torch.empty(H, W, device=dev), torch.empty(H, W, device=dev)) for _ in cams]
@@ -574,6 +574,9 @@ def main():
                      "fma_ops_per_s": fma_ops, "mufu_ex2_ops_per_s": ex2_ops,
                      "peak_source": "fe_bench_peak microbenchmarks on this GPU (FFMA and MUFU.EX2)"},
         "stages_ms": stages,
+        "stages_note": ("emit + radix sort binning" if radix_path else
+                        "tile-major binning: keys and ranges come from the emit stage; scan, "
+                        "sort and ranges are empty (the gap between two events)"),
         "stages_hbm_gbs": hbm, "hbm_peak_gbs": peaks.get("hbm_gbs"), "hbm_peak_kind": peak_kind,
         "num_keys": nk,
         "evals_per_camera": per_cam_evals,
