@@ -111,3 +111,26 @@ def test_jax_binding_reports_missing_jax():
         pass
     with pytest.raises(ImportError, match="JAX"):
         importlib.import_module("fuzzy_ellipses.jax_ops")
+
+
+@pytest.mark.parametrize("n", [1, 2, 7, 8, 9, 16])
+def test_running_sums_give_the_column_moments(n):
+    """The backward pixel loop (blend_bwd.cu) keeps, per lane of a pixel pair, the running sums
+    S0 = sum h, C1 = sum of S0, C2 = sum of C1 over the row's n pair steps, and forms
+    sum h du = D0 S0 + 2 (n S0 - C1) and
+    sum h du^2 = D0^2 S0 + 4 D0 (n S0 - C1) + 4 (n^2 S0 - (2n+1) C1 + 2 C2)
+    with du = D0 + 2 i at step i. Checked here in float64 against the direct sums."""
+    rng = np.random.default_rng(n)
+    h = rng.normal(size=n)
+    d0 = -7.5 + rng.integers(0, 2)
+    s0 = c1 = c2 = 0.0
+    for i in range(n):
+        s0 += h[i]
+        c1 += s0
+        c2 += c1
+    du = d0 + 2.0 * np.arange(n)
+    i1 = n * s0 - c1
+    i2 = n * n * s0 - (2 * n + 1) * c1 + 2 * c2
+    assert np.isclose(d0 * s0 + 2 * i1, (h * du).sum(), rtol=1e-12, atol=1e-12)
+    assert np.isclose(d0 * d0 * s0 + 4 * d0 * i1 + 4 * i2, (h * du * du).sum(), rtol=1e-12,
+                      atol=1e-10)
