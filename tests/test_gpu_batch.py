@@ -143,6 +143,25 @@ def _host_forward_matches(b, m, p, w, pinned=True):
     assert st["device_error"] == 0
 
 
+@pytest.mark.parametrize("layout", ["depth_first", "alpha_first", "gapped"])
+def test_forward_host_images_in_one_buffer(cuda_device, layout):
+    """Depth and alpha as two views of one host buffer: each band leaves in one 2-D copy whose
+    row pitch is the distance between them, in either order and with a gap between them."""
+    b, items, views, (m, p, w) = make_batch(cuda_device, n_scenes=4, seed=4)
+    depth, alpha = b.forward(m, p, w)
+    torch.cuda.synchronize()
+    n = b.n_pixels
+    gap = 1000 if layout == "gapped" else 0
+    buf = torch.full((2 * n + gap,), -7.0).pin_memory()
+    lo, hi = buf[:n], buf[n + gap:]
+    hd, ha = (hi, lo) if layout == "alpha_first" else (lo, hi)
+    b.forward_host(m.cpu(), p.cpu(), w.cpu(), hd, ha)
+    assert torch.equal(hd, depth.cpu()) and torch.equal(ha, alpha.cpu())
+    if gap:
+        assert torch.all(buf[n:n + gap] == -7.0)  # nothing written between the two images
+    assert b.status()["device_error"] == 0
+
+
 @pytest.mark.parametrize("pinned", [True, False])
 def test_forward_host_equals_device_forward(cuda_device, pinned):
     b, items, views, (m, p, w) = make_batch(cuda_device, n_scenes=6, seed=3)
