@@ -302,8 +302,15 @@ int run_binning(const Pipeline& p, int64_t worst, DevBuf& recbuf, DevBuf& keybuf
   return FE_OK;
 }
 
-// Tile count below which a single-view render defaults to two pixels per blend thread.
-constexpr int64_t kSingleViewPx2Tiles = 3000;
+// Tile count below which a launch defaults to two pixels per blend thread.
+constexpr int64_t kPx2Tiles = 3000;
+
+// Pixels per blend thread when the descriptor leaves it at 0: two for small launches (see the
+// measurements at single_view_pipeline), else the launcher's default for the tile shape.
+int default_px(int px, int tw, int th, int64_t n_tiles) {
+  if (px == 0 && !(tw == 8 && th == 8) && n_tiles < kPx2Tiles) return 2;
+  return px;
+}
 
 Pipeline single_view_pipeline(const fe_render_desc* d, const float* means, const float* prec,
                               const float* logw, const float* quat, const float* trans) {
@@ -324,13 +331,13 @@ Pipeline single_view_pipeline(const fe_render_desc* d, const float* means, const
   p.n_pix = (int64_t)d->height * d->width;
   p.tile_w = tw;
   p.tile_h = th;
-  // One view alone rarely fills the GPU, and its heaviest tile sets the blend's duration: below
-  // about two resident blends' worth of tiles, two pixels per thread (twice the threads per
-  // tile, half the per-thread work) finish sooner. 16 single-view calls of 1000 Gaussians,
+  // A small launch does not fill the GPU, and its heaviest tile sets the blend's duration:
+  // below about two resident blends' worth of tiles, two pixels per thread (twice the threads
+  // per tile, half the per-thread work) finish sooner. 16 single-view calls of 1000 Gaussians,
   // 16x16 tiles, 2 vs 4 pixels per thread: 320x240 0.545 vs 0.587 ms, 640x480 0.727 vs 0.841;
-  // 1280x960 1.337 vs 1.272 (4 per thread wins above about 3000 tiles).
-  p.px = (int)d->px_per_thread;
-  if (p.px == 0 && !(tw == 8 && th == 8) && p.n_tiles < kSingleViewPx2Tiles) p.px = 2;
+  // 1280x960 1.337 vs 1.272. Batched forwards: 8 x 128x128 0.058 vs 0.064 ms, 4 x 256x256
+  // 0.056 vs 0.064; 16 x 320x240 (4800 tiles) 0.112 vs 0.108, 8 x 640x480 0.154 vs 0.140.
+  p.px = default_px((int)d->px_per_thread, tw, th, p.n_tiles);
   p.chunk = (int)(d->flags >> 8) & 0xff;
   p.radix = (d->flags & FE_FLAG_RADIX_BINNING) != 0;
   p.cull_mode = d->cull_mode;
@@ -1124,7 +1131,7 @@ static Pipeline batch_pipeline(fe_batch* b, const float* means, const float* pre
   p.n_pix = b->n_pix;
   p.tile_w = b->tile_w;
   p.tile_h = b->tile_h;
-  p.px = (int)b->desc.px_per_thread;
+  p.px = default_px((int)b->desc.px_per_thread, b->tile_w, b->tile_h, p.n_tiles);
   p.chunk = (int)(b->desc.flags >> 8) & 0xff;
   p.radix = (b->desc.flags & FE_FLAG_RADIX_BINNING) != 0;
   p.cull_mode = b->desc.cull_mode;

@@ -92,7 +92,8 @@ typedef struct fe_render_desc {
   int32_t tile_h;
   uint32_t flags;      /* FE_FLAG_* */
   int32_t px_per_thread; /* blend pixels per thread: 1, 2 or 4 (8x8 tiles: 1 or 2); 0 = default:
-                          * 2 for 8x8 tiles and for single views of fewer than 3000 tiles, else 4 */
+                          * 2 for 8x8 tiles and for renders or batches of fewer than 3000 tiles,
+                          * else 4 */
 } fe_render_desc;
 
 /* Fill d with defaults for an HxW image of n Gaussians. */
