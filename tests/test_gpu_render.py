@@ -8,7 +8,7 @@ import fuzzy_ellipses as fe
 from fuzzy_ellipses import synthetic as S
 from oracle import fm_render_np as O
 from tests.helpers import (TOL_ALPHA, TOL_DEPTH_REL, floor_dominated, oracle_pixels, parity_errors,
-                           scene_to_dev, tile_lists_from_keys, to_dev)
+                           scene_to_dev, tile_lists_from_keys)
 
 pytestmark = pytest.mark.gpu
 TILES = [(8, 8), (16, 16), (32, 8)]

@@ -9,7 +9,6 @@ import torch
 import fuzzy_ellipses as fe
 from fuzzy_ellipses import autotune, serve
 from fuzzy_ellipses import synthetic as S
-from oracle import fm_render_torch as OT
 
 pytestmark = pytest.mark.gpu
 
