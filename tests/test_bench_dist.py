@@ -45,3 +45,27 @@ def test_job_value_takes_the_slowest_rank():
     for _, value, dev_s in res:
         assert dev_s == pytest.approx(1.5)
         assert value == pytest.approx(2 * 1e6 * 10 / 1.5 / 1e6)
+
+
+def test_reference_arm_prints_the_contract_line():
+    """`bench.py --impl reference` runs the CPU restatement of the path (no GPU needed) and prints
+    one JSON line with the metric, the reference marker, its CPU baseline and an e2e without
+    host-device copies."""
+    import json
+    import subprocess
+    import sys
+
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    r = subprocess.run([sys.executable, os.path.join(root, "bench.py"), "--impl", "reference",
+                        "--steps", "1", "--warmup", "1"], capture_output=True, text=True,
+                       timeout=300, cwd=root)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [ln for ln in r.stdout.splitlines() if ln.startswith("{")]
+    assert len(lines) == 1
+    d = json.loads(lines[0])
+    assert d["impl"] == "reference" and d["metric"] == "Mray-Gaussian evals/s"
+    assert d["unit"] == "Mevals/s" and d["value"] > 0 and d["higher_is_better"] is True
+    assert d["cpu_baseline"]["kind"] == "port" and d["cpu_baseline"]["cores"] >= 1
+    assert d["cpu_baseline"]["value"] == d["value"] and d["cpu_baseline"]["sample"]
+    assert d["e2e"] == {"value": d["value"], "unit": "Mevals/s", "h2d_bytes_per_step": 0,
+                        "d2h_bytes_per_step": 0}
