@@ -191,21 +191,54 @@ def count_evals(fe, cams, mpw):
     return per_cam
 
 
-def cpu_baseline_sample(scene, cam, n_pix, seconds_cap=30.0):
-    """Time the float64 fm_render restatement (dense) on a bounded pixel sample; px/s."""
-    from oracle import fm_render_np as O
-    rng = np.random.default_rng(0)
-    pix = rng.choice(cam.height * cam.width, n_pix, replace=False)
-    rays = O.pinhole_rays(cam.height, cam.width, cam.fx, cam.fy, cam.cx, cam.cy)[pix]
-    t0 = time.perf_counter()
-    done = 0
-    for s in range(0, n_pix, 1024):
-        O.render_func_quat(scene.means, scene.prec, scene.logw, rays[s:s + 1024], cam.quat,
-                           cam.trans, 21.4, 2.66)
-        done += min(1024, n_pix - s)
-        if time.perf_counter() - t0 > seconds_cap:
-            break
-    return done / (time.perf_counter() - t0), done
+CPU_SAMPLE_PIXELS = 4096
+
+
+def cpu_reference(scene, cams, steps, warmup, n_pix=CPU_SAMPLE_PIXELS, seed=0):
+    """Time the CPU implementation of the path -- the float64 restatement of fm_render
+    (baseline/fm_render.py:11-126) in torch, dense over all Gaussians, on every host core this
+    process may use -- on one bounded sample per step: ``n_pix`` random pixels of one camera
+    (camera i mod 16 at step i). Both the main line's cpu_baseline and the reference arm use it.
+
+    Returns seconds per step and the host facts (nproc, affinity, threads)."""
+    import torch
+
+    from oracle import fm_render_torch as OT
+    affinity = sorted(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else None
+    threads = len(affinity) if affinity else (os.cpu_count() or 1)
+    torch.set_num_threads(threads)
+    m = torch.from_numpy(scene.means).double()
+    p = torch.from_numpy(scene.prec).double()
+    w = torch.from_numpy(scene.logw).double()
+    rng = np.random.default_rng(seed)
+    times = []
+    with torch.no_grad():
+        for i in range(warmup + steps):
+            c = cams[i % len(cams)]
+            rays_all = OT.pinhole_rays(c.height, c.width, c.fx, c.fy, c.cx, c.cy)
+            pix = torch.from_numpy(rng.choice(c.height * c.width, n_pix, replace=False))
+            t0 = time.perf_counter()
+            OT.render_func_quat(m, p, w, rays_all[pix], torch.from_numpy(c.quat).double(),
+                                torch.from_numpy(c.trans).double(), 21.4, 2.66)
+            if i >= warmup:
+                times.append(time.perf_counter() - t0)
+    return {"s_per_step": statistics.mean(times), "n_pix": n_pix, "n": scene.n,
+            "threads": torch.get_num_threads(), "nproc": os.cpu_count(),
+            "affinity": (f"{len(affinity)} cpus: {affinity[0]}-{affinity[-1]}" if affinity
+                         else "unknown"),
+            "impl": "torch float64 restatement of fm_render (oracle/fm_render_torch.py), dense "
+                    f"over N={scene.n}, torch.set_num_threads({threads})"}
+
+
+def cpu_baseline_line(cpu, e_render, n_render_pixels):
+    """The cpu_baseline object in the metric's unit: renders/s x evaluations per render."""
+    px_s = cpu["n_pix"] / cpu["s_per_step"]
+    renders_s = px_s / n_render_pixels
+    return {"value": renders_s * e_render / 1e6, "unit": "Mevals/s", "cores": cpu["threads"],
+            "kind": "port", "nproc": cpu["nproc"], "affinity": cpu["affinity"],
+            "sample": f"{cpu['n_pix']} random pixels of one 640x480 camera per step (camera i "
+                      f"mod 16), {cpu['impl']}",
+            "renders_per_s": renders_s, "dense_evals_per_s": px_s * cpu["n"]}
 
 
 def run_reference(args):
@@ -214,47 +247,24 @@ def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
         return
-    import torch
-
     from fuzzy_ellipses import synthetic as S
-    from oracle import fm_render_torch as OT
     from oracle import screen_bounds as SB
-    torch.set_num_threads(os.cpu_count() or 1)
     scene, cams = S.config1(seed=0)
     # Evaluations of one tile-binned render (8x8 tiles), from the float64 restatement of the
     # renderer's screen bounds: the unit that converts renders/s into the metric.
     per_cam_evals = [SB.evals_per_render(scene.means, scene.prec, scene.logw, c) for c in cams]
     e_render = float(np.mean(per_cam_evals))
-    m = torch.from_numpy(scene.means).double()
-    p = torch.from_numpy(scene.prec).double()
-    w = torch.from_numpy(scene.logw).double()
-    H, W = 480, 640
-    n_pix = 4096
-    rng = np.random.default_rng(0)
-    times = []
-    with torch.no_grad():
-        for i in range(args.warmup + args.steps):
-            c = cams[i % len(cams)]
-            rays_all = OT.pinhole_rays(H, W, c.fx, c.fy, c.cx, c.cy)
-            pix = torch.from_numpy(rng.choice(H * W, n_pix, replace=False))
-            t0 = time.perf_counter()
-            OT.render_func_quat(m, p, w, rays_all[pix], torch.from_numpy(c.quat).double(),
-                                torch.from_numpy(c.trans).double(), 21.4, 2.66)
-            if i >= args.warmup:
-                times.append(time.perf_counter() - t0)
-    px_s = n_pix / statistics.mean(times)
-    renders_s = px_s / (H * W)
-    value = renders_s * e_render / 1e6
+    cpu = cpu_reference(scene, cams, args.steps, args.warmup)
+    base = cpu_baseline_line(cpu, e_render, cams[0].height * cams[0].width)
+    value = base["value"]
     out = {"metric": METRIC, "value": value, "unit": "Mevals/s", "impl": "reference",
            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
-           "ms_per_step": 1e3 * statistics.mean(times), "higher_is_better": True,
+           "ms_per_step": 1e3 * cpu["s_per_step"], "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-           "config": {"workload": WORKLOAD, "sample_per_step": f"{n_pix} pixels of one camera"},
-           "renders_per_s": renders_s, "dense_evals_per_s": px_s * scene.n,
-           "cpu_baseline": {"value": value, "unit": "Mevals/s", "cores": torch.get_num_threads(),
-                            "kind": "port",
-                            "sample": f"{n_pix} random pixels of one 640x480 camera per step, "
-                                      "dense over N=1000 (torch float64 restatement of fm_render)"},
+           "config": {"workload": WORKLOAD,
+                      "sample_per_step": f"{cpu['n_pix']} pixels of one camera"},
+           "renders_per_s": base["renders_per_s"], "dense_evals_per_s": base["dense_evals_per_s"],
+           "cpu_baseline": base,
            "e2e": {"value": value, "unit": "Mevals/s", "h2d_bytes_per_step": 0,
                    "d2h_bytes_per_step": 0}}
     print(json.dumps(out), flush=True)
@@ -514,19 +524,18 @@ def main():
     next_rows = None if args.no_next else next_rows_bench(fe, dev, scene, cams, fma_ops, ex2_ops,
                                                           peaks["hbm_gbs"])
 
+    # ---- batched uneven renders (256 scenes) ----------------------------------------------
+    config3 = None if args.no_next else config3_bench(fe, dev, max(5, args.steps // 2), fma_ops,
+                                                      ex2_ops)
+
     # ---- served mixed requests vs the plain per-call drop-in ------------------------------
     served = None if args.no_serve else serve_bench(fe, dev)
 
     # ---- CPU baseline (oracle on the host cores, bounded sample) ---------------------------
     cpu = None
     if not args.no_cpu_baseline:
-        px_s, done = cpu_baseline_sample(scene, cams[0], 16384, seconds_cap=25.0)
-        cpu_renders_s = px_s / npix
-        cpu = {"value": cpu_renders_s * (e_step / len(cams)) / 1e6, "unit": "Mevals/s",
-               "cores": 1, "kind": "port",
-               "sample": f"{done} random pixels of camera 0 (of 16), dense over N=1000, numpy "
-                         "float64 restatement of fm_render, single thread",
-               "renders_per_s": cpu_renders_s, "dense_evals_per_s": px_s * scene.n}
+        cpu = cpu_baseline_line(cpu_reference(scene, cams, steps=16, warmup=1), e_step / len(cams),
+                                npix)
 
     blend_achieved = blend_evals_per_s / 1e9
     out = {
@@ -583,6 +592,7 @@ def main():
         "cpu_baseline": cpu,
         "backward": backward,
         "next_rows": next_rows,
+        "batched_uneven_256_scenes": config3,
         "served": served,
         "autotune": tuned and {"bucket": tuned["bucket"],
                                "candidates_ms": {f"{c['tile'][0]}x{c['tile'][1]}/px{c['px']}/ch{c['chunk']}": round(c["ms"], 4)
@@ -600,11 +610,17 @@ def _silhouette(h, w):
     return (((u - w / 2) ** 2 + (v - h / 2) ** 2) < (0.3 * min(h, w)) ** 2).astype(np.float32)
 
 
-def serve_bench(fe, dev, n_requests=500, plain_requests=60, seed=0):
+SERVE_LOAD_FRACTIONS = (0.1, 0.25, 0.5, 0.75, 1.0)
+
+
+def serve_bench(fe, dev, n_requests=500, seed=0):
     """Served mixed requests (N log-uniform in [20, 2000], 1-32 poses, sides 96-480, 30% with a
-    silhouette-BCE backward): saturating arrivals for throughput, Poisson arrivals at half that
-    rate for latency; the plain per-call drop-in (one fe_render_fwd / autograd render per camera,
-    synchronised per request) on the same requests for comparison."""
+    silhouette-BCE backward): saturating arrivals for throughput, then Poisson arrivals swept
+    over SERVE_LOAD_FRACTIONS of that rate (renders/s, p50, p99 per rate); the plain per-call
+    drop-in on the same 500 requests for comparison -- one fe_render_fwd (forward requests) or
+    differentiable render (backward requests) per camera, the silhouette loss and its cotangent
+    from the same fused kernel the server uses (fe_silhouette_bce), results and gradients read
+    back per request."""
     import threading
 
     import torch
@@ -651,12 +667,15 @@ def serve_bench(fe, dev, n_requests=500, plain_requests=60, seed=0):
                 "batches": st["batches"], "wall_s": wall, "lane_busy_s": st["busy_s"]}
 
     sat = run([0.0] * len(reqs))
-    rate = 0.5 * sat["requests_per_s"]
+    sweep = []
     rng = np.random.default_rng(seed + 1)
-    poisson = run(list(rng.exponential(1.0 / rate, size=len(reqs))))
-    poisson["arrival_rate_hz"] = rate
+    for frac in SERVE_LOAD_FRACTIONS:
+        rate = frac * sat["requests_per_s"]
+        r = run(list(rng.exponential(1.0 / rate, size=len(reqs))))
+        r.update(load_fraction=frac, arrival_rate_hz=rate)
+        sweep.append(r)
 
-    # plain per-call drop-in on a prefix of the same requests
+    # The plain per-call drop-in on all the same requests.
     def plain(req):
         m, p, w = [torch.from_numpy(x).to(dev) for x in (req.means, req.prec, req.logw)]
         if req.targets is None:
@@ -665,29 +684,40 @@ def serve_bench(fe, dev, n_requests=500, plain_requests=60, seed=0):
                 d.cpu(), a.cpu()
             return
         m.requires_grad_(); p.requires_grad_(); w.requires_grad_()
-        loss, cnt = 0.0, 0
+        total = sum(c.height * c.width for c in req.cameras)
+        loss = 0.0
         for c, t in zip(req.cameras, req.targets):
             d, a = fe.render(m, p, w, c.fx, c.fy, c.cx, c.cy, c.quat, c.trans, c.height, c.width)
-            ac = a.double().clamp(3e-8, 1 - 3e-8)
-            tt = torch.from_numpy(t).to(dev).double()
-            loss = loss - (tt * torch.log(ac) + (1 - tt) * torch.log(1 - ac)).sum()
-            cnt += a.numel()
-            a.detach().cpu()
-        (loss / cnt).backward()
+            hw = c.height * c.width
+            tt = torch.from_numpy(t).to(dev).reshape(-1)
+            seg = torch.full((1,), hw, dtype=torch.int64, device=dev)
+            # the request's loss is the mean over all its pixels: weight each camera's mean by
+            # its share of the pixels (the server's segment is the whole request)
+            lc, ga = fe.silhouette_bce(a.detach().reshape(-1), tt, seg)
+            ga.mul_(hw / total)
+            loss = loss + lc * (hw / total)
+            torch.autograd.backward(a, ga.view(c.height, c.width))
+            d.detach().cpu(), a.detach().cpu()
+        float(loss)
         m.grad.cpu(), p.grad.cpu(), w.grad.cpu()
 
     for r in reqs[:3]:
         plain(r)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    for r in reqs[:plain_requests]:
+    for r in reqs:
         plain(r)
     torch.cuda.synchronize()
     pw = time.perf_counter() - t0
-    plain_rs = sum(len(r.cameras) for r in reqs[:plain_requests]) / pw
+    plain_rs = renders / pw
+    half = next(r for r in sweep if r["load_fraction"] == 0.5)
     return {"workload": f"{n_requests} requests: N logU[20,2000], 1-32 poses at 0.5 m, side U[96,480], "
                         "30% forward+backward (silhouette BCE), fp32",
-            "saturating": sat, "poisson_half_load": poisson,
+            "saturating": sat,
+            "poisson_sweep": sweep,
+            "poisson_half_load": half,
+            "plain_per_call": {"renders_per_s": plain_rs, "wall_s": pw, "requests": len(reqs),
+                               "loss": "fe_silhouette_bce per camera (the server's fused kernel)"},
             "plain_per_call_renders_per_s": plain_rs,
             "served_over_plain": sat["renders_per_s"] / plain_rs}
 
@@ -764,6 +794,84 @@ def next_rows_bench(fe, dev, scene, cams, fma_ops, ex2_ops, hbm_gbs):
     out["transform_points"] = {"workload": f"{n_p} points", "ms": ms, "hbm_gbs": gbs,
                                "roofline": {"bound": "hbm", "achieved": gbs, "peak": hbm_gbs,
                                             "unit": "GB/s", "frac": gbs / hbm_gbs}}
+    return out
+
+
+def config3_bench(fe, dev, steps, fma_ops, ex2_ops):
+    """Batched uneven renders at their stated size: 256 scenes (N logU[8,512]), 1-8 poses each at
+    0.5 m, sides {64, 128, 256}; one persistent launch sequence with the autotuned tile shape,
+    pixels per thread and record chunk, captured once as a CUDA graph and replayed (L2 flushed
+    between replays). Evaluations counted as for the headline (8x8-tile keys x tile pixels)."""
+    import torch
+
+    from fuzzy_ellipses import synthetic as S
+    items = S.config3(seed=0)
+    means, prec, logw, scenes, views, cams = [], [], [], [], [], []
+    off = 0
+    for si, (sc, cs) in enumerate(items):
+        means.append(sc.means); prec.append(sc.prec); logw.append(sc.logw)
+        scenes.append((off, sc.n))
+        off += sc.n
+        for c in cs:
+            views.append(dict(scene=si, height=c.height, width=c.width, fx=c.fx, fy=c.fy,
+                              cx=c.cx, cy=c.cy, quat=c.quat, trans=c.trans))
+            cams.append((si, c))
+    m, p, w = [torch.from_numpy(np.concatenate(x)).to(dev) for x in (means, prec, logw)]
+    tuner = fe.autotune.Autotuner(persist=False)
+    tuned = tuner.tune(scenes, views, m, p, w, reps=3)
+    b = fe.Batch(scenes, views, tile=tuned["tile"], px=tuned["px"], chunk=tuned["chunk"])
+    depth = torch.empty(b.n_pixels, device=dev)
+    alpha = torch.empty(b.n_pixels, device=dev)
+    e_total = 0
+    for si, c in cams:
+        sl = slice(scenes[si][0], scenes[si][0] + scenes[si][1])
+        e_total += count_evals(fe, [c], (m[sl], p[sl], w[sl]))[0]
+    cap = torch.cuda.Stream(device=dev)
+    cap.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(cap):
+        b.forward(m, p, w, depth, alpha)
+    torch.cuda.current_stream().wait_stream(cap)
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g, stream=cap):
+        b.forward(m, p, w, depth, alpha)
+    for _ in range(3):
+        g.replay()
+    torch.cuda.synchronize()
+    st = b.status()
+    assert st["device_error"] == 0 and st["num_keys"] == st["want_keys"], st
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(steps)]
+    for i in range(steps):
+        flush.fill_(i & 0xFF)
+        ev[i][0].record()
+        g.replay()
+        ev[i][1].record()
+    torch.cuda.synchronize()
+    ms = statistics.median(a.elapsed_time(z) for a, z in ev)
+    stage_runs = []
+    for _ in range(5):
+        flush.fill_(1)
+        _, _, sm = b.forward_timed(m, p, w, depth, alpha)
+        stage_runs.append(sm)
+    stages = {k: statistics.median(r[k] for r in stage_runs) for k in b.STAGES}
+    peak = min(fma_ops / PER_EVAL_FMA, ex2_ops / PER_EVAL_MUFU)
+    blend_evals_s = e_total / (stages["blend"] * 1e-3)
+    out = {"workload": f"256 scenes (N logU[8,512]), {len(views)} views of 64^2/128^2/256^2, "
+                       f"{b.n_pixels} pixels, fp32",
+           "launch": "one persistent launch sequence, CUDA graph replay, L2 flushed between",
+           "autotuned": {"tile": f"{tuned['tile'][0]}x{tuned['tile'][1]}", "px": tuned["px"],
+                         "chunk": tuned["chunk"], "bucket": tuned["bucket"],
+                         "candidates_ms": {f"{c['tile'][0]}x{c['tile'][1]}/px{c['px']}/ch{c['chunk']}": round(c["ms"], 4)
+                                           for c in tuned["candidates"]}},
+           "views": len(views), "ms_per_step": ms, "renders_per_s": len(views) / (ms * 1e-3),
+           "evals_per_step": e_total, "mevals_per_s": e_total / (ms * 1e-3) / 1e6,
+           "num_keys": st["num_keys"], "stages_ms": stages,
+           "gpu_launches_per_step": b.launches_per_forward,
+           "blend_roofline": {"bound": "fma+xu", "achieved": blend_evals_s / 1e9,
+                              "peak": peak / 1e9, "unit": "Gevals/s",
+                              "frac": blend_evals_s / peak}}
+    b.close()
     return out
 
 

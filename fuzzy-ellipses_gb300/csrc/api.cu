@@ -629,7 +629,7 @@ void fe_pixlist_desc_init(fe_pixlist_desc* d, int32_t n, int32_t n_poses, int64_
                           float inv_f) {
   std::memset(d, 0, sizeof(*d));
   d->magic = FE_DESC_MAGIC;
-  d->version = FE_DESC_VERSION;
+  d->version = FE_PIXLIST_DESC_VERSION;
   d->n_gaussians = n;
   d->n_poses = n_poses;
   d->n_rays = n_rays;
@@ -638,17 +638,34 @@ void fe_pixlist_desc_init(fe_pixlist_desc* d, int32_t n, int32_t n_poses, int64_
   d->beta3 = 2.66f;
   d->cull_mode = FE_CULL_EPS;
   d->cull_param = kDefaultCullEps;
+  d->ray_mode = FE_RAYS_POSE_INDEXED;
+  d->aspect = 1.f;
+  d->shift_x = 0.5f;
+  d->shift_y = 0.5f;
 }
 
-int fe_render_pixels(const fe_pixlist_desc* d, const float* means, const float* prec,
+int fe_render_pixels(const fe_pixlist_desc* d_in, const float* means, const float* prec,
                      const float* logw, const float* poses, const float* rays,
                      const float* features, float* depth, float* alpha, float* flow_next,
                      float* flow_prev, float* out_features, float* weights,
                      fe_stream_t stream_) {
   cudaStream_t st = reinterpret_cast<cudaStream_t>(stream_);
-  if (!d) return fail(FE_ERR_INVALID_ARGUMENT, "descriptor is NULL");
-  if (d->magic != FE_DESC_MAGIC || d->version != FE_DESC_VERSION)
+  if (!d_in) return fail(FE_ERR_INVALID_ARGUMENT, "descriptor is NULL");
+  if (d_in->magic != FE_DESC_MAGIC || (d_in->version != 1 && d_in->version != 2))
     return fail(FE_ERR_DESCRIPTOR, "pixel-list descriptor magic/version mismatch");
+  // A version-1 descriptor is the version-2 layout cut before ray_mode: read only that prefix.
+  fe_pixlist_desc dv;
+  fe_pixlist_desc_init(&dv, 0, 1, 0, 1.f);
+  std::memcpy(&dv, d_in, d_in->version == 1 ? offsetof(fe_pixlist_desc, ray_mode) : sizeof(dv));
+  const fe_pixlist_desc* d = &dv;
+  const bool cam = d->ray_mode == FE_RAYS_QUAT_CAM;
+  if (d->ray_mode != FE_RAYS_POSE_INDEXED && !cam)
+    return fail(FE_ERR_INVALID_ARGUMENT, "unknown ray mode");
+  if (cam && (!(d->aspect > 0.f) || !std::isfinite(d->aspect) || !std::isfinite(d->shift_x) ||
+              !std::isfinite(d->shift_y)))
+    return fail(FE_ERR_INVALID_ARGUMENT, "aspect must be finite and positive, shifts finite");
+  if (cam && (flow_next || flow_prev))
+    return fail(FE_ERR_INVALID_ARGUMENT, "flow needs pose-indexed rays");
   if (d->n_gaussians < 0 || d->n_poses < 1 || d->n_rays < 0)
     return fail(FE_ERR_INVALID_ARGUMENT, "need n_gaussians >= 0, n_poses >= 1, n_rays >= 0");
   if (!(d->inv_f != 0.f) || !std::isfinite(d->inv_f))
@@ -669,8 +686,14 @@ int fe_render_pixels(const fe_pixlist_desc* d, const float* means, const float* 
   rc = a->rec.reserve(std::max<size_t>(pixlist_scratch_bytes(d->n_gaussians, d->n_poses), 256),
                       st);
   if (rc) return rc;
-  launch_render_pixels(d->n_gaussians, d->n_poses, means, prec, logw, poses, d->n_rays, rays,
-                       d->inv_f, d->beta2, d->beta3, d->cull_mode, d->cull_param, features,
+  PixRayModel rm;
+  rm.inv_f = d->inv_f;
+  rm.aspect = cam ? d->aspect : 1.f;
+  rm.shift_x = cam ? d->shift_x : 0.f;
+  rm.shift_y = cam ? d->shift_y : 0.f;
+  rm.stride = cam ? 3 : 4;
+  launch_render_pixels(d->n_gaussians, cam ? 1 : d->n_poses, means, prec, logw, poses, d->n_rays,
+                       rays, rm, d->beta2, d->beta3, d->cull_mode, d->cull_param, features,
                        d->n_features, depth, alpha, flow_next, flow_prev, out_features, weights,
                        a->rec.ptr, st);
   FE_CUDA(cudaGetLastError());

@@ -119,13 +119,20 @@ void launch_transform_points_bwd(int64_t n, const float* points, const float* po
                                  cudaStream_t st);
 
 // pixlist.cu
-// Multi-pose pixel-list render (fm_render.py render_func_idx_quattrans[_flow]); scratch:
-// pixlist_scratch_bytes(n, n_poses). feats (n x nf, nf <= 16), flows, out_feats and weights
-// (n x n_rays) are optional (NULL).
+// Pixel-list render (fm_render.py render_func_idx_quattrans[_flow], render_func_quat_cam);
+// scratch: pixlist_scratch_bytes(n, n_poses). feats (n x nf, nf <= 16), flows, out_feats and
+// weights (n x n_rays) are optional (NULL).
+// Ray model: rows of `stride` floats (x, y, c[, pose]); the camera ray is
+// ((x - shift_x) inv_f, (y - shift_y) aspect inv_f, c) of pose `pose` (stride 4) or pose 0.
+struct PixRayModel {
+  float inv_f, aspect, shift_x, shift_y;
+  int stride;
+};
 size_t pixlist_scratch_bytes(int n, int n_poses);
 void launch_render_pixels(int n, int n_poses, const float* means, const float* prec,
                           const float* logw, const float* poses, int64_t n_rays, const float* rays,
-                          float inv_f, float beta2, float beta3, int cull_mode, float cull_param,
+                          const PixRayModel& rm, float beta2, float beta3, int cull_mode,
+                          float cull_param,
                           const float* feats, int nf, float* depth, float* alpha,
                           float* flow_next, float* flow_prev, float* out_feats, float* weights,
                           void* scratch, cudaStream_t st);

@@ -1,17 +1,20 @@
 // pixlist.cu -- multi-pose pixel-list renderer with optical flow.
 //
-// Restates baseline/fm_render.py:151-224 (render_func_idx_quattrans and its _flow variant) with
-// the argument order of their render_func_rays calls fixed (they pass the Gaussians where the
-// rays belong). Input rays are the reference's pixel_posei rows (x, y, c, pose): the camera ray is
-// (x invF, y invF, c) of pose `pose` (poses: (n_poses, 7) = quaternion (4, scalar first),
-// translation (3)). Outputs per ray: depth and alpha as render_func_rays computes them (culled at
+// Restates baseline/fm_render.py:151-224 (render_func_idx_quattrans and its _flow variant) and
+// :130-144 (render_func_quat_cam) with the argument order of their render_func_rays calls fixed
+// (they pass the Gaussians where the rays belong). Input rays are the reference's pixel_posei rows
+// (x, y, c, pose): the camera ray is (x invF, y invF, c) of pose `pose` (poses: (n_poses, 7) =
+// quaternion (4, scalar first), translation (3)); or render_func_quat_cam's pixel_list rows
+// (x, y, c) of one pose, whose camera ray is ((x - 0.5) invF, (y - 0.5) aspect invF, c) -- the
+// same model with focal lengths 1/invF and 1/(aspect invF) and the pixel offsets shifted.
+// Outputs per ray: depth and alpha as render_func_rays computes them (culled at
 // the renderer's density cut-off), optionally the softmax-weighted per-Gaussian features
 // (fm_render's w applied to a feature table) and the dense weights w (N x rays), and the
 // forward / backward optical flow to poses pose+1 / pose-1 (clamped), fm_render.py:186-222.
 //
 // Work: pixlist_prep_kernel builds, per (pose, Gaussian), the same float32 record and screen
-// bound as the image preprocess (fe_footprint.cuh) with focal 1/invF and the principal point at 0
-// (pixel offsets x/c, y/c). pixlist_kernel gives each ray one thread that tests every Gaussian's
+// bound as the image preprocess (fe_footprint.cuh) with focal lengths 1/invF, 1/(aspect invF) and
+// the principal point at 0 (pixel offsets (x - shift_x)/c, (y - shift_y)/c). pixlist_kernel gives each ray one thread that tests every Gaussian's
 // bound of its pose (a warp of rays of one pose reads the same record: broadcast loads) and
 // evaluates only the Gaussians whose k-sigma projection contains the ray.
 #include <algorithm>
@@ -35,11 +38,10 @@ __device__ __forceinline__ void pose_rot(const float* pose, float R[9]) {
 __global__ void pixlist_prep_kernel(int n, int n_poses, const float* __restrict__ means,
                                     const float* __restrict__ prec,
                                     const float* __restrict__ logw,
-                                    const float* __restrict__ poses, float inv_f, int cull_mode,
-                                    float cull_param, PixRec* __restrict__ recs) {
+                                    const float* __restrict__ poses, float fx, float fy,
+                                    int cull_mode, float cull_param, PixRec* __restrict__ recs) {
   const int64_t total = (int64_t)n * n_poses;
-  const float f = 1.f / inv_f;
-  const float L = 4.f * f;  // expansion centres within four focal lengths of the axis
+  const float L = 4.f * fmaxf(fabsf(fx), fabsf(fy));  // expansion centres within four focal lengths
   for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
        idx += (int64_t)gridDim.x * blockDim.x) {
     const int k = (int)(idx / n);
@@ -54,14 +56,14 @@ __global__ void pixlist_prep_kernel(int n, int n_poses, const float* __restrict_
     r.ulo = INFINITY; r.uhi = -INFINITY; r.vlo = INFINITY; r.vhi = -INFINITY;  // empty
     if (k2 > 0.f) {
       float ulo = 0.f, uhi = 0.f, vlo = 0.f, vhi = 0.f;
-      if (screen_bounds(ct, k2, f, f, 0.f, 0.f, ulo, uhi, vlo, vhi) == kFootBounded) {
+      if (screen_bounds(ct, k2, fx, fy, 0.f, 0.f, ulo, uhi, vlo, vhi) == kFootBounded) {
         const float margin = 0.02f;  // covers the float32 rounding of the bounds
         r.ulo = ulo - margin; r.uhi = uhi + margin; r.vlo = vlo - margin; r.vhi = vhi + margin;
       } else {
         r.ulo = -INFINITY; r.uhi = INFINITY; r.vlo = -INFINITY; r.vhi = INFINITY;
       }
     }
-    make_record(ct, lw, f, f, 0.f, 0.f, 0.f, 0.f, -L, L, -L, L, r.g);
+    make_record(ct, lw, fx, fy, 0.f, 0.f, 0.f, 0.f, -L, L, -L, L, r.g);
     recs[idx] = r;
   }
 }
@@ -87,21 +89,28 @@ __device__ __forceinline__ void reproject(const float* poses, int a, int b, floa
 
 __global__ void __launch_bounds__(128) pixlist_kernel(
     int n, int n_poses, const PixRec* __restrict__ recs, int64_t n_rays,
-    const float* __restrict__ rays, float inv_f, float beta2, float beta3,
+    const float* __restrict__ rays, PixRayModel rm, float beta2, float beta3,
     const float* __restrict__ poses, const float* __restrict__ feats, int nf,
     float* __restrict__ depth, float* __restrict__ alpha, float* __restrict__ flow_next,
     float* __restrict__ flow_prev, float* __restrict__ out_feats, float* __restrict__ weights) {
   const float nb2 = -beta2 * kLog2e;
   const float kn = -0.5f * kLog2e;
+  const float inv_f = rm.inv_f;
   for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < n_rays;
        j += (int64_t)gridDim.x * blockDim.x) {
-    const float rx = rays[4 * j], ry = rays[4 * j + 1], rc = rays[4 * j + 2];
-    int k = (int)rays[4 * j + 3];  // astype(int); out-of-range indices clamp, as JAX gathers do
-    k = min(max(k, 0), n_poses - 1);
-    // The record is evaluated on the unit-depth ray (x/c, y/c, 1); the ray parameter of
-    // (x inv_f, y inv_f, c), which the softmax logits, the z > 0 mask and the depth use, is z / c.
+    const float* row = rays + rm.stride * j;
+    const float rx = row[0], ry = row[1], rc = row[2];
+    int k = 0;
+    if (rm.stride == 4) {
+      k = (int)row[3];  // astype(int); out-of-range indices clamp, as JAX gathers do
+      k = min(max(k, 0), n_poses - 1);
+    }
+    // The record is evaluated on the unit-depth ray (u/fx, v/fy, 1) with pixel offsets
+    // u = (x - shift_x)/c, v = (y - shift_y)/c; the parameter of the input ray
+    // ((x - shift_x) inv_f, (y - shift_y) aspect inv_f, c), which the softmax logits, the z > 0
+    // mask and the depth use, is z / c.
     const float ic = 1.f / rc;
-    const float u = rx * ic, v = ry * ic;
+    const float u = (rx - rm.shift_x) * ic, v = (ry - rm.shift_y) * ic;
     const PixRec* pr = recs + (int64_t)k * n;
     float A = 0.f, m = -1e30f, W = 0.f, Z = 0.f;
     constexpr int kMaxF = 16;
@@ -213,8 +222,8 @@ size_t pixlist_scratch_bytes(int n, int n_poses) { return sizeof(PixRec) * (size
 
 void launch_render_pixels(int n, int n_poses, const float* means, const float* prec,
                           const float* logw, const float* poses, int64_t n_rays, const float* rays,
-                          float inv_f, float beta2, float beta3, int cull_mode, float cull_param,
-                          const float* feats, int nf, float* depth, float* alpha,
+                          const PixRayModel& rm, float beta2, float beta3, int cull_mode,
+                          float cull_param, const float* feats, int nf, float* depth, float* alpha,
                           float* flow_next, float* flow_prev, float* out_feats, float* weights,
                           void* scratch, cudaStream_t st) {
   if (n_rays <= 0) return;
@@ -222,12 +231,13 @@ void launch_render_pixels(int n, int n_poses, const float* means, const float* p
   const int64_t total = (int64_t)n * n_poses;
   if (total > 0) {
     const int64_t b = (total + 127) / 128;
+    const float fx = 1.f / rm.inv_f, fy = 1.f / (rm.aspect * rm.inv_f);
     pixlist_prep_kernel<<<(unsigned)std::min<int64_t>(b, 152 * 16), 128, 0, st>>>(
-        n, n_poses, means, prec, logw, poses, inv_f, cull_mode, cull_param, recs);
+        n, n_poses, means, prec, logw, poses, fx, fy, cull_mode, cull_param, recs);
   }
   const int64_t b = (n_rays + 127) / 128;
   pixlist_kernel<<<(unsigned)std::min<int64_t>(b, 152 * 32), 128, 0, st>>>(
-      n, n_poses, recs, n_rays, rays, inv_f, beta2, beta3, poses, feats, nf, depth, alpha,
+      n, n_poses, recs, n_rays, rays, rm, beta2, beta3, poses, feats, nf, depth, alpha,
       flow_next, flow_prev, out_feats, weights);
 }
 

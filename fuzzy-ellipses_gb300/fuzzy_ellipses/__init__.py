@@ -12,6 +12,7 @@ from ._native import FEError, NativeLibraryMissing, load as load_native  # noqa:
 from .api import (Batch, bench_peak, device_status, gmm_log_likelihood,  # noqa: F401
                   projection_matrix, rasterize, reference_binning, reference_num_stds, render,
                   render_binning, render_features, render_forward, render_pixels,
+                  render_pixels_cam,
                   silhouette_bce)
 
 __version__ = "0.1.0"

@@ -17,6 +17,9 @@ LIB_PATH = os.path.join(_HERE, "_lib", "libfuzzy_ellipses.so")
 
 FE_DESC_MAGIC = 0x31644546
 FE_DESC_VERSION = 1
+FE_PIXLIST_DESC_VERSION = 2
+FE_RAYS_POSE_INDEXED = 0
+FE_RAYS_QUAT_CAM = 1
 FE_CULL_EPS = 0
 FE_CULL_NSTD = 1
 FE_DEVERR_CAPACITY = 1
@@ -91,7 +94,9 @@ class PixlistDesc(ctypes.Structure):
                 ("n_gaussians", ctypes.c_int32), ("n_poses", ctypes.c_int32),
                 ("n_rays", ctypes.c_int64), ("inv_f", ctypes.c_float), ("beta2", ctypes.c_float),
                 ("beta3", ctypes.c_float), ("cull_mode", ctypes.c_int32),
-                ("cull_param", ctypes.c_float), ("n_features", ctypes.c_int32)]
+                ("cull_param", ctypes.c_float), ("n_features", ctypes.c_int32),
+                ("ray_mode", ctypes.c_int32), ("aspect", ctypes.c_float),
+                ("shift_x", ctypes.c_float), ("shift_y", ctypes.c_float)]
 
 
 class ServerConfig(ctypes.Structure):

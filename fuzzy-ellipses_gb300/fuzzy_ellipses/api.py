@@ -251,6 +251,53 @@ def render_pixels(means, prec, logw, pixel_posei, inv_f, poses, beta2=21.4, beta
     return out + ((of,) if feats is not None else ())
 
 
+def render_pixels_cam(means, prec, logw, pixel_list, aspect, inv_f, quat, t, beta2=21.4,
+                      beta3=2.66, *, weights=False, features=None, cull="eps", cull_param=None,
+                      shift=(0.5, 0.5)):
+    """Pixel-list render of one pose with a single inverse focal length and an aspect ratio
+    (baseline/fm_render.py:130-144 ``render_func_quat_cam``).
+
+    ``pixel_list`` (P, 3): rows (x, y, c); the camera ray is ((x - 0.5) inv_f,
+    (y - 0.5) aspect inv_f, c), rotated by ``quat_to_rot(quat)`` and starting at ``t``. Returns
+    ``(depth, alpha, None, w)`` like the reference (``w`` the dense (N, P) weights when
+    ``weights=True``, else None), with the softmax-weighted features (P, F) appended when
+    ``features`` (N, F) is given. Forward only."""
+    lib = N.load()
+    n = _check_inputs(means, prec, logw)
+    dev = means.device
+    rays = torch.as_tensor(pixel_list).to(device=dev, dtype=torch.float32).contiguous()
+    if rays.dim() != 2 or rays.shape[1] != 3:
+        raise ValueError("pixel_list must be (P, 3)")
+    pose = torch.cat([torch.as_tensor(quat, dtype=torch.float32).reshape(4),
+                      torch.as_tensor(t, dtype=torch.float32).reshape(3)]).to(dev).reshape(1, 7)
+    P = rays.shape[0]
+    d = N.PixlistDesc()
+    lib.fe_pixlist_desc_init(ctypes.byref(d), n, 1, P, float(inv_f))
+    d.ray_mode = N.FE_RAYS_QUAT_CAM
+    d.aspect = float(aspect)
+    d.shift_x, d.shift_y = float(shift[0]), float(shift[1])
+    d.beta2, d.beta3 = float(beta2), float(beta3)
+    if cull == "eps":
+        d.cull_mode, d.cull_param = N.FE_CULL_EPS, (1e-7 if cull_param is None else float(cull_param))
+    else:
+        d.cull_mode, d.cull_param = N.FE_CULL_NSTD, (3.0 if cull_param is None else float(cull_param))
+    feats = None
+    if features is not None:
+        feats = features.to(device=dev, dtype=torch.float32).contiguous()
+        if feats.dim() != 2 or feats.shape[0] != n:
+            raise ValueError("features must be (N, F)")
+        d.n_features = feats.shape[1]
+    depth = torch.empty(P, device=dev)
+    alpha = torch.empty(P, device=dev)
+    of = torch.empty((P, d.n_features), device=dev) if feats is not None else None
+    w = torch.empty((n, P), device=dev) if weights else None
+    N.check(lib.fe_render_pixels(ctypes.byref(d), _ptr(means), _ptr(prec), _ptr(logw), _ptr(pose),
+                                 _ptr(rays), _ptr(feats), _ptr(depth), _ptr(alpha), None, None,
+                                 _ptr(of), _ptr(w), _stream()))
+    out = (depth, alpha, None, w)
+    return out + ((of,) if feats is not None else ())
+
+
 def gmm_log_likelihood(means, prec, logw, points, *, return_matrix=False):
     """Log-likelihood of points (P, 3) under the mixture (the reference's ``log_likelihood``,
     baseline/fm_render.py:231-259): returns ``(nll, point_ll)`` -- the mean negative

@@ -410,11 +410,15 @@ int fe_gmm_log_likelihood(const float *d_means, const float *d_prec, const float
                           int32_t n, const float *d_points, int64_t n_points, float *d_point_ll,
                           float *d_res, double *d_total, fe_stream_t stream);
 
-/* Multi-pose pixel-list render with optical flow: the reference's render_func_idx_quattrans and
- * render_func_idx_quattrans_flow (baseline/fm_render.py:151-224, whose render_func_rays calls pass
- * the Gaussians where the rays belong; the intended argument order is used here).
- *   d_rays (n_rays, 4): the reference's pixel_posei rows (x, y, c, pose); the camera ray is
- *     (x inv_f, y inv_f, c) of pose `pose` (truncated to an integer and clamped to the poses);
+/* Pixel-list render: the reference's render_func_idx_quattrans, render_func_idx_quattrans_flow
+ * and render_func_quat_cam (baseline/fm_render.py:130-224, whose render_func_rays calls pass the
+ * Gaussians where the rays belong; the intended argument order is used here). Two ray modes:
+ *   FE_RAYS_POSE_INDEXED (render_func_idx_quattrans[_flow]): d_rays (n_rays, 4), the reference's
+ *     pixel_posei rows (x, y, c, pose); the camera ray is (x inv_f, y inv_f, c) of pose `pose`
+ *     (truncated to an integer and clamped to the poses);
+ *   FE_RAYS_QUAT_CAM (render_func_quat_cam): d_rays (n_rays, 3), the reference's pixel_list rows
+ *     (x, y, c) of the single pose 0; the camera ray is ((x - shift_x) inv_f,
+ *     (y - shift_y) aspect inv_f, c) (the reference shifts by 0.5, 0.5); no flow;
  *   d_poses (n_poses, 7): quaternion (4, scalar first) and translation (3) per pose;
  *   d_features (n, n_features) or NULL: per-Gaussian features (n_features <= 16);
  * outputs per ray: d_depth, d_alpha; optional (NULL to skip): d_flow_next / d_flow_prev
@@ -433,7 +437,14 @@ typedef struct fe_pixlist_desc {
   int32_t cull_mode;   /* fe_cull_mode */
   float cull_param;
   int32_t n_features;
+  /* Version 2 fields (a version-1 descriptor ends before them and renders FE_RAYS_POSE_INDEXED) */
+  int32_t ray_mode;    /* fe_ray_mode */
+  float aspect;        /* FE_RAYS_QUAT_CAM: y scale of the ray relative to x (1 by default) */
+  float shift_x, shift_y; /* FE_RAYS_QUAT_CAM: pixel shift subtracted first (0.5, 0.5 by default) */
 } fe_pixlist_desc;
+
+#define FE_PIXLIST_DESC_VERSION 2
+typedef enum fe_ray_mode { FE_RAYS_POSE_INDEXED = 0, FE_RAYS_QUAT_CAM = 1 } fe_ray_mode;
 
 void fe_pixlist_desc_init(fe_pixlist_desc *desc, int32_t n, int32_t n_poses, int64_t n_rays,
                           float inv_f);

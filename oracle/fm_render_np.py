@@ -8,6 +8,8 @@ It restates, operation for operation and in float64 NumPy:
 
 * ``render_func_rays``  -- ``baseline/fm_render.py:11-109``
 * ``render_func_quat``  -- ``baseline/fm_render.py:113-126``
+* ``render_func_quat_cam`` -- ``baseline/fm_render.py:130-144``
+* ``render_func_idx_quattrans[_flow]`` -- ``baseline/fm_render.py:151-224``
 * ``jax_stable_exp``    -- ``baseline/util_render.py:5-9``
 * ``quat_to_rot``       -- ``baseline/util_render.py:51-76``
 
@@ -22,9 +24,11 @@ Details kept exactly as the reference has them:
 The reference evaluates ``jax.lax.map`` in batches of 16 (``:79,86``); batching does not change
 results, so this restatement evaluates a dense ``[N, pixels]`` block per chunk of pixels.
 
-JAX is not installed on either machine this project runs on, so ``fm_render.py`` itself cannot be
-executed; this restatement is pinned by analytic known-answer cases (see ``tests/test_oracle.py``)
-rather than by running the reference.
+JAX is not installed on either machine this project runs on. The restatement is pinned against
+the reference's own ``fm_render.py``, imported unmodified with a float64 NumPy stand-in for JAX
+(``tests/golden/numpy_jax.py``): ``tests/golden/make_fm_render_golden.py`` ran it and committed
+its outputs as ``tests/golden/fm_render_golden.npz``, and ``tests/test_oracle.py`` checks this
+module against them (agreement to about 1e-13), beside analytic known-answer cases.
 
 A *culled* variant (``render_culled``) evaluates each pixel only over the Gaussians listed for its
 tile. It defines the quantity a tile-binned renderer computes, so arithmetic error (kernel vs
@@ -43,6 +47,7 @@ __all__ = [
     "pinhole_rays",
     "render_pinhole",
     "render_culled",
+    "render_func_quat_cam",
     "ray_gaussian_terms",
 ]
 
@@ -207,6 +212,16 @@ def render_culled(means, prec_full, weights_log, height, width, fx, fy, cx, cy, 
             depth.ravel()[pix] = d
             alpha.ravel()[pix] = a
     return depth, alpha
+
+
+def render_func_quat_cam(means, prec_full, weights_log, pixel_list, aspect, invF, quat, t,
+                         beta_2, beta_3, return_weights=False):
+    """``fm_render.py:130-144`` (argument order of its render_func_rays call fixed): rays
+    ``(pixel_list - [0.5, 0.5, 0]) * [invF, aspect invF, 1]`` rotated by ``quat_to_rot(quat)``."""
+    pl = np.asarray(pixel_list, dtype=np.float64)
+    rays = (pl - np.array([0.5, 0.5, 0.0])) * np.array([invF, aspect * invF, 1.0])   # :133-135
+    return render_func_quat(means, prec_full, weights_log, rays, quat, t, beta_2, beta_3,
+                            return_weights=return_weights)                           # :137-144
 
 
 def _pose_rays(pixel_posei, invF, poses):

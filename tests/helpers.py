@@ -1,9 +1,53 @@
-"""Shared helpers for the GPU parity tests."""
+"""Shared helpers for the parity tests."""
+
+import functools
+import os
 
 import numpy as np
 import torch
 
+from fuzzy_ellipses import synthetic as S
 from oracle import fm_render_np as O
+
+# Outputs of the reference's own baseline/fm_render.py (imported unmodified, float64), made by
+# tests/golden/make_fm_render_golden.py; inputs are stored beside them.
+GOLDEN_FM = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden",
+                         "fm_render_golden.npz")
+
+
+@functools.lru_cache(maxsize=1)
+def golden():
+    with np.load(GOLDEN_FM) as z:
+        return {k: z[k] for k in z.files}
+
+
+def golden_scene(key):
+    g = golden()
+    return S.Scene(g[f"{key}_means"], g[f"{key}_prec"], g[f"{key}_logw"])
+
+
+def golden_camera(key):
+    """The camera of a full-view fixture: (Camera, depth (H, W), alpha (H, W))."""
+    g = golden()
+    h, w, fx, fy, cx, cy = g[f"{key}_cam"]
+    cam = S.Camera(int(h), int(w), float(fx), float(fy), float(cx), float(cy), g[f"{key}_quat"],
+                   g[f"{key}_trans"])
+    return cam, g[f"{key}_depth"], g[f"{key}_alpha"]
+
+
+def golden_cameras(key):
+    """The cameras of a multi-camera fixture (cfg1, cfg2)."""
+    g = golden()
+    out = []
+    for row, q, t in zip(g[f"{key}_cams"], g[f"{key}_quats"], g[f"{key}_trans"]):
+        h, w, fx, fy, cx, cy = row
+        out.append(S.Camera(int(h), int(w), float(fx), float(fy), float(cx), float(cy), q, t))
+    return out
+
+
+# Full-view fixtures of the edge scenes, in the order the generator writes them.
+GOLDEN_VIEWS = ["cfg0", "behind", "straddle", "subpixel", "tiny1x1", "tiny3x17", "tiny37x23",
+                "tiny64x1"]
 
 # Stated tolerances (the benchmark spec): absolute alpha, relative depth on pixels where the oracle's
 # alpha exceeds DEPTH_MASK_ALPHA (fm_render's depth on near-empty pixels is a softmax over far

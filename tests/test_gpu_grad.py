@@ -1,5 +1,7 @@
 """The hand-written backward against torch float64 autograd of the fm_render restatement (the
-stand-in for jax.grad of fm_render) and against central differences of the CUDA forward."""
+stand-in for jax.grad of fm_render, itself checked against central differences of the reference's
+own fm_render in tests/test_oracle.py), against those reference central differences directly, and
+against central differences of the CUDA forward."""
 
 import numpy as np
 import pytest
@@ -9,7 +11,7 @@ import fuzzy_ellipses as fe
 from fuzzy_ellipses import synthetic as S
 from oracle import fm_render_torch as OT
 from oracle import fm_render_np as O
-from tests.helpers import scene_to_dev
+from tests.helpers import golden, golden_cameras, golden_scene, scene_to_dev
 
 pytestmark = pytest.mark.gpu
 GRAD_TOL = 2e-3  # relative L2 error per parameter group
@@ -21,13 +23,14 @@ def rel(a, b):
 
 @pytest.fixture(scope="module")
 def cfg2():
-    gt, model, cams = S.config2(seed=0)
-    cams = cams[::5]  # 4 of the 20 views keep the float64 autograd reference fast
-    targets = []
-    for c in cams:
-        _, a = O.render_pinhole(gt.means, gt.prec, gt.logw, c.height, c.width, c.fx, c.fy, c.cx,
-                                c.cy, c.quat, c.trans)
-        targets.append((a > 0.5).astype(np.float64))
+    """The differentiable-step configuration at its stated size: the 200-Gaussian model, all 20
+    views at 128x128, silhouettes (alpha > 0.5 of the ground-truth scene) as the reference's own
+    fm_render rendered them."""
+    g = golden()
+    model = golden_scene("cfg2")
+    cams = golden_cameras("cfg2")
+    targets = [g["cfg2_targets"][i].astype(np.float64) for i in range(len(cams))]
+    assert len(cams) == 20
     return model, cams, targets
 
 
@@ -42,24 +45,29 @@ def gpu_loss_and_grads(dev, model, cams, targets):
     return loss.item(), m.grad.double().cpu(), p.grad.double().cpu(), w.grad.double().cpu()
 
 
-def oracle_loss_and_grads(model, cams, targets):
-    m = torch.from_numpy(model.means).double().requires_grad_()
-    p = torch.from_numpy(model.prec).double().requires_grad_()
-    w = torch.from_numpy(model.logw).double().requires_grad_()
-    loss = 0.0
+def oracle_loss_and_grads(model, cams, targets, dev="cpu"):
+    """float64 autograd of the torch restatement, one view at a time (gradients accumulate), on
+    ``dev`` (the GPU evaluates the float64 checker quickly for all 20 views)."""
+    m = torch.from_numpy(model.means).double().to(dev).requires_grad_()
+    p = torch.from_numpy(model.prec).double().to(dev).requires_grad_()
+    w = torch.from_numpy(model.logw).double().to(dev).requires_grad_()
+    total = 0.0
     for c, tgt in zip(cams, targets):
         _, a = OT.render_pinhole(m, p, w, c.height, c.width, c.fx, c.fy, c.cx, c.cy,
-                                 torch.from_numpy(c.quat).double(), torch.from_numpy(c.trans).double())
-        loss = loss + OT.bce_silhouette_loss(a.reshape(c.height, c.width), torch.from_numpy(tgt))
-    loss = loss / len(cams)
-    loss.backward()
-    return loss.item(), m.grad, p.grad, w.grad
+                                 torch.from_numpy(c.quat).double().to(dev),
+                                 torch.from_numpy(c.trans).double().to(dev))
+        loss = OT.bce_silhouette_loss(a.reshape(c.height, c.width),
+                                      torch.from_numpy(tgt).to(dev)) / len(cams)
+        loss.backward()
+        total += loss.item()
+    return total, m.grad.cpu(), p.grad.cpu(), w.grad.cpu()
 
 
 def test_silhouette_bce_gradients_match_float64_autograd(cuda_device, cfg2):
+    """All 20 views of the differentiable-step configuration."""
     model, cams, targets = cfg2
     l_gpu, gm, gp, gw = gpu_loss_and_grads(cuda_device, model, cams, targets)
-    l_ref, rm, rp, rw = oracle_loss_and_grads(model, cams, targets)
+    l_ref, rm, rp, rw = oracle_loss_and_grads(model, cams, targets, dev=cuda_device)
     assert abs(l_gpu - l_ref) <= 1e-5 * abs(l_ref)
     assert rel(gm, rm) < GRAD_TOL, rel(gm, rm)
     assert rel(gp, rp) < GRAD_TOL, rel(gp, rp)
@@ -93,11 +101,33 @@ def test_depth_gradients_match_float64_autograd(cuda_device, H, W, tile):
     assert rel(w.grad.double().cpu(), w64.grad) < GRAD_TOL
 
 
+def test_gradients_match_reference_central_differences(cuda_device, cfg2):
+    """The CUDA backward against float64 central differences (h = 1e-6) of the reference's own
+    fm_render on 48 parameters (means, upper and strictly-lower precision entries, log-weights),
+    silhouette BCE over views 0, 5, 10 and 15."""
+    model, cams, targets = cfg2
+    g = golden()
+    views = [int(v) for v in g["cfg2_fd_views"]]
+    _, gm, gp, gw = gpu_loss_and_grads(cuda_device, model, [cams[v] for v in views],
+                                       [targets[v] for v in views])
+    ana = []
+    for kind, gi, i, j in g["cfg2_fd_params"]:
+        ana.append(float(gm[gi, i] if kind == 0 else gp[gi, i, j] if kind == 1 else gw[gi]))
+    ana = np.array(ana)
+    fd = g["cfg2_fd_grad"]
+    scale = np.abs(fd).max()
+    err = np.abs(ana - fd)
+    assert np.all(err <= 2e-2 * np.abs(fd) + 2e-3 * scale), (err / scale).max()
+    lower = [k for k, (kind, _, i, j) in enumerate(g["cfg2_fd_params"]) if kind == 1 and i > j]
+    assert np.all(ana[lower] == 0)
+
+
 def test_gradients_match_central_differences(cuda_device, cfg2):
-    """64 random parameters, central differences with eps = 1e-4 of the CUDA forward's loss."""
+    """64 random parameters, central differences with eps = 1e-4 of the CUDA forward's loss
+    (views 0 and 5 of the 20: two forwards per parameter)."""
     model, cams, targets = cfg2
     dev = cuda_device
-    cams, targets = cams[:2], targets[:2]
+    cams, targets = [cams[0], cams[5]], [targets[0], targets[5]]
     _, gm, gp, gw = gpu_loss_and_grads(dev, model, cams, targets)
     base = scene_to_dev(model, dev)
     tg = [torch.from_numpy(t).to(dev) for t in targets]

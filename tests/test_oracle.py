@@ -1,7 +1,9 @@
-"""The float64 oracle (restatement of baseline/fm_render.py) against analytic known answers and
-against its torch restatement. No GPU."""
+"""The float64 oracle (restatement of baseline/fm_render.py) against the reference's own
+fm_render.py outputs (committed fixtures), analytic known answers and its torch restatement.
+No GPU."""
 
 import math
+import sys
 
 import numpy as np
 import pytest
@@ -214,3 +216,176 @@ def test_pixel_list_oracle_matches_image_oracle_and_flow_is_consistent():
     z = np.full(H * W, 0.8)
     fp, _ = O.flow_from_depth(pp, inv_f, poses, z)
     assert np.allclose(fp[:, 0], 0.05 * f / 0.8, rtol=1e-9) and np.allclose(fp[:, 1], 0, atol=1e-9)
+
+
+# --- The oracle against the reference's own fm_render.py ---------------------------------------
+# tests/golden/fm_render_golden.npz holds outputs of baseline/fm_render.py itself, imported
+# unmodified and run in float64 through tests/golden/numpy_jax.py. The restatement above must
+# reproduce them to rounding.
+
+def _view_errors(key):
+    from tests.helpers import golden_camera, golden_scene
+    sc = golden_scene(key)
+    cam, d_ref, a_ref = golden_camera(key)
+    d, a = O.render_pinhole(sc.means, sc.prec, sc.logw, cam.height, cam.width, cam.fx, cam.fy,
+                            cam.cx, cam.cy, cam.quat, cam.trans)
+    ed = float(np.max(np.abs(d - d_ref) / np.maximum(np.abs(d_ref), 1e-300)))
+    return ed, float(np.abs(a - a_ref).max())
+
+
+@pytest.mark.parametrize("key", ["cfg0", "behind", "straddle", "subpixel", "tiny1x1", "tiny3x17",
+                                 "tiny37x23", "tiny64x1"])
+def test_oracle_equals_reference_fm_render_full_views(key):
+    ed, ea = _view_errors(key)
+    assert ed <= 1e-12 and ea <= 1e-13, (key, ed, ea)
+
+
+def test_oracle_equals_reference_fm_render_weights_and_config2_views():
+    from tests.helpers import golden, golden_cameras, golden_scene
+    g = golden()
+    sc = golden_scene("cfg0")
+    from tests.helpers import golden_camera
+    cam, _, _ = golden_camera("cfg0")
+    rays = O.pinhole_rays(cam.height, cam.width, cam.fx, cam.fy, cam.cx, cam.cy)[g["cfg0_wpix"]]
+    _, _, _, w = O.render_func_quat(sc.means, sc.prec, sc.logw, rays, cam.quat, cam.trans, 21.4,
+                                    2.66, return_weights=True)
+    assert np.abs(w - g["cfg0_w"]).max() <= 1e-13
+    model = golden_scene("cfg2")
+    cams = golden_cameras("cfg2")
+    for vi in (0, 11):
+        c = cams[vi]
+        d, a = O.render_pinhole(model.means, model.prec, model.logw, c.height, c.width, c.fx, c.fy,
+                                c.cx, c.cy, c.quat, c.trans)
+        assert np.allclose(d, g[f"cfg2_v{vi}_depth"], rtol=1e-12, atol=0)
+        assert np.abs(a - g[f"cfg2_v{vi}_alpha"]).max() <= 1e-13
+
+
+def test_oracle_equals_reference_fm_render_config1_samples():
+    from tests.helpers import golden, golden_cameras, golden_scene
+    g = golden()
+    sc = golden_scene("cfg1")
+    for ci, cam in enumerate(golden_cameras("cfg1")):
+        pix = g["cfg1_pix"][ci]
+        rays = O.pinhole_rays(cam.height, cam.width, cam.fx, cam.fy, cam.cx, cam.cy)[pix]
+        d, a, _, _ = O.render_func_quat(sc.means, sc.prec, sc.logw, rays, cam.quat, cam.trans,
+                                        21.4, 2.66)
+        assert np.allclose(d, g["cfg1_depth"][ci], rtol=1e-12, atol=0), ci
+        assert np.abs(a - g["cfg1_alpha"][ci]).max() <= 1e-13, ci
+
+
+def test_oracle_equals_reference_pixel_lists_quat_cam_and_gmm():
+    from oracle import gmm_np
+    from tests.helpers import golden, golden_scene
+    g = golden()
+    sc = golden_scene("pix")
+    d, a, _, w, fp, fm = O.render_func_idx_quattrans_flow(
+        sc.means, sc.prec, sc.logw, g["pix_rays"], float(g["pix_invf"]), g["pix_poses"], 21.4, 2.66,
+        return_weights=True)
+    assert np.allclose(d, g["pix_depth"], rtol=1e-12, atol=1e-15)
+    assert np.abs(a - g["pix_alpha"]).max() <= 1e-13
+    assert np.abs(w - g["pix_w"]).max() <= 1e-12
+    assert np.abs(fp - g["pix_flowp"]).max() <= 1e-10 and np.abs(fm - g["pix_flowm"]).max() <= 1e-10
+    sc = golden_scene("cam")
+    inv_f, aspect = g["cam_invf_aspect"]
+    d, a, _, _ = O.render_func_quat_cam(sc.means, sc.prec, sc.logw, g["cam_pixels"], aspect, inv_f,
+                                        g["cam_quat"], g["cam_trans"], 21.4, 2.66)
+    assert np.allclose(d, g["cam_depth"], rtol=1e-12, atol=1e-15)
+    assert np.abs(a - g["cam_alpha"]).max() <= 1e-13
+    sc = golden_scene("gmm")
+    ll, res, _ = gmm_np.log_likelihood(sc.means, sc.prec, sc.logw, g["gmm_points"])
+    assert abs(ll - g["gmm_ll"]) <= 1e-12 * abs(g["gmm_ll"])
+    assert np.abs(res - g["gmm_res"]).max() <= 1e-11
+
+
+def test_gradient_oracle_equals_reference_central_differences():
+    """torch float64 autograd of the restatement (the stand-in for jax.grad of fm_render) against
+    float64 central differences of the reference's own fm_render on 48 parameters of the config-2
+    model, four views, silhouette BCE; strictly-lower precision entries have zero gradient."""
+    from tests.helpers import golden, golden_cameras, golden_scene
+    g = golden()
+    model = golden_scene("cfg2")
+    cams = golden_cameras("cfg2")
+    m = torch.from_numpy(model.means).double().requires_grad_()
+    p = torch.from_numpy(model.prec).double().requires_grad_()
+    w = torch.from_numpy(model.logw).double().requires_grad_()
+    loss = 0.0
+    views = g["cfg2_fd_views"]
+    for v in views:
+        c = cams[v]
+        _, a = OT.render_pinhole(m, p, w, c.height, c.width, c.fx, c.fy, c.cx, c.cy,
+                                 torch.from_numpy(c.quat).double(), torch.from_numpy(c.trans).double())
+        loss = loss + OT.bce_silhouette_loss(a, torch.from_numpy(g["cfg2_targets"][v]).double())
+    loss = loss / len(views)
+    loss.backward()
+    assert abs(loss.item() - float(g["cfg2_fd_loss"])) <= 1e-13 * abs(loss.item())
+    ana = []
+    for kind, gi, i, j in g["cfg2_fd_params"]:
+        ana.append(m.grad[gi, i] if kind == 0 else p.grad[gi, i, j] if kind == 1 else w.grad[gi])
+    ana = np.array([float(x) for x in ana])
+    fd = g["cfg2_fd_grad"]
+    scale = np.abs(fd).max()
+    assert np.all(np.abs(ana - fd) <= 1e-6 * np.abs(fd) + 1e-8 * scale), np.abs(ana - fd).max() / scale
+    lower = [k for k, (kind, _, i, j) in enumerate(g["cfg2_fd_params"]) if kind == 1 and i > j]
+    assert lower and np.all(fd[lower] == 0) and np.all(ana[lower] == 0)
+
+
+def test_numpy_jax_standin_maps_equal_python_loops():
+    """The stand-in's lax.map / vmap (vectorised by batch levels) equal a plain per-element loop,
+    for the constructs the reference uses: nested maps over a dict and an array, closures over
+    the outer element, matmul in both orders, indexing, .T, reductions, a gather by a mapped
+    index, iteration over a mapped vector and jnp.array of mapped scalars."""
+    from tests.golden import numpy_jax as J
+    rng = np.random.default_rng(0)
+    A = rng.normal(size=(5, 3, 3))
+    b = rng.normal(size=(5,))
+    m = rng.normal(size=(5, 3))
+    rays = rng.normal(size=(7, 2, 3))
+    with J.installed() as jax:
+        jnp = jax.numpy
+
+        def outer(args):
+            a, w, mi = args[0], args[1], args[2]
+            prc = a.T
+
+            def inner(rt):
+                r, t = rt[0], rt[1]
+                p = mi - t
+                q = prc @ p
+                return (q * (prc @ r)).sum() / ((prc @ r) ** 2).sum(), -0.5 * (q ** 2).sum() + w
+
+            return jax.lax.map(inner, rays, batch_size=4)
+
+        z, d = jax.lax.map(outer, {0: jnp.triu(A), 1: b, 2: m}, batch_size=2)
+
+        def qrot(q):
+            w_, x, y, zz = q
+            return jnp.array([[w_ * x, 1.0 - y], [zz / 2.0, x]])
+
+        quats = rng.normal(size=(6, 4))
+        R = jax.vmap(qrot)(quats)
+        idx = np.array([3, 0, 5, 5, 1], np.float64)
+        tab = rng.normal(size=(6, 3)).view(J.JArray)
+
+        def gather(i, v):
+            k = i.astype(int)
+            return v @ R[k][:, :1], tab[k, 1:]
+
+        vs = rng.normal(size=(5, 2))
+        g1, g2 = jax.vmap(gather)(idx, vs)
+    zl = np.zeros((5, 7))
+    dl = np.zeros((5, 7))
+    for i in range(5):
+        prc = np.triu(A[i]).T
+        for j in range(7):
+            r, t = rays[j]
+            q = prc @ (m[i] - t)
+            zl[i, j] = (q * (prc @ r)).sum() / ((prc @ r) ** 2).sum()
+            dl[i, j] = -0.5 * (q ** 2).sum() + b[i]
+    assert np.allclose(z, zl, rtol=1e-13) and np.allclose(d, dl, rtol=1e-13)
+    Rl = np.array([[[q[0] * q[1], 1.0 - q[2]], [q[3] / 2.0, q[1]]] for q in quats])
+    assert np.allclose(R, Rl)
+    for i in range(5):
+        k = int(idx[i])
+        assert np.allclose(g1[i], vs[i] @ Rl[k][:, :1])
+        assert np.allclose(g2[i], np.asarray(tab)[k, 1:])
+    assert "jax" not in sys.modules or not getattr(sys.modules["jax"], "__numpy_standin__", False)

@@ -48,9 +48,9 @@ def _call(entry, scene_dev, cam, desc, outs, err=None):
     return rc
 
 
-def _desc(scene, cam, tile=(16, 16), px=0):
+def _desc(scene, cam, tile=(16, 16), px=0, flags=0):
     return N.make_desc(scene.n, cam.height, cam.width, cam.fx, cam.fy, cam.cx, cam.cy,
-                       tile=tile, px=px)
+                       tile=tile, px=px, flags=flags)
 
 
 def _assert_close(ref, got):
@@ -96,6 +96,26 @@ def test_noalloc_smaller_request_then_larger_again(cuda_device):
         got = _outputs(cam.height, cam.width, cuda_device)
         assert _call("fe_render_fwd", sd, cam, desc, ref) == 0
         assert _call("fe_render_fwd_noalloc", sd, cam, desc, got) == 0
+        _assert_close(ref, got)
+
+
+@pytest.mark.parametrize("n,flags", [(1000, N.FE_FLAG_RADIX_BINNING), (5000, 0)])
+def test_noalloc_emit_and_radix_sort_branch(cuda_device, n, flags):
+    """The binning branch that carves the scan space, the second key buffer and the sort
+    histograms out of the fixed array: forced by FE_FLAG_RADIX_BINNING, and chosen by the size
+    rule for 5000 Gaussians on one 640x480 view (above the tile-major limit, 6 M worst-case
+    pairs, inside the fixed scratch). Two calls in a row against the arena entry."""
+    rng = np.random.default_rng(13)
+    scene = S.random_gaussians(n, 0.3, rng)
+    cam = S.config1(seed=0)[1][5]
+    sd = scene_to_dev(scene, cuda_device)
+    desc = _desc(scene, cam, flags=flags)
+    ref = _outputs(cam.height, cam.width, cuda_device)
+    assert _call("fe_render_fwd", sd, cam, desc, ref) == 0
+    for _ in range(2):
+        got = _outputs(cam.height, cam.width, cuda_device)
+        assert _call("fe_render_fwd_noalloc", sd, cam, desc, got) == 0, \
+            N.load().fe_last_error_message()
         _assert_close(ref, got)
 
 
