@@ -41,12 +41,24 @@ WORKLOAD = ("N=1000 Gaussians (means U[-0.3,0.3]^3 m, scales logU[0.005,0.03] m,
 # the logit and the three accumulations) and 3 MUFU operations (rcp and two ex2).
 PER_EVAL_FMA = 22
 PER_EVAL_MUFU = 3
-# Backward, counted from blend_bwd_kernel's per-pixel loop: 32 FMA-pipe operations (pixel
-# offsets 2, the three row-folded polynomials 5, peak and logit 4, chain rule 12, running sums
-# of the coefficient gradients 9) and 3 MUFU (rcp, ex2 of the density, ex2 of the softmax
-# weight).
-PER_EVAL_BWD_FMA = 32
+# Backward, algorithmic cost of one ray-Gaussian evaluation from the maths of the gradient, in the
+# same mat-vec formulation as the forward's 22 (per-pixel constants -- the saved max, 1/W, the
+# depth D, gd/W and g_alpha (1 - alpha) -- are formed once per pixel, not per evaluation):
+#   recompute without accumulating: a = L r 6, |a|^2 3, a.b 3, z 1, d0 1, s 1, s log2(e) 1,
+#     logit 2, shift by the saved max 1                                            = 19
+#   chain rule: t = e_w gd/W 1; dL/dl = t (z - D) 2; dL/ds = g_a(1-a) e_d + beta3 dL/dl 2;
+#     dL/dz = t - beta2 dL/dl 1; dL/dpsv = dL/dz q + dL/ds z 2;
+#     dL/dvsv = -z q (dL/dz + dL/ds z / 2) 4; dL/da = 2 dL/dvsv a + dL/dpsv b 6    = 18
+#   per-key accumulations: dL/db += dL/dpsv a 3; dL/dL += dL/da r^T (6 lower entries) 6;
+#     sum of dL/ds (log-weight and |b|^2) 1                                        = 10
+# = 47 FMA-pipe operations and 3 MUFU (rcp, ex2 of the density, ex2 of the softmax weight).
+PER_EVAL_BWD_FMA = 47
 PER_EVAL_BWD_MUFU = 3
+# What blend_bwd_kernel itself issues per evaluation in its per-pixel loop (polynomials in the
+# pixel offset, row-folded; running sums of the coefficient gradients): 32 FMA-pipe operations
+# (pixel offsets 2, the three polynomials 5, peak and logit 4, chain rule 12, running sums 9) and
+# the same 3 MUFU.
+KERNEL_EVAL_BWD_FMA = 32
 
 
 def parse():
@@ -515,7 +527,12 @@ def main():
                 "roofline": {"bound": "fma+xu", "achieved": bwd_evals_s / 1e9,
                              "peak": bwd_peak / 1e9, "unit": "Gevals/s",
                              "frac": bwd_evals_s / bwd_peak,
-                             "per_eval": {"fma_pipe": PER_EVAL_BWD_FMA, "mufu": PER_EVAL_BWD_MUFU},
+                             "per_eval": {"fma_pipe": PER_EVAL_BWD_FMA, "mufu": PER_EVAL_BWD_MUFU,
+                                          "basis": "algorithmic (maths of the gradient)"},
+                             "kernel_per_eval": {"fma_pipe": KERNEL_EVAL_BWD_FMA,
+                                                 "mufu": PER_EVAL_BWD_MUFU},
+                             "frac_of_kernel_count": bwd_evals_s / min(
+                                 fma_ops / KERNEL_EVAL_BWD_FMA, ex2_ops / PER_EVAL_BWD_MUFU),
                              "scope": "whole backward (per-key recompute and coefficient "
                                       "gradients, record VJP) of the 16-view step, reusing the "
                                       "forward's binning"}}

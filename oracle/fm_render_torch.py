@@ -66,17 +66,17 @@ def render_func_quat(means, prec_full, weights_log, camera_rays, quat, t, beta_2
     return render_func_rays(rays, origins, means, prec_full, weights_log, beta_2, beta_3)
 
 
-def pinhole_rays(height, width, fx, fy, cx, cy, dtype=torch.float64):
+def pinhole_rays(height, width, fx, fy, cx, cy, dtype=torch.float64, device=None):
     """Camera-frame rays, pixel index v*W+u (``baseline/ycb_fmb_rotscale.py:182-189``)."""
-    v, u = torch.meshgrid(torch.arange(height, dtype=dtype), torch.arange(width, dtype=dtype),
-                          indexing="ij")
+    v, u = torch.meshgrid(torch.arange(height, dtype=dtype, device=device),
+                          torch.arange(width, dtype=dtype, device=device), indexing="ij")
     return torch.stack([(u.reshape(-1) - cx) / fx, (v.reshape(-1) - cy) / fy,
-                        torch.ones(height * width, dtype=dtype)], 1)
+                        torch.ones(height * width, dtype=dtype, device=device)], 1)
 
 
 def render_pinhole(means, prec_full, weights_log, height, width, fx, fy, cx, cy, quat, t,
                    beta_2=21.4, beta_3=2.66):
-    rays = pinhole_rays(height, width, fx, fy, cx, cy, dtype=means.dtype)
+    rays = pinhole_rays(height, width, fx, fy, cx, cy, dtype=means.dtype, device=means.device)
     d, a = render_func_quat(means, prec_full, weights_log, rays, quat, t, beta_2, beta_3)
     return d.reshape(height, width), a.reshape(height, width)
 
