@@ -315,8 +315,9 @@ def main():
     else:
         tuner = fe.autotune.Autotuner(persist=False)
         tuned = tuner.tune([(0, scene.n)], views, m, p, w, reps=3)
-        cfg = {k: tuned[k] for k in ("tile", "px", "chunk")}
+        cfg = {k: tuned[k] for k in ("tile", "px", "chunk", "heavy_first")}
     batch = fe.Batch([(0, scene.n)], views, tile=cfg["tile"], px=cfg["px"], chunk=cfg["chunk"],
+                     heavy_first=cfg["heavy_first"],
                      keep_binning=True, binning=args.binning)
     per_cam_evals = count_evals(fe, cams, mpw) if not args.profile_step else [0] * len(cams)
     e_step = float(sum(per_cam_evals))
@@ -562,7 +563,8 @@ def main():
         "data": "synthetic",
         "config": {"workload": WORKLOAD, "step": "batched forward of all 16 cameras",
                    "tile": f"{cfg['tile'][0]}x{cfg['tile'][1]}", "px_per_thread": cfg["px"],
-                   "chunk_pairs": cfg["chunk"], "autotuned": tuned is not None,
+                   "chunk_pairs": cfg["chunk"], "heavy_tiles_first": cfg["heavy_first"],
+                   "autotuned": tuned is not None,
                    "binning": "tile-major (keys emitted in sorted order)" if args.binning == "tiles"
                    else "key emission + radix sort",
                    "launch": "CUDA graph replay of the batched forward (captured once)",
@@ -612,7 +614,7 @@ def main():
         "batched_uneven_256_scenes": config3,
         "served": served,
         "autotune": tuned and {"bucket": tuned["bucket"],
-                               "candidates_ms": {f"{c['tile'][0]}x{c['tile'][1]}/px{c['px']}/ch{c['chunk']}": round(c["ms"], 4)
+                               "candidates_ms": {f"{c['tile'][0]}x{c['tile'][1]}/px{c['px']}/ch{c['chunk']}{'/heavy' if c['heavy_first'] else ''}": round(c["ms"], 4)
                                                  for c in tuned["candidates"]}},
         "clocks": clocks,
         "gpu_launches": batch.launches_per_forward * args.steps,
@@ -836,7 +838,8 @@ def config3_bench(fe, dev, steps, fma_ops, ex2_ops):
     m, p, w = [torch.from_numpy(np.concatenate(x)).to(dev) for x in (means, prec, logw)]
     tuner = fe.autotune.Autotuner(persist=False)
     tuned = tuner.tune(scenes, views, m, p, w, reps=3)
-    b = fe.Batch(scenes, views, tile=tuned["tile"], px=tuned["px"], chunk=tuned["chunk"])
+    b = fe.Batch(scenes, views, tile=tuned["tile"], px=tuned["px"], chunk=tuned["chunk"],
+                 heavy_first=tuned["heavy_first"])
     depth = torch.empty(b.n_pixels, device=dev)
     alpha = torch.empty(b.n_pixels, device=dev)
     e_total = 0
@@ -878,8 +881,9 @@ def config3_bench(fe, dev, steps, fma_ops, ex2_ops):
                        f"{b.n_pixels} pixels, fp32",
            "launch": "one persistent launch sequence, CUDA graph replay, L2 flushed between",
            "autotuned": {"tile": f"{tuned['tile'][0]}x{tuned['tile'][1]}", "px": tuned["px"],
-                         "chunk": tuned["chunk"], "bucket": tuned["bucket"],
-                         "candidates_ms": {f"{c['tile'][0]}x{c['tile'][1]}/px{c['px']}/ch{c['chunk']}": round(c["ms"], 4)
+                         "chunk": tuned["chunk"], "heavy_first": tuned["heavy_first"],
+                         "bucket": tuned["bucket"],
+                         "candidates_ms": {f"{c['tile'][0]}x{c['tile'][1]}/px{c['px']}/ch{c['chunk']}{'/heavy' if c['heavy_first'] else ''}": round(c["ms"], 4)
                                            for c in tuned["candidates"]}},
            "views": len(views), "ms_per_step": ms, "renders_per_s": len(views) / (ms * 1e-3),
            "evals_per_step": e_total, "mevals_per_s": e_total / (ms * 1e-3) / 1e6,

@@ -111,6 +111,7 @@ struct RecSpace {
   unsigned long long* scan_tmp;
   uint2* ranges;
   unsigned long long* row_tot;  // tile-major binning: row key-count differences per view
+  uint32_t* order;  // tile-major binning: tile ids per work class (kTileClasses lists of n_tiles)
   RecGrad* rgrad;  // backward only
 };
 
@@ -133,6 +134,7 @@ size_t carve_rec(char* base, int64_t n_rec, int64_t n_tiles, int64_t n_pix, bool
   s.scan_tmp = c.take<unsigned long long>(scan_grid(std::max(n_rec, n_tiles)));
   s.ranges = c.take<uint2>(n_tiles);
   s.row_tot = c.take<unsigned long long>(n_tiles + 1);
+  s.order = c.take<uint32_t>((int64_t)kTileClasses * n_tiles);
   s.rgrad = bwd ? c.take<RecGrad>(n_rec) : nullptr;
   out(s);
   return c.off;
@@ -212,6 +214,7 @@ struct Pipeline {
   int px;     // pixels per thread in the blend (0 = default)
   int chunk;  // record pairs per shared-memory stage in the blend (0 = default)
   bool radix;  // FE_FLAG_RADIX_BINNING: emit + sort even where tile-major binning applies
+  bool heavy_first;  // FE_FLAG_HEAVY_TILES_FIRST: work-class tile lists for the blend
   int cull_mode;
   float cull_param;
   float beta2, beta3;
@@ -290,9 +293,10 @@ int run_binning(const Pipeline& p, int64_t worst, DevBuf& recbuf, DevBuf& keybuf
   if (rc) return rc;
   carve_keys(keybuf.ptr, cap, [&](const KeySpace& s) { ks = s; });
   if (exact && !rp.ok) launch_scan(rs.touched, rs.incl, p.n_rec, cap, rs.scan_tmp, rs.ctrl, st);
+  if (!rp.ok || !p.heavy_first) rs.order = nullptr;  // the blend takes tiles in index order
   if (rp.ok) {
     launch_tile_binning_emit(p.va, rp.n_views, rp.max_gy, rs.rects, rs.row_tot, cap, rs.ctrl,
-                             rs.ranges, ks.keys_a, st);
+                             rs.ranges, ks.keys_a, rs.order, p.n_tiles, st);
     sorted = ks.keys_a;
   } else {
     launch_emit_keys(p.va, rs.incl, rs.rects, p.n_rec, rs.ctrl, ks.keys_a, cap, st);
@@ -340,6 +344,7 @@ Pipeline single_view_pipeline(const fe_render_desc* d, const float* means, const
   p.px = default_px((int)d->px_per_thread, tw, th, p.n_tiles);
   p.chunk = (int)(d->flags >> 8) & 0xff;
   p.radix = (d->flags & FE_FLAG_RADIX_BINNING) != 0;
+  p.heavy_first = (d->flags & FE_FLAG_HEAVY_TILES_FIRST) != 0;
   p.cull_mode = d->cull_mode;
   p.cull_param = d->cull_param;
   p.beta2 = d->beta2;
@@ -422,8 +427,8 @@ int fe_render_fwd(const fe_render_desc* d, const float* means, const float* prec
   rc = run_binning(p, p.n_rec * p.n_tiles, a->rec, a->keys, a->h_pinned, false, st, rs, ks, cap,
                    sorted);
   if (rc) return rc;
-  launch_blend_fwd(p.va, p.tile_w, p.tile_h, p.px, p.chunk, p.n_tiles, sorted, rs.recs, rs.ranges, p.beta2, p.beta3,
-                   depth, alpha, stats, npix, rs.ctrl, st);
+  launch_blend_fwd(p.va, p.tile_w, p.tile_h, p.px, p.chunk, p.n_tiles, rs.order, sorted, rs.recs,
+                   rs.ranges, p.beta2, p.beta3, depth, alpha, stats, npix, rs.ctrl, st);
   FE_CUDA(cudaGetLastError());
   return FE_OK;
 }
@@ -871,8 +876,8 @@ int fe_rasterize_legacy(const fe_legacy_desc* d, const float* means, const float
   launch_emit_keys(va, rs.incl, rs.rects, P, rs.ctrl, ks.keys_a, cap, st);
   uint64_t* sorted = launch_sort(ks.keys_a, ks.keys_b, bits_for(T), rs.ctrl, cap, ks.hist, st);
   launch_ranges(sorted, rs.ctrl, cap, rs.ranges, st);
-  launch_blend_fwd(va, 8, 8, 0, 0, T, sorted, rs.recs, rs.ranges, 21.4f, 2.66f, out_z, out_alpha, nullptr, 0,
-                   rs.ctrl, st);
+  launch_blend_fwd(va, 8, 8, 0, 0, T, nullptr, sorted, rs.recs, rs.ranges, 21.4f, 2.66f, out_z,
+                   out_alpha, nullptr, 0, rs.ctrl, st);
   FE_CUDA(cudaGetLastError());
   return FE_OK;
 }
@@ -1157,12 +1162,18 @@ static Pipeline batch_pipeline(fe_batch* b, const float* means, const float* pre
   p.px = default_px((int)b->desc.px_per_thread, b->tile_w, b->tile_h, p.n_tiles);
   p.chunk = (int)(b->desc.flags >> 8) & 0xff;
   p.radix = (b->desc.flags & FE_FLAG_RADIX_BINNING) != 0;
+  p.heavy_first = (b->desc.flags & FE_FLAG_HEAVY_TILES_FIRST) != 0;
   p.cull_mode = b->desc.cull_mode;
   p.cull_param = b->desc.cull_param;
   p.beta2 = b->desc.beta2;
   p.beta3 = b->desc.beta3;
   p.means = means; p.prec = prec; p.logw = logw; p.quat = b->quat_d; p.trans = b->trans_d;
   return p;
+}
+
+// The work-class tile lists of the last binning, when it was tile-major (else NULL).
+static const uint32_t* batch_order(const fe_batch* b, const Pipeline& p) {
+  return (p.heavy_first && !p.radix && b->rows.ok) ? b->rs.order : nullptr;
 }
 
 // Binning of a batch. With exact key sizing the key count is read back after the scan (one
@@ -1202,7 +1213,8 @@ static int batch_binning(fe_batch* b, const Pipeline& p, cudaStream_t st, cudaEv
   const KeySpace& ks = b->ks;
   if (rp.ok) {
     launch_tile_binning_emit(p.va, rp.n_views, rp.max_gy, rs.rects, rs.row_tot, b->cap, rs.ctrl,
-                             rs.ranges, ks.keys_a, st);
+                             rs.ranges, ks.keys_a, p.heavy_first ? rs.order : nullptr, p.n_tiles,
+                             st);
     if (ev) FE_CUDA(cudaEventRecord(ev[3], st));
     b->sorted = ks.keys_a;
     if (ev) FE_CUDA(cudaEventRecord(ev[4], st));
@@ -1281,8 +1293,9 @@ int fe_batch_fwd(fe_batch* b, const float* means, const float* prec, const float
   int rc = batch_binning(b, p, st, nullptr);
   if (rc) return rc;
   note_binning(b, means, prec, logw);
-  launch_blend_fwd(p.va, p.tile_w, p.tile_h, p.px, p.chunk, p.n_tiles, b->sorted, b->rs.recs,
-                   b->rs.ranges, p.beta2, p.beta3, depth, alpha, stats, p.n_pix, b->rs.ctrl, st);
+  launch_blend_fwd(p.va, p.tile_w, p.tile_h, p.px, p.chunk, p.n_tiles, batch_order(b, p),
+                   b->sorted, b->rs.recs, b->rs.ranges, p.beta2, p.beta3, depth, alpha, stats,
+                   p.n_pix, b->rs.ctrl, st);
   FE_CUDA(cudaGetLastError());
   return FE_OK;
 }
@@ -1429,8 +1442,9 @@ int fe_batch_fwd_timed(fe_batch* b, const float* means, const float* prec, const
     return rc;
   }
   note_binning(b, means, prec, logw);
-  launch_blend_fwd(p.va, p.tile_w, p.tile_h, p.px, p.chunk, p.n_tiles, b->sorted, b->rs.recs,
-                   b->rs.ranges, p.beta2, p.beta3, depth, alpha, stats, p.n_pix, b->rs.ctrl, st);
+  launch_blend_fwd(p.va, p.tile_w, p.tile_h, p.px, p.chunk, p.n_tiles, batch_order(b, p),
+                   b->sorted, b->rs.recs, b->rs.ranges, p.beta2, p.beta3, depth, alpha, stats,
+                   p.n_pix, b->rs.ctrl, st);
   FE_CUDA(cudaEventRecord(ev[6], st));
   FE_CUDA(cudaEventSynchronize(ev[6]));
   for (int i = 0; i < 6; ++i) FE_CUDA(cudaEventElapsedTime(&stage_ms[i], ev[i], ev[i + 1]));
@@ -1442,8 +1456,8 @@ int fe_batch_fwd_timed(fe_batch* b, const float* means, const float* prec, const
 int fe_batch_launch_count(const fe_batch* b) {
   if (!b) return 0;
   const bool radix = (b->desc.flags & FE_FLAG_RADIX_BINNING) != 0;
-  // Tile-major binning: preprocess, emission, blend.
-  if (b->rows.ok && !radix) return 3;
+  // Tile-major binning: preprocess, (row bases for many views,) emission, blend.
+  if (b->rows.ok && !radix) return b->rows.n_views > kRowBaseViews ? 4 : 3;
   // Emit + sort: preprocess, scan, emission, three kernels per radix pass, ranges, blend.
   const int passes = (bits_for(b->n_tiles) + 7) / 8;
   const int scan = b->n_rec <= 65536 ? 1 : 3;
@@ -1562,17 +1576,18 @@ int fe_render_fwd_noalloc(const fe_render_desc* d, const float* means, const flo
                     p.cull_param, p.tile_w, p.tile_h, rs.recs, rs.rects, rs.touched,
                     rp.ok ? rs.row_tot : nullptr, rp.max_gy, rs.ctrl, st);
   uint64_t* sorted = ks.keys_a;
+  if (!rp.ok || !p.heavy_first) rs.order = nullptr;
   if (rp.ok) {
     launch_tile_binning_emit(p.va, rp.n_views, rp.max_gy, rs.rects, rs.row_tot, worst, rs.ctrl,
-                             rs.ranges, ks.keys_a, st);
+                             rs.ranges, ks.keys_a, rs.order, p.n_tiles, st);
   } else {
     launch_scan(rs.touched, rs.incl, p.n_rec, worst, rs.scan_tmp, rs.ctrl, st);
     launch_emit_keys(p.va, rs.incl, rs.rects, p.n_rec, rs.ctrl, ks.keys_a, worst, st);
     sorted = launch_sort(ks.keys_a, ks.keys_b, bits_for(p.n_tiles), rs.ctrl, worst, ks.hist, st);
     launch_ranges(sorted, rs.ctrl, worst, rs.ranges, st);
   }
-  launch_blend_fwd(p.va, p.tile_w, p.tile_h, p.px, p.chunk, p.n_tiles, sorted, rs.recs, rs.ranges,
-                   p.beta2, p.beta3, depth, alpha, stats, npix, rs.ctrl, st);
+  launch_blend_fwd(p.va, p.tile_w, p.tile_h, p.px, p.chunk, p.n_tiles, rs.order, sorted, rs.recs,
+                   rs.ranges, p.beta2, p.beta3, depth, alpha, stats, npix, rs.ctrl, st);
   if (device_error)
     FE_CUDA(cudaMemcpyAsync(device_error, &rs.ctrl->error, sizeof(uint32_t),
                             cudaMemcpyDeviceToDevice, st));

@@ -417,10 +417,46 @@ __device__ __forceinline__ uint32_t filter_row(const TileRect* __restrict__ vr, 
   return total;
 }
 
+// Row bases of many views at once (one block): turns row_tot's per-view differences of the row
+// key counts into every row's first key slot (the exclusive prefix over views in order, rows in
+// order), in place, so that the emit blocks read their base instead of each summing the rows of
+// every view before theirs (quadratic in the number of views). Thread t takes the consecutive
+// views [t vpt, t vpt + vpt).
+__global__ void __launch_bounds__(kRowThreads) row_bases_kernel(ViewsArg va, int n_views,
+                                                                 int stride,
+                                                                 unsigned long long* row_tot) {
+  __shared__ unsigned long long ws[kRowWarps];
+  const int vpt = (n_views + kRowThreads - 1) / kRowThreads;
+  const int v0 = (int)threadIdx.x * vpt, v1 = min(n_views, v0 + vpt);
+  unsigned long long mine = 0;  // keys of this thread's views
+  for (int v = v0; v < v1; ++v) {
+    const int gy = view_at(va, v).gy;
+    const unsigned long long* d = row_tot + (int64_t)v * stride;
+    long long cnt = 0;
+    for (int r = 0; r < gy; ++r) {
+      cnt += (long long)d[r];
+      mine += (unsigned long long)cnt;
+    }
+  }
+  unsigned long long base;
+  block_exclusive_scan<unsigned long long>(mine, base, ws);
+  for (int v = v0; v < v1; ++v) {
+    const int gy = view_at(va, v).gy;
+    unsigned long long* d = row_tot + (int64_t)v * stride;
+    long long cnt = 0;
+    for (int r = 0; r < gy; ++r) {
+      cnt += (long long)d[r];
+      d[r] = base;
+      base += (unsigned long long)cnt;
+    }
+  }
+}
+
 __global__ void __launch_bounds__(kRowThreads) tile_emit_kernel(
     ViewsArg va, const TileRect* __restrict__ rects,
-    const unsigned long long* __restrict__ row_tot, int64_t capacity, Control* __restrict__ ctrl,
-    uint2* __restrict__ ranges, uint64_t* __restrict__ keys) {
+    const unsigned long long* __restrict__ row_tot, bool bases, int64_t capacity,
+    Control* __restrict__ ctrl, uint2* __restrict__ ranges, uint64_t* __restrict__ keys,
+    uint32_t* __restrict__ order, int64_t n_tiles) {
   __shared__ RowRect list[kRowSeg];
   __shared__ int diff[kMaxRowTiles + 1];         // +1 at x0, -1 at x1 of every covering rectangle
   __shared__ uint32_t pos[kMaxRowTiles];  // per tile: next key slot within the row
@@ -450,16 +486,22 @@ __global__ void __launch_bounds__(kRowThreads) tile_emit_kernel(
   // row_tot holds, per view, the difference of the row key counts (stride max_gy + 1): the count
   // of row r is the sum of entries 0..r, so the keys before row `row` of this view are
   // sum_{r' < row} d[r'] (row - r'), and a whole earlier view holds sum_{r' < gy} d[r'] (gy - r').
+  // With `bases` set, row_bases_kernel has already replaced the differences by the row bases.
   const int stride = (int)gridDim.x + 1;
-  long long b = 0;
-  for (int idx = tid; idx < (int)blockIdx.y * stride; idx += kRowThreads) {
-    const int v2 = idx / stride, r2 = idx - v2 * stride;
-    const int gy2 = view_at(va, v2).gy;
-    if (r2 < gy2) b += (long long)row_tot[idx] * (gy2 - r2);
+  unsigned long long row_base;
+  if (bases) {
+    row_base = row_tot[(int64_t)blockIdx.y * stride + row];
+  } else {
+    long long b = 0;
+    for (int idx = tid; idx < (int)blockIdx.y * stride; idx += kRowThreads) {
+      const int v2 = idx / stride, r2 = idx - v2 * stride;
+      const int gy2 = view_at(va, v2).gy;
+      if (r2 < gy2) b += (long long)row_tot[idx] * (gy2 - r2);
+    }
+    for (int r2 = tid; r2 < row; r2 += kRowThreads)
+      b += (long long)row_tot[(int64_t)blockIdx.y * stride + r2] * (row - r2);
+    row_base = block_sum_u64((unsigned long long)b, wsu);
   }
-  for (int r2 = tid; r2 < row; r2 += kRowThreads)
-    b += (long long)row_tot[(int64_t)blockIdx.y * stride + r2] * (row - r2);
-  const unsigned long long row_base = block_sum_u64((unsigned long long)b, wsu);
   // Keys of this row: slot p (relative to the row's base) for p < lim.
   uint64_t* row_keys = keys + row_base;
   const unsigned long long left = K > row_base ? K - row_base : 0ull;
@@ -522,6 +564,31 @@ __global__ void __launch_bounds__(kRowThreads) tile_emit_kernel(
       const unsigned long long hi = min(row_base + cex + (unsigned)cnt[q], K);
       if (hi > lo) ranges[tile0 + x] = make_uint2((uint32_t)lo, (uint32_t)hi);
       cex += (unsigned)cnt[q];
+    }
+  }
+  if (order) {
+    // Work classes: every tile of the row joins its class's list (order + c n_tiles), a shared
+    // count per class and one global atomic per class and row giving the slots.
+    __shared__ uint32_t cls_n[kTileClasses], cls_base[kTileClasses];
+    if (tid < kTileClasses) cls_n[tid] = 0u;
+    __syncthreads();
+    int cl[kTilesPer];
+    uint32_t rank[kTilesPer];
+#pragma unroll
+    for (int q = 0; q < kTilesPer; ++q) {
+      const int x = kTilesPer * tid + q;
+      cl[q] = tile_class((uint32_t)cnt[q]);
+      rank[q] = x < gx ? atomicAdd(&cls_n[cl[q]], 1u) : 0u;
+    }
+    __syncthreads();
+    if (tid < kTileClasses && cls_n[tid] != 0u)
+      cls_base[tid] = atomicAdd(&ctrl->tile_class[tid], cls_n[tid]);
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < kTilesPer; ++q) {
+      const int x = kTilesPer * tid + q;
+      if (x < gx)
+        order[(int64_t)cl[q] * n_tiles + cls_base[cl[q]] + rank[q]] = (uint32_t)(tile0 + x);
     }
   }
   __syncthreads();
@@ -611,11 +678,16 @@ uint64_t* launch_sort(uint64_t* a, uint64_t* b, int key_bits, const Control* ctr
 
 
 void launch_tile_binning_emit(const ViewsArg& va, int n_views, int max_gy, const TileRect* rects,
-                              const unsigned long long* row_tot, int64_t capacity, Control* ctrl,
-                              uint2* ranges, uint64_t* keys, cudaStream_t st) {
+                              unsigned long long* row_tot, int64_t capacity, Control* ctrl,
+                              uint2* ranges, uint64_t* keys, uint32_t* order, int64_t n_tiles,
+                              cudaStream_t st) {
   if (n_views <= 0 || max_gy <= 0) return;
+  // Beyond a few dozen views the per-block sums over earlier views cost more than one extra
+  // single-block launch that forms all row bases.
+  const bool bases = n_views > kRowBaseViews;
+  if (bases) row_bases_kernel<<<1, kRowThreads, 0, st>>>(va, n_views, max_gy + 1, row_tot);
   tile_emit_kernel<<<dim3((unsigned)max_gy, (unsigned)n_views), kRowThreads, 0, st>>>(
-      va, rects, row_tot, capacity, ctrl, ranges, keys);
+      va, rects, row_tot, bases, capacity, ctrl, ranges, keys, order, n_tiles);
 }
 
 void launch_ranges(const uint64_t* keys, const Control* ctrl, int64_t capacity, uint2* ranges,

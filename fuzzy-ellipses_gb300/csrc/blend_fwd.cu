@@ -38,6 +38,7 @@ struct BlendSmem {
   GaussRec src[2 * CH];     // source records of the next chunk (TMA bulk copies), record r at src[r]
   uint64_t bar;             // completion of the source-record copies, one phase per chunk
   uint32_t tile;
+  uint32_t cls_base[kTileClasses + 1];  // first work index of each tile class (with `order`)
 };
 
 // Write a null record into slot `sl` (0 = .x, 1 = .y) of a pair: vsv = 1, psv = 0 (z = 0,
@@ -150,8 +151,8 @@ template <int TW, int TH, int PX, int CH>
 __global__ void __launch_bounds__(BlendShape<TW, TH, PX, CH>::NT,
                                   BlendShape<TW, TH, PX, CH>::MIN_CTAS) blend_fwd_kernel(
     ViewsArg va, uint32_t tile_begin, uint32_t tile_end, uint32_t* __restrict__ counter,
-    const uint64_t* __restrict__ keys, const GaussRec* __restrict__ recs,
-    const uint2* __restrict__ ranges, float nb2, float beta3,
+    const uint32_t* __restrict__ order, const uint64_t* __restrict__ keys,
+    const GaussRec* __restrict__ recs, const uint2* __restrict__ ranges, float nb2, float beta3,
     float* __restrict__ depth, float* __restrict__ alpha, float* __restrict__ stats,
     int64_t stats_stride, Control* __restrict__ ctrl) {
   using Sh = BlendShape<TW, TH, PX, CH>;
@@ -174,14 +175,37 @@ __global__ void __launch_bounds__(BlendShape<TW, TH, PX, CH>::NT,
   constexpr int RC = 2 * CH;                     // records per chunk
   constexpr int RPT = (RC + Sh::NT - 1) / Sh::NT;  // records each thread stages and builds
   const float hw = 0.5f * (TW - 1), hh = 0.5f * (TH - 1);
+  // Heaviest tiles first: with `order` (the tile-major binning's per-class tile lists over all
+  // tiles [0, tile_end)) work index w of class c maps to order[c tile_end + w - cls_base[c]], so
+  // the tiles taken last, which set the kernel's tail, are the lightest. The lists are used only
+  // when they hold every tile exactly once (their counts sum to tile_end); else tiles go in
+  // index order.
+  bool use_order = false;
   if (tid == 0) {
     mbar_init(&sm.bar, 1);
     fence_mbar_init();
+    if (order && tile_begin == 0) {
+      uint32_t b = 0;
+      for (int c = 0; c < kTileClasses; ++c) {
+        sm.cls_base[c] = b;
+        b += ctrl->tile_class[c];
+      }
+      sm.cls_base[kTileClasses] = b;
+      use_order = b == tile_end;
+    }
   }
   uint32_t phase = 0;  // parity of the next completion of sm.bar
 
   while (true) {
-    if (tid == 0) sm.tile = tile_begin + atomicAdd(counter, 1u);
+    if (tid == 0) {
+      uint32_t w = tile_begin + atomicAdd(counter, 1u);
+      if (use_order && w < tile_end) {
+        int c = 0;
+        while (c + 1 < kTileClasses && w >= sm.cls_base[c + 1]) ++c;
+        w = order[(int64_t)c * tile_end + (w - sm.cls_base[c])];
+      }
+      sm.tile = w;
+    }
     __syncthreads();
     const uint32_t tile = sm.tile;
     if (tile >= tile_end) break;
@@ -342,31 +366,56 @@ __global__ void __launch_bounds__(BlendShape<TW, TH, PX, CH>::NT,
 
 template <int TW, int TH, int PX, int CH>
 void launch_tiles(const ViewsArg& va, int64_t tile_begin, int64_t tile_end, uint32_t* counter,
-                  const uint64_t* keys, const GaussRec* recs, const uint2* ranges, float nb2,
-                  float beta3, float* depth, float* alpha, float* stats, int64_t stats_stride,
-                  Control* ctrl, cudaStream_t st) {
+                  const uint32_t* order, const uint64_t* keys, const GaussRec* recs,
+                  const uint2* ranges, float nb2, float beta3, float* depth, float* alpha,
+                  float* stats, int64_t stats_stride, Control* ctrl, cudaStream_t st) {
   constexpr int NT = BlendShape<TW, TH, PX, CH>::NT;
   constexpr auto kern = blend_fwd_kernel<TW, TH, PX, CH>;
   const int64_t grid = std::min<int64_t>(tile_end - tile_begin, resident_ctas<kern>(NT));
-  kern<<<(unsigned)grid, NT, 0, st>>>(va, (uint32_t)tile_begin, (uint32_t)tile_end, counter, keys,
-                                      recs, ranges, nb2, beta3, depth, alpha, stats, stats_stride,
-                                      ctrl);
+  kern<<<(unsigned)grid, NT, 0, st>>>(va, (uint32_t)tile_begin, (uint32_t)tile_end, counter,
+                                      order, keys, recs, ranges, nb2, beta3, depth, alpha, stats,
+                                      stats_stride, ctrl);
 }
 
 template <int TW, int TH, int PX>
 void launch_chunk(int chunk, const ViewsArg& va, int64_t tile_begin, int64_t tile_end,
-                  uint32_t* counter, const uint64_t* keys, const GaussRec* recs,
-                  const uint2* ranges, float nb2, float beta3, float* depth, float* alpha,
-                  float* stats, int64_t stats_stride, Control* ctrl, cudaStream_t st) {
+                  uint32_t* counter, const uint32_t* order, const uint64_t* keys,
+                  const GaussRec* recs, const uint2* ranges, float nb2, float beta3, float* depth,
+                  float* alpha, float* stats, int64_t stats_stride, Control* ctrl,
+                  cudaStream_t st) {
   if (chunk == 8)
-    launch_tiles<TW, TH, PX, 8>(va, tile_begin, tile_end, counter, keys, recs, ranges, nb2, beta3,
-                                depth, alpha, stats, stats_stride, ctrl, st);
+    launch_tiles<TW, TH, PX, 8>(va, tile_begin, tile_end, counter, order, keys, recs, ranges, nb2,
+                                beta3, depth, alpha, stats, stats_stride, ctrl, st);
   else if (chunk == 16)
-    launch_tiles<TW, TH, PX, 16>(va, tile_begin, tile_end, counter, keys, recs, ranges, nb2,
-                                 beta3, depth, alpha, stats, stats_stride, ctrl, st);
+    launch_tiles<TW, TH, PX, 16>(va, tile_begin, tile_end, counter, order, keys, recs, ranges,
+                                 nb2, beta3, depth, alpha, stats, stats_stride, ctrl, st);
   else
-    launch_tiles<TW, TH, PX, 32>(va, tile_begin, tile_end, counter, keys, recs, ranges, nb2,
-                                 beta3, depth, alpha, stats, stats_stride, ctrl, st);
+    launch_tiles<TW, TH, PX, 32>(va, tile_begin, tile_end, counter, order, keys, recs, ranges,
+                                 nb2, beta3, depth, alpha, stats, stats_stride, ctrl, st);
+}
+
+}  // namespace
+
+namespace {
+
+void blend_dispatch(const ViewsArg& va, int tile_w, int tile_h, int px, int chunk,
+                    int64_t tile_begin, int64_t tile_end, uint32_t* counter, const uint32_t* order,
+                    const uint64_t* keys, const GaussRec* recs, const uint2* ranges, float beta2,
+                    float beta3, float* depth, float* alpha, float* stats, int64_t stats_stride,
+                    Control* ctrl, cudaStream_t st) {
+  if (tile_end <= tile_begin) return;
+  const float nb2 = -beta2 * kLog2e;
+#define FE_BLEND(TW_, TH_, PX_)                                                                 \
+  launch_chunk<TW_, TH_, PX_>(chunk, va, tile_begin, tile_end, counter, order, keys, recs, ranges, \
+                              nb2, beta3, depth, alpha, stats, stats_stride, ctrl, st)
+  if (tile_w == 8 && tile_h == 8) {
+    if (px == 1) FE_BLEND(8, 8, 1); else FE_BLEND(8, 8, 2);
+  } else if (tile_w == 32 && tile_h == 8) {
+    if (px == 1) FE_BLEND(32, 8, 1); else if (px == 2) FE_BLEND(32, 8, 2); else FE_BLEND(32, 8, 4);
+  } else {
+    if (px == 1) FE_BLEND(16, 16, 1); else if (px == 2) FE_BLEND(16, 16, 2); else FE_BLEND(16, 16, 4);
+  }
+#undef FE_BLEND
 }
 
 }  // namespace
@@ -378,27 +427,17 @@ void launch_blend_fwd_band(const ViewsArg& va, int tile_w, int tile_h, int px, i
                            const uint64_t* keys, const GaussRec* recs, const uint2* ranges,
                            float beta2, float beta3, float* depth, float* alpha, float* stats,
                            int64_t stats_stride, Control* ctrl, cudaStream_t st) {
-  if (tile_end <= tile_begin) return;
-  const float nb2 = -beta2 * kLog2e;
-#define FE_BLEND(TW_, TH_, PX_)                                                                 \
-  launch_chunk<TW_, TH_, PX_>(chunk, va, tile_begin, tile_end, counter, keys, recs, ranges, nb2,  \
-                              beta3, depth, alpha, stats, stats_stride, ctrl, st)
-  if (tile_w == 8 && tile_h == 8) {
-    if (px == 1) FE_BLEND(8, 8, 1); else FE_BLEND(8, 8, 2);
-  } else if (tile_w == 32 && tile_h == 8) {
-    if (px == 1) FE_BLEND(32, 8, 1); else if (px == 2) FE_BLEND(32, 8, 2); else FE_BLEND(32, 8, 4);
-  } else {
-    if (px == 1) FE_BLEND(16, 16, 1); else if (px == 2) FE_BLEND(16, 16, 2); else FE_BLEND(16, 16, 4);
-  }
-#undef FE_BLEND
+  blend_dispatch(va, tile_w, tile_h, px, chunk, tile_begin, tile_end, counter, nullptr, keys, recs,
+                 ranges, beta2, beta3, depth, alpha, stats, stats_stride, ctrl, st);
 }
 
 void launch_blend_fwd(const ViewsArg& va, int tile_w, int tile_h, int px, int chunk,
-                      int64_t n_tiles, const uint64_t* keys, const GaussRec* recs,
-                      const uint2* ranges, float beta2, float beta3, float* depth, float* alpha,
-                      float* stats, int64_t stats_stride, Control* ctrl, cudaStream_t st) {
-  launch_blend_fwd_band(va, tile_w, tile_h, px, chunk, 0, n_tiles, &ctrl->next_tile, keys, recs,
-                        ranges, beta2, beta3, depth, alpha, stats, stats_stride, ctrl, st);
+                      int64_t n_tiles, const uint32_t* order, const uint64_t* keys,
+                      const GaussRec* recs, const uint2* ranges, float beta2, float beta3,
+                      float* depth, float* alpha, float* stats, int64_t stats_stride,
+                      Control* ctrl, cudaStream_t st) {
+  blend_dispatch(va, tile_w, tile_h, px, chunk, 0, n_tiles, &ctrl->next_tile, order, keys, recs,
+                 ranges, beta2, beta3, depth, alpha, stats, stats_stride, ctrl, st);
 }
 
 }  // namespace fe

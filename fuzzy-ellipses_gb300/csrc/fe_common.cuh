@@ -105,14 +105,27 @@ struct __align__(8) TileRect {
   uint16_t x0, y0, x1, y1;
 };
 
+// Tile work classes of the tile-major binning, heaviest first: class c < kTileClasses - 2 holds
+// tiles with 2^(kTileClasses - 2 - c) <= keys < 2^(kTileClasses - 1 - c) (class 0 open-ended),
+// class kTileClasses - 2 one key, class kTileClasses - 1 none.
+constexpr int kTileClasses = 10;
+__host__ __device__ __forceinline__ int tile_class(uint32_t keys) {
+  if (keys == 0) return kTileClasses - 1;
+  int b = 0;
+  while ((keys >> (b + 1)) != 0u && b < 31) ++b;  // floor(log2(keys))
+  const int c = (kTileClasses - 2) - b;
+  return c < 0 ? 0 : c;
+}
+
 // Small device-side control block at the start of every arena.
 struct Control {
   unsigned long long num_keys;  // keys produced by the last run (clamped to capacity)
   unsigned long long want_keys; // keys the run needed
   uint32_t error;               // FE_DEVERR_* bits
   uint32_t next_tile;           // work counter of the persistent blend
-  uint32_t pad[10];
+  uint32_t tile_class[kTileClasses];  // tiles per work class (tile-major binning)
 };
+static_assert(sizeof(Control) == 64, "Control layout");
 
 // View lookup: the plain single-render path passes its one view by value (so it needs no
 // upload and stays capturable); batches pass a device table.

@@ -43,11 +43,17 @@ uint64_t* launch_sort(uint64_t* a, uint64_t* b, int key_bits, const Control* ctr
 // pass (one block per tile row of every view) sets ctrl->num_keys = min(want_keys, capacity)
 // (FE_DEVERR_CAPACITY past it) and writes the keys of every tile in ascending Gaussian id at their
 // place in the sorted order (keys past num_keys dropped) and the non-empty tile ranges (ranges
-// zeroed beforehand). Same keys and ranges as emit + stable sort + ranges.
+// zeroed beforehand). Same keys and ranges as emit + stable sort + ranges. For many views the
+// row totals are first turned into row bases in place (row_tot is consumed). With `order`
+// (kTileClasses lists of n_tiles entries, ctrl's class counts zeroed) every tile's id is also
+// appended to the list of its work class (tile_class of its key count), which
+// launch_blend_fwd then serves heaviest class first.
 constexpr int kMaxRowTiles = 1024;
+constexpr int kRowBaseViews = 32;  // above this many views the row bases are formed first
 void launch_tile_binning_emit(const ViewsArg& va, int n_views, int max_gy, const TileRect* rects,
-                              const unsigned long long* row_tot, int64_t capacity, Control* ctrl,
-                              uint2* ranges, uint64_t* keys, cudaStream_t st);
+                              unsigned long long* row_tot, int64_t capacity, Control* ctrl,
+                              uint2* ranges, uint64_t* keys, uint32_t* order, int64_t n_tiles,
+                              cudaStream_t st);
 // Tile ranges of the sorted keys (ranges zeroed beforehand; empty tiles keep {0,0}).
 void launch_ranges(const uint64_t* keys, const Control* ctrl, int64_t capacity, uint2* ranges,
                    cudaStream_t st);
@@ -56,9 +62,11 @@ void launch_ranges(const uint64_t* keys, const Control* ctrl, int64_t capacity, 
 // px: pixels per thread (1, 2 or 4; 0 = default for the tile shape); chunk: record pairs per
 // shared-memory stage (8, 16 or 32; 0 = 32). The blend builds each key's tile record itself from
 // the sorted keys and the Gaussian records (no gathered record stream). Persistent:
-// ctrl->next_tile must be zero.
+// ctrl->next_tile must be zero. `order`: the tile-major binning's per-class tile lists (heaviest
+// tiles are then taken first) or NULL (tiles in index order).
 void launch_blend_fwd(const ViewsArg& va, int tile_w, int tile_h, int px, int chunk, int64_t n_tiles,
-                      const uint64_t* keys, const GaussRec* recs, const uint2* ranges, float beta2,
+                      const uint32_t* order, const uint64_t* keys, const GaussRec* recs,
+                      const uint2* ranges, float beta2,
                       float beta3, float* depth, float* alpha, float* stats, int64_t stats_stride,
                       Control* ctrl, cudaStream_t st);
 // The blend over global tiles [tile_begin, tile_end) only, taking tiles from `counter` (zero at

@@ -461,17 +461,19 @@ class Batch:
     host synchronisation and can be captured in a CUDA graph; ``exact_keys=True`` sizes the key
     scratch from the device-side count instead (one 8-byte readback per run).
     ``tile``, ``px`` (pixels per thread) and ``chunk`` (record pairs per shared-memory stage)
-    select the blend configuration. ``keep_binning=True`` lets ``backward`` reuse the binning of
+    select the blend configuration; ``heavy_first=True`` makes the blend take the tiles with the
+    most keys first (tile-major binning only; see FE_FLAG_HEAVY_TILES_FIRST). ``keep_binning=True`` lets ``backward`` reuse the binning of
     the preceding ``forward`` on the same Gaussian tensors (their contents must not change in
     between) instead of recomputing it.
     """
 
     def __init__(self, scenes, views, beta2=21.4, beta3=2.66, *, cull="eps", cull_param=None,
                  tile=(16, 16), px=0, chunk=0, exact_keys=False, keep_binning=False,
-                 binning="tiles"):
+                 binning="tiles", heavy_first=False):
         lib = N.load()
         flags = (N.flag_chunk(chunk) | (N.FE_FLAG_EXACT_KEYS if exact_keys else 0)
-                 | (N.FE_FLAG_KEEP_BINNING if keep_binning else 0) | _binning_flag(binning))
+                 | (N.FE_FLAG_KEEP_BINNING if keep_binning else 0) | _binning_flag(binning)
+                 | (N.FE_FLAG_HEAVY_TILES_FIRST if heavy_first else 0))
         desc = N.make_desc(0, 1, 1, 1.0, 1.0, 0.0, 0.0, beta2, beta3, cull, cull_param, tile,
                            flags=flags, px=px)
         sc, nsc, vs, nvs = self._tables(scenes, views)

@@ -7,7 +7,10 @@ Three knobs change the work and its mapping onto the GPU:
   more tile records to build;
 * ``px``    -- pixels of one tile row per thread (1, 2, 4): shares each record's shared-memory
   loads and row-constant polynomial terms across more evaluations, at the cost of registers;
-* ``chunk`` -- record pairs per shared-memory stage of the blend's record ring (8, 16, 32).
+* ``chunk`` -- record pairs per shared-memory stage of the blend's record ring (8, 16, 32);
+* ``heavy_first`` -- whether the blend takes the tiles with the most keys first (tried on the
+  fastest of the above): it shortens the persistent schedule's tail on batches of a few heavy
+  tiles per CTA and costs time where light tiles dominate.
 
 ``Autotuner.tune`` times every candidate on the actual batch (median of per-stage CUDA-event
 timings of the whole pipeline, not just the blend) and caches the fastest per workload bucket
@@ -23,7 +26,7 @@ import os
 import statistics
 import threading
 
-DEFAULT = {"tile": (16, 16), "px": 4, "chunk": 16}
+DEFAULT = {"tile": (16, 16), "px": 4, "chunk": 16, "heavy_first": False}
 
 CANDIDATES = [
     ((8, 8), 1, 16), ((8, 8), 2, 8), ((8, 8), 2, 16),
@@ -65,7 +68,8 @@ class Autotuner:
         e = self.table.get(bucket(scenes, views))
         if not e:
             return dict(DEFAULT)
-        return {"tile": tuple(e["tile"]), "px": e["px"], "chunk": e["chunk"]}
+        return {"tile": tuple(e["tile"]), "px": e["px"], "chunk": e["chunk"],
+                "heavy_first": bool(e.get("heavy_first", False))}
 
     def tune(self, scenes, views, means, prec, logw, candidates=CANDIDATES, reps=5, **batch_kw):
         """Time every candidate on this batch; cache and return the fastest configuration."""
@@ -73,9 +77,9 @@ class Autotuner:
 
         from .api import Batch
 
-        results = []
-        for tile, px, chunk in candidates:
-            b = Batch(scenes, views, tile=tile, px=px, chunk=chunk, **batch_kw)
+        def time_one(tile, px, chunk, heavy_first):
+            b = Batch(scenes, views, tile=tile, px=px, chunk=chunk, heavy_first=heavy_first,
+                      **batch_kw)
             depth = torch.empty(b.n_pixels, device=means.device)
             alpha = torch.empty(b.n_pixels, device=means.device)
             b.forward(means, prec, logw, depth, alpha)
@@ -85,14 +89,18 @@ class Autotuner:
                 totals.append(sum(ms.values()))
                 stages.append(ms)
             b.close()
-            med = statistics.median(totals)
-            results.append({"tile": list(tile), "px": px, "chunk": chunk, "ms": med,
-                            "blend_ms": statistics.median(s["blend"] for s in stages)})
+            return {"tile": list(tile), "px": px, "chunk": chunk, "heavy_first": heavy_first,
+                    "ms": statistics.median(totals),
+                    "blend_ms": statistics.median(s["blend"] for s in stages)}
+
+        results = [time_one(tile, px, chunk, False) for tile, px, chunk in candidates]
+        best = min(results, key=lambda r: r["ms"])
+        results.append(time_one(tuple(best["tile"]), best["px"], best["chunk"], True))
         best = min(results, key=lambda r: r["ms"])
         key = bucket(scenes, views)
         with self._lock:
             self.table[key] = {"tile": best["tile"], "px": best["px"], "chunk": best["chunk"],
-                               "ms": best["ms"]}
+                               "heavy_first": best["heavy_first"], "ms": best["ms"]}
             if self.persist:
                 try:
                     os.makedirs(os.path.dirname(self.path), exist_ok=True)
@@ -103,4 +111,5 @@ class Autotuner:
                 except OSError:
                     pass
         return {"tile": tuple(best["tile"]), "px": best["px"], "chunk": best["chunk"],
-                "ms": best["ms"], "candidates": results, "bucket": key}
+                "heavy_first": best["heavy_first"], "ms": best["ms"], "candidates": results,
+                "bucket": key}

@@ -188,3 +188,32 @@ def test_tile_major_batch_equals_radix_batch(cuda_device):
         out.append((d, a, st["num_keys"]))
     assert out[0][2] == out[1][2]
     assert torch.equal(out[0][0], out[1][0]) and torch.equal(out[0][1], out[1][1])
+
+
+def test_many_view_batch_row_bases_equal_radix_batch(cuda_device):
+    """Past the view count where the tile-major binning first forms every row's key base in one
+    block (row_bases_kernel), a batch of 60 uneven views of 12 scenes still renders bit-identically
+    to the radix-sorted batch."""
+    items = S.config3(seed=7, n_scenes=12)
+    means, prec, logw, scenes, views = [], [], [], [], []
+    off = 0
+    for si, (sc, cams) in enumerate(items):
+        means.append(sc.means); prec.append(sc.prec); logw.append(sc.logw)
+        scenes.append((off, sc.n))
+        off += sc.n
+        for c in cams:
+            views.append(dict(scene=si, height=c.height, width=c.width, fx=c.fx, fy=c.fy,
+                              cx=c.cx, cy=c.cy, quat=c.quat, trans=c.trans))
+    while len(views) < 60:  # repeat poses until past the threshold
+        views.append(dict(views[len(views) % 20]))
+    m, p, w = [torch.from_numpy(np.concatenate(x)).to(cuda_device) for x in (means, prec, logw)]
+    out = []
+    for binning in ("tiles", "radix"):
+        b = fe.Batch(scenes, views, binning=binning)
+        assert binning != "tiles" or b.launches_per_forward == 4
+        d, a = b.forward(m, p, w)
+        st = b.status()
+        assert st["device_error"] == 0 and st["num_keys"] == st["want_keys"]
+        out.append((d, a, st["num_keys"]))
+    assert out[0][2] == out[1][2]
+    assert torch.equal(out[0][0], out[1][0]) and torch.equal(out[0][1], out[1][1])

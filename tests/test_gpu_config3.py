@@ -46,7 +46,8 @@ def test_config3_full_batch_graph_replay(cuda_device, cfg3, tmp_path):
     items, scenes, views, owner, (m, p, w) = cfg3
     tuner = autotune.Autotuner(path=str(tmp_path / "tune.json"))
     best = tuner.tune(scenes, views, m, p, w, reps=2)
-    b = fe.Batch(scenes, views, tile=best["tile"], px=best["px"], chunk=best["chunk"])
+    b = fe.Batch(scenes, views, tile=best["tile"], px=best["px"], chunk=best["chunk"],
+                 heavy_first=best["heavy_first"])
     depth = torch.empty(b.n_pixels, device=cuda_device)
     alpha = torch.empty(b.n_pixels, device=cuda_device)
     b.forward(m, p, w, depth, alpha)
