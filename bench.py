@@ -79,7 +79,22 @@ def parse():
     ap.add_argument("--binning", choices=["tiles", "radix"], default="tiles",
                     help="binning of the batched step: tile-major (default) or key emission + "
                          "radix sort (to profile the sort path)")
+    ap.add_argument("--blend", default=None,
+                    help="with --profile-step: blend configuration TILExTILE/PX/CHUNK[/heavy] "
+                         "(e.g. 16x16/4/32/heavy, the one the autotuner picks on the 16-camera "
+                         "step); default: the autotuner's untuned default")
+    ap.add_argument("--profile-single", type=int, default=0, metavar="CALLS",
+                    help="build the workload, then run CALLS plain single-view fe_render_fwd calls "
+                         "(camera i mod 16) and exit (the per-call path's ncu capture)")
     return ap.parse_args()
+
+
+def blend_cfg(spec):
+    """TILExTILE/PX/CHUNK[/heavy] -> the Batch keyword arguments."""
+    parts = spec.split("/")
+    tw, th = (int(x) for x in parts[0].split("x"))
+    return {"tile": (tw, th), "px": int(parts[1]), "chunk": int(parts[2]),
+            "heavy_first": len(parts) > 3 and parts[3] == "heavy"}
 
 
 def job_value(dev_s, units_per_step, steps, world, device):
@@ -309,9 +324,17 @@ def main():
     npix = H * W
     views = [dict(scene=0, height=c.height, width=c.width, fx=c.fx, fy=c.fy, cx=c.cx, cy=c.cy,
                   quat=c.quat, trans=c.trans) for c in cams]
+    if args.profile_single:
+        out = (torch.empty(H, W, device=dev), torch.empty(H, W, device=dev))
+        for i in range(args.profile_single):
+            c = cams[i % len(cams)]
+            fe.render_forward(m, p, w, c.fx, c.fy, c.cx, c.cy, c.quat, c.trans, H, W, out=out)
+        torch.cuda.synchronize()
+        assert fe.device_status() == 0
+        return
     tuned = None
     if args.profile_step:
-        cfg = dict(fe.autotune.DEFAULT)
+        cfg = blend_cfg(args.blend) if args.blend else dict(fe.autotune.DEFAULT)
     else:
         tuner = fe.autotune.Autotuner(persist=False)
         tuned = tuner.tune([(0, scene.n)], views, m, p, w, reps=3)
