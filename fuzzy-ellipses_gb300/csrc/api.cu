@@ -122,18 +122,27 @@ struct KeySpace {
   uint32_t* hist;
 };
 
+// Zero the control block and the first `rows` row-total entries with one memset (row_tot is
+// carved directly after the control block).
+inline cudaError_t zero_ctrl_rows(const RecSpace& rs, int64_t rows, cudaStream_t st) {
+  const size_t bytes = (size_t)(reinterpret_cast<char*>(rs.row_tot + rows) -
+                                reinterpret_cast<char*>(rs.ctrl));
+  return cudaMemsetAsync(rs.ctrl, 0, bytes, st);
+}
+
 template <class F>
 size_t carve_rec(char* base, int64_t n_rec, int64_t n_tiles, int64_t n_pix, bool bwd, F&& out) {
   Carver c{base};
   RecSpace s;
   s.ctrl = c.take<Control>(1);
+  // (directly after the control block: one memset clears both; see zero_ctrl_rows)
+  s.row_tot = c.take<unsigned long long>(n_tiles + 1);
   s.recs = c.take<GaussRec>(n_rec);
   s.rects = c.take<TileRect>(n_rec);
   s.touched = c.take<uint32_t>(n_rec);
   s.incl = c.take<uint32_t>(n_rec);
   s.scan_tmp = c.take<unsigned long long>(scan_grid(std::max(n_rec, n_tiles)));
   s.ranges = c.take<uint2>(n_tiles);
-  s.row_tot = c.take<unsigned long long>(n_tiles + 1);
   s.order = c.take<uint32_t>((int64_t)kTileClasses * n_tiles);
   s.rgrad = bwd ? c.take<RecGrad>(n_rec) : nullptr;
   out(s);
@@ -269,10 +278,10 @@ int run_binning(const Pipeline& p, int64_t worst, DevBuf& recbuf, DevBuf& keybuf
 
   // The single-view pipelines describe their view on the host (va.one).
   const RowPlan rp = (p.va.table || p.radix) ? RowPlan{} : row_plan(&p.va.one, 1);
-  FE_CUDA(cudaMemsetAsync(rs.ctrl, 0, sizeof(Control), st));
-  FE_CUDA(cudaMemsetAsync(rs.ranges, 0, sizeof(uint2) * (size_t)p.n_tiles, st));
-  if (rp.ok)
-    FE_CUDA(cudaMemsetAsync(rs.row_tot, 0, sizeof(unsigned long long) * (rp.max_gy + 1), st));
+  // The tile-major emission writes every tile's range; the emit + sort path writes only the
+  // non-empty ones.
+  FE_CUDA(zero_ctrl_rows(rs, rp.ok ? rp.max_gy + 1 : 0, st));
+  if (!rp.ok) FE_CUDA(cudaMemsetAsync(rs.ranges, 0, sizeof(uint2) * (size_t)p.n_tiles, st));
   launch_preprocess(p.va, p.n_rec, p.means, p.prec, p.logw, p.quat, nullptr, p.trans, p.cull_mode,
                     p.cull_param, p.tile_w, p.tile_h, rs.recs, rs.rects, rs.touched,
                     rp.ok ? rs.row_tot : nullptr, rp.max_gy, rs.ctrl, st);
@@ -1181,12 +1190,8 @@ static const uint32_t* batch_order(const fe_batch* b, const Pipeline& p) {
 static int batch_binning(fe_batch* b, const Pipeline& p, cudaStream_t st, cudaEvent_t* ev) {
   const RecSpace& rs = b->rs;
   const RowPlan rp = p.radix ? RowPlan{} : b->rows;
-  FE_CUDA(cudaMemsetAsync(rs.ctrl, 0, sizeof(Control), st));
-  FE_CUDA(cudaMemsetAsync(rs.ranges, 0, sizeof(uint2) * (size_t)p.n_tiles, st));
-  if (rp.ok)
-    FE_CUDA(cudaMemsetAsync(rs.row_tot, 0,
-                            sizeof(unsigned long long) * (size_t)rp.n_views * (rp.max_gy + 1),
-                            st));
+  FE_CUDA(zero_ctrl_rows(rs, rp.ok ? (int64_t)rp.n_views * (rp.max_gy + 1) : 0, st));
+  if (!rp.ok) FE_CUDA(cudaMemsetAsync(rs.ranges, 0, sizeof(uint2) * (size_t)p.n_tiles, st));
   if (ev) FE_CUDA(cudaEventRecord(ev[0], st));
   launch_preprocess(p.va, p.n_rec, p.means, p.prec, p.logw, p.quat, nullptr, p.trans, p.cull_mode,
                     p.cull_param, p.tile_w, p.tile_h, rs.recs, rs.rects, rs.touched,
@@ -1565,13 +1570,13 @@ int fe_render_fwd_noalloc(const fe_render_desc* d, const float* means, const flo
   carve_rec(base, p.n_rec, p.n_tiles, p.n_pix, false, [&](const RecSpace& s) { rs = s; });
   carve_keys(base + rec_bytes, worst, [&](const KeySpace& s) { ks = s; });
 
-  // Must start at zero on every call: the control block (key counters, device error word and
-  // the blend's tile counter) and the tile ranges (tiles without keys keep an empty range).
-  FE_CUDA(cudaMemsetAsync(rs.ctrl, 0, sizeof(Control), st));
-  FE_CUDA(cudaMemsetAsync(rs.ranges, 0, sizeof(uint2) * (size_t)p.n_tiles, st));
+  // Must start at zero on every call: the control block (key counters, device error word, the
+  // blend's tile counter and work-class counts), the row totals of the tile-major binning, and on
+  // the emit + sort path the tile ranges (tiles without keys keep an empty range; the tile-major
+  // emission writes every tile's range itself).
   const RowPlan rp = p.radix ? RowPlan{} : row_plan(&p.va.one, 1);
-  if (rp.ok)
-    FE_CUDA(cudaMemsetAsync(rs.row_tot, 0, sizeof(unsigned long long) * (rp.max_gy + 1), st));
+  FE_CUDA(zero_ctrl_rows(rs, rp.ok ? rp.max_gy + 1 : 0, st));
+  if (!rp.ok) FE_CUDA(cudaMemsetAsync(rs.ranges, 0, sizeof(uint2) * (size_t)p.n_tiles, st));
   launch_preprocess(p.va, p.n_rec, p.means, p.prec, p.logw, p.quat, nullptr, p.trans, p.cull_mode,
                     p.cull_param, p.tile_w, p.tile_h, rs.recs, rs.rects, rs.touched,
                     rp.ok ? rs.row_tot : nullptr, rp.max_gy, rs.ctrl, st);

@@ -456,7 +456,7 @@ __global__ void __launch_bounds__(kRowThreads) tile_emit_kernel(
     ViewsArg va, const TileRect* __restrict__ rects,
     const unsigned long long* __restrict__ row_tot, bool bases, int64_t capacity,
     Control* __restrict__ ctrl, uint2* __restrict__ ranges, uint64_t* __restrict__ keys,
-    uint32_t* __restrict__ order, int64_t n_tiles) {
+    uint32_t* __restrict__ order, int64_t n_tiles, int nseg) {
   __shared__ RowRect list[kRowSeg];
   __shared__ int diff[kMaxRowTiles + 1];         // +1 at x0, -1 at x1 of every covering rectangle
   __shared__ uint32_t pos[kMaxRowTiles];  // per tile: next key slot within the row
@@ -473,13 +473,18 @@ __global__ void __launch_bounds__(kRowThreads) tile_emit_kernel(
     if (want > cap) atomicOr(&ctrl->error, FE_DEVERR_CAPACITY);
   }
   const ViewDev& V = view_at(va, blockIdx.y);
-  const int row = blockIdx.x;
+  // nseg blocks share a row: each forms the whole row's tile counts but writes the ranges, work
+  // classes and keys of its own slice of the row's tiles [x_lo, x_hi) only.
+  const int row = (int)blockIdx.x / nseg, seg = (int)blockIdx.x - row * nseg;
   if (row >= V.gy) return;  // (uniform over the block)
   if (V.gx > kMaxRowTiles) {  // the host plans this path only for narrower views
     if (tid == 0) atomicOr(&ctrl->error, FE_DEVERR_CAPACITY);
     return;
   }
   const int gx = V.gx, n = V.n;
+  const int seg_w = (gx + nseg - 1) / nseg;
+  const int x_lo = seg * seg_w, x_hi = min(gx, x_lo + seg_w);
+  if (x_lo >= x_hi) return;  // (uniform over the block)
   const int64_t tile0 = V.tile_base + (int64_t)row * gx;
   const TileRect* vr = rects + V.rec_base;
 
@@ -487,7 +492,7 @@ __global__ void __launch_bounds__(kRowThreads) tile_emit_kernel(
   // of row r is the sum of entries 0..r, so the keys before row `row` of this view are
   // sum_{r' < row} d[r'] (row - r'), and a whole earlier view holds sum_{r' < gy} d[r'] (gy - r').
   // With `bases` set, row_bases_kernel has already replaced the differences by the row bases.
-  const int stride = (int)gridDim.x + 1;
+  const int stride = (int)gridDim.x / nseg + 1;
   unsigned long long row_base;
   if (bases) {
     row_base = row_tot[(int64_t)blockIdx.y * stride + row];
@@ -558,13 +563,14 @@ __global__ void __launch_bounds__(kRowThreads) tile_emit_kernel(
 #pragma unroll
   for (int q = 0; q < kTilesPer; ++q) {
     const int x = kTilesPer * tid + q;
-    if (x < gx) {
+    if (x >= x_lo && x < x_hi) {
       pos[x] = cex < lim ? (uint32_t)cex : lim;  // (slots from lim on are dropped)
       const unsigned long long lo = min(row_base + cex, K);
       const unsigned long long hi = min(row_base + cex + (unsigned)cnt[q], K);
-      if (hi > lo) ranges[tile0 + x] = make_uint2((uint32_t)lo, (uint32_t)hi);
-      cex += (unsigned)cnt[q];
+      // every tile of the slice: empty tiles (or tiles whose keys were all dropped) get {0,0}
+      ranges[tile0 + x] = hi > lo ? make_uint2((uint32_t)lo, (uint32_t)hi) : make_uint2(0u, 0u);
     }
+    cex += (unsigned)cnt[q];
   }
   if (order) {
     // Work classes: every tile of the row joins its class's list (order + c n_tiles), a shared
@@ -578,7 +584,7 @@ __global__ void __launch_bounds__(kRowThreads) tile_emit_kernel(
     for (int q = 0; q < kTilesPer; ++q) {
       const int x = kTilesPer * tid + q;
       cl[q] = tile_class((uint32_t)cnt[q]);
-      rank[q] = x < gx ? atomicAdd(&cls_n[cl[q]], 1u) : 0u;
+      rank[q] = (x >= x_lo && x < x_hi) ? atomicAdd(&cls_n[cl[q]], 1u) : 0u;
     }
     __syncthreads();
     if (tid < kTileClasses && cls_n[tid] != 0u)
@@ -587,21 +593,22 @@ __global__ void __launch_bounds__(kRowThreads) tile_emit_kernel(
 #pragma unroll
     for (int q = 0; q < kTilesPer; ++q) {
       const int x = kTilesPer * tid + q;
-      if (x < gx)
+      if (x >= x_lo && x < x_hi)
         order[(int64_t)cl[q] * n_tiles + cls_base[cl[q]] + rank[q]] = (uint32_t)(tile0 + x);
     }
   }
   __syncthreads();
   for (int s0 = 0; s0 < n; s0 += kRowSeg) {
     if (n > kRowSeg) total = filter_row(vr, n, s0, row, list, ws);  // else still in shared memory
-    // Each warp takes kTileBlock of its tiles at a time (tiles warp + kRowWarps t), keeping their
-    // next slots in registers, and reads each 32-entry chunk of the list once for all of them.
-    for (int xb = warp; xb < gx; xb += kRowWarps * kTileBlock) {
+    // Each warp takes kTileBlock of its tiles at a time (tiles warp + kRowWarps t of the slice),
+    // keeping their next slots in registers, and reads each 32-entry chunk of the list once for
+    // all of them.
+    for (int xb = x_lo + warp; xb < x_hi; xb += kRowWarps * kTileBlock) {
       uint32_t p[kTileBlock];
 #pragma unroll
       for (int t = 0; t < kTileBlock; ++t) {
         const int x = xb + kRowWarps * t;
-        p[t] = x < gx ? (uint32_t)pos[x] : 0u;
+        p[t] = x < x_hi ? (uint32_t)pos[x] : 0u;
       }
       for (uint32_t j0 = 0; j0 < total; j0 += 32) {
         const uint32_t j = j0 + lane;
@@ -609,8 +616,8 @@ __global__ void __launch_bounds__(kRowThreads) tile_emit_kernel(
         if (j < total) e = list[j];
 #pragma unroll
         for (int t = 0; t < kTileBlock; ++t) {
-          const int x = xb + kRowWarps * t;  // (x >= gx: no rectangle reaches it)
-          const bool cov = e.x0 <= x && x < e.x1;
+          const int x = xb + kRowWarps * t;
+          const bool cov = x < x_hi && e.x0 <= x && x < e.x1;
           const uint32_t bal = __ballot_sync(full, cov);
           if (cov) {
             const uint32_t k = p[t] + __popc(bal & lt_mask);
@@ -623,7 +630,7 @@ __global__ void __launch_bounds__(kRowThreads) tile_emit_kernel(
 #pragma unroll
         for (int t = 0; t < kTileBlock; ++t) {
           const int x = xb + kRowWarps * t;
-          if (x < gx) pos[x] = p[t];
+          if (x < x_hi) pos[x] = p[t];
         }
       }
     }
@@ -686,8 +693,12 @@ void launch_tile_binning_emit(const ViewsArg& va, int n_views, int max_gy, const
   // single-block launch that forms all row bases.
   const bool bases = n_views > kRowBaseViews;
   if (bases) row_bases_kernel<<<1, kRowThreads, 0, st>>>(va, n_views, max_gy + 1, row_tot);
-  tile_emit_kernel<<<dim3((unsigned)max_gy, (unsigned)n_views), kRowThreads, 0, st>>>(
-      va, rects, row_tot, bases, capacity, ctrl, ranges, keys, order, n_tiles);
+  // Launches of few rows (single views) split each row over up to 8 blocks so that the key
+  // writing, the longest part of a row's work, is spread over more SMs.
+  const int64_t rows = (int64_t)max_gy * n_views;
+  const int nseg = rows >= 2 * 152 ? 1 : (int)std::min<int64_t>(8, (2 * 152 + rows - 1) / rows);
+  tile_emit_kernel<<<dim3((unsigned)(max_gy * nseg), (unsigned)n_views), kRowThreads, 0, st>>>(
+      va, rects, row_tot, bases, capacity, ctrl, ranges, keys, order, n_tiles, nseg);
 }
 
 void launch_ranges(const uint64_t* keys, const Control* ctrl, int64_t capacity, uint2* ranges,

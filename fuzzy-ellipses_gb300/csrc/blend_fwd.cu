@@ -196,9 +196,14 @@ __global__ void __launch_bounds__(BlendShape<TW, TH, PX, CH>::NT,
   }
   uint32_t phase = 0;  // parity of the next completion of sm.bar
 
+  // Work index of the CTA's first tile: its own index (the grid never exceeds the tiles), so the
+  // launch does not start with every CTA contending for the counter; later tiles come from the
+  // counter, offset by the grid.
+  bool first = true;
   while (true) {
     if (tid == 0) {
-      uint32_t w = tile_begin + atomicAdd(counter, 1u);
+      uint32_t w = first ? tile_begin + blockIdx.x
+                         : tile_begin + gridDim.x + atomicAdd(counter, 1u);
       if (use_order && w < tile_end) {
         int c = 0;
         while (c + 1 < kTileClasses && w >= sm.cls_base[c + 1]) ++c;
@@ -206,6 +211,7 @@ __global__ void __launch_bounds__(BlendShape<TW, TH, PX, CH>::NT,
       }
       sm.tile = w;
     }
+    first = false;
     __syncthreads();
     const uint32_t tile = sm.tile;
     if (tile >= tile_end) break;

@@ -42,8 +42,9 @@ uint64_t* launch_sort(uint64_t* a, uint64_t* b, int key_bits, const Control* ctr
 // run's key count to ctrl->want_keys; the emit
 // pass (one block per tile row of every view) sets ctrl->num_keys = min(want_keys, capacity)
 // (FE_DEVERR_CAPACITY past it) and writes the keys of every tile in ascending Gaussian id at their
-// place in the sorted order (keys past num_keys dropped) and the non-empty tile ranges (ranges
-// zeroed beforehand). Same keys and ranges as emit + stable sort + ranges. For many views the
+// place in the sorted order (keys past num_keys dropped) and every tile's range ({0,0} for an
+// empty tile, so the ranges need no zeroing). Same keys and ranges as emit + stable sort +
+// ranges. For many views the
 // row totals are first turned into row bases in place (row_tot is consumed). With `order`
 // (kTileClasses lists of n_tiles entries, ctrl's class counts zeroed) every tile's id is also
 // appended to the list of its work class (tile_class of its key count), which
