@@ -269,6 +269,24 @@ def cpu_baseline_line(cpu, e_render, n_render_pixels):
             "renders_per_s": renders_s, "dense_evals_per_s": px_s * cpu["n"]}
 
 
+def cpu_baseline_child(steps=16, warmup=3):
+    """The CPU baseline of the main line: the reference arm itself (same implementation, same
+    sample, same conversion), run as a child process so that this process's GPU-side threads do
+    not share the host cores with it."""
+    env = {k: v for k, v in os.environ.items()
+           if k not in ("RANK", "WORLD_SIZE", "LOCAL_RANK", "MASTER_ADDR", "MASTER_PORT")}
+    r = subprocess.run([sys.executable, os.path.abspath(__file__), "--impl", "reference",
+                        "--steps", str(steps), "--warmup", str(warmup)],
+                       capture_output=True, text=True, env=env, timeout=600)
+    if r.returncode != 0:
+        raise RuntimeError(f"CPU baseline child failed: {r.stderr[-2000:]}")
+    line = json.loads(r.stdout.strip().splitlines()[-1])
+    out = dict(line["cpu_baseline"])
+    out["run"] = (f"bench.py --impl reference --steps {steps} --warmup {warmup} in a child "
+                  "process (the reference arm)")
+    return out
+
+
 def run_reference(args):
     """The reference arm: the CPU implementation of the path (float64 restatement of fm_render,
     torch, all host threads), same workload and metric, bounded per-step sample."""
@@ -595,8 +613,7 @@ def main():
     # ---- CPU baseline (oracle on the host cores, bounded sample) ---------------------------
     cpu = None
     if not args.no_cpu_baseline:
-        cpu = cpu_baseline_line(cpu_reference(scene, cams, steps=16, warmup=1), e_step / len(cams),
-                                npix)
+        cpu = cpu_baseline_child()
 
     blend_achieved = blend_evals_per_s / 1e9
     out = {
