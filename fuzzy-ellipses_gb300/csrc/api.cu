@@ -304,8 +304,9 @@ int run_binning(const Pipeline& p, int64_t worst, DevBuf& recbuf, DevBuf& keybuf
   if (exact && !rp.ok) launch_scan(rs.touched, rs.incl, p.n_rec, cap, rs.scan_tmp, rs.ctrl, st);
   if (!rp.ok || !p.heavy_first) rs.order = nullptr;  // the blend takes tiles in index order
   if (rp.ok) {
-    launch_tile_binning_emit(p.va, rp.n_views, rp.max_gy, rs.rects, rs.row_tot, cap, rs.ctrl,
-                             rs.ranges, ks.keys_a, rs.order, p.n_tiles, st);
+    launch_tile_binning_emit(p.va, rp.n_views, rp.max_gy, rs.rects,
+                             rs.row_tot, cap, rs.ctrl, rs.ranges, ks.keys_a, rs.order, p.n_tiles,
+                             st);
     sorted = ks.keys_a;
   } else {
     launch_emit_keys(p.va, rs.incl, rs.rects, p.n_rec, rs.ctrl, ks.keys_a, cap, st);
@@ -1217,9 +1218,9 @@ static int batch_binning(fe_batch* b, const Pipeline& p, cudaStream_t st, cudaEv
   if (ev) FE_CUDA(cudaEventRecord(ev[2], st));
   const KeySpace& ks = b->ks;
   if (rp.ok) {
-    launch_tile_binning_emit(p.va, rp.n_views, rp.max_gy, rs.rects, rs.row_tot, b->cap, rs.ctrl,
-                             rs.ranges, ks.keys_a, p.heavy_first ? rs.order : nullptr, p.n_tiles,
-                             st);
+    launch_tile_binning_emit(p.va, rp.n_views, rp.max_gy, rs.rects,
+                             rs.row_tot, b->cap, rs.ctrl, rs.ranges, ks.keys_a,
+                             p.heavy_first ? rs.order : nullptr, p.n_tiles, st);
     if (ev) FE_CUDA(cudaEventRecord(ev[3], st));
     b->sorted = ks.keys_a;
     if (ev) FE_CUDA(cudaEventRecord(ev[4], st));
@@ -1461,8 +1462,8 @@ int fe_batch_fwd_timed(fe_batch* b, const float* means, const float* prec, const
 int fe_batch_launch_count(const fe_batch* b) {
   if (!b) return 0;
   const bool radix = (b->desc.flags & FE_FLAG_RADIX_BINNING) != 0;
-  // Tile-major binning: preprocess, (row bases for many views,) emission, blend.
-  if (b->rows.ok && !radix) return b->rows.n_views > kRowBaseViews ? 4 : 3;
+  // Tile-major binning: preprocess, (row offsets and view bases for many views,) emission, blend.
+  if (b->rows.ok && !radix) return b->rows.n_views > kRowBaseViews ? 5 : 3;
   // Emit + sort: preprocess, scan, emission, three kernels per radix pass, ranges, blend.
   const int passes = (bits_for(b->n_tiles) + 7) / 8;
   const int scan = b->n_rec <= 65536 ? 1 : 3;
@@ -1583,8 +1584,9 @@ int fe_render_fwd_noalloc(const fe_render_desc* d, const float* means, const flo
   uint64_t* sorted = ks.keys_a;
   if (!rp.ok || !p.heavy_first) rs.order = nullptr;
   if (rp.ok) {
-    launch_tile_binning_emit(p.va, rp.n_views, rp.max_gy, rs.rects, rs.row_tot, worst, rs.ctrl,
-                             rs.ranges, ks.keys_a, rs.order, p.n_tiles, st);
+    launch_tile_binning_emit(p.va, rp.n_views, rp.max_gy, rs.rects,
+                             rs.row_tot, worst, rs.ctrl, rs.ranges, ks.keys_a, rs.order, p.n_tiles,
+                             st);
   } else {
     launch_scan(rs.touched, rs.incl, p.n_rec, worst, rs.scan_tmp, rs.ctrl, st);
     launch_emit_keys(p.va, rs.incl, rs.rects, p.n_rec, rs.ctrl, ks.keys_a, worst, st);

@@ -417,38 +417,63 @@ __device__ __forceinline__ uint32_t filter_row(const TileRect* __restrict__ vr, 
   return total;
 }
 
-// Row bases of many views at once (one block): turns row_tot's per-view differences of the row
-// key counts into every row's first key slot (the exclusive prefix over views in order, rows in
-// order), in place, so that the emit blocks read their base instead of each summing the rows of
-// every view before theirs (quadratic in the number of views). Thread t takes the consecutive
-// views [t vpt, t vpt + vpt).
-__global__ void __launch_bounds__(kRowThreads) row_bases_kernel(ViewsArg va, int n_views,
-                                                                 int stride,
-                                                                 unsigned long long* row_tot) {
+// Row bases of many views, in two launches instead of a sum over all earlier views in every
+// emission block (quadratic in the number of views). row_tot holds per view (stride max_gy + 1)
+// the differences of the row key counts; entry gy <= max_gy of a view is the unused "past the last
+// row" difference, and entry max_gy is free for the view's total.
+// Pass 1, one warp per view: the rows' key counts (prefix of the differences) and their exclusive
+// prefix within the view, in place; the view's key total into entry max_gy.
+__global__ void __launch_bounds__(kRowThreads) row_offsets_kernel(ViewsArg va, int n_views,
+                                                                   int max_gy,
+                                                                   unsigned long long* row_tot) {
+  const int lane = threadIdx.x & 31;
+  const int v = (int)blockIdx.x * kRowWarps + (threadIdx.x >> 5);
+  if (v >= n_views) return;  // (uniform over the warp)
+  const unsigned full = 0xffffffffu;
+  const int gy = view_at(va, v).gy;
+  unsigned long long* d = row_tot + (int64_t)v * (max_gy + 1);
+  long long cnt_carry = 0;            // count of the row before this chunk
+  unsigned long long off_carry = 0;   // keys of the rows before this chunk
+  for (int r0 = 0; r0 < gy; r0 += 32) {
+    const int r = r0 + lane;
+    long long c = r < gy ? (long long)d[r] : 0;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const long long y = __shfl_up_sync(full, c, o);
+      if (lane >= o) c += y;
+    }
+    c += cnt_carry;  // this row's key count
+    unsigned long long k = r < gy ? (unsigned long long)c : 0ull;
+    unsigned long long incl = k;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const unsigned long long y = __shfl_up_sync(full, incl, o);
+      if (lane >= o) incl += y;
+    }
+    if (r < gy) d[r] = off_carry + incl - k;
+    cnt_carry = __shfl_sync(full, c, 31);
+    off_carry += __shfl_sync(full, incl, 31);
+  }
+  if (lane == 0) d[max_gy] = off_carry;
+}
+
+// Pass 2, one block: exclusive prefix of the view totals over the views, into entry max_gy.
+// Thread t takes the consecutive views [t vpt, t vpt + vpt).
+__global__ void __launch_bounds__(kRowThreads) view_bases_kernel(int n_views, int max_gy,
+                                                                  unsigned long long* row_tot) {
   __shared__ unsigned long long ws[kRowWarps];
+  const int stride = max_gy + 1;
   const int vpt = (n_views + kRowThreads - 1) / kRowThreads;
   const int v0 = (int)threadIdx.x * vpt, v1 = min(n_views, v0 + vpt);
-  unsigned long long mine = 0;  // keys of this thread's views
-  for (int v = v0; v < v1; ++v) {
-    const int gy = view_at(va, v).gy;
-    const unsigned long long* d = row_tot + (int64_t)v * stride;
-    long long cnt = 0;
-    for (int r = 0; r < gy; ++r) {
-      cnt += (long long)d[r];
-      mine += (unsigned long long)cnt;
-    }
-  }
+  unsigned long long mine = 0;
+  for (int v = v0; v < v1; ++v) mine += row_tot[(int64_t)v * stride + max_gy];
   unsigned long long base;
   block_exclusive_scan<unsigned long long>(mine, base, ws);
   for (int v = v0; v < v1; ++v) {
-    const int gy = view_at(va, v).gy;
-    unsigned long long* d = row_tot + (int64_t)v * stride;
-    long long cnt = 0;
-    for (int r = 0; r < gy; ++r) {
-      cnt += (long long)d[r];
-      d[r] = base;
-      base += (unsigned long long)cnt;
-    }
+    unsigned long long* t = row_tot + (int64_t)v * stride + max_gy;
+    const unsigned long long tot = *t;
+    *t = base;
+    base += tot;
   }
 }
 
@@ -491,11 +516,13 @@ __global__ void __launch_bounds__(kRowThreads) tile_emit_kernel(
   // row_tot holds, per view, the difference of the row key counts (stride max_gy + 1): the count
   // of row r is the sum of entries 0..r, so the keys before row `row` of this view are
   // sum_{r' < row} d[r'] (row - r'), and a whole earlier view holds sum_{r' < gy} d[r'] (gy - r').
-  // With `bases` set, row_bases_kernel has already replaced the differences by the row bases.
+  // With `bases` set, row_offsets_kernel and view_bases_kernel have already turned the
+  // differences into row offsets within the view and view bases.
   const int stride = (int)gridDim.x / nseg + 1;
   unsigned long long row_base;
-  if (bases) {
-    row_base = row_tot[(int64_t)blockIdx.y * stride + row];
+  if (bases) {  // view base (entry max_gy) + the row's offset within the view
+    row_base = row_tot[(int64_t)blockIdx.y * stride + stride - 1] +
+               row_tot[(int64_t)blockIdx.y * stride + row];
   } else {
     long long b = 0;
     for (int idx = tid; idx < (int)blockIdx.y * stride; idx += kRowThreads) {
@@ -689,10 +716,14 @@ void launch_tile_binning_emit(const ViewsArg& va, int n_views, int max_gy, const
                               uint2* ranges, uint64_t* keys, uint32_t* order, int64_t n_tiles,
                               cudaStream_t st) {
   if (n_views <= 0 || max_gy <= 0) return;
-  // Beyond a few dozen views the per-block sums over earlier views cost more than one extra
-  // single-block launch that forms all row bases.
+  // Beyond a few dozen views the per-block sums over earlier views cost more than two extra
+  // launches that form all row bases.
   const bool bases = n_views > kRowBaseViews;
-  if (bases) row_bases_kernel<<<1, kRowThreads, 0, st>>>(va, n_views, max_gy + 1, row_tot);
+  if (bases) {
+    row_offsets_kernel<<<(unsigned)((n_views + kRowWarps - 1) / kRowWarps), kRowThreads, 0, st>>>(
+        va, n_views, max_gy, row_tot);
+    view_bases_kernel<<<1, kRowThreads, 0, st>>>(n_views, max_gy, row_tot);
+  }
   // Launches of few rows (single views) split each row over up to 8 blocks so that the key
   // writing, the longest part of a row's work, is spread over more SMs.
   const int64_t rows = (int64_t)max_gy * n_views;

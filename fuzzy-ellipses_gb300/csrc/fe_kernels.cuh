@@ -44,11 +44,10 @@ uint64_t* launch_sort(uint64_t* a, uint64_t* b, int key_bits, const Control* ctr
 // (FE_DEVERR_CAPACITY past it) and writes the keys of every tile in ascending Gaussian id at their
 // place in the sorted order (keys past num_keys dropped) and every tile's range ({0,0} for an
 // empty tile, so the ranges need no zeroing). Same keys and ranges as emit + stable sort +
-// ranges. For many views the
-// row totals are first turned into row bases in place (row_tot is consumed). With `order`
-// (kTileClasses lists of n_tiles entries, ctrl's class counts zeroed) every tile's id is also
-// appended to the list of its work class (tile_class of its key count), which
-// launch_blend_fwd then serves heaviest class first.
+// ranges. For many views the row totals are first turned into row offsets and view bases in
+// place (row_tot is consumed). With `order` (kTileClasses lists of n_tiles entries, ctrl's class
+// counts zeroed) every tile's id is also appended to the list of its work class (tile_class of
+// its key count), which launch_blend_fwd then serves heaviest class first.
 constexpr int kMaxRowTiles = 1024;
 constexpr int kRowBaseViews = 32;  // above this many views the row bases are formed first
 void launch_tile_binning_emit(const ViewsArg& va, int n_views, int max_gy, const TileRect* rects,
