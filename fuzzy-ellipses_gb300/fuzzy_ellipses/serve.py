@@ -176,16 +176,17 @@ class RenderServer:
         if self._closed:
             raise RuntimeError("server is closed")
         n = req.n
-        means = np.ascontiguousarray(req.means, dtype=np.float32)
-        prec = np.ascontiguousarray(req.prec, dtype=np.float32)
-        logw = np.ascontiguousarray(req.logw, dtype=np.float32)
         views = _view_table(req)
-        pixels = int((views["height"].astype(np.int64) * views["width"]).sum())
-        # Outputs in one pinned block per request: [loss (f64) | depth | alpha | grads]. The
-        # lanes' copies into it are asynchronous at full link speed (no page faults), and the
-        # block returns to torch's pinned-memory cache once the result arrays are dropped.
+        sizes = (views["height"].astype(np.int64) * views["width"])
+        pixels = int(sizes.sum())
+        # One pinned block per request: [loss (f64) | depth | alpha | grads] for the outputs, then
+        # [means | prec | logw | targets] for the inputs, copied in here on the submitting
+        # thread. The lanes' copies from and into it are then asynchronous DMA at full link speed
+        # (a copy from pageable memory is staged by the driver and holds the lane), and the block
+        # returns to torch's pinned-memory cache once the result arrays are dropped.
         n_out = 2 * pixels + ((2 + 13 * n) if req.backward else 0)
-        block = torch.empty(n_out, dtype=torch.float32, pin_memory=True).numpy()
+        n_in = 13 * n + (pixels if req.backward else 0)
+        block = torch.empty(n_out + n_in, dtype=torch.float32, pin_memory=True).numpy()
         o = 2 if req.backward else 0
         out = {"depth": block[o:o + pixels], "alpha": block[o + pixels:o + 2 * pixels]}
         if req.backward:
@@ -194,16 +195,29 @@ class RenderServer:
                        grad_means=block[g:g + 3 * n].reshape(n, 3),
                        grad_prec=block[g + 3 * n:g + 12 * n].reshape(n, 3, 3),
                        grad_logw=block[g + 12 * n:g + 13 * n])
-        keep = [means, prec, logw, views]
+        i = n_out
+        means = block[i:i + 3 * n].reshape(n, 3)
+        prec = block[i + 3 * n:i + 12 * n].reshape(n, 3, 3)
+        logw = block[i + 12 * n:i + 13 * n]
+        np.copyto(means, req.means, casting="same_kind")
+        np.copyto(prec, req.prec, casting="same_kind")
+        np.copyto(logw, req.logw, casting="same_kind")
+        keep = [views]
         r = N.Request()
         r.n_gaussians, r.n_views = n, len(req.cameras)
         r.means, r.prec, r.logw = means.ctypes.data, prec.ctypes.data, logw.ctypes.data
         r.views = views.ctypes.data
         r.depth, r.alpha = out["depth"].ctypes.data, out["alpha"].ctypes.data
         if req.backward:
-            targets = [np.ascontiguousarray(t, dtype=np.float32) for t in req.targets]
+            targets = []
+            t0 = i + 13 * n
+            for t, hw in zip(req.targets, sizes.tolist()):
+                dst = block[t0:t0 + hw]
+                np.copyto(dst, np.asarray(t).reshape(-1), casting="same_kind")
+                targets.append(dst)
+                t0 += hw
             tptr = (ctypes.c_void_p * len(targets))(*[t.ctypes.data for t in targets])
-            keep += [targets, tptr]
+            keep += [tptr]
             r.targets = ctypes.cast(tptr, ctypes.c_void_p)
             r.grad_means = out["grad_means"].ctypes.data
             r.grad_prec = out["grad_prec"].ctypes.data
