@@ -106,11 +106,12 @@ struct RecSpace {
   Control* ctrl;
   GaussRec* recs;
   TileRect* rects;
+  FootRows* foot;  // footprint rows (unless FE_FLAG_RECT_BINNING)
   uint32_t* touched;
   uint32_t* incl;
   unsigned long long* scan_tmp;
   uint2* ranges;
-  unsigned long long* row_tot;  // tile-major binning: row key-count differences per view
+  unsigned long long* row_tot;  // tile-major binning: key counts of the tile rows, per view
   uint32_t* order;  // tile-major binning: tile ids per work class (kTileClasses lists of n_tiles)
   RecGrad* rgrad;  // backward only
 };
@@ -139,6 +140,7 @@ size_t carve_rec(char* base, int64_t n_rec, int64_t n_tiles, int64_t n_pix, bool
   s.row_tot = c.take<unsigned long long>(n_tiles + 1);
   s.recs = c.take<GaussRec>(n_rec);
   s.rects = c.take<TileRect>(n_rec);
+  s.foot = c.take<FootRows>(n_rec);
   s.touched = c.take<uint32_t>(n_rec);
   s.incl = c.take<uint32_t>(n_rec);
   s.scan_tmp = c.take<unsigned long long>(scan_grid(std::max(n_rec, n_tiles)));
@@ -223,6 +225,7 @@ struct Pipeline {
   int px;     // pixels per thread in the blend (0 = default)
   int chunk;  // record pairs per shared-memory stage in the blend (0 = default)
   bool radix;  // FE_FLAG_RADIX_BINNING: emit + sort even where tile-major binning applies
+  bool rect_binning;  // FE_FLAG_RECT_BINNING: every tile of each footprint's rectangle
   bool heavy_first;  // FE_FLAG_HEAVY_TILES_FIRST: work-class tile lists for the blend
   int cull_mode;
   float cull_param;
@@ -265,6 +268,11 @@ RowPlan row_plan(const ViewDev* views, int n_views) {
   return r;
 }
 
+// Footprint rows of the records, or NULL when each footprint's whole rectangle is binned.
+inline FootRows* foot_of(const Pipeline& p, const RecSpace& rs) {
+  return p.rect_binning ? nullptr : rs.foot;
+}
+
 int run_binning(const Pipeline& p, int64_t worst, DevBuf& recbuf, DevBuf& keybuf,
                 unsigned long long* h_pinned, bool bwd, cudaStream_t st, RecSpace& rs,
                 KeySpace& ks, int64_t& cap, uint64_t*& sorted) {
@@ -283,8 +291,8 @@ int run_binning(const Pipeline& p, int64_t worst, DevBuf& recbuf, DevBuf& keybuf
   FE_CUDA(zero_ctrl_rows(rs, rp.ok ? rp.max_gy + 1 : 0, st));
   if (!rp.ok) FE_CUDA(cudaMemsetAsync(rs.ranges, 0, sizeof(uint2) * (size_t)p.n_tiles, st));
   launch_preprocess(p.va, p.n_rec, p.means, p.prec, p.logw, p.quat, nullptr, p.trans, p.cull_mode,
-                    p.cull_param, p.tile_w, p.tile_h, rs.recs, rs.rects, rs.touched,
-                    rp.ok ? rs.row_tot : nullptr, rp.max_gy, rs.ctrl, st);
+                    p.cull_param, p.tile_w, p.tile_h, rs.recs, rs.rects, foot_of(p, rs),
+                    rs.touched, rp.ok ? rs.row_tot : nullptr, rp.max_gy, rs.ctrl, st);
   if (exact) {
     cap = worst;
   } else {
@@ -304,12 +312,13 @@ int run_binning(const Pipeline& p, int64_t worst, DevBuf& recbuf, DevBuf& keybuf
   if (exact && !rp.ok) launch_scan(rs.touched, rs.incl, p.n_rec, cap, rs.scan_tmp, rs.ctrl, st);
   if (!rp.ok || !p.heavy_first) rs.order = nullptr;  // the blend takes tiles in index order
   if (rp.ok) {
-    launch_tile_binning_emit(p.va, rp.n_views, rp.max_gy, rs.rects,
-                             rs.row_tot, cap, rs.ctrl, rs.ranges, ks.keys_a, rs.order, p.n_tiles,
-                             st);
+    launch_tile_binning_emit(p.va, rp.n_views, rp.max_gy, rs.rects, foot_of(p, rs), p.tile_w,
+                             p.tile_h, rs.row_tot, cap, rs.ctrl, rs.ranges, ks.keys_a, rs.order,
+                             p.n_tiles, st);
     sorted = ks.keys_a;
   } else {
-    launch_emit_keys(p.va, rs.incl, rs.rects, p.n_rec, rs.ctrl, ks.keys_a, cap, st);
+    launch_emit_keys(p.va, rs.incl, rs.rects, foot_of(p, rs), p.tile_w, p.tile_h, p.n_rec, rs.ctrl,
+                     ks.keys_a, cap, st);
     sorted = launch_sort(ks.keys_a, ks.keys_b, bits_for(p.n_tiles), rs.ctrl, cap, ks.hist, st);
     launch_ranges(sorted, rs.ctrl, cap, rs.ranges, st);
   }
@@ -354,6 +363,7 @@ Pipeline single_view_pipeline(const fe_render_desc* d, const float* means, const
   p.px = default_px((int)d->px_per_thread, tw, th, p.n_tiles);
   p.chunk = (int)(d->flags >> 8) & 0xff;
   p.radix = (d->flags & FE_FLAG_RADIX_BINNING) != 0;
+  p.rect_binning = (d->flags & FE_FLAG_RECT_BINNING) != 0;
   p.heavy_first = (d->flags & FE_FLAG_HEAVY_TILES_FIRST) != 0;
   p.cull_mode = d->cull_mode;
   p.cull_param = d->cull_param;
@@ -802,7 +812,7 @@ int fe_reference_binning(int32_t P, int32_t height, int32_t width, float n_std,
   ViewsArg va{};
   va.count = 1;
   va.one.H = height; va.one.W = width; va.one.gx = gx; va.one.gy = gy; va.one.n = P;
-  launch_emit_keys(va, tiles_touched, rs.rects, P, rs.ctrl, keys, K, st);
+  launch_emit_keys(va, tiles_touched, rs.rects, nullptr, 8, 8, P, rs.ctrl, keys, K, st);
   uint64_t* sorted = launch_sort(keys, ks.keys_b, bits_for(T), rs.ctrl, K, ks.hist, st);
   if (sorted != keys)
     FE_CUDA(cudaMemcpyAsync(keys, sorted, sizeof(uint64_t) * (size_t)K, cudaMemcpyDeviceToDevice, st));
@@ -883,7 +893,7 @@ int fe_rasterize_legacy(const fe_legacy_desc* d, const float* means, const float
   rc = a->keys.reserve(kb, st);
   if (rc) return rc;
   carve_keys(a->keys.ptr, cap, [&](const KeySpace& s_) { ks = s_; });
-  launch_emit_keys(va, rs.incl, rs.rects, P, rs.ctrl, ks.keys_a, cap, st);
+  launch_emit_keys(va, rs.incl, rs.rects, nullptr, 8, 8, P, rs.ctrl, ks.keys_a, cap, st);
   uint64_t* sorted = launch_sort(ks.keys_a, ks.keys_b, bits_for(T), rs.ctrl, cap, ks.hist, st);
   launch_ranges(sorted, rs.ctrl, cap, rs.ranges, st);
   launch_blend_fwd(va, 8, 8, 0, 0, T, nullptr, sorted, rs.recs, rs.ranges, 21.4f, 2.66f, out_z,
@@ -1172,6 +1182,7 @@ static Pipeline batch_pipeline(fe_batch* b, const float* means, const float* pre
   p.px = default_px((int)b->desc.px_per_thread, b->tile_w, b->tile_h, p.n_tiles);
   p.chunk = (int)(b->desc.flags >> 8) & 0xff;
   p.radix = (b->desc.flags & FE_FLAG_RADIX_BINNING) != 0;
+  p.rect_binning = (b->desc.flags & FE_FLAG_RECT_BINNING) != 0;
   p.heavy_first = (b->desc.flags & FE_FLAG_HEAVY_TILES_FIRST) != 0;
   p.cull_mode = b->desc.cull_mode;
   p.cull_param = b->desc.cull_param;
@@ -1195,8 +1206,8 @@ static int batch_binning(fe_batch* b, const Pipeline& p, cudaStream_t st, cudaEv
   if (!rp.ok) FE_CUDA(cudaMemsetAsync(rs.ranges, 0, sizeof(uint2) * (size_t)p.n_tiles, st));
   if (ev) FE_CUDA(cudaEventRecord(ev[0], st));
   launch_preprocess(p.va, p.n_rec, p.means, p.prec, p.logw, p.quat, nullptr, p.trans, p.cull_mode,
-                    p.cull_param, p.tile_w, p.tile_h, rs.recs, rs.rects, rs.touched,
-                    rp.ok ? rs.row_tot : nullptr, rp.max_gy, rs.ctrl, st);
+                    p.cull_param, p.tile_w, p.tile_h, rs.recs, rs.rects, foot_of(p, rs),
+                    rs.touched, rp.ok ? rs.row_tot : nullptr, rp.max_gy, rs.ctrl, st);
   if (ev) FE_CUDA(cudaEventRecord(ev[1], st));
   if (b->exact) {
     if (!rp.ok)
@@ -1218,14 +1229,15 @@ static int batch_binning(fe_batch* b, const Pipeline& p, cudaStream_t st, cudaEv
   if (ev) FE_CUDA(cudaEventRecord(ev[2], st));
   const KeySpace& ks = b->ks;
   if (rp.ok) {
-    launch_tile_binning_emit(p.va, rp.n_views, rp.max_gy, rs.rects,
-                             rs.row_tot, b->cap, rs.ctrl, rs.ranges, ks.keys_a,
+    launch_tile_binning_emit(p.va, rp.n_views, rp.max_gy, rs.rects, foot_of(p, rs), p.tile_w,
+                             p.tile_h, rs.row_tot, b->cap, rs.ctrl, rs.ranges, ks.keys_a,
                              p.heavy_first ? rs.order : nullptr, p.n_tiles, st);
     if (ev) FE_CUDA(cudaEventRecord(ev[3], st));
     b->sorted = ks.keys_a;
     if (ev) FE_CUDA(cudaEventRecord(ev[4], st));
   } else {
-    launch_emit_keys(p.va, rs.incl, rs.rects, p.n_rec, rs.ctrl, ks.keys_a, b->cap, st);
+    launch_emit_keys(p.va, rs.incl, rs.rects, foot_of(p, rs), p.tile_w, p.tile_h, p.n_rec, rs.ctrl,
+                     ks.keys_a, b->cap, st);
     if (ev) FE_CUDA(cudaEventRecord(ev[3], st));
     b->sorted = launch_sort(ks.keys_a, ks.keys_b, bits_for(p.n_tiles), rs.ctrl, b->cap, ks.hist, st);
     if (ev) FE_CUDA(cudaEventRecord(ev[4], st));
@@ -1579,17 +1591,18 @@ int fe_render_fwd_noalloc(const fe_render_desc* d, const float* means, const flo
   FE_CUDA(zero_ctrl_rows(rs, rp.ok ? rp.max_gy + 1 : 0, st));
   if (!rp.ok) FE_CUDA(cudaMemsetAsync(rs.ranges, 0, sizeof(uint2) * (size_t)p.n_tiles, st));
   launch_preprocess(p.va, p.n_rec, p.means, p.prec, p.logw, p.quat, nullptr, p.trans, p.cull_mode,
-                    p.cull_param, p.tile_w, p.tile_h, rs.recs, rs.rects, rs.touched,
-                    rp.ok ? rs.row_tot : nullptr, rp.max_gy, rs.ctrl, st);
+                    p.cull_param, p.tile_w, p.tile_h, rs.recs, rs.rects, foot_of(p, rs),
+                    rs.touched, rp.ok ? rs.row_tot : nullptr, rp.max_gy, rs.ctrl, st);
   uint64_t* sorted = ks.keys_a;
   if (!rp.ok || !p.heavy_first) rs.order = nullptr;
   if (rp.ok) {
-    launch_tile_binning_emit(p.va, rp.n_views, rp.max_gy, rs.rects,
-                             rs.row_tot, worst, rs.ctrl, rs.ranges, ks.keys_a, rs.order, p.n_tiles,
-                             st);
+    launch_tile_binning_emit(p.va, rp.n_views, rp.max_gy, rs.rects, foot_of(p, rs), p.tile_w,
+                             p.tile_h, rs.row_tot, worst, rs.ctrl, rs.ranges, ks.keys_a, rs.order,
+                             p.n_tiles, st);
   } else {
     launch_scan(rs.touched, rs.incl, p.n_rec, worst, rs.scan_tmp, rs.ctrl, st);
-    launch_emit_keys(p.va, rs.incl, rs.rects, p.n_rec, rs.ctrl, ks.keys_a, worst, st);
+    launch_emit_keys(p.va, rs.incl, rs.rects, foot_of(p, rs), p.tile_w, p.tile_h, p.n_rec, rs.ctrl,
+                     ks.keys_a, worst, st);
     sorted = launch_sort(ks.keys_a, ks.keys_b, bits_for(p.n_tiles), rs.ctrl, worst, ks.hist, st);
     launch_ranges(sorted, rs.ctrl, worst, rs.ranges, st);
   }

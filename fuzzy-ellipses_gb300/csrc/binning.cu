@@ -118,28 +118,61 @@ __global__ void scan_down_kernel(const uint32_t* __restrict__ in, uint32_t* __re
   }
 }
 
-// One warp per record: the lanes write the record's rectangle of keys, row by row, at its scan
-// offset (coalesced), skipping anything beyond the device-side key count.
+// One warp per record: the lanes write the record's keys, row by row, at its scan offset
+// (coalesced), skipping anything beyond the device-side key count. Without `foot` every row spans
+// the record's rectangle; with it each row spans the tiles its footprint reaches there
+// (foot_row_tiles), and the lanes first take 32 rows at a time to form the rows' spans and their
+// offsets.
 __global__ void emit_keys_kernel(ViewsArg va, const uint32_t* __restrict__ incl,
-                                 const TileRect* __restrict__ rects, int64_t n,
-                                 const Control* __restrict__ ctrl, uint64_t* __restrict__ keys) {
+                                 const TileRect* __restrict__ rects,
+                                 const FootRows* __restrict__ foot, int tile_w, int tile_h,
+                                 int64_t n, const Control* __restrict__ ctrl,
+                                 uint64_t* __restrict__ keys) {
   const int64_t K = (int64_t)ctrl->num_keys;
   const int lane = threadIdx.x & 31;
+  const unsigned full = 0xffffffffu;
   const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
   for (int64_t i = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; i < n; i += warps) {
     const int64_t end = (int64_t)incl[i];
     const int64_t off = i ? (int64_t)incl[i - 1] : 0;
     if (end == off || off >= K) continue;
     const TileRect r = rects[i];
-    const int w = r.x1 - r.x0;
     const int vi = find_view<&ViewDev::rec_base>(va, i);
     const ViewDev& V = view_at(va, vi);
     const uint64_t gid = (uint64_t)(i - V.rec_base);
-    const int64_t cnt = min(end, K) - off;
-    for (int64_t j = lane; j < cnt; j += 32) {
-      const int x = r.x0 + (int)(j % w), y = r.y0 + (int)(j / w);
-      const uint64_t tile = (uint64_t)(V.tile_base + (int64_t)y * V.gx + x);
-      keys[off + j] = (tile << 32) | gid;
+    if (!foot) {
+      const int w = r.x1 - r.x0;
+      const int64_t cnt = min(end, K) - off;
+      for (int64_t j = lane; j < cnt; j += 32) {
+        const int x = r.x0 + (int)(j % w), y = r.y0 + (int)(j / w);
+        const uint64_t tile = (uint64_t)(V.tile_base + (int64_t)y * V.gx + x);
+        keys[off + j] = (tile << 32) | gid;
+      }
+      continue;
+    }
+    const FootRows f = foot[i];
+    int64_t o = off;
+    for (int y0 = r.y0; y0 < r.y1 && o < K; y0 += 32) {
+      const int y = y0 + lane;
+      int x0 = 0, x1 = 0;
+      if (y < r.y1) foot_row_tiles(f, r, y, tile_w, tile_h, x0, x1);
+      const int w = x1 - x0;
+      int incl_w = w;
+#pragma unroll
+      for (int s = 1; s < 32; s <<= 1) {
+        const int t = __shfl_up_sync(full, incl_w, s);
+        if (lane >= s) incl_w += t;
+      }
+      const int rows = min(32, r.y1 - y0);
+      for (int l = 0; l < rows; ++l) {
+        const int wl = __shfl_sync(full, w, l);
+        const int xl = __shfl_sync(full, x0, l);
+        const int64_t ol = o + __shfl_sync(full, incl_w - w, l);
+        const uint64_t row_tile = (uint64_t)(V.tile_base + (int64_t)(y0 + l) * V.gx + xl);
+        for (int j = lane; j < wl; j += 32)
+          if (ol + j < K) keys[ol + j] = ((row_tile + (uint64_t)j) << 32) | gid;
+      }
+      o += __shfl_sync(full, incl_w, 31);
     }
   }
 }
@@ -353,13 +386,13 @@ __global__ void __launch_bounds__(kRangeThreads) ranges_kernel(const uint64_t* _
 
 // ---- Tile-major binning ---------------------------------------------------------------------
 // The keys of a tile are its Gaussians in ascending id: the order the stable sort of the
-// Gaussian-major key list produces. The preprocess has recorded every footprint rectangle's width
-// as a difference of the row key counts of its view (+w at its first row, -w past its last:
-// row_tot) and the total in ctrl->want_keys. One block per (view, tile row) then takes the row's
-// base (the keys of the rows before it, from those differences), per-tile
-// counts from a difference array over the covering rectangles, writes the tile ranges, and places
-// the keys: the covering rectangles in id order (order-preserving compaction into shared memory)
-// are walked 32 at a time by a warp per tile, a ballot giving each covering rectangle its slot.
+// Gaussian-major key list produces. The preprocess has added every record's keys in each tile row
+// to that row's key count (row_tot, per view) and the total to ctrl->want_keys. One block per
+// (view, tile row) then takes the row's base (the keys of the rows before it), per-tile counts
+// from a difference array over the covering spans (each record's tiles in the row: its
+// rectangle's, or with `foot` the ones its footprint reaches there), writes the tile ranges, and
+// places the keys: the covering spans in id order (order-preserving compaction into shared
+// memory) are walked 32 at a time by a warp per tile, a ballot giving each span its slot.
 constexpr int kRowThreads = kScanThreads;  // block_exclusive_scan works on kScanThreads threads
 constexpr int kRowWarps = kRowThreads / 32;
 constexpr int kRowPer = 4;                          // rectangles per thread per filter segment
@@ -391,19 +424,32 @@ __device__ __forceinline__ unsigned long long block_sum_u64(unsigned long long v
   return t;
 }
 
-// Order-preserving compaction of the segment's rectangles that cover `row` into `list`
-// (thread t takes rectangles s0 + kRowPer t .. + kRowPer - 1); returns their number. Ends with a
-// barrier after the list is written.
-__device__ __forceinline__ uint32_t filter_row(const TileRect* __restrict__ vr, int n, int s0,
-                                               int row, RowRect* list, uint32_t* ws) {
+// Order-preserving compaction of the segment's records that reach `row` into `list` with their
+// span of tiles in the row (thread t takes records s0 + kRowPer t .. + kRowPer - 1); returns their
+// number. Without `foot` a record's span is its rectangle's; with it, the tiles its footprint
+// reaches in the row (records whose footprint misses the row are left out). Ends with a barrier
+// after the list is written.
+__device__ __forceinline__ uint32_t filter_row(const TileRect* __restrict__ vr,
+                                               const FootRows* __restrict__ vf, int tile_w,
+                                               int tile_h, int n, int s0, int row, RowRect* list,
+                                               uint32_t* ws) {
   const int tid = threadIdx.x;
-  TileRect r[kRowPer];
+  uint16_t x0[kRowPer], x1[kRowPer];
   uint32_t hits = 0, c = 0;
 #pragma unroll
   for (int q = 0; q < kRowPer; ++q) {
     const int i = s0 + kRowPer * tid + q;
-    r[q] = i < n ? vr[i] : TileRect{0, 0, 0, 0};
-    const bool h = covers_row(r[q], row);
+    const TileRect r = i < n ? vr[i] : TileRect{0, 0, 0, 0};
+    bool h = covers_row(r, row);
+    x0[q] = r.x0;
+    x1[q] = r.x1;
+    if (h && vf) {
+      int a, b;
+      foot_row_tiles(vf[i], r, row, tile_w, tile_h, a, b);
+      x0[q] = (uint16_t)a;
+      x1[q] = (uint16_t)b;
+      h = b > a;
+    }
     hits |= (uint32_t)h << q;
     c += h;
   }
@@ -411,18 +457,16 @@ __device__ __forceinline__ uint32_t filter_row(const TileRect* __restrict__ vr, 
   const uint32_t total = block_exclusive_scan<uint32_t>(c, at, ws);  // ends with a barrier
 #pragma unroll
   for (int q = 0; q < kRowPer; ++q)
-    if ((hits >> q) & 1u)
-      list[at++] = RowRect{r[q].x0, r[q].x1, (uint32_t)(s0 + kRowPer * tid + q)};
+    if ((hits >> q) & 1u) list[at++] = RowRect{x0[q], x1[q], (uint32_t)(s0 + kRowPer * tid + q)};
   __syncthreads();
   return total;
 }
 
 // Row bases of many views, in two launches instead of a sum over all earlier views in every
 // emission block (quadratic in the number of views). row_tot holds per view (stride max_gy + 1)
-// the differences of the row key counts; entry gy <= max_gy of a view is the unused "past the last
-// row" difference, and entry max_gy is free for the view's total.
-// Pass 1, one warp per view: the rows' key counts (prefix of the differences) and their exclusive
-// prefix within the view, in place; the view's key total into entry max_gy.
+// the key counts of its rows; entry max_gy is free for the view's total.
+// Pass 1, one warp per view: the exclusive prefix of the row counts within the view, in place;
+// the view's key total into entry max_gy.
 __global__ void __launch_bounds__(kRowThreads) row_offsets_kernel(ViewsArg va, int n_views,
                                                                    int max_gy,
                                                                    unsigned long long* row_tot) {
@@ -432,18 +476,10 @@ __global__ void __launch_bounds__(kRowThreads) row_offsets_kernel(ViewsArg va, i
   const unsigned full = 0xffffffffu;
   const int gy = view_at(va, v).gy;
   unsigned long long* d = row_tot + (int64_t)v * (max_gy + 1);
-  long long cnt_carry = 0;            // count of the row before this chunk
   unsigned long long off_carry = 0;   // keys of the rows before this chunk
   for (int r0 = 0; r0 < gy; r0 += 32) {
     const int r = r0 + lane;
-    long long c = r < gy ? (long long)d[r] : 0;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const long long y = __shfl_up_sync(full, c, o);
-      if (lane >= o) c += y;
-    }
-    c += cnt_carry;  // this row's key count
-    unsigned long long k = r < gy ? (unsigned long long)c : 0ull;
+    const unsigned long long k = r < gy ? d[r] : 0ull;
     unsigned long long incl = k;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
@@ -451,7 +487,6 @@ __global__ void __launch_bounds__(kRowThreads) row_offsets_kernel(ViewsArg va, i
       if (lane >= o) incl += y;
     }
     if (r < gy) d[r] = off_carry + incl - k;
-    cnt_carry = __shfl_sync(full, c, 31);
     off_carry += __shfl_sync(full, incl, 31);
   }
   if (lane == 0) d[max_gy] = off_carry;
@@ -478,8 +513,9 @@ __global__ void __launch_bounds__(kRowThreads) view_bases_kernel(int n_views, in
 }
 
 __global__ void __launch_bounds__(kRowThreads) tile_emit_kernel(
-    ViewsArg va, const TileRect* __restrict__ rects,
-    const unsigned long long* __restrict__ row_tot, bool bases, int64_t capacity,
+    ViewsArg va, const TileRect* __restrict__ rects, const FootRows* __restrict__ foot,
+    int tile_w, int tile_h, const unsigned long long* __restrict__ row_tot, bool bases,
+    int64_t capacity,
     Control* __restrict__ ctrl, uint2* __restrict__ ranges, uint64_t* __restrict__ keys,
     uint32_t* __restrict__ order, int64_t n_tiles, int nseg) {
   __shared__ RowRect list[kRowSeg];
@@ -512,12 +548,11 @@ __global__ void __launch_bounds__(kRowThreads) tile_emit_kernel(
   if (x_lo >= x_hi) return;  // (uniform over the block)
   const int64_t tile0 = V.tile_base + (int64_t)row * gx;
   const TileRect* vr = rects + V.rec_base;
+  const FootRows* vf = foot ? foot + V.rec_base : nullptr;
 
-  // row_tot holds, per view, the difference of the row key counts (stride max_gy + 1): the count
-  // of row r is the sum of entries 0..r, so the keys before row `row` of this view are
-  // sum_{r' < row} d[r'] (row - r'), and a whole earlier view holds sum_{r' < gy} d[r'] (gy - r').
-  // With `bases` set, row_offsets_kernel and view_bases_kernel have already turned the
-  // differences into row offsets within the view and view bases.
+  // row_tot holds, per view, the key counts of its rows (stride max_gy + 1). With `bases` set,
+  // row_offsets_kernel and view_bases_kernel have already turned them into row offsets within
+  // the view and view bases.
   const int stride = (int)gridDim.x / nseg + 1;
   unsigned long long row_base;
   if (bases) {  // view base (entry max_gy) + the row's offset within the view
@@ -527,11 +562,10 @@ __global__ void __launch_bounds__(kRowThreads) tile_emit_kernel(
     long long b = 0;
     for (int idx = tid; idx < (int)blockIdx.y * stride; idx += kRowThreads) {
       const int v2 = idx / stride, r2 = idx - v2 * stride;
-      const int gy2 = view_at(va, v2).gy;
-      if (r2 < gy2) b += (long long)row_tot[idx] * (gy2 - r2);
+      if (r2 < view_at(va, v2).gy) b += (long long)row_tot[idx];
     }
     for (int r2 = tid; r2 < row; r2 += kRowThreads)
-      b += (long long)row_tot[(int64_t)blockIdx.y * stride + r2] * (row - r2);
+      b += (long long)row_tot[(int64_t)blockIdx.y * stride + r2];
     row_base = block_sum_u64((unsigned long long)b, wsu);
   }
   // Keys of this row: slot p (relative to the row's base) for p < lim.
@@ -542,7 +576,7 @@ __global__ void __launch_bounds__(kRowThreads) tile_emit_kernel(
   __syncthreads();
   uint32_t total = 0;
   for (int s0 = 0; s0 < n; s0 += kRowSeg) {
-    total = filter_row(vr, n, s0, row, list, ws);
+    total = filter_row(vr, vf, tile_w, tile_h, n, s0, row, list, ws);
     for (uint32_t j = tid; j < total; j += kRowThreads) {
       atomicAdd(&diff[list[j].x0], 1);
       atomicAdd(&diff[list[j].x1], -1);
@@ -626,7 +660,8 @@ __global__ void __launch_bounds__(kRowThreads) tile_emit_kernel(
   }
   __syncthreads();
   for (int s0 = 0; s0 < n; s0 += kRowSeg) {
-    if (n > kRowSeg) total = filter_row(vr, n, s0, row, list, ws);  // else still in shared memory
+    // (with a single segment the list is still in shared memory)
+    if (n > kRowSeg) total = filter_row(vr, vf, tile_w, tile_h, n, s0, row, list, ws);
     // Each warp takes kTileBlock of its tiles at a time (tiles warp + kRowWarps t of the slice),
     // keeping their next slots in registers, and reads each 32-entry chunk of the list once for
     // all of them.
@@ -687,10 +722,12 @@ void launch_scan(const uint32_t* touched, uint32_t* incl, int64_t n, int64_t cap
   scan_down_kernel<<<nb, kScanThreads, 0, st>>>(touched, incl, n, scratch);
 }
 
-void launch_emit_keys(const ViewsArg& va, const uint32_t* incl, const TileRect* rects, int64_t n,
+void launch_emit_keys(const ViewsArg& va, const uint32_t* incl, const TileRect* rects,
+                      const FootRows* foot, int tile_w, int tile_h, int64_t n,
                       const Control* ctrl, uint64_t* keys, int64_t capacity, cudaStream_t st) {
   (void)capacity;
-  emit_keys_kernel<<<grid_for(n * 32, 256, 152 * 16), 256, 0, st>>>(va, incl, rects, n, ctrl, keys);
+  emit_keys_kernel<<<grid_for(n * 32, 256, 152 * 16), 256, 0, st>>>(va, incl, rects, foot, tile_w,
+                                                                    tile_h, n, ctrl, keys);
 }
 
 uint64_t* launch_sort(uint64_t* a, uint64_t* b, int key_bits, const Control* ctrl,
@@ -712,6 +749,7 @@ uint64_t* launch_sort(uint64_t* a, uint64_t* b, int key_bits, const Control* ctr
 
 
 void launch_tile_binning_emit(const ViewsArg& va, int n_views, int max_gy, const TileRect* rects,
+                              const FootRows* foot, int tile_w, int tile_h,
                               unsigned long long* row_tot, int64_t capacity, Control* ctrl,
                               uint2* ranges, uint64_t* keys, uint32_t* order, int64_t n_tiles,
                               cudaStream_t st) {
@@ -729,7 +767,8 @@ void launch_tile_binning_emit(const ViewsArg& va, int n_views, int max_gy, const
   const int64_t rows = (int64_t)max_gy * n_views;
   const int nseg = rows >= 2 * 152 ? 1 : (int)std::min<int64_t>(8, (2 * 152 + rows - 1) / rows);
   tile_emit_kernel<<<dim3((unsigned)(max_gy * nseg), (unsigned)n_views), kRowThreads, 0, st>>>(
-      va, rects, row_tot, bases, capacity, ctrl, ranges, keys, order, n_tiles, nseg);
+      va, rects, foot, tile_w, tile_h, row_tot, bases, capacity, ctrl, ranges, keys, order, n_tiles,
+      nseg);
 }
 
 void launch_ranges(const uint64_t* keys, const Control* ctrl, int64_t capacity, uint2* ranges,

@@ -105,6 +105,50 @@ struct __align__(8) TileRect {
   uint16_t x0, y0, x1, y1;
 };
 
+// Row form of a bounded record's footprint: the ellipse of pixels (u, v) whose rays pass within
+// Mahalanobis distance k of the mean. At pixel row v it spans
+//     u in [uc + c1 (v - vc) - sqrt(H), uc + c1 (v - vc) + sqrt(H)],  H = hc + h2 (v - vc)^2
+// ((uc, vc): the ellipse's centre, hc its squared half-width there, h2 < 0); vl and vr are the
+// rows of its leftmost and rightmost points. hc = NaN marks a footprint without this form
+// (unbounded or degenerate): every row of its rectangle spans the rectangle's full width.
+struct __align__(16) FootRows {
+  float uc, vc, c1, hc, h2, vl, vr, pad;
+};
+static_assert(sizeof(FootRows) == 32, "FootRows layout");
+
+// Tiles [x0, x1) of tile row `row` (tiles tw x th pixels) that the footprint reaches, within its
+// rectangle r; x0 == x1 when it reaches none. The row's pixel rows are [row th, row th + th - 1].
+// Over that band the footprint's leftmost pixel lies in the band row nearest vl (at vl itself
+// when vl is inside the band: the rectangle's left edge), and likewise on the right, since the
+// ellipse's left boundary is convex in v and its right boundary concave. The 0.1 px margin covers
+// the float32 rounding of the bound; a pixel it could still leave out lies on the cut-off
+// boundary, where the Gaussian's density is the cut-off density.
+__device__ __forceinline__ void foot_row_tiles(const FootRows& f, const TileRect& r, int row,
+                                               int tw, int th, int& x0, int& x1) {
+  x0 = r.x0;
+  x1 = r.x1;
+  if (!(f.hc == f.hc)) return;
+  const float va = (float)(row * th), vb = va + (float)(th - 1);
+  const float itw = 1.f / (float)tw;  // exact: tile widths are powers of two
+  constexpr float kMargin = 0.1f;
+  auto half = [&](float v) {
+    const float dv = v - f.vc;
+    float h;
+    asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(h) : "f"(fmaxf(fmaf(f.h2 * dv, dv, f.hc), 0.f)));
+    return h;
+  };
+  if (!(f.vl >= va && f.vl <= vb)) {
+    const float v = f.vl < va ? va : vb;
+    const float t = floorf((fmaf(f.c1, v - f.vc, f.uc) - half(v) - kMargin) * itw);
+    if (t > (float)x0) x0 = t < (float)x1 ? (int)t : x1;
+  }
+  if (!(f.vr >= va && f.vr <= vb)) {
+    const float v = f.vr < va ? va : vb;
+    const float t = floorf((fmaf(f.c1, v - f.vc, f.uc) + half(v) + kMargin) * itw) + 1.f;
+    if (t < (float)x1) x1 = t > (float)x0 ? (int)t : x0;
+  }
+}
+
 // Tile work classes of the tile-major binning, heaviest first: class c < kTileClasses - 2 holds
 // tiles with 2^(kTileClasses - 2 - c) <= keys < 2^(kTileClasses - 1 - c) (class 0 open-ended),
 // class kTileClasses - 2 one key, class kTileClasses - 1 none.

@@ -9,8 +9,9 @@ namespace fe {
 void launch_preprocess(const ViewsArg& va, int64_t n_rec, const float* means, const float* prec,
                        const float* logw, const float* quat, const float* rotm,
                        const float* trans, int cull_mode, float cull_param, int tile_w,
-                       int tile_h, GaussRec* recs, TileRect* rects, uint32_t* touched,
-                       unsigned long long* row_tot, int max_gy, Control* ctrl, cudaStream_t st);
+                       int tile_h, GaussRec* recs, TileRect* rects, FootRows* foot,
+                       uint32_t* touched, unsigned long long* row_tot, int max_gy, Control* ctrl,
+                       cudaStream_t st);
 void launch_preprocess_reference(int P, float n_std, const float* means, const float* scales,
                                  const float* rots, const float* viewmatrix,
                                  const float* projmatrix, int W, int H, float tan_fovx,
@@ -30,27 +31,31 @@ int sort_grid(int64_t key_capacity);
 // scratch: scan_grid(n) * 8 bytes.
 void launch_scan(const uint32_t* touched, uint32_t* incl, int64_t n, int64_t capacity,
                  unsigned long long* scratch, Control* ctrl, cudaStream_t st);
-void launch_emit_keys(const ViewsArg& va, const uint32_t* incl, const TileRect* rects, int64_t n,
+// foot: the records' footprint rows (each row's keys span the tiles the footprint reaches there),
+// or NULL (every row of a record's rectangle spans its full width).
+void launch_emit_keys(const ViewsArg& va, const uint32_t* incl, const TileRect* rects,
+                      const FootRows* foot, int tile_w, int tile_h, int64_t n,
                       const Control* ctrl, uint64_t* keys, int64_t capacity, cudaStream_t st);
 // Stable LSD radix sort of keys on bits [32, 32+key_bits); returns the buffer holding the
 // result (a or b). hist: 256 * (sort_grid(capacity) + 1) uint32.
 uint64_t* launch_sort(uint64_t* a, uint64_t* b, int key_bits, const Control* ctrl,
                       int64_t capacity, uint32_t* hist, cudaStream_t st);
 // Tile-major binning for views at most kMaxRowTiles tiles wide. launch_preprocess with row_tot
-// (n_views * (max_gy + 1) zeroed entries, view v's at v * (max_gy + 1)) records every rectangle's
-// width as a difference of its view's row key counts (+w at row y0, -w at row y1) and adds the
-// run's key count to ctrl->want_keys; the emit
-// pass (one block per tile row of every view) sets ctrl->num_keys = min(want_keys, capacity)
+// (n_views * (max_gy + 1) zeroed entries, view v's at v * (max_gy + 1)) adds each record's keys in
+// every tile row to that row's count and the run's key count to ctrl->want_keys; the emit pass
+// (one block per tile row of every view) sets ctrl->num_keys = min(want_keys, capacity)
 // (FE_DEVERR_CAPACITY past it) and writes the keys of every tile in ascending Gaussian id at their
 // place in the sorted order (keys past num_keys dropped) and every tile's range ({0,0} for an
 // empty tile, so the ranges need no zeroing). Same keys and ranges as emit + stable sort +
-// ranges. For many views the row totals are first turned into row offsets and view bases in
-// place (row_tot is consumed). With `order` (kTileClasses lists of n_tiles entries, ctrl's class
-// counts zeroed) every tile's id is also appended to the list of its work class (tile_class of
-// its key count), which launch_blend_fwd then serves heaviest class first.
+// ranges, with the same `foot` (see launch_emit_keys). For many views the row counts are first
+// turned into row offsets and view bases in place (row_tot is consumed). With `order`
+// (kTileClasses lists of n_tiles entries, ctrl's class counts zeroed) every tile's id is also
+// appended to the list of its work class (tile_class of its key count), which launch_blend_fwd
+// then serves heaviest class first.
 constexpr int kMaxRowTiles = 1024;
 constexpr int kRowBaseViews = 32;  // above this many views the row bases are formed first
 void launch_tile_binning_emit(const ViewsArg& va, int n_views, int max_gy, const TileRect* rects,
+                              const FootRows* foot, int tile_w, int tile_h,
                               unsigned long long* row_tot, int64_t capacity, Control* ctrl,
                               uint2* ranges, uint64_t* keys, uint32_t* order, int64_t n_tiles,
                               cudaStream_t st);

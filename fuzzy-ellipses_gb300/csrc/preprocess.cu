@@ -108,14 +108,59 @@ __device__ __forceinline__ int clamp_tile(double x, int lo, int hi) {
 // Exact-projection binning (float32, cancellation-free forms)
 // ------------------------------------------------------------------------------------------
 
-// Record and tile footprint of one (Gaussian, view) pair in float32 (fe_footprint.cuh).
+// Row form of the footprint ellipse of a bounded record (FootRows), from the record's terms. With
+// (du, dv) the pixel offset from the record's expansion centre, the ellipse is
+// Q(du, dv) = |y|^2 - k2 |a|^2 <= 0 (the peak's Mahalanobis distance d0 = |y|^2 / |a|^2 at most k),
+// a quadratic form Quu du^2 + 2 Quv du dv + Qvv dv^2 + 2 Qu du + 2 Qv dv + Q0. Its centre c solves
+// the 2x2 system; along a row the squared half-width is -Q(u_row(dv), dv) / Quu, which is
+// -Q(c)/Quu - det/Quu^2 (dv - dv_c)^2; the leftmost and rightmost points lie on the line through c
+// where dQ/dv = 0, at c -+ lam (Qvv, -Quv) with lam^2 = -Q(c) / (Qvv det). float32 suffices: the
+// |y|^2 terms dominate the quadratic coefficients for a footprint of bounded size, the expansion
+// centre is the projected mean (near c), and a rounding of the bound moves it by far less than
+// the 0.1 px margin of foot_row_tiles (FP64 would cost the preprocess more than it saves).
+__device__ __forceinline__ void foot_rows(const GaussRec& g, float k2, FootRows& f) {
+  f.uc = f.vc = f.c1 = f.h2 = f.vl = f.vr = f.pad = 0.f;
+  f.hc = __int_as_float(0x7fc00000);  // NaN: the whole rectangle
+  auto d = [](const float* a, const float* b) {
+    return fmaf(a[2], b[2], fmaf(a[1], b[1], a[0] * b[0]));
+  };
+  const float Quu = d(g.y1, g.y1) - k2 * d(g.a1, g.a1);
+  const float Quv = d(g.y1, g.y2) - k2 * d(g.a1, g.a2);
+  const float Qvv = d(g.y2, g.y2) - k2 * d(g.a2, g.a2);
+  const float Qu = d(g.y0, g.y1) - k2 * d(g.a0, g.a1);
+  const float Qv = d(g.y0, g.y2) - k2 * d(g.a0, g.a2);
+  const float Q0 = d(g.y0, g.y0) - k2 * d(g.a0, g.a0);
+  const float det = fmaf(Quu, Qvv, -Quv * Quv);
+  if (!(Quu > 0.f && Qvv > 0.f && det > 0.f)) return;
+  const float idet = 1.f / det;
+  const float du_c = fmaf(Qv, Quv, -Qu * Qvv) * idet, dv_c = fmaf(Qu, Quv, -Qv * Quu) * idet;
+  const float qc = fmaf(Qv, dv_c, fmaf(Qu, du_c, Q0));
+  if (!(qc < 0.f)) return;
+  const float iq = 1.f / Quu;
+  const float lam = sqrtf(-qc * idet / Qvv);
+  const float vc = g.vc + dv_c;
+  f.uc = g.uc + du_c;
+  f.vc = vc;
+  f.c1 = -Quv * iq;
+  f.hc = -qc * iq;
+  f.h2 = -det * iq * iq;
+  f.vl = fmaf(lam, Quv, vc);
+  f.vr = fmaf(-lam, Quv, vc);
+  if (!(isfinite(f.uc) && isfinite(f.vc) && isfinite(f.c1) && isfinite(f.hc) && isfinite(f.h2) &&
+        isfinite(f.vl) && isfinite(f.vr)))
+    f.hc = __int_as_float(0x7fc00000);
+}
+
+// Record and tile footprint of one (Gaussian, view) pair in float32 (fe_footprint.cuh); with
+// `foot`, also the footprint's row form (FootRows) when it is bounded.
 __device__ __forceinline__ void footprint_and_record(
     const float* mean, const float* prec, float logw, const float* R, const float* t,
     const ViewDev& V, int cull_mode, float cull_param, int tile_w, int tile_h, GaussRec& rec,
-    int& tx0, int& ty0, int& tx1, int& ty1) {
+    int& tx0, int& ty0, int& tx1, int& ty1, FootRows* foot) {
   const CamTerms ct = camera_terms(mean, prec, R, t);
   const float k2 = cutoff_k2(logw, cull_mode, cull_param);
   tx0 = ty0 = tx1 = ty1 = 0;
+  bool bounded = false;
   if (k2 > 0.f) {
     float ulo = 0.f, uhi = 0.f, vlo = 0.f, vhi = 0.f;
     if (screen_bounds(ct, k2, V.fx, V.fy, V.cx, V.cy, ulo, uhi, vlo, vhi) == kFootBounded) {
@@ -125,6 +170,7 @@ __device__ __forceinline__ void footprint_and_record(
       tx1 = clamp_tile(floorf((uhi + margin) / tile_w) + 1.f, 0, V.gx);
       ty0 = clamp_tile(floorf((vlo - margin) / tile_h), 0, V.gy);
       ty1 = clamp_tile(floorf((vhi + margin) / tile_h) + 1.f, 0, V.gy);
+      bounded = true;
     } else {
       tx0 = 0; ty0 = 0; tx1 = V.gx; ty1 = V.gy;
     }
@@ -133,14 +179,25 @@ __device__ __forceinline__ void footprint_and_record(
   // Record around the projected mean (image centre when the projection is unbounded).
   make_record(ct, logw, V.fx, V.fy, V.cx, V.cy, 0.5f * V.W, 0.5f * V.H, -1.f * V.W, 2.f * V.W,
               -1.f * V.H, 2.f * V.H, rec);
+  if (foot) {
+    FootRows f;
+    if (bounded && tx1 > tx0) {
+      foot_rows(rec, k2, f);
+    } else {
+      f.uc = f.vc = f.c1 = f.h2 = f.vl = f.vr = f.pad = 0.f;
+      f.hc = __int_as_float(0x7fc00000);
+    }
+    *foot = f;
+  }
 }
 
 __global__ void __launch_bounds__(64) preprocess_kernel(
     ViewsArg va, int64_t n_rec, const float* __restrict__ means, const float* __restrict__ prec,
     const float* __restrict__ logw, const float* __restrict__ quat, const float* __restrict__ rotm,
     const float* __restrict__ trans, int cull_mode, float cull_param, int tile_w, int tile_h,
-    GaussRec* __restrict__ recs, TileRect* __restrict__ rects, uint32_t* __restrict__ touched,
-    unsigned long long* __restrict__ row_tot, int max_gy, Control* __restrict__ ctrl) {
+    GaussRec* __restrict__ recs, TileRect* __restrict__ rects, FootRows* __restrict__ foot,
+    uint32_t* __restrict__ touched, unsigned long long* __restrict__ row_tot, int max_gy,
+    Control* __restrict__ ctrl) {
   unsigned long long keys = 0;  // this thread's keys (row_tot != NULL)
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n_rec;
        i += (int64_t)gridDim.x * blockDim.x) {
@@ -162,21 +219,37 @@ __global__ void __launch_bounds__(64) preprocess_kernel(
 #pragma unroll
     for (int k = 0; k < 9; ++k) pr[k] = prec[9 * gi + k];
     GaussRec rec;
+    FootRows f;
     int tx0, ty0, tx1, ty1;
     footprint_and_record(m, pr, logw[gi], R, t, V, cull_mode, cull_param, tile_w, tile_h, rec, tx0,
-                         ty0, tx1, ty1);
+                         ty0, tx1, ty1, foot ? &f : nullptr);
     recs[i] = rec;
-    rects[i] = TileRect{(uint16_t)tx0, (uint16_t)ty0, (uint16_t)tx1, (uint16_t)ty1};
-    touched[i] = (uint32_t)((tx1 - tx0) * (ty1 - ty0));
-    if (row_tot != nullptr && tx1 > tx0) {
-      // Tile-major binning: the rectangle adds its width to the key count of rows [ty0, ty1),
-      // recorded as a difference (+w at ty0, -w at ty1; the emit pass takes the prefix sums).
-      unsigned long long* rd = row_tot + (int64_t)vi * (max_gy + 1);
-      const unsigned long long w = (unsigned long long)(tx1 - tx0);
-      atomicAdd(&rd[ty0], w);
-      atomicAdd(&rd[ty1], 0ull - w);
-      keys += w * (unsigned long long)(ty1 - ty0);
+    const TileRect tr{(uint16_t)tx0, (uint16_t)ty0, (uint16_t)tx1, (uint16_t)ty1};
+    rects[i] = tr;
+    uint32_t n_keys;
+    if (foot) {
+      foot[i] = f;
+      // Keys of every tile row the footprint reaches (its rows' spans differ).
+      unsigned long long* rc = row_tot ? row_tot + (int64_t)vi * (max_gy + 1) : nullptr;
+      n_keys = 0;
+      for (int y = ty0; y < ty1; ++y) {
+        int x0, x1;
+        foot_row_tiles(f, tr, y, tile_w, tile_h, x0, x1);
+        const uint32_t w = (uint32_t)(x1 - x0);
+        if (rc && w) atomicAdd(&rc[y], (unsigned long long)w);
+        n_keys += w;
+      }
+    } else {
+      // Every row of the rectangle spans its full width.
+      const uint32_t w = (uint32_t)(tx1 - tx0);
+      n_keys = w * (uint32_t)(ty1 - ty0);
+      if (row_tot && w) {
+        unsigned long long* rc = row_tot + (int64_t)vi * (max_gy + 1);
+        for (int y = ty0; y < ty1; ++y) atomicAdd(&rc[y], (unsigned long long)w);
+      }
     }
+    touched[i] = n_keys;
+    keys += n_keys;
   }
   if (row_tot != nullptr) {
 #pragma unroll
@@ -391,15 +464,16 @@ __global__ void legacy_records_kernel(ViewsArg va, int P, const float* __restric
 void launch_preprocess(const ViewsArg& va, int64_t n_rec, const float* means, const float* prec,
                        const float* logw, const float* quat, const float* rotm,
                        const float* trans, int cull_mode, float cull_param, int tile_w,
-                       int tile_h, GaussRec* recs, TileRect* rects, uint32_t* touched,
-                       unsigned long long* row_tot, int max_gy, Control* ctrl, cudaStream_t st) {
+                       int tile_h, GaussRec* recs, TileRect* rects, FootRows* foot,
+                       uint32_t* touched, unsigned long long* row_tot, int max_gy, Control* ctrl,
+                       cudaStream_t st) {
   if (n_rec <= 0) return;
   const int threads = 64;
   const int64_t want = (n_rec + threads - 1) / threads;
   const int blocks = (int)(want < 65535 ? want : 65535);
   preprocess_kernel<<<blocks, threads, 0, st>>>(va, n_rec, means, prec, logw, quat, rotm, trans,
                                                 cull_mode, cull_param, tile_w, tile_h, recs,
-                                                rects, touched, row_tot, max_gy, ctrl);
+                                                rects, foot, touched, row_tot, max_gy, ctrl);
 }
 
 void launch_preprocess_reference(int P, float n_std, const float* means, const float* scales,

@@ -28,6 +28,7 @@ FE_FLAG_EXACT_KEYS = 2
 FE_FLAG_KEEP_BINNING = 4
 FE_FLAG_RADIX_BINNING = 8
 FE_FLAG_HEAVY_TILES_FIRST = 0x10000
+FE_FLAG_RECT_BINNING = 0x20000
 FE_VIEW_NO_GRAD = 1
 FE_ERR_OUT_OF_MEMORY = 4
 

@@ -152,24 +152,30 @@ def render_features(means, prec, logw, features, fx, fy, cx, cy, quat, t, height
     return depth, alpha, out
 
 
-def _binning_flag(binning):
+def _binning_flag(binning, footprint="ellipse"):
     if binning not in ("tiles", "radix"):
         raise ValueError("binning must be 'tiles' or 'radix'")
-    return N.FE_FLAG_RADIX_BINNING if binning == "radix" else 0
+    if footprint not in ("ellipse", "rect"):
+        raise ValueError("footprint must be 'ellipse' or 'rect'")
+    return ((N.FE_FLAG_RADIX_BINNING if binning == "radix" else 0)
+            | (N.FE_FLAG_RECT_BINNING if footprint == "rect" else 0))
 
 
 def render_binning(means, prec, logw, fx, fy, cx, cy, quat, t, height, width, *, cull="eps",
-                   cull_param=None, tile=(16, 16), key_capacity=None, binning="tiles"):
+                   cull_param=None, tile=(16, 16), key_capacity=None, binning="tiles",
+                   footprint="ellipse"):
     """The tile binning ``render`` uses: returns (keys (K,) int64 holding (tile << 32 | gaussian),
     ranges (T, 2) int64). Synchronises once. ``binning="radix"`` forces key emission + radix sort
-    instead of the tile-major binning (same result)."""
+    instead of the tile-major binning (same result). ``footprint="rect"`` bins each Gaussian to
+    every tile of its footprint's bounding rectangle (FE_FLAG_RECT_BINNING) instead of the tiles
+    its footprint ellipse reaches in each tile row."""
     lib = N.load()
     n = _check_inputs(means, prec, logw)
     dev = means.device
     q = _as_dev(quat, dev, (4,))
     tt = _as_dev(t, dev, (3,))
     desc = N.make_desc(n, height, width, fx, fy, cx, cy, 21.4, 2.66, cull, cull_param, tile,
-                       flags=_binning_flag(binning))
+                       flags=_binning_flag(binning, footprint))
     gx = (width + tile[0] - 1) // tile[0]
     gy = (height + tile[1] - 1) // tile[1]
     cap = int(key_capacity) if key_capacity is not None else max(1, n * gx * gy)
@@ -462,17 +468,20 @@ class Batch:
     scratch from the device-side count instead (one 8-byte readback per run).
     ``tile``, ``px`` (pixels per thread) and ``chunk`` (record pairs per shared-memory stage)
     select the blend configuration; ``heavy_first=True`` makes the blend take the tiles with the
-    most keys first (tile-major binning only; see FE_FLAG_HEAVY_TILES_FIRST). ``keep_binning=True`` lets ``backward`` reuse the binning of
-    the preceding ``forward`` on the same Gaussian tensors (their contents must not change in
-    between) instead of recomputing it.
+    most keys first (tile-major binning only; see FE_FLAG_HEAVY_TILES_FIRST).
+    ``keep_binning=True`` lets ``backward`` reuse the binning of the preceding ``forward`` on the
+    same Gaussian tensors (their contents must not change in between) instead of recomputing it.
+    ``footprint="rect"`` bins every tile of each footprint's bounding rectangle
+    (FE_FLAG_RECT_BINNING) instead of the tiles its footprint ellipse reaches in each tile row.
     """
 
     def __init__(self, scenes, views, beta2=21.4, beta3=2.66, *, cull="eps", cull_param=None,
                  tile=(16, 16), px=0, chunk=0, exact_keys=False, keep_binning=False,
-                 binning="tiles", heavy_first=False):
+                 binning="tiles", heavy_first=False, footprint="ellipse"):
         lib = N.load()
         flags = (N.flag_chunk(chunk) | (N.FE_FLAG_EXACT_KEYS if exact_keys else 0)
-                 | (N.FE_FLAG_KEEP_BINNING if keep_binning else 0) | _binning_flag(binning)
+                 | (N.FE_FLAG_KEEP_BINNING if keep_binning else 0)
+                 | _binning_flag(binning, footprint)
                  | (N.FE_FLAG_HEAVY_TILES_FIRST if heavy_first else 0))
         desc = N.make_desc(0, 1, 1, 1.0, 1.0, 0.0, 0.0, beta2, beta3, cull, cull_param, tile,
                            flags=flags, px=px)

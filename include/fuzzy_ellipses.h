@@ -80,6 +80,12 @@ typedef enum fe_cull_mode {
  * GPU (measured slower on a 1135-view batch of small images and on single views); the
  * autotuner times it on the live batch. */
 #define FE_FLAG_HEAVY_TILES_FIRST 0x10000u
+/* Bin every Gaussian to all tiles of its footprint's bounding rectangle (the reference
+ * rasterizer's rule) instead of, in each tile row, only the tiles its footprint ellipse reaches.
+ * The ellipse is the set of pixels whose rays pass within the cut-off's Mahalanobis distance of
+ * the mean, so the tiles dropped by default hold only pixels where the Gaussian's density is
+ * below the cut-off; on 16 views of 640x480 they are a quarter of the rectangle's keys. */
+#define FE_FLAG_RECT_BINNING 0x20000u
 
 /* Render descriptor: everything a render needs besides the Gaussian and pose buffers. It is also
  * the opaque payload of the XLA custom call targets (bit-copied; the size and magic are checked).

@@ -105,3 +105,82 @@ def evals_per_render(means, prec, logw, cam, tile_w=8, tile_h=8, **kw):
     cols = wcum[rect[:, 2]] - wcum[rect[:, 0]]
     rows = hcum[rect[:, 3]] - hcum[rect[:, 1]]
     return int((cols * rows).sum())
+
+
+def footprint_rows(means, prec, logw, cam, cull="eps", cull_param=None):
+    """Row form of every Gaussian's footprint ellipse in float64, in pixel coordinates: the
+    pixels (u, v) whose rays pass within Mahalanobis distance k of the mean,
+    Q(u, v) = |Y (r x pc)|^2 - k^2 |M r|^2 <= 0 with r = ((u - cx)/fx, (v - cy)/fy, 1), M = U^T R^T,
+    Y = cof(M) (|M r x M pc| = |Y (r x pc)|, so Q <= 0 is d0 = |y|^2 / |a|^2 <= k^2).
+    Returns (ok, uc, vc, c1, hc, h2, vl, vr): at row v the ellipse spans
+    uc + c1 (v - vc) -+ sqrt(hc + h2 (v - vc)^2); vl, vr are the rows of its leftmost and rightmost
+    points; ok is False where the footprint is unbounded or degenerate. This restates the
+    product's footprint rows (preprocess.cu, foot_rows) from the Gaussian parameters directly."""
+    means = np.asarray(means, np.float64)
+    U = np.triu(np.asarray(prec, np.float64))
+    logw = np.asarray(logw, np.float64)
+    R = quat_to_rot(np.asarray(cam.quat, np.float64))
+    pc = (means - np.asarray(cam.trans, np.float64)) @ R.T
+    M = np.swapaxes(U, -1, -2) @ R.T
+    Y = _cofactor(M)
+    if cull == "eps":
+        eps = DEFAULT_CULL_EPS if not cull_param else float(cull_param)
+        k2 = 2.0 * (logw - np.log(eps))
+    else:
+        k = 3.0 if not cull_param else float(cull_param)
+        k2 = np.full(len(logw), k * k)
+    r0 = np.array([-cam.cx / cam.fx, -cam.cy / cam.fy, 1.0])
+    eu = np.array([1.0 / cam.fx, 0.0, 0.0])
+    ev = np.array([0.0, 1.0 / cam.fy, 0.0])
+    a = [M @ r for r in (r0, eu, ev)]
+    y = [np.einsum("nij,nj->ni", Y, np.cross(np.broadcast_to(r, pc.shape), pc)) for r in (r0, eu, ev)]
+
+    def q(i, j):
+        return (y[i] * y[j]).sum(1) - k2 * (a[i] * a[j]).sum(1)
+
+    with np.errstate(all="ignore"):
+        Quu, Quv, Qvv, Qu, Qv, Q0 = q(1, 1), q(1, 2), q(2, 2), q(0, 1), q(0, 2), q(0, 0)
+        det = Quu * Qvv - Quv * Quv
+        uc = (Qv * Quv - Qu * Qvv) / det
+        vc = (Qu * Quv - Qv * Quu) / det
+        qc = Q0 + Qu * uc + Qv * vc
+        lam = np.sqrt(-qc / (Qvv * det))
+        ok = (k2 > 0) & (Quu > 0) & (Qvv > 0) & (det > 0) & (qc < 0) & np.isfinite(lam)
+        # the camera outside the ellipsoid and the ellipsoid in front of it (bounded projection)
+        ok &= pc[:, 2] > 0
+        return (ok, uc, vc, -Quv / Quu, -qc / Quu, -det / (Quu * Quu), vc + lam * Quv,
+                vc - lam * Quv)
+
+
+def tile_row_spans(means, prec, logw, cam, tile_w, tile_h, margin=0.1, cull="eps",
+                   cull_param=None):
+    """(N, gy, 2) int64 tile spans [x0, x1) of every Gaussian in every tile row: the tiles its
+    footprint ellipse reaches in the row (pixel rows [row th, row th + th - 1], widened by
+    `margin` pixels), within its rectangle (tile_rects); rows outside the rectangle are empty.
+    Unbounded footprints span their whole rectangle."""
+    rect = tile_rects(means, prec, logw, cam, tile_w, tile_h, cull=cull, cull_param=cull_param)
+    ok, uc, vc, c1, hc, h2, vl, vr = footprint_rows(means, prec, logw, cam, cull, cull_param)
+    gy = -(-cam.height // tile_h)
+    out = np.zeros((len(rect), gy, 2), np.int64)
+    for row in range(gy):
+        va, vb = float(row * tile_h), float(row * tile_h + tile_h - 1)
+        inrow = (rect[:, 1] <= row) & (row < rect[:, 3]) & (rect[:, 0] < rect[:, 2])
+        x0 = rect[:, 0].astype(np.float64)
+        x1 = rect[:, 2].astype(np.float64)
+        with np.errstate(all="ignore"):
+            for edge, side in ((vl, -1.0), (vr, 1.0)):
+                inside = (edge >= va) & (edge <= vb)
+                dv = np.where(edge < va, va, vb) - vc
+                h = np.sqrt(np.maximum(hc + h2 * dv * dv, 0.0))
+                u = uc + c1 * dv + side * (h + margin)
+                if side < 0:
+                    t = np.floor(u / tile_w)
+                    x0 = np.where(ok & ~inside & (t > x0), np.minimum(t, x1), x0)
+                else:
+                    t = np.floor(u / tile_w) + 1
+                    x1 = np.where(ok & ~inside & (t < x1), np.maximum(t, x0), x1)
+        out[:, row, 0] = np.where(inrow, x0, 0)
+        out[:, row, 1] = np.where(inrow, x1, 0)
+    empty = out[:, :, 1] <= out[:, :, 0]
+    out[empty] = 0
+    return out

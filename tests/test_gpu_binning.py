@@ -100,15 +100,16 @@ def test_legacy_rasterize_matches_culled_oracle(cuda_device):
 
 @pytest.mark.parametrize("tile", [(8, 8), (16, 16), (32, 8)])
 def test_product_tile_sets_match_float64_screen_bounds(cuda_device, tile):
-    """Every Gaussian's tiles in the product binning (float32) form the rectangle of the float64
-    restatement of its k-sigma screen bound; boundary cases may differ by one tile row/column."""
+    """With rectangle binning, every Gaussian's tiles in the product binning (float32) form the
+    rectangle of the float64 restatement of its k-sigma screen bound; boundary cases may differ by
+    one tile row/column."""
     from oracle import screen_bounds as SB
     scene, cams = S.config1(seed=2)
     m, p, w = [torch.from_numpy(x).to(cuda_device) for x in (scene.means, scene.prec, scene.logw)]
     exact, total = 0, 0
     for c in cams[:6]:
         keys, _ = fe.render_binning(m, p, w, c.fx, c.fy, c.cx, c.cy, c.quat, c.trans, c.height,
-                                    c.width, tile=tile)
+                                    c.width, tile=tile, footprint="rect")
         k = keys.cpu().numpy().astype(np.uint64)
         tiles = (k >> np.uint64(32)).astype(np.int64)
         gid = (k & np.uint64(0xFFFFFFFF)).astype(np.int64)
@@ -130,15 +131,54 @@ def test_product_tile_sets_match_float64_screen_bounds(cuda_device, tile):
     assert exact >= 0.999 * total
 
 
+@pytest.mark.parametrize("tile", [(8, 8), (16, 16), (32, 8)])
+def test_product_row_spans_match_float64_footprint_rows(cuda_device, tile):
+    """By default every Gaussian is binned, in each tile row, to the tiles its footprint ellipse
+    reaches there: the product's float32 spans equal the float64 restatement's
+    (screen_bounds.tile_row_spans) for at least 99.5% of the Gaussians, the others differ by
+    boundary tiles only; and the spans hold about a quarter fewer keys than the rectangles."""
+    from oracle import screen_bounds as SB
+    scene, cams = S.config1(seed=2)
+    m, p, w = [torch.from_numpy(x).to(cuda_device) for x in (scene.means, scene.prec, scene.logw)]
+    exact, total, n_ell, n_rect = 0, 0, 0, 0
+    for c in cams[:6]:
+        args = (m, p, w, c.fx, c.fy, c.cx, c.cy, c.quat, c.trans, c.height, c.width)
+        keys, _ = fe.render_binning(*args, tile=tile)
+        krect, _ = fe.render_binning(*args, tile=tile, footprint="rect")
+        n_ell += keys.numel()
+        n_rect += krect.numel()
+        k = keys.cpu().numpy().astype(np.uint64)
+        tiles = (k >> np.uint64(32)).astype(np.int64)
+        gid = (k & np.uint64(0xFFFFFFFF)).astype(np.int64)
+        gx = -(-c.width // tile[0])
+        spans = SB.tile_row_spans(scene.means, scene.prec, scene.logw, c, *tile)
+        order = np.argsort(gid, kind="stable")
+        starts = np.searchsorted(gid[order], np.arange(scene.n + 1))
+        for g in range(scene.n):
+            got = set(tiles[order[starts[g]:starts[g + 1]]].tolist())
+            want = {ty * gx + tx for ty in range(spans.shape[1])
+                    for tx in range(spans[g, ty, 0], spans[g, ty, 1])}
+            total += 1
+            if got == want:
+                exact += 1
+                continue
+            # boundary differences only: at most two tiles per row the footprint spans
+            rows = max(1, int((spans[g, :, 1] > spans[g, :, 0]).sum()))
+            assert len(got ^ want) <= 2 * rows + 2, (g, len(got ^ want), rows)
+    assert exact >= 0.995 * total, (exact, total)
+    assert n_ell < 0.85 * n_rect, (n_ell, n_rect)
+
+
 def test_eval_counts_match_float64_screen_bounds(cuda_device):
-    """The benchmark's unit (evaluations of a tile-binned render) from the GPU binning equals the
-    float64 restatement's count on the 16-camera workload."""
+    """The benchmark's unit (evaluations of a render binned to footprint rectangles of 8x8 tiles,
+    the reference rasterizer's rule) from the GPU binning equals the float64 restatement's count
+    on the 16-camera workload."""
     from oracle import screen_bounds as SB
     scene, cams = S.config1(seed=0)
     m, p, w = [torch.from_numpy(x).to(cuda_device) for x in (scene.means, scene.prec, scene.logw)]
     for c in cams:
         _, ranges = fe.render_binning(m, p, w, c.fx, c.fy, c.cx, c.cy, c.quat, c.trans,
-                                      c.height, c.width, tile=(8, 8))
+                                      c.height, c.width, tile=(8, 8), footprint="rect")
         r = ranges.cpu().numpy()
         gx = (c.width + 7) // 8
         t = np.arange(r.shape[0])
@@ -148,17 +188,19 @@ def test_eval_counts_match_float64_screen_bounds(cuda_device):
         assert abs(gpu - cpu) <= 1e-4 * cpu
 
 
+@pytest.mark.parametrize("footprint", ["ellipse", "rect"])
 @pytest.mark.parametrize("tile", [(8, 8), (16, 16), (32, 8)])
-def test_tile_major_binning_equals_radix_sort(cuda_device, tile):
-    """The tile-major binning (per tile row: rectangles filtered in id order, a ballot per tile)
-    and key emission + stable radix sort give the same keys and ranges bit for bit; the keys are
-    ascending and every non-empty tile's range is exactly its run of keys."""
+def test_tile_major_binning_equals_radix_sort(cuda_device, tile, footprint):
+    """The tile-major binning (per tile row: spans filtered in id order, a ballot per tile) and
+    key emission + stable radix sort give the same keys and ranges bit for bit, with footprint
+    rows and with whole rectangles; the keys are ascending and every non-empty tile's range is
+    exactly its run of keys."""
     scene, cams = S.config1(seed=4)
     m, p, w = [torch.from_numpy(x).to(cuda_device) for x in (scene.means, scene.prec, scene.logw)]
     for c in cams[:4]:
         args = (m, p, w, c.fx, c.fy, c.cx, c.cy, c.quat, c.trans, c.height, c.width)
-        k1, r1 = fe.render_binning(*args, tile=tile, binning="tiles")
-        k2, r2 = fe.render_binning(*args, tile=tile, binning="radix")
+        k1, r1 = fe.render_binning(*args, tile=tile, binning="tiles", footprint=footprint)
+        k2, r2 = fe.render_binning(*args, tile=tile, binning="radix", footprint=footprint)
         assert torch.equal(k1, k2) and torch.equal(r1, r2)
         k = k1.cpu().numpy().astype(np.uint64)
         assert np.all(k[1:] > k[:-1])

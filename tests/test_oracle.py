@@ -148,6 +148,37 @@ def test_screen_bounds_contain_the_k_sigma_ellipsoid():
             assert ty.min() <= y0 + 1 and ty.max() >= y1 - 2
 
 
+def test_footprint_row_spans_hold_every_pixel_above_the_cut_off():
+    """The float64 footprint rows (screen_bounds.tile_row_spans) list, in every tile row, each tile
+    holding a pixel where the Gaussian's peak density along the ray reaches the cut-off (its
+    Mahalanobis distance at most k), and little else: the spans' tiles exceed the tiles holding
+    such a pixel by under 12% (tiles grazed between pixel centres), while the rectangles hold far
+    more."""
+    from fuzzy_ellipses import synthetic as S
+    from oracle import screen_bounds as SB
+    rng = np.random.default_rng(1)
+    scene = S.random_gaussians(40, 0.1, rng)
+    cam = S.Camera(240, 320, 300.0, 300.0, 160.0, 120.0, *S.look_at([0.6, 0.1, 0.2]))
+    rays = O.pinhole_rays(cam.height, cam.width, cam.fx, cam.fy, cam.cx, cam.cy) @ \
+        O.quat_to_rot(cam.quat)
+    _, stds = O.ray_gaussian_terms(rays, np.tile(cam.trans.astype(np.float64), (rays.shape[0], 1)),
+                                   scene.means, scene.prec, scene.logw)
+    for tw, th in ((8, 8), (16, 16), (32, 8)):
+        spans = SB.tile_row_spans(scene.means, scene.prec, scene.logw, cam, tw, th)
+        rect = SB.tile_rects(scene.means, scene.prec, scene.logw, cam, tw, th)
+        v, u = np.divmod(np.arange(cam.height * cam.width), cam.width)
+        n_need, n_span = 0, 0
+        for g in range(scene.n):
+            need = stds[g] >= np.log(1e-7)
+            ty, tx = v[need] // th, u[need] // tw
+            assert np.all(spans[g, ty, 0] <= tx) and np.all(tx < spans[g, ty, 1]), g
+            n_need += len(np.unique(ty * 1000 + tx))
+            n_span += int((spans[g, :, 1] - spans[g, :, 0]).sum())
+        n_rect = int(((rect[:, 2] - rect[:, 0]) * (rect[:, 3] - rect[:, 1])).sum())
+        assert n_span <= 1.12 * n_need + 40, (tw, th, n_span, n_need)
+        assert n_span < 0.9 * n_rect, (tw, th, n_span, n_rect)
+
+
 def test_gmm_oracle_matches_sklearn_score_samples():
     """The restated log_likelihood equals scikit-learn's GaussianMixture.score_samples with the
     same weights, means and precision Cholesky factors (fm_render's prec_full is sklearn's
