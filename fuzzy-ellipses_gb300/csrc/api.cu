@@ -111,6 +111,7 @@ struct RecSpace {
   uint32_t* incl;
   unsigned long long* scan_tmp;
   uint2* ranges;
+  uint32_t* tile_view;  // tile-major binning of a batch: the view of every tile
   unsigned long long* row_tot;  // tile-major binning: key counts of the tile rows, per view
   uint32_t* order;  // tile-major binning: tile ids per work class (kTileClasses lists of n_tiles)
   RecGrad* rgrad;  // backward only
@@ -145,6 +146,7 @@ size_t carve_rec(char* base, int64_t n_rec, int64_t n_tiles, int64_t n_pix, bool
   s.incl = c.take<uint32_t>(n_rec);
   s.scan_tmp = c.take<unsigned long long>(scan_grid(std::max(n_rec, n_tiles)));
   s.ranges = c.take<uint2>(n_tiles);
+  s.tile_view = c.take<uint32_t>(n_tiles);
   s.order = c.take<uint32_t>((int64_t)kTileClasses * n_tiles);
   s.rgrad = bwd ? c.take<RecGrad>(n_rec) : nullptr;
   out(s);
@@ -313,8 +315,8 @@ int run_binning(const Pipeline& p, int64_t worst, DevBuf& recbuf, DevBuf& keybuf
   if (!rp.ok || !p.heavy_first) rs.order = nullptr;  // the blend takes tiles in index order
   if (rp.ok) {
     launch_tile_binning_emit(p.va, rp.n_views, rp.max_gy, rs.rects, foot_of(p, rs), p.tile_w,
-                             p.tile_h, rs.row_tot, cap, rs.ctrl, rs.ranges, ks.keys_a, rs.order,
-                             p.n_tiles, st);
+                             p.tile_h, rs.row_tot, cap, rs.ctrl, rs.ranges, nullptr, ks.keys_a,
+                             rs.order, p.n_tiles, st);
     sorted = ks.keys_a;
   } else {
     launch_emit_keys(p.va, rs.incl, rs.rects, foot_of(p, rs), p.tile_w, p.tile_h, p.n_rec, rs.ctrl,
@@ -1174,6 +1176,9 @@ static Pipeline batch_pipeline(fe_batch* b, const float* means, const float* pre
   Pipeline p{};
   p.va.table = b->views_d;
   p.va.count = b->n_views;
+  // (written by the tile-major emission, read from the blend on)
+  p.va.tile_view = (b->rows.ok && !(b->desc.flags & FE_FLAG_RADIX_BINNING)) ? b->rs.tile_view
+                                                                             : nullptr;
   p.n_rec = b->n_rec;
   p.n_tiles = b->n_tiles;
   p.n_pix = b->n_pix;
@@ -1230,8 +1235,8 @@ static int batch_binning(fe_batch* b, const Pipeline& p, cudaStream_t st, cudaEv
   const KeySpace& ks = b->ks;
   if (rp.ok) {
     launch_tile_binning_emit(p.va, rp.n_views, rp.max_gy, rs.rects, foot_of(p, rs), p.tile_w,
-                             p.tile_h, rs.row_tot, b->cap, rs.ctrl, rs.ranges, ks.keys_a,
-                             p.heavy_first ? rs.order : nullptr, p.n_tiles, st);
+                             p.tile_h, rs.row_tot, b->cap, rs.ctrl, rs.ranges, rs.tile_view,
+                             ks.keys_a, p.heavy_first ? rs.order : nullptr, p.n_tiles, st);
     if (ev) FE_CUDA(cudaEventRecord(ev[3], st));
     b->sorted = ks.keys_a;
     if (ev) FE_CUDA(cudaEventRecord(ev[4], st));
@@ -1597,8 +1602,8 @@ int fe_render_fwd_noalloc(const fe_render_desc* d, const float* means, const flo
   if (!rp.ok || !p.heavy_first) rs.order = nullptr;
   if (rp.ok) {
     launch_tile_binning_emit(p.va, rp.n_views, rp.max_gy, rs.rects, foot_of(p, rs), p.tile_w,
-                             p.tile_h, rs.row_tot, worst, rs.ctrl, rs.ranges, ks.keys_a, rs.order,
-                             p.n_tiles, st);
+                             p.tile_h, rs.row_tot, worst, rs.ctrl, rs.ranges, nullptr, ks.keys_a,
+                             rs.order, p.n_tiles, st);
   } else {
     launch_scan(rs.touched, rs.incl, p.n_rec, worst, rs.scan_tmp, rs.ctrl, st);
     launch_emit_keys(p.va, rs.incl, rs.rects, foot_of(p, rs), p.tile_w, p.tile_h, p.n_rec, rs.ctrl,

@@ -516,8 +516,8 @@ __global__ void __launch_bounds__(kRowThreads) tile_emit_kernel(
     ViewsArg va, const TileRect* __restrict__ rects, const FootRows* __restrict__ foot,
     int tile_w, int tile_h, const unsigned long long* __restrict__ row_tot, bool bases,
     int64_t capacity,
-    Control* __restrict__ ctrl, uint2* __restrict__ ranges, uint64_t* __restrict__ keys,
-    uint32_t* __restrict__ order, int64_t n_tiles, int nseg) {
+    Control* __restrict__ ctrl, uint2* __restrict__ ranges, uint32_t* __restrict__ tile_view,
+    uint64_t* __restrict__ keys, uint32_t* __restrict__ order, int64_t n_tiles, int nseg) {
   __shared__ RowRect list[kRowSeg];
   __shared__ int diff[kMaxRowTiles + 1];         // +1 at x0, -1 at x1 of every covering rectangle
   __shared__ uint32_t pos[kMaxRowTiles];  // per tile: next key slot within the row
@@ -630,6 +630,7 @@ __global__ void __launch_bounds__(kRowThreads) tile_emit_kernel(
       const unsigned long long hi = min(row_base + cex + (unsigned)cnt[q], K);
       // every tile of the slice: empty tiles (or tiles whose keys were all dropped) get {0,0}
       ranges[tile0 + x] = hi > lo ? make_uint2((uint32_t)lo, (uint32_t)hi) : make_uint2(0u, 0u);
+      if (tile_view) tile_view[tile0 + x] = blockIdx.y;
     }
     cex += (unsigned)cnt[q];
   }
@@ -751,8 +752,8 @@ uint64_t* launch_sort(uint64_t* a, uint64_t* b, int key_bits, const Control* ctr
 void launch_tile_binning_emit(const ViewsArg& va, int n_views, int max_gy, const TileRect* rects,
                               const FootRows* foot, int tile_w, int tile_h,
                               unsigned long long* row_tot, int64_t capacity, Control* ctrl,
-                              uint2* ranges, uint64_t* keys, uint32_t* order, int64_t n_tiles,
-                              cudaStream_t st) {
+                              uint2* ranges, uint32_t* tile_view, uint64_t* keys, uint32_t* order,
+                              int64_t n_tiles, cudaStream_t st) {
   if (n_views <= 0 || max_gy <= 0) return;
   // Beyond a few dozen views the per-block sums over earlier views cost more than two extra
   // launches that form all row bases.
@@ -767,8 +768,8 @@ void launch_tile_binning_emit(const ViewsArg& va, int n_views, int max_gy, const
   const int64_t rows = (int64_t)max_gy * n_views;
   const int nseg = rows >= 2 * 152 ? 1 : (int)std::min<int64_t>(8, (2 * 152 + rows - 1) / rows);
   tile_emit_kernel<<<dim3((unsigned)(max_gy * nseg), (unsigned)n_views), kRowThreads, 0, st>>>(
-      va, rects, foot, tile_w, tile_h, row_tot, bases, capacity, ctrl, ranges, keys, order, n_tiles,
-      nseg);
+      va, rects, foot, tile_w, tile_h, row_tot, bases, capacity, ctrl, ranges, tile_view, keys,
+      order, n_tiles, nseg);
 }
 
 void launch_ranges(const uint64_t* keys, const Control* ctrl, int64_t capacity, uint2* ranges,

@@ -73,7 +73,7 @@ __global__ void __launch_bounds__(32 * kBwdWarps) blend_bwd_kernel(
     if (tile >= n_tiles) break;
     const uint2 range = ranges[tile];
     if (range.y <= range.x) continue;
-    const int vi = find_view<&ViewDev::tile_base>(va, tile);
+    const int vi = view_of_tile(va, tile);
     const ViewDev& V = view_at(va, vi);
     if (V.flags & FE_VIEW_NO_GRAD) continue;
     const int lt = (int)(tile - V.tile_base);

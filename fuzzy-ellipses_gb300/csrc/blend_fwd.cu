@@ -215,7 +215,7 @@ __global__ void __launch_bounds__(BlendShape<TW, TH, PX, CH>::NT,
     __syncthreads();
     const uint32_t tile = sm.tile;
     if (tile >= tile_end) break;
-    const int vi = find_view<&ViewDev::tile_base>(va, tile);
+    const int vi = view_of_tile(va, tile);
     const int gx = view_at(va, vi).gx;
     const int lt = (int)(tile - view_at(va, vi).tile_base);
     const int tx = lt % gx, ty = lt / gx;

@@ -51,14 +51,15 @@ uint64_t* launch_sort(uint64_t* a, uint64_t* b, int key_bits, const Control* ctr
 // turned into row offsets and view bases in place (row_tot is consumed). With `order`
 // (kTileClasses lists of n_tiles entries, ctrl's class counts zeroed) every tile's id is also
 // appended to the list of its work class (tile_class of its key count), which launch_blend_fwd
-// then serves heaviest class first.
+// then serves heaviest class first. With `tile_view` (n_tiles entries) every tile's view index is
+// written beside its range (ViewsArg::tile_view).
 constexpr int kMaxRowTiles = 1024;
 constexpr int kRowBaseViews = 32;  // above this many views the row bases are formed first
 void launch_tile_binning_emit(const ViewsArg& va, int n_views, int max_gy, const TileRect* rects,
                               const FootRows* foot, int tile_w, int tile_h,
                               unsigned long long* row_tot, int64_t capacity, Control* ctrl,
-                              uint2* ranges, uint64_t* keys, uint32_t* order, int64_t n_tiles,
-                              cudaStream_t st);
+                              uint2* ranges, uint32_t* tile_view, uint64_t* keys, uint32_t* order,
+                              int64_t n_tiles, cudaStream_t st);
 // Tile ranges of the sorted keys (ranges zeroed beforehand; empty tiles keep {0,0}).
 void launch_ranges(const uint64_t* keys, const Control* ctrl, int64_t capacity, uint2* ranges,
                    cudaStream_t st);

@@ -38,7 +38,7 @@ __global__ void __launch_bounds__(32 * kFeatWarps) features_kernel(
     if (lane == 0) tile = atomicAdd(&ctrl->next_tile, 1u);
     tile = __shfl_sync(full, tile, 0);
     if (tile >= n_tiles) break;
-    const int vi = find_view<&ViewDev::tile_base>(va, tile);
+    const int vi = view_of_tile(va, tile);
     const ViewDev& V = view_at(va, vi);
     const int lt = (int)(tile - V.tile_base);
     const int tx = lt % V.gx, ty = lt / V.gx;
