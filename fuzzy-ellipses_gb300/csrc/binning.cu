@@ -667,6 +667,8 @@ __global__ void __launch_bounds__(kRowThreads) tile_emit_kernel(
     // keeping their next slots in registers, and reads each 32-entry chunk of the list once for
     // all of them.
     for (int xb = x_lo + warp; xb < x_hi; xb += kRowWarps * kTileBlock) {
+      // the warp's tiles in this pass: xb + kRowWarps t for t < nt (uniform over the warp)
+      const int nt = min(kTileBlock, (x_hi - xb + kRowWarps - 1) / kRowWarps);
       uint32_t p[kTileBlock];
 #pragma unroll
       for (int t = 0; t < kTileBlock; ++t) {
@@ -679,8 +681,9 @@ __global__ void __launch_bounds__(kRowThreads) tile_emit_kernel(
         if (j < total) e = list[j];
 #pragma unroll
         for (int t = 0; t < kTileBlock; ++t) {
+          if (t >= nt) break;
           const int x = xb + kRowWarps * t;
-          const bool cov = x < x_hi && e.x0 <= x && x < e.x1;
+          const bool cov = e.x0 <= x && x < e.x1;
           const uint32_t bal = __ballot_sync(full, cov);
           if (cov) {
             const uint32_t k = p[t] + __popc(bal & lt_mask);
