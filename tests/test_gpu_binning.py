@@ -12,7 +12,7 @@ from fuzzy_ellipses import synthetic as S
 from oracle import fm_render_np as O
 from oracle.ref_binning import ref_binning
 from tests.golden.binning_cases import binning_cases, num_stds, projection, tan_full_fov
-from tests.helpers import TOL_ALPHA, TOL_DEPTH_REL, parity_errors
+from tests.helpers import TOL_ALPHA, TOL_DEPTH_REL, parity_errors, tile_lists_from_keys
 
 pytestmark = pytest.mark.gpu
 GOLDEN = os.path.join(os.path.dirname(__file__), "golden", "ref_binning_golden.npz")
@@ -259,3 +259,58 @@ def test_many_view_batch_row_bases_equal_radix_batch(cuda_device):
         out.append((d, a, st["num_keys"]))
     assert out[0][2] == out[1][2]
     assert torch.equal(out[0][0], out[1][0]) and torch.equal(out[0][1], out[1][1])
+
+
+def _footprint_scenes():
+    rng = np.random.default_rng(21)
+    out = {}
+    scene, cams = S.config0(seed=3)
+    out["config0"] = (scene, cams[0])
+    sub = S.random_gaussians(60, 0.1, rng, scale_lo=0.002, scale_hi=0.006)
+    q, t = S.look_at(0.5 * S.random_unit_vectors(1, rng)[0])
+    out["subpixel"] = (sub, S.Camera(64, 80, 64.0, 64.0, 40.0, 32.0, q, t))
+    thin = S.random_gaussians(60, 0.1, rng, scale_lo=0.001, scale_hi=0.05)
+    q, t = S.look_at(0.45 * S.random_unit_vectors(1, rng)[0])
+    out["elongated"] = (thin, S.Camera(96, 120, 110.0, 110.0, 60.0, 48.0, q, t))
+    # the camera inside one Gaussian's k-sigma region and beside others: unbounded footprints
+    means = np.array([[0.3, 0.0, 0.02], [0.0, 0.0, 0.6], [0.05, -0.04, 0.3]], np.float32)
+    prec = np.stack([np.triu(np.eye(3) / 0.1), np.triu(np.eye(3) / 0.05),
+                     np.triu(np.eye(3) / 0.02)]).astype(np.float32)
+    logw = np.array([0.0, 0.5, -0.3], np.float32)
+    out["straddling"] = (S.Scene(means, prec, logw),
+                         S.Camera(40, 48, 40.0, 40.0, 24.0, 20.0, np.array([1, 0, 0, 0], np.float32),
+                                  np.zeros(3, np.float32)))
+    return out
+
+
+@pytest.mark.parametrize("cull", ["eps", "nstd"])
+@pytest.mark.parametrize("tile", [(8, 8), (16, 16), (32, 8)])
+@pytest.mark.parametrize("name", ["config0", "subpixel", "elongated", "straddling"])
+def test_footprint_rows_list_every_pixel_above_the_cut_off(cuda_device, name, tile, cull):
+    """Footprint-row binning is conservative: wherever a Gaussian's peak density along a pixel's
+    ray clears the cut-off (its Mahalanobis distance below k, by 1e-5 in k^2), the Gaussian is
+    listed for that pixel's tile; on config-0, sub-pixel, strongly elongated and
+    camera-straddling Gaussians, every tile shape and both cut-off modes (dense float64 oracle
+    over every pixel)."""
+    scene, cam = _footprint_scenes()[name]
+    m, p, w = [torch.from_numpy(x).to(cuda_device) for x in (scene.means, scene.prec, scene.logw)]
+    param = 1e-7 if cull == "eps" else 3.0
+    keys, ranges = fe.render_binning(m, p, w, cam.fx, cam.fy, cam.cx, cam.cy, cam.quat, cam.trans,
+                                     cam.height, cam.width, cull=cull, cull_param=param,
+                                     tile=tile)
+    lists = tile_lists_from_keys(keys, ranges.shape[0])
+    rays = O.pinhole_rays(cam.height, cam.width, cam.fx, cam.fy, cam.cx, cam.cy) @ \
+        O.quat_to_rot(cam.quat)
+    _, stds = O.ray_gaussian_terms(rays, np.tile(cam.trans.astype(np.float64), (rays.shape[0], 1)),
+                                   scene.means, scene.prec, scene.logw)
+    logw = scene.logw.astype(np.float64)[:, None]
+    d0 = 2.0 * (logw - stds)  # Mahalanobis distance of each ray's peak, squared
+    k2 = 2.0 * (logw - np.log(param)) if cull == "eps" else np.full_like(logw, param * param)
+    need = d0 < k2 - 1e-5
+    gx = -(-cam.width // tile[0])
+    v, u = np.divmod(np.arange(cam.height * cam.width), cam.width)
+    tid = (v // tile[1]) * gx + u // tile[0]
+    listed = [set(l.tolist()) for l in lists]
+    for g in range(scene.n):
+        for t in np.unique(tid[need[g]]):
+            assert g in listed[t], (name, tile, cull, g, int(t))
