@@ -314,3 +314,35 @@ def test_footprint_rows_list_every_pixel_above_the_cut_off(cuda_device, name, ti
     for g in range(scene.n):
         for t in np.unique(tid[need[g]]):
             assert g in listed[t], (name, tile, cull, g, int(t))
+
+
+def test_footprint_rows_and_rectangles_render_alike(cuda_device):
+    """A batch binned to footprint rows and the same batch binned to whole rectangles
+    (FE_FLAG_RECT_BINNING) render alike: the tiles the rows leave out hold only pixels where the
+    dropped Gaussian's density is below the cut-off, so alpha moves by far less than its 1e-5
+    tolerance and depth by far less than its 1e-4 (where alpha > 1e-3); the forward statistics
+    and the backward's gradients agree as well."""
+    scene, cams = S.config1(seed=6)
+    m, p, w = [torch.from_numpy(x).to(cuda_device) for x in (scene.means, scene.prec, scene.logw)]
+    views = [dict(scene=0, height=c.height, width=c.width, fx=c.fx, fy=c.fy, cx=c.cx, cy=c.cy,
+                  quat=c.quat, trans=c.trans) for c in cams[:4]]
+    out = {}
+    for fp in ("ellipse", "rect"):
+        b = fe.Batch([(0, scene.n)], views, footprint=fp, keep_binning=True)
+        stats = torch.empty(3 * b.n_pixels, device=cuda_device)
+        d, a = b.forward(m, p, w, stats=stats)
+        gen = torch.Generator(device=cuda_device).manual_seed(3)
+        gd = torch.randn(b.n_pixels, device=cuda_device, generator=gen) * (a > 1e-3)
+        ga = torch.randn(b.n_pixels, device=cuda_device, generator=gen)
+        grads = b.backward(m, p, w, d, a, stats, gd, ga)
+        st = b.status()
+        assert st["device_error"] == 0
+        out[fp] = (d, a, grads, st["num_keys"])
+        b.close()
+    (d0, a0, g0, k0), (d1, a1, g1, k1) = out["ellipse"], out["rect"]
+    assert k0 < 0.85 * k1
+    assert float((a0 - a1).abs().max()) <= 1e-6
+    mask = a1 > 1e-3
+    assert float(((d0 - d1).abs()[mask] / d1[mask]).max()) <= 1e-5
+    for x, y in zip(g0, g1):
+        assert float((x - y).norm() / y.norm()) <= 1e-4
