@@ -93,8 +93,8 @@ __global__ void __launch_bounds__(32 * kBwdWarps) blend_bwd_kernel(
         const int o = ly * Slice::ROW + lx;
         sl.plane[0][o] = depth[pi];
         sl.plane[1][o] = -m;
-        sl.plane[2][o] = W > 0.f ? gD / W : 0.f;
-        sl.plane[3][o] = gA * expf(-A) * kLn2;
+        sl.plane[2][o] = W > 0.f ? gD * rcp_approx(W) : 0.f;
+        sl.plane[3][o] = gA * ex2_approx(-A * kLog2e) * kLn2;
       }
     }
     __syncwarp();
