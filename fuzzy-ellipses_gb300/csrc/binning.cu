@@ -512,11 +512,11 @@ __global__ void __launch_bounds__(kRowThreads) view_bases_kernel(int n_views, in
   }
 }
 
-__global__ void __launch_bounds__(kRowThreads) tile_emit_kernel(
+__device__ __forceinline__ void tile_emit_body(
     ViewsArg va, const TileRect* __restrict__ rects, const FootRows* __restrict__ foot,
     int tile_w, int tile_h, const unsigned long long* __restrict__ row_tot, bool bases,
-    int64_t capacity,
-    Control* __restrict__ ctrl, uint2* __restrict__ ranges, uint32_t* __restrict__ tile_view,
+    int64_t capacity, Control* __restrict__ ctrl, uint2* __restrict__ ranges,
+    uint32_t* __restrict__ tile_view,
     uint64_t* __restrict__ keys, uint32_t* __restrict__ order, int64_t n_tiles, int nseg) {
   __shared__ RowRect list[kRowSeg];
   __shared__ int diff[kMaxRowTiles + 1];         // +1 at x0, -1 at x1 of every covering rectangle
@@ -704,6 +704,27 @@ __global__ void __launch_bounds__(kRowThreads) tile_emit_kernel(
   }
 }
 
+// The emission kernel at the registers its single-wave launches run fastest with (48), and a copy
+// sized for 8 resident blocks per SM (32 registers, a few spills) for launches of many waves.
+__global__ void __launch_bounds__(kRowThreads) tile_emit_kernel(
+    ViewsArg va, const TileRect* __restrict__ rects, const FootRows* __restrict__ foot,
+    int tile_w, int tile_h, const unsigned long long* __restrict__ row_tot, bool bases,
+    int64_t capacity, Control* __restrict__ ctrl, uint2* __restrict__ ranges,
+    uint32_t* __restrict__ tile_view,
+    uint64_t* __restrict__ keys, uint32_t* __restrict__ order, int64_t n_tiles, int nseg) {
+  tile_emit_body(va, rects, foot, tile_w, tile_h, row_tot, bases, capacity, ctrl, ranges,
+                 tile_view, keys, order, n_tiles, nseg);
+}
+__global__ void __launch_bounds__(kRowThreads, 8) tile_emit_kernel_waves(
+    ViewsArg va, const TileRect* __restrict__ rects, const FootRows* __restrict__ foot,
+    int tile_w, int tile_h, const unsigned long long* __restrict__ row_tot, bool bases,
+    int64_t capacity, Control* __restrict__ ctrl, uint2* __restrict__ ranges,
+    uint32_t* __restrict__ tile_view,
+    uint64_t* __restrict__ keys, uint32_t* __restrict__ order, int64_t n_tiles, int nseg) {
+  tile_emit_body(va, rects, foot, tile_w, tile_h, row_tot, bases, capacity, ctrl, ranges,
+                 tile_view, keys, order, n_tiles, nseg);
+}
+
 inline int grid_for(int64_t work, int threads, int cap) {
   const int64_t b = (work + threads - 1) / threads;
   return (int)(b < 1 ? 1 : (b > cap ? cap : b));
@@ -770,9 +791,19 @@ void launch_tile_binning_emit(const ViewsArg& va, int n_views, int max_gy, const
   // writing, the longest part of a row's work, is spread over more SMs.
   const int64_t rows = (int64_t)max_gy * n_views;
   const int nseg = rows >= 2 * 152 ? 1 : (int)std::min<int64_t>(8, (2 * 152 + rows - 1) / rows);
-  tile_emit_kernel<<<dim3((unsigned)(max_gy * nseg), (unsigned)n_views), kRowThreads, 0, st>>>(
-      va, rects, foot, tile_w, tile_h, row_tot, bases, capacity, ctrl, ranges, tile_view, keys,
-      order, n_tiles, nseg);
+  const dim3 grid((unsigned)(max_gy * nseg), (unsigned)n_views);
+  // Many row blocks (several waves: the 1135-view batch has 18 K) go faster with more of them
+  // resident at a time, at 32 registers and a few spills (110 -> 100 us there); a single wave
+  // (16 views of 640x480: 480 blocks) goes faster with the 48 registers it needs (22.5 us
+  // against 26.5).
+  if ((int64_t)grid.x * grid.y > 2 * 5 * 152)
+    tile_emit_kernel_waves<<<grid, kRowThreads, 0, st>>>(va, rects, foot, tile_w, tile_h, row_tot,
+                                                         bases, capacity, ctrl, ranges, tile_view,
+                                                         keys, order, n_tiles, nseg);
+  else
+    tile_emit_kernel<<<grid, kRowThreads, 0, st>>>(va, rects, foot, tile_w, tile_h, row_tot, bases,
+                                                   capacity, ctrl, ranges, tile_view, keys, order,
+                                                   n_tiles, nseg);
 }
 
 void launch_ranges(const uint64_t* keys, const Control* ctrl, int64_t capacity, uint2* ranges,
