@@ -84,6 +84,10 @@ def parse():
                     help="with --profile-step: blend configuration TILExTILE/PX/CHUNK[/heavy] "
                          "(e.g. 16x16/4/32/heavy, the one the autotuner picks on the 16-camera "
                          "step); default: the autotuner's untuned default")
+    ap.add_argument("--profile-batch3", action="store_true",
+                    help="build the 256-scene batch, run its forward twice with the blend the "
+                         "autotuner picks there (16x16 tiles, 4 pixels per thread, 32-pair "
+                         "chunks) and exit (the batch's ncu launch list)")
     ap.add_argument("--profile-single", type=int, default=0, metavar="CALLS",
                     help="build the workload, then run CALLS plain single-view fe_render_fwd calls "
                          "(camera i mod 16) and exit (the per-call path's ncu capture)")
@@ -347,6 +351,9 @@ def main():
     npix = H * W
     views = [dict(scene=0, height=c.height, width=c.width, fx=c.fx, fy=c.fy, cx=c.cx, cy=c.cy,
                   quat=c.quat, trans=c.trans) for c in cams]
+    if args.profile_batch3:
+        profile_batch3(fe, dev)
+        return
     if args.profile_single:
         out = (torch.empty(H, W, device=dev), torch.empty(H, W, device=dev))
         for i in range(args.profile_single):
@@ -900,6 +907,36 @@ def next_rows_bench(fe, dev, scene, cams, fma_ops, ex2_ops, hbm_gbs):
                                "roofline": {"bound": "hbm", "achieved": gbs, "peak": hbm_gbs,
                                             "unit": "GB/s", "frac": gbs / hbm_gbs}}
     return out
+
+
+def config3_workload(fe, dev):
+    """The 256-scene batch's scenes, views and concatenated Gaussians on `dev`."""
+    import torch
+
+    from fuzzy_ellipses import synthetic as S
+    items = S.config3(seed=0)
+    means, prec, logw, scenes, views = [], [], [], [], []
+    off = 0
+    for si, (sc, cs) in enumerate(items):
+        means.append(sc.means); prec.append(sc.prec); logw.append(sc.logw)
+        scenes.append((off, sc.n))
+        off += sc.n
+        for c in cs:
+            views.append(dict(scene=si, height=c.height, width=c.width, fx=c.fx, fy=c.fy,
+                              cx=c.cx, cy=c.cy, quat=c.quat, trans=c.trans))
+    m, p, w = [torch.from_numpy(np.concatenate(x)).to(dev) for x in (means, prec, logw)]
+    return scenes, views, (m, p, w)
+
+
+def profile_batch3(fe, dev):
+    import torch
+    scenes, views, (m, p, w) = config3_workload(fe, dev)
+    b = fe.Batch(scenes, views, tile=(16, 16), px=4, chunk=32)
+    for _ in range(2):
+        b.forward(m, p, w)
+    torch.cuda.synchronize()
+    assert b.status()["device_error"] == 0
+    b.close()
 
 
 def config3_bench(fe, dev, steps, fma_ops, ex2_ops):
