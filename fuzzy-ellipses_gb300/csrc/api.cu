@@ -113,7 +113,8 @@ struct RecSpace {
   uint2* ranges;
   uint32_t* tile_view;  // tile-major binning of a batch: the view of every tile
   unsigned long long* row_tot;  // tile-major binning: key counts of the tile rows, per view
-  uint32_t* order;  // tile-major binning: tile ids per work class (kTileClasses lists of n_tiles)
+  uint32_t* order;  // tile-major binning: per work class (kTileClasses lists of n_tiles) the
+                    // tiles as uint4 entries (tile id, first key, end key, view)
   RecGrad* rgrad;  // backward only
 };
 
@@ -147,7 +148,7 @@ size_t carve_rec(char* base, int64_t n_rec, int64_t n_tiles, int64_t n_pix, bool
   s.scan_tmp = c.take<unsigned long long>(scan_grid(std::max(n_rec, n_tiles)));
   s.ranges = c.take<uint2>(n_tiles);
   s.tile_view = c.take<uint32_t>(n_tiles);
-  s.order = c.take<uint32_t>((int64_t)kTileClasses * n_tiles);
+  s.order = c.take<uint32_t>((int64_t)kTileClasses * n_tiles * 4);  // uint4 entries
   s.rgrad = bwd ? c.take<RecGrad>(n_rec) : nullptr;
   out(s);
   return c.off;

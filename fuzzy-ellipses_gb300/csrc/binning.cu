@@ -621,15 +621,18 @@ __device__ __forceinline__ void tile_emit_body(
     for (int w = 0; w < warp; ++w) before += wsu[w];
     cex = before + x - csum;
   }
+  uint2 rgq[kTilesPer];
 #pragma unroll
   for (int q = 0; q < kTilesPer; ++q) {
     const int x = kTilesPer * tid + q;
+    rgq[q] = make_uint2(0u, 0u);
     if (x >= x_lo && x < x_hi) {
       pos[x] = cex < lim ? (uint32_t)cex : lim;  // (slots from lim on are dropped)
       const unsigned long long lo = min(row_base + cex, K);
       const unsigned long long hi = min(row_base + cex + (unsigned)cnt[q], K);
       // every tile of the slice: empty tiles (or tiles whose keys were all dropped) get {0,0}
-      ranges[tile0 + x] = hi > lo ? make_uint2((uint32_t)lo, (uint32_t)hi) : make_uint2(0u, 0u);
+      rgq[q] = hi > lo ? make_uint2((uint32_t)lo, (uint32_t)hi) : make_uint2(0u, 0u);
+      ranges[tile0 + x] = rgq[q];
       if (tile_view) tile_view[tile0 + x] = blockIdx.y;
     }
     cex += (unsigned)cnt[q];
@@ -656,7 +659,8 @@ __device__ __forceinline__ void tile_emit_body(
     for (int q = 0; q < kTilesPer; ++q) {
       const int x = kTilesPer * tid + q;
       if (x >= x_lo && x < x_hi)
-        order[(int64_t)cl[q] * n_tiles + cls_base[cl[q]] + rank[q]] = (uint32_t)(tile0 + x);
+        reinterpret_cast<uint4*>(order)[(int64_t)cl[q] * n_tiles + cls_base[cl[q]] + rank[q]] =
+            make_uint4((uint32_t)(tile0 + x), rgq[q].x, rgq[q].y, blockIdx.y);
     }
   }
   __syncthreads();

@@ -38,6 +38,7 @@ struct BlendSmem {
   GaussRec src[2 * CH];     // source records of the next chunk (TMA bulk copies), record r at src[r]
   uint64_t bar;             // completion of the source-record copies, one phase per chunk
   uint32_t tile;
+  uint4 entry;              // the work-class list entry of the tile: id, range, view
   uint32_t cls_base[kTileClasses + 1];  // first work index of each tile class (with `order`)
 };
 
@@ -176,10 +177,11 @@ __global__ void __launch_bounds__(BlendShape<TW, TH, PX, CH>::NT,
   constexpr int RPT = (RC + Sh::NT - 1) / Sh::NT;  // records each thread stages and builds
   const float hw = 0.5f * (TW - 1), hh = 0.5f * (TH - 1);
   // Heaviest tiles first: with `order` (the tile-major binning's per-class tile lists over all
-  // tiles [0, tile_end)) work index w of class c maps to order[c tile_end + w - cls_base[c]], so
-  // the tiles taken last, which set the kernel's tail, are the lightest. The lists are used only
-  // when they hold every tile exactly once (their counts sum to tile_end); else tiles go in
-  // index order.
+  // tiles [0, tile_end), uint4 entries: tile id, first key, end key, view) work index w of class
+  // c maps to entry c tile_end + w - cls_base[c], so the tiles taken last, which set the
+  // kernel's tail, are the lightest, and a tile's range and view come with its id. The lists are
+  // used only when they hold every tile exactly once (their counts sum to tile_end); else tiles
+  // go in index order.
   bool use_order = false;
   if (tid == 0) {
     mbar_init(&sm.bar, 1);
@@ -194,6 +196,8 @@ __global__ void __launch_bounds__(BlendShape<TW, TH, PX, CH>::NT,
       use_order = b == tile_end;
     }
   }
+  __syncthreads();
+  const bool use_order_all = order && tile_begin == 0 && sm.cls_base[kTileClasses] == tile_end;
   uint32_t phase = 0;  // parity of the next completion of sm.bar
 
   // Work index of the CTA's first tile: its own index (the grid never exceeds the tiles), so the
@@ -207,7 +211,10 @@ __global__ void __launch_bounds__(BlendShape<TW, TH, PX, CH>::NT,
       if (use_order && w < tile_end) {
         int c = 0;
         while (c + 1 < kTileClasses && w >= sm.cls_base[c + 1]) ++c;
-        w = order[(int64_t)c * tile_end + (w - sm.cls_base[c])];
+        const uint4 e = reinterpret_cast<const uint4*>(order)[(int64_t)c * tile_end +
+                                                              (w - sm.cls_base[c])];
+        sm.entry = e;
+        w = e.x;
       }
       sm.tile = w;
     }
@@ -215,14 +222,16 @@ __global__ void __launch_bounds__(BlendShape<TW, TH, PX, CH>::NT,
     __syncthreads();
     const uint32_t tile = sm.tile;
     if (tile >= tile_end) break;
-    const int vi = view_of_tile(va, tile);
+    // With the work-class lists the entry carries the tile's range and view.
+    const bool listed = order && tile_begin == 0 && use_order_all;
+    const int vi = listed ? (int)sm.entry.w : view_of_tile(va, tile);
     const int gx = view_at(va, vi).gx;
     const int lt = (int)(tile - view_at(va, vi).tile_base);
     const int tx = lt % gx, ty = lt / gx;
     const GaussRec* vrec = recs + view_at(va, vi).rec_base;
     const float tcu = tx * TW + hw, tcv = ty * TH + hh;  // tile centre (pixels)
 
-    const uint2 rg = ranges[tile];
+    const uint2 rg = listed ? make_uint2(sm.entry.y, sm.entry.z) : ranges[tile];
     // m starts finite (kNoLogit) so that logit - m is never (-inf) - (-inf); masked logits are
     // -inf and give weight 0.
     f2_t A2[PX], W2[PX], Z2[PX];

@@ -49,9 +49,10 @@ uint64_t* launch_sort(uint64_t* a, uint64_t* b, int key_bits, const Control* ctr
 // empty tile, so the ranges need no zeroing). Same keys and ranges as emit + stable sort +
 // ranges, with the same `foot` (see launch_emit_keys). For many views the row counts are first
 // turned into row offsets and view bases in place (row_tot is consumed). With `order`
-// (kTileClasses lists of n_tiles entries, ctrl's class counts zeroed) every tile's id is also
-// appended to the list of its work class (tile_class of its key count), which launch_blend_fwd
-// then serves heaviest class first. With `tile_view` (n_tiles entries) every tile's view index is
+// (kTileClasses lists of n_tiles uint4 entries, 16-byte aligned; ctrl's class counts zeroed)
+// every tile is also appended to the list of its work class (tile_class of its key count) as
+// (tile id, first key, end key, view), which launch_blend_fwd then serves heaviest class first
+// without reading the tile's range or view again. With `tile_view` (n_tiles entries) every tile's view index is
 // written beside its range (ViewsArg::tile_view).
 constexpr int kMaxRowTiles = 1024;
 constexpr int kRowBaseViews = 32;  // above this many views the row bases are formed first
