@@ -559,8 +559,8 @@ def main():
         out_b[batch.n_pixels:].copy_(alp_b, non_blocking=True)
         torch.cuda.current_stream().synchronize()
 
-    # fe_batch_fwd_host, the C-ABI call: host Gaussians in, banded blend, each band's images
-    # copied back while the next bands render; then the stream is synchronised. The same call
+    # fe_batch_fwd_host, the C-ABI call: host Gaussians in, the blend storing depth and alpha
+    # into the pinned host buffers as it renders; then the stream is synchronised. The same call
     # through the Python wrapper (Batch.forward_host, argument checks included) is timed beside.
     lib = fe._native.load()
     host_args = (batch._h, m_h.data_ptr(), p_h.data_ptr(), w_h.data_ptr(), out_b.data_ptr(),
@@ -663,10 +663,10 @@ def main():
         "e2e": {"value": e2e_value, "unit": "Mevals/s", "h2d_bytes_per_step": h2d_batch,
                 "d2h_bytes_per_step": out_b.numel() * 4,
                 "path": "fe_batch_fwd_host C-ABI call (ctypes) over the 16 cameras: pinned "
-                        "host Gaussians in, depth and alpha out to pinned host buffers, the "
-                        "blend in bands of tile rows whose images are copied back while the next "
-                        "bands render; poses part of the batch plan; wall clock per call "
-                        "including the final sync",
+                        "host Gaussians in, depth and alpha out to pinned host buffers, which "
+                        "the blend stores into through their device mapping as it renders (one "
+                        "launch, tiles in index order, no copy after the last tile); poses part "
+                        "of the batch plan; wall clock per call including the final sync",
                 "ms_per_step": 1e3 * e2e_s,
                 "python_wrapper": {"value": e_step / e2e_wrapper_s / 1e6,
                                    "ms_per_step": 1e3 * e2e_wrapper_s,

@@ -1278,6 +1278,33 @@ static int host_band_streams() {
   return v;
 }
 
+// FE_HOST_DIRECT=0 makes fe_batch_fwd_host use the banded copies even for pinned outputs.
+static bool host_direct_enabled() {
+  static const bool v = [] {
+    const char* s = std::getenv("FE_HOST_DIRECT");
+    return !(s && std::atoi(s) == 0);
+  }();
+  return v;
+}
+
+// The device address of n floats of host memory at h when the whole range is pinned memory
+// mapped into the current device's address space (its first and last elements resolve to
+// device addresses the same distance apart), else nullptr. Pageable memory gives nullptr.
+static float* mapped_host_floats(float* h, int64_t n) {
+  if (n <= 0) return nullptr;
+  cudaPointerAttributes a{}, e{};
+  if (cudaPointerGetAttributes(&a, h) != cudaSuccess ||
+      cudaPointerGetAttributes(&e, h + (n - 1)) != cudaSuccess) {
+    (void)cudaGetLastError();
+    return nullptr;
+  }
+  if (a.type != cudaMemoryTypeHost || e.type != cudaMemoryTypeHost || !a.devicePointer ||
+      !e.devicePointer)
+    return nullptr;
+  float* d0 = static_cast<float*>(a.devicePointer);
+  return static_cast<float*>(e.devicePointer) == d0 + (n - 1) ? d0 : nullptr;
+}
+
 static void plan_host_bands(fe_batch* b) {
   b->bands.clear();
   const int64_t k =
@@ -1304,12 +1331,11 @@ static void plan_host_bands(fe_batch* b) {
   if (open) b->bands.push_back(cur);
 }
 
-extern "C" {
-
-int fe_batch_fwd(fe_batch* b, const float* means, const float* prec, const float* logw,
-                 float* depth, float* alpha, float* stats, fe_stream_t stream_) {
-  if (!b || !depth || !alpha) return fail(FE_ERR_INVALID_ARGUMENT, "NULL argument");
-  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream_);
+// Binning and one blend launch over every tile; `heavy_order` lets the blend take the batch's
+// heaviest-first tile lists when it has them (else tiles go in index order).
+static int batch_forward(fe_batch* b, const float* means, const float* prec, const float* logw,
+                         float* depth, float* alpha, float* stats, bool heavy_order,
+                         cudaStream_t st) {
   Pipeline p = batch_pipeline(b, means, prec, logw);
   if (p.n_rec > 0 && (!means || !prec || !logw))
     return fail(FE_ERR_INVALID_ARGUMENT, "NULL Gaussian pointer");
@@ -1317,11 +1343,20 @@ int fe_batch_fwd(fe_batch* b, const float* means, const float* prec, const float
   int rc = batch_binning(b, p, st, nullptr);
   if (rc) return rc;
   note_binning(b, means, prec, logw);
-  launch_blend_fwd(p.va, p.tile_w, p.tile_h, p.px, p.chunk, p.n_tiles, batch_order(b, p),
-                   b->sorted, b->rs.recs, b->rs.ranges, p.beta2, p.beta3, depth, alpha, stats,
-                   p.n_pix, b->rs.ctrl, st);
+  launch_blend_fwd(p.va, p.tile_w, p.tile_h, p.px, p.chunk, p.n_tiles,
+                   heavy_order ? batch_order(b, p) : nullptr, b->sorted, b->rs.recs,
+                   b->rs.ranges, p.beta2, p.beta3, depth, alpha, stats, p.n_pix, b->rs.ctrl, st);
   FE_CUDA(cudaGetLastError());
   return FE_OK;
+}
+
+extern "C" {
+
+int fe_batch_fwd(fe_batch* b, const float* means, const float* prec, const float* logw,
+                 float* depth, float* alpha, float* stats, fe_stream_t stream_) {
+  if (!b || !depth || !alpha) return fail(FE_ERR_INVALID_ARGUMENT, "NULL argument");
+  return batch_forward(b, means, prec, logw, depth, alpha, stats, true,
+                       reinterpret_cast<cudaStream_t>(stream_));
 }
 
 int fe_batch_fwd_host(fe_batch* b, const float* h_means, const float* h_prec,
@@ -1331,6 +1366,31 @@ int fe_batch_fwd_host(fe_batch* b, const float* h_means, const float* h_prec,
   if (n > 0 && (!h_means || !h_prec || !h_logw))
     return fail(FE_ERR_INVALID_ARGUMENT, "NULL Gaussian pointer");
   cudaStream_t st = reinterpret_cast<cudaStream_t>(stream_);
+  // Pinned outputs: the blend stores depth and alpha through their device mapping as it
+  // renders, in one launch over all tiles, so the images cross the host link while the tiles
+  // after them render and no copy follows the last tile. The tiles go in index order: the host
+  // link is slower than the blend's output rate, and index order spreads the light and heavy
+  // tiles, hence the stores, evenly over the launch (heaviest-first bunches the light tiles'
+  // stores at its end). Other outputs: bands of tile rows, each band's images copied back while
+  // the next bands render.
+  float* dep_map = host_direct_enabled() ? mapped_host_floats(h_depth, b->n_pix) : nullptr;
+  float* alp_map = dep_map ? mapped_host_floats(h_alpha, b->n_pix) : nullptr;
+  if (dep_map && alp_map) {
+    Carver c{nullptr};
+    c.take<float>(3 * n); c.take<float>(9 * n); c.take<float>(n);
+    int rc = b->io.reserve(c.off, st);
+    if (rc) return rc;
+    Carver t{b->io.ptr};
+    float* m_d = t.take<float>(3 * n);
+    float* p_d = t.take<float>(9 * n);
+    float* w_d = t.take<float>(n);
+    if (n > 0) {
+      FE_CUDA(cudaMemcpyAsync(m_d, h_means, sizeof(float) * 3 * n, cudaMemcpyHostToDevice, st));
+      FE_CUDA(cudaMemcpyAsync(p_d, h_prec, sizeof(float) * 9 * n, cudaMemcpyHostToDevice, st));
+      FE_CUDA(cudaMemcpyAsync(w_d, h_logw, sizeof(float) * n, cudaMemcpyHostToDevice, st));
+    }
+    return batch_forward(b, m_d, p_d, w_d, dep_map, alp_map, nullptr, false, st);
+  }
   if (b->bands.empty()) plan_host_bands(b);
   const int nb = (int)b->bands.size();
 

@@ -54,8 +54,9 @@ __device__ __forceinline__ void null_slot(TilePair& p, int sl) {
   }
 }
 
-// Threads per CTA for a tile of TW x TH pixels with PX pixels per thread (PX pixels of one row,
-// CW = TW/PX apart); GP record pairs per online-softmax group (one max update per group).
+// Threads per CTA for a tile of TW x TH pixels with PX pixels per thread (PX consecutive pixels
+// of one row, CW = TW/PX threads per row); GP record pairs per online-softmax group (one max
+// update per group).
 template <int TW, int TH, int PX, int CH>
 struct BlendShape {
   static constexpr int NT = TW * TH / PX;
@@ -73,6 +74,24 @@ struct BlendShape {
 
 // Initial running max: finite, far below any logit, so logit - max is never inf - inf.
 constexpr float kNoLogit = -1e30f;
+
+// Store a thread's PX consecutive pixels of one row (`room` pixels of the row remain from the
+// first): one vector store when all PX lie inside the image and the address is aligned to it,
+// else one store per pixel inside the image. The outputs may be pinned host memory mapped into
+// the device's address space, where whole vectors keep the link's write rate.
+template <int PX>
+__device__ __forceinline__ void store_pixels(float* dst, const float (&x)[PX], int room) {
+  const bool whole = room >= PX && (reinterpret_cast<uintptr_t>(dst) & (sizeof(float) * PX - 1)) == 0;
+  if (PX == 4 && whole) {
+    *reinterpret_cast<float4*>(dst) = make_float4(x[0], x[1], x[2 % PX], x[3 % PX]);
+  } else if (PX == 2 && whole) {
+    *reinterpret_cast<float2*>(dst) = make_float2(x[0], x[1 % PX]);
+  } else {
+#pragma unroll
+    for (int k = 0; k < PX; ++k)
+      if (k < room) dst[k] = x[k];
+  }
+}
 
 // One group of GP record pairs for the thread's PX pixels: evaluate every logit, raise the running
 // maxima once (rescaling W and Z), then accumulate. MASK applies the z > 0 mask to the logits.
@@ -165,10 +184,12 @@ __global__ void __launch_bounds__(BlendShape<TW, TH, PX, CH>::NT,
   const float dv = ly - 0.5f * (TH - 1);
   const f2_t DV = f2_pack(dv, dv), DVSQ = f2_pack(dv * dv, dv * dv);
   const f2_t B3 = f2_pack(beta3, beta3), NB2 = f2_pack(nb2, nb2);
+  // The thread's pixels are PX consecutive pixels of its row, so its outputs leave as one vector
+  // store per plane.
   f2_t DU[PX];
 #pragma unroll
   for (int k = 0; k < PX; ++k) {
-    const float du = (cx + k * Sh::CW) - 0.5f * (TW - 1);
+    const float du = (cx * PX + k) - 0.5f * (TW - 1);
     DU[k] = f2_pack(du, du);
   }
   const f2_t ZERO2 = f2_pack(0.f, 0.f);
@@ -356,27 +377,31 @@ __global__ void __launch_bounds__(BlendShape<TW, TH, PX, CH>::NT,
 
     const ViewDev& V = view_at(va, vi);
     const int v = ty * TH + ly;
+    const int u0 = tx * TW + cx * PX;
+    if (v < V.H) {
+      float dep[PX], alp[PX], wsum[PX], asum[PX];
 #pragma unroll
-    for (int k = 0; k < PX; ++k) {
-      const int u = tx * TW + cx + k * Sh::CW;
-      if (u < V.W && v < V.H) {
+      for (int k = 0; k < PX; ++k) {
         float a0, a1, w0, w1, z0, z1;
         f2_unpack(A2[k], a0, a1);
         f2_unpack(W2[k], w0, w1);
         f2_unpack(Z2[k], z0, z1);
         const float A = a0 + a1, W = w0 + w1, Z = z0 + z1;
-        const int64_t pix = V.pix_base + (int64_t)v * V.W + u;
-        depth[pix] = W > 0.f ? Z * rcp_approx(W) : 0.f;
+        dep[k] = W > 0.f ? Z * rcp_approx(W) : 0.f;
         // alpha = 1 - exp(-A): a Taylor polynomial below A = 1/64 (relative error under 1e-9),
         // else from the hardware exp2 (absolute error under 3e-7).
-        alpha[pix] = A < 0.015625f
-                         ? A * fmaf(A, fmaf(A, fmaf(A, -1.f / 24.f, 1.f / 6.f), -0.5f), 1.f)
-                         : 1.f - ex2_approx(-A * kLog2e);
-        if (stats) {
-          stats[pix] = m[k];
-          stats[stats_stride + pix] = W;
-          stats[2 * stats_stride + pix] = A;
-        }
+        alp[k] = A < 0.015625f ? A * fmaf(A, fmaf(A, fmaf(A, -1.f / 24.f, 1.f / 6.f), -0.5f), 1.f)
+                               : 1.f - ex2_approx(-A * kLog2e);
+        wsum[k] = W;
+        asum[k] = A;
+      }
+      const int64_t pix = V.pix_base + (int64_t)v * V.W + u0;
+      store_pixels<PX>(depth + pix, dep, V.W - u0);
+      store_pixels<PX>(alpha + pix, alp, V.W - u0);
+      if (stats) {
+        store_pixels<PX>(stats + pix, m, V.W - u0);
+        store_pixels<PX>(stats + stats_stride + pix, wsum, V.W - u0);
+        store_pixels<PX>(stats + 2 * stats_stride + pix, asum, V.W - u0);
       }
     }
     __syncthreads();  // sm.tile is rewritten next iteration

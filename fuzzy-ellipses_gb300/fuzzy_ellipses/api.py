@@ -568,8 +568,9 @@ class Batch:
 
     def forward_host(self, means, prec, logw, depth=None, alpha=None):
         """forward() from host tensors to host tensors (fe_batch_fwd_host): the Gaussians are
-        copied in, the blend runs in bands whose outputs are copied back while the next bands
-        render. Outputs default to new pinned tensors; returns after the copies have landed."""
+        copied in; into pinned outputs the blend stores depth and alpha directly as it renders,
+        into pageable ones it runs in bands whose outputs are copied back while the next bands
+        render. Outputs default to new pinned tensors; returns once the outputs have landed."""
         lib = N.load()
         host = []  # keeps converted copies alive until the call returns
         for t in (means, prec, logw):

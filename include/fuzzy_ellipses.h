@@ -261,13 +261,17 @@ int64_t fe_batch_scratch_bytes(const fe_batch *b);
 int fe_batch_fwd(fe_batch *b, const float *d_means, const float *d_prec, const float *d_logw,
                  float *d_depth, float *d_alpha, float *d_stats, fe_stream_t stream);
 /* fe_batch_fwd from HOST memory to HOST memory: h_means (n,3), h_prec (n,3,3), h_logw (n) are
- * copied in on `stream`; the blend runs in bands of whole tile rows (alternating between
- * `stream` and a second stream of the batch, so one band's tail overlaps the next band's start)
- * and each band's depth and alpha rows are copied back on a copy stream of the batch as soon as
- * the band is done, so only the last band's copy follows the render. Pinned host buffers give
- * asynchronous copies; pageable ones work but the calling thread waits in the copies. Returns
- * once everything is enqueued; `stream` is ordered after the last copy, so synchronising it
- * makes the outputs readable. The outputs are indexed by fe_view.pixel_offset. */
+ * copied in on `stream`. When h_depth and h_alpha are pinned host memory mapped into the
+ * device's address space (cudaHostAlloc / cudaHostRegister; every pinned allocation on a
+ * unified-addressing system), the blend stores the images through that mapping as it renders,
+ * in one launch on `stream`, so they cross the host link while later tiles render and no copy
+ * follows the last tile (environment FE_HOST_DIRECT=0 turns this off). Otherwise the blend runs
+ * in bands of whole tile rows (alternating between `stream` and a second stream of the batch, so
+ * one band's tail overlaps the next band's start) and each band's depth and alpha rows are
+ * copied back on a copy stream of the batch as soon as the band is done, so only the last
+ * band's copy follows the render; pageable buffers work but the calling thread waits in the
+ * copies. Returns once everything is enqueued; synchronising `stream` makes the outputs
+ * readable. The outputs are indexed by fe_view.pixel_offset. */
 int fe_batch_fwd_host(fe_batch *b, const float *h_means, const float *h_prec, const float *h_logw,
                       float *h_depth, float *h_alpha, fe_stream_t stream);
 /* Backward of fe_batch_fwd; gradients are accumulated over all views of a scene. */

@@ -145,8 +145,9 @@ def _host_forward_matches(b, m, p, w, pinned=True):
 
 @pytest.mark.parametrize("layout", ["depth_first", "alpha_first", "gapped"])
 def test_forward_host_images_in_one_buffer(cuda_device, layout):
-    """Depth and alpha as two views of one host buffer: each band leaves in one 2-D copy whose
-    row pitch is the distance between them, in either order and with a gap between them."""
+    """Depth and alpha as two views of one pinned host buffer, in either order and with a gap
+    between them: the blend stores into both through the buffer's device mapping and writes
+    nothing between them."""
     b, items, views, (m, p, w) = make_batch(cuda_device, n_scenes=4, seed=4)
     depth, alpha = b.forward(m, p, w)
     torch.cuda.synchronize()
@@ -176,20 +177,52 @@ def test_forward_host_bands_within_and_across_views(cuda_device):
     # 16 views of 640x480: several bands, each ending at a view or tile-row boundary.
     views = [dict(scene=0, height=c.height, width=c.width, fx=c.fx, fy=c.fy, cx=c.cx, cy=c.cy,
                   quat=c.quat, trans=c.trans) for c in cams]
+    # Pageable outputs take the banded copies; pinned ones the direct stores.
     b = fe.Batch([(0, scene.n)], views, tile=(16, 16))
-    _host_forward_matches(b, m, p, w)
+    _host_forward_matches(b, m, p, w, pinned=False)
+    _host_forward_matches(b, m, p, w, pinned=True)
     # One large view (1280x968: the last tile row is partial): bands of tile rows inside it.
     c = cams[0]
     big = [dict(scene=0, height=968, width=1280, fx=2 * c.fx, fy=2 * c.fy, cx=640.0, cy=484.0,
                 quat=c.quat, trans=c.trans)]
     b.reset([(0, scene.n)], big)
-    _host_forward_matches(b, m, p, w)
+    _host_forward_matches(b, m, p, w, pinned=False)
+    _host_forward_matches(b, m, p, w, pinned=True)
     # Views laid out in reverse order in the output: no band spans two views.
     n_px = [v["height"] * v["width"] for v in views[:5]]
     offs = np.cumsum([0] + n_px[::-1][:-1])[::-1]
     rev = [dict(v, pixel_offset=int(o)) for v, o in zip(views[:5], offs)]
     b2 = fe.Batch([(0, scene.n)], rev, tile=(32, 8))
-    _host_forward_matches(b2, m, p, w)
+    _host_forward_matches(b2, m, p, w, pinned=False)
+    _host_forward_matches(b2, m, p, w, pinned=True)
+
+
+def test_forward_host_mixed_and_ragged_outputs(cuda_device):
+    """One pinned and one pageable output take the banded copies; ragged widths (not a multiple
+    of the thread's pixel vector) and an output base off the vector alignment take the per-pixel
+    stores at row ends and the direct path's unaligned rows."""
+    dev = cuda_device
+    scene, cams = S.config1(seed=1)
+    m, p, w = [torch.from_numpy(x).to(dev) for x in (scene.means, scene.prec, scene.logw)]
+    c = cams[2]
+    views = [dict(scene=0, height=h, width=wd, fx=c.fx * wd / 640, fy=c.fy * h / 480,
+                  cx=wd / 2, cy=h / 2, quat=c.quat, trans=c.trans)
+             for h, wd in ((131, 197), (64, 61), (250, 333))]
+    b = fe.Batch([(0, scene.n)], views, tile=(16, 16), px=4)
+    depth, alpha = b.forward(m, p, w)
+    torch.cuda.synchronize()
+    n = b.n_pixels
+    hd = torch.full((n,), -7.0).pin_memory()
+    ha = torch.full((n,), -7.0)
+    b.forward_host(m.cpu(), p.cpu(), w.cpu(), hd, ha)
+    assert torch.equal(hd, depth.cpu()) and torch.equal(ha, alpha.cpu())
+    # Outputs starting one float past a 16-byte boundary of a pinned buffer.
+    buf = torch.full((2 * n + 2,), -7.0).pin_memory()
+    hd, ha = buf[1:n + 1], buf[n + 2:]
+    b.forward_host(m.cpu(), p.cpu(), w.cpu(), hd, ha)
+    assert torch.equal(hd, depth.cpu()) and torch.equal(ha, alpha.cpu())
+    assert buf[0] == -7.0 and buf[n + 1] == -7.0
+    assert b.status()["device_error"] == 0
 
 
 _OVERFLOW_CHILD = r"""
