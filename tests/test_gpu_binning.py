@@ -214,16 +214,22 @@ def test_tile_major_binning_equals_radix_sort(cuda_device, tile, footprint):
         assert not r[~nonempty].any()
 
 
-def test_tile_major_batch_equals_radix_batch(cuda_device):
+@pytest.mark.parametrize("tile,n_views,n_gauss", [((16, 16), 6, 1000), ((16, 16), 16, 1000),
+                                                  ((8, 8), 16, 1000), ((16, 16), 4, 3000)])
+def test_tile_major_batch_equals_radix_batch(cuda_device, tile, n_views, n_gauss):
     """A batch binned tile-major renders bit-identically to the same batch binned by radix sort
-    (same keys, so the same tile records and the same evaluation order)."""
+    (same keys, so the same tile records and the same evaluation order). The cases cover rows
+    split over several emission blocks, whole 40- and 80-tile rows, and rows filtered in
+    several segments of records (3000 Gaussians)."""
     scene, cams = S.config1(seed=5)
+    if n_gauss != scene.n:
+        scene = S.random_gaussians(n_gauss, 0.3, np.random.default_rng(5))
     m, p, w = [torch.from_numpy(x).to(cuda_device) for x in (scene.means, scene.prec, scene.logw)]
     views = [dict(scene=0, height=c.height, width=c.width, fx=c.fx, fy=c.fy, cx=c.cx, cy=c.cy,
-                  quat=c.quat, trans=c.trans) for c in cams[:6]]
+                  quat=c.quat, trans=c.trans) for c in cams[:n_views]]
     out = []
     for binning in ("tiles", "radix"):
-        b = fe.Batch([(0, scene.n)], views, binning=binning)
+        b = fe.Batch([(0, scene.n)], views, tile=tile, binning=binning)
         d, a = b.forward(m, p, w)
         st = b.status()
         assert st["device_error"] == 0
