@@ -562,8 +562,13 @@ def main():
     # fe_batch_fwd_host, the C-ABI call: host Gaussians in, the blend storing depth and alpha
     # into the pinned host buffers as it renders; then the stream is synchronised. The same call
     # through the Python wrapper (Batch.forward_host, argument checks included) is timed beside.
+    # Its batch is the autotuner's pick for host outputs, where the host link bounds the call.
+    tuned_h = fe.autotune.Autotuner(persist=False).tune([(0, scene.n)], views, m, p, w, reps=3,
+                                                         target="host")
+    batch_h = fe.Batch([(0, scene.n)], views, tile=tuned_h["tile"], px=tuned_h["px"],
+                       chunk=tuned_h["chunk"], binning=args.binning)
     lib = fe._native.load()
-    host_args = (batch._h, m_h.data_ptr(), p_h.data_ptr(), w_h.data_ptr(), out_b.data_ptr(),
+    host_args = (batch_h._h, m_h.data_ptr(), p_h.data_ptr(), w_h.data_ptr(), out_b.data_ptr(),
                  out_b.data_ptr() + 4 * batch.n_pixels)
 
     def e2e_batch_step():
@@ -572,7 +577,7 @@ def main():
         cs.synchronize()
 
     def e2e_wrapper_step():
-        batch.forward_host(m_h, p_h, w_h, out_b[:batch.n_pixels], out_b[batch.n_pixels:])
+        batch_h.forward_host(m_h, p_h, w_h, out_b[:batch.n_pixels], out_b[batch.n_pixels:])
 
     def timed_host(step):
         for _ in range(3):
@@ -668,6 +673,12 @@ def main():
                         "launch, tiles in index order, no copy after the last tile); poses part "
                         "of the batch plan; wall clock per call including the final sync",
                 "ms_per_step": 1e3 * e2e_s,
+                "autotuned": {"tile": f"{tuned_h['tile'][0]}x{tuned_h['tile'][1]}",
+                              "px": tuned_h["px"], "chunk": tuned_h["chunk"],
+                              "target": "host",
+                              "candidates_ms": {f"{c['tile'][0]}x{c['tile'][1]}/px{c['px']}"
+                                                f"/ch{c['chunk']}": round(c["ms"], 4)
+                                                for c in tuned_h["candidates"]}},
                 "python_wrapper": {"value": e_step / e2e_wrapper_s / 1e6,
                                    "ms_per_step": 1e3 * e2e_wrapper_s,
                                    "path": "the same call through Batch.forward_host"},

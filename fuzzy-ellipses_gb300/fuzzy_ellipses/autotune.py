@@ -16,6 +16,11 @@ Three knobs change the work and its mapping onto the GPU:
 timings of the whole pipeline, not just the blend) and caches the fastest per workload bucket
 (mean pixels per view, mean Gaussians per view and number of views, each on a log2 scale) in a
 JSON file (``FE_AUTOTUNE_CACHE`` or ``~/.cache/fuzzy_ellipses/autotune.json``).
+
+``target="host"`` tunes the host-to-host call instead (``Batch.forward_host`` into pinned
+outputs, which the blend stores into through their device mapping, tiles in index order): the
+host link, not the blend, bounds it, and tiles with longer rows (32x8: 128-byte row segments)
+use that link better. Its entries are cached under the bucket with a ``_host`` suffix.
 """
 
 from __future__ import annotations
@@ -63,23 +68,28 @@ class Autotuner:
             except (OSError, ValueError):
                 self.table = {}
 
-    def lookup(self, scenes, views):
+    def lookup(self, scenes, views, target="device"):
         """Cached best configuration for the batch's bucket, or the default."""
-        e = self.table.get(bucket(scenes, views))
+        e = self.table.get(bucket(scenes, views) + ("_host" if target == "host" else ""))
         if not e:
             return dict(DEFAULT)
         return {"tile": tuple(e["tile"]), "px": e["px"], "chunk": e["chunk"],
                 "heavy_first": bool(e.get("heavy_first", False))}
 
-    def tune(self, scenes, views, means, prec, logw, candidates=CANDIDATES, reps=5, **batch_kw):
-        """Time every candidate on this batch; cache and return the fastest configuration."""
+    def tune(self, scenes, views, means, prec, logw, candidates=CANDIDATES, reps=5,
+             target="device", **batch_kw):
+        """Time every candidate on this batch; cache and return the fastest configuration.
+        ``target="host"`` times the host-to-host call into pinned outputs instead."""
         import torch
 
+        from . import _native as N
         from .api import Batch
 
-        def time_one(tile, px, chunk, heavy_first):
-            b = Batch(scenes, views, tile=tile, px=px, chunk=chunk, heavy_first=heavy_first,
-                      **batch_kw)
+        if target == "host":
+            host_in = [t.detach().cpu().contiguous().float().pin_memory()
+                       for t in (means, prec, logw)]
+
+        def time_device(b):
             depth = torch.empty(b.n_pixels, device=means.device)
             alpha = torch.empty(b.n_pixels, device=means.device)
             b.forward(means, prec, logw, depth, alpha)
@@ -88,16 +98,42 @@ class Autotuner:
                 _, _, ms = b.forward_timed(means, prec, logw, depth, alpha)
                 totals.append(sum(ms.values()))
                 stages.append(ms)
+            return statistics.median(totals), statistics.median(s["blend"] for s in stages)
+
+        def time_host(b):
+            # The call's device span on the caller's stream (it joins every stream it uses back
+            # into that one), from the C ABI as a host caller makes it.
+            lib = N.load()
+            out = torch.empty(2 * b.n_pixels, dtype=torch.float32).pin_memory()
+            args = (b._h, host_in[0].data_ptr(), host_in[1].data_ptr(), host_in[2].data_ptr(),
+                    out.data_ptr(), out.data_ptr() + 4 * b.n_pixels)
+            st = torch.cuda.current_stream()
+            N.check(lib.fe_batch_fwd_host(*args, st.cuda_stream))
+            st.synchronize()
+            times = []
+            for _ in range(reps):
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(st)
+                N.check(lib.fe_batch_fwd_host(*args, st.cuda_stream))
+                e1.record(st)
+                e1.synchronize()
+                times.append(e0.elapsed_time(e1))
+            return statistics.median(times), None
+
+        def time_one(tile, px, chunk, heavy_first):
+            b = Batch(scenes, views, tile=tile, px=px, chunk=chunk, heavy_first=heavy_first,
+                      **batch_kw)
+            ms, blend_ms = (time_host if target == "host" else time_device)(b)
             b.close()
             return {"tile": list(tile), "px": px, "chunk": chunk, "heavy_first": heavy_first,
-                    "ms": statistics.median(totals),
-                    "blend_ms": statistics.median(s["blend"] for s in stages)}
+                    "ms": ms, "blend_ms": blend_ms}
 
         results = [time_one(tile, px, chunk, False) for tile, px, chunk in candidates]
         best = min(results, key=lambda r: r["ms"])
-        results.append(time_one(tuple(best["tile"]), best["px"], best["chunk"], True))
-        best = min(results, key=lambda r: r["ms"])
-        key = bucket(scenes, views)
+        if target != "host":  # (the host path's direct stores take tiles in index order)
+            results.append(time_one(tuple(best["tile"]), best["px"], best["chunk"], True))
+            best = min(results, key=lambda r: r["ms"])
+        key = bucket(scenes, views) + ("_host" if target == "host" else "")
         with self._lock:
             self.table[key] = {"tile": best["tile"], "px": best["px"], "chunk": best["chunk"],
                                "heavy_first": best["heavy_first"], "ms": best["ms"]}

@@ -142,6 +142,20 @@ def test_autotuner_picks_a_candidate(cuda_device, tmp_path):
             ref = a.clone()
         assert torch.allclose(a, ref, atol=2e-6, rtol=0)
         b.close()
+    # Tuned for host outputs: its own cache entry, no heavy-first trial (the direct stores take
+    # tiles in index order), and the picked batch's host call equals its device forward.
+    host = tuner.tune(scenes, views, m, p, w, reps=2, target="host")
+    assert (tuple(host["tile"]), host["px"], host["chunk"]) in \
+        [(t, x, c) for t, x, c in autotune.CANDIDATES]
+    assert len(host["candidates"]) == len(autotune.CANDIDATES)
+    assert host["bucket"].endswith("_host")
+    assert tuner.lookup(scenes, views, target="host")["tile"] == tuple(host["tile"])
+    assert tuner.lookup(scenes, views)["tile"] == tuple(best["tile"])
+    b = fe.Batch(scenes, views, tile=host["tile"], px=host["px"], chunk=host["chunk"])
+    d, a = b.forward(m, p, w)
+    hd, ha = b.forward_host(m.cpu(), p.cpu(), w.cpu())
+    assert torch.equal(hd, d.cpu()) and torch.equal(ha, a.cpu())
+    b.close()
 
 
 def test_device_without_index_and_malformed_request(cuda_device):
