@@ -39,6 +39,7 @@ from __future__ import annotations
 
 import argparse
 import importlib
+import json
 import math
 import os
 import sys
@@ -334,16 +335,56 @@ def case_quat_cam(fm, out):
 CASES = [case_cfg0, case_cfg1, case_cfg2, case_edges, case_gmm, case_pixel_lists, case_quat_cam]
 
 
+def time_reference(fm, n_pix, n_cams):
+    """Throughput of the reference's own ``render_func_quat`` (through the float64 NumPy
+    stand-in) on a fixed sample of ``n_pix`` pixels of each of the first ``n_cams`` config-1
+    cameras, in the benchmark's unit: the metric's evaluations of the sampled pixels (the
+    reference tiling's culled count of each camera, scaled by the sampled fraction of its
+    pixels) per second, beside the dense rate (every ray against every Gaussian)."""
+    from oracle import screen_bounds as SB
+
+    scene, cams = S.config1(seed=0)
+    rng = np.random.default_rng(7)
+    metric_evals, dense_evals, seconds = 0.0, 0, 0.0
+    for cam in cams[:n_cams]:
+        p = np.sort(rng.choice(cam.height * cam.width, n_pix, replace=False))
+        rays = pinhole_rays(cam.height, cam.width, cam.fx, cam.fy, cam.cx, cam.cy)[p]
+        t0 = time.perf_counter()
+        render(fm, scene.means, scene.prec, scene.logw, rays, cam.quat, cam.trans)
+        seconds += time.perf_counter() - t0
+        metric_evals += SB.evals_per_render(scene.means, scene.prec, scene.logw, cam) * \
+            n_pix / (cam.height * cam.width)
+        dense_evals += n_pix * scene.n
+    try:
+        from threadpoolctl import threadpool_info
+        threads = max([i.get("num_threads", 1) for i in threadpool_info()] or [1])
+    except ImportError:
+        threads = None
+    print(json.dumps({"impl": "reference fm_render.render_func_quat (float64 NumPy stand-in "
+                              "for JAX)",
+                      "sample": f"{n_pix} pixels of each of {n_cams} config-1 cameras",
+                      "mevals_per_s": metric_evals / seconds / 1e6,
+                      "dense_mevals_per_s": dense_evals / seconds / 1e6,
+                      "seconds": seconds, "cpu_count": os.cpu_count(),
+                      "blas_threads": threads}))
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__.split("\n\n")[0])
     ap.add_argument("--reference", default=os.environ.get("FE_REFERENCE_DIR"),
                     help="reference checkout (default: $FE_REFERENCE_DIR)")
     ap.add_argument("--out", default=OUT)
     ap.add_argument("--only", nargs="*", help="case names to run (default: all)")
+    ap.add_argument("--time", type=int, default=0, metavar="PIXELS",
+                    help="time the reference's render_func_quat on PIXELS sampled pixels of "
+                         "four config-1 cameras and print one JSON line; write no fixtures")
     args = ap.parse_args()
     if not args.reference:
         raise SystemExit("set FE_REFERENCE_DIR or pass --reference")
     fm = import_reference(os.path.abspath(args.reference))
+    if args.time:
+        time_reference(fm, args.time, 4)
+        return
     out = {}
     for case in CASES:
         if args.only and case.__name__[5:] not in args.only:
