@@ -91,6 +91,10 @@ def parse():
     ap.add_argument("--profile-single", type=int, default=0, metavar="CALLS",
                     help="build the workload, then run CALLS plain single-view fe_render_fwd calls "
                          "(camera i mod 16) and exit (the per-call path's ncu capture)")
+    ap.add_argument("--profile-host", type=int, default=0, metavar="CALLS",
+                    help="build the 16-camera batch with --blend (default 32x8/2/16, the "
+                         "autotuner's pick for host outputs there), run CALLS fe_batch_fwd_host "
+                         "calls into pinned host outputs and exit (the host-to-host ncu capture)")
     return ap.parse_args()
 
 
@@ -353,6 +357,15 @@ def main():
                   quat=c.quat, trans=c.trans) for c in cams]
     if args.profile_batch3:
         profile_batch3(fe, dev)
+        return
+    if args.profile_host:
+        cfg = blend_cfg(args.blend or "32x8/2/16")
+        b = fe.Batch([(0, scene.n)], views, tile=cfg["tile"], px=cfg["px"], chunk=cfg["chunk"])
+        host_in = [t.cpu().pin_memory() for t in (m, p, w)]
+        out = torch.empty(2 * b.n_pixels, dtype=torch.float32).pin_memory()
+        for _ in range(args.profile_host):
+            b.forward_host(*host_in, out[:b.n_pixels], out[b.n_pixels:])
+        assert b.status()["device_error"] == 0
         return
     if args.profile_single:
         out = (torch.empty(H, W, device=dev), torch.empty(H, W, device=dev))
