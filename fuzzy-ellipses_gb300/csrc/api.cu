@@ -358,11 +358,15 @@ Pipeline single_view_pipeline(const fe_render_desc* d, const float* means, const
   p.tile_w = tw;
   p.tile_h = th;
   // A small launch does not fill the GPU, and its heaviest tile sets the blend's duration:
-  // below about two resident blends' worth of tiles, two pixels per thread (twice the threads
-  // per tile, half the per-thread work) finish sooner. 16 single-view calls of 1000 Gaussians,
-  // 16x16 tiles, 2 vs 4 pixels per thread: 320x240 0.545 vs 0.587 ms, 640x480 0.727 vs 0.841;
-  // 1280x960 1.337 vs 1.272. Batched forwards: 8 x 128x128 0.058 vs 0.064 ms, 4 x 256x256
-  // 0.056 vs 0.064; 16 x 320x240 (4800 tiles) 0.112 vs 0.108, 8 x 640x480 0.154 vs 0.140.
+  // below about 3000 tiles, two pixels per thread (twice the threads per tile, half the
+  // per-thread work) mostly finish sooner. Device time per forward of 1000 Gaussians, 16x16
+  // tiles, 2 vs 4 pixels per thread: single views 320x240 (300 tiles) 33.4 vs 36.8 us, 480x360
+  // 38.5 vs 39.1, 560x420 38.4 vs 38.9, 640x480 (1200) 41.6 vs 39.3, 720x540 (1530) 44.5 vs
+  // 46.5, 800x600 (1900) 47.9 vs 50.0, 960x720 (2700) 55.7 vs 55.6, 1120x840 (3710) 64.9 vs
+  // 61.0, 1280x960 74.0 vs 68.6; batches 8 x 128x128 (512 tiles) 52.9 vs 59.0 us, 4 x 256x256
+  // (1024) 50.8 vs 54.9, 16 x 320x240 (4800) 102.0 vs 95.9, 8 x 640x480 134.8 vs 118.4. (The
+  // window is not monotonic: 640x480's 1200 tiles fit the four-pixel blend's resident CTAs in
+  // one round but not the two-pixel blend's.)
   p.px = default_px((int)d->px_per_thread, tw, th, p.n_tiles);
   p.chunk = (int)(d->flags >> 8) & 0xff;
   p.radix = (d->flags & FE_FLAG_RADIX_BINNING) != 0;
