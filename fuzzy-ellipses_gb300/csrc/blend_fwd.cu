@@ -303,12 +303,12 @@ __global__ void __launch_bounds__(BlendShape<TW, TH, PX, CH>::NT,
         }
       };
       // Build chunk c's record pairs from the staged source records (after the wait every
-      // thread sees all of them; each builds its own) and null the slots past the tile's keys up
-      // to a whole group of pairs.
+      // thread sees all of them; each builds its own) and null the slot past the tile's keys
+      // that completes the last pair.
       auto build = [&](int c) {
         TilePair* pb = sm.buf[c & 1];
         const int cnt = min(RC, nk - c * RC);
-        const int padded = (cnt + 2 * GP - 1) / (2 * GP) * (2 * GP);
+        const int padded = (cnt + 1) & ~1;
 #pragma unroll
         for (int q = 0; q < RPT; ++q) {
           const int r = tid + q * Sh::NT;
@@ -342,9 +342,10 @@ __global__ void __launch_bounds__(BlendShape<TW, TH, PX, CH>::NT,
       }
       for (int c = 0; c < nchunks; ++c) {
         const int cnt = min(RC, nk - c * RC);
-        const int padded = (cnt + 2 * GP - 1) / (2 * GP) * (2 * GP) / 2;  // pairs, whole groups
+        const int pairs = (cnt + 1) >> 1;
         const TilePair* pb = sm.buf[c & 1];
-        for (int j = 0; j < padded; j += GP) {
+        int j = 0;
+        for (; j + GP <= pairs; j += GP) {
           // Uniform over the CTA: the z > 0 mask is only evaluated for groups holding a record
           // whose psv is not positive over the whole tile (null slots included).
           bool need_mask = false;
@@ -357,6 +358,24 @@ __global__ void __launch_bounds__(BlendShape<TW, TH, PX, CH>::NT,
             blend_group<PX, GP, true>(&pb[j], DU, DV, DVSQ, B3, NB2, A2, W2, Z2, m);
           else
             blend_group<PX, GP, false>(&pb[j], DU, DV, DVSQ, B3, NB2, A2, W2, Z2, m);
+        }
+        // The pairs after the last whole group, in groups of two pairs, then one.
+        for (; j < pairs;) {
+          if (GP > 2 && j + 2 <= pairs) {
+            const float2 f0 = pb[j].f[18], f1 = pb[j + 1].f[18];
+            if (!(f0.x != 0.f && f0.y != 0.f && f1.x != 0.f && f1.y != 0.f))
+              blend_group<PX, 2, true>(&pb[j], DU, DV, DVSQ, B3, NB2, A2, W2, Z2, m);
+            else
+              blend_group<PX, 2, false>(&pb[j], DU, DV, DVSQ, B3, NB2, A2, W2, Z2, m);
+            j += 2;
+          } else {
+            const float2 f0 = pb[j].f[18];
+            if (!(f0.x != 0.f && f0.y != 0.f))
+              blend_group<PX, 1, true>(&pb[j], DU, DV, DVSQ, B3, NB2, A2, W2, Z2, m);
+            else
+              blend_group<PX, 1, false>(&pb[j], DU, DV, DVSQ, B3, NB2, A2, W2, Z2, m);
+            j += 1;
+          }
         }
         if (c + 1 < nchunks) {
           // Chunk c + 1: wait for its source records, build its pairs (buf[(c + 1) & 1] was last
