@@ -248,6 +248,7 @@ constexpr int kRowPlanBlocks = 152;  // row blocks that fill a GB300 (its SM cou
 struct RowPlan {
   bool ok = false;
   int max_gy = 0;
+  int max_gx = 0;
   int n_views = 0;
 };
 
@@ -261,6 +262,7 @@ RowPlan row_plan(const ViewDev* views, int n_views) {
     const ViewDev& V = views[i];
     if (V.gx > kMaxRowTiles || V.gy > 65535) r.ok = false;
     r.max_gy = std::max(r.max_gy, (int)V.gy);
+    r.max_gx = std::max(r.max_gx, (int)V.gx);
     max_n = std::max(max_n, (int)V.n);
     tests += (int64_t)V.gy * V.n;
     rows += V.gy;
@@ -315,9 +317,9 @@ int run_binning(const Pipeline& p, int64_t worst, DevBuf& recbuf, DevBuf& keybuf
   if (exact && !rp.ok) launch_scan(rs.touched, rs.incl, p.n_rec, cap, rs.scan_tmp, rs.ctrl, st);
   if (!rp.ok || !p.heavy_first) rs.order = nullptr;  // the blend takes tiles in index order
   if (rp.ok) {
-    launch_tile_binning_emit(p.va, rp.n_views, rp.max_gy, rs.rects, foot_of(p, rs), p.tile_w,
-                             p.tile_h, rs.row_tot, cap, rs.ctrl, rs.ranges, nullptr, ks.keys_a,
-                             rs.order, p.n_tiles, st);
+    launch_tile_binning_emit(p.va, rp.n_views, rp.max_gy, rp.max_gx, rs.rects, foot_of(p, rs),
+                             p.tile_w, p.tile_h, rs.row_tot, cap, rs.ctrl, rs.ranges, nullptr,
+                             ks.keys_a, rs.order, p.n_tiles, st);
     sorted = ks.keys_a;
   } else {
     launch_emit_keys(p.va, rs.incl, rs.rects, foot_of(p, rs), p.tile_w, p.tile_h, p.n_rec, rs.ctrl,
@@ -1239,9 +1241,10 @@ static int batch_binning(fe_batch* b, const Pipeline& p, cudaStream_t st, cudaEv
   if (ev) FE_CUDA(cudaEventRecord(ev[2], st));
   const KeySpace& ks = b->ks;
   if (rp.ok) {
-    launch_tile_binning_emit(p.va, rp.n_views, rp.max_gy, rs.rects, foot_of(p, rs), p.tile_w,
-                             p.tile_h, rs.row_tot, b->cap, rs.ctrl, rs.ranges, rs.tile_view,
-                             ks.keys_a, p.heavy_first ? rs.order : nullptr, p.n_tiles, st);
+    launch_tile_binning_emit(p.va, rp.n_views, rp.max_gy, rp.max_gx, rs.rects, foot_of(p, rs),
+                             p.tile_w, p.tile_h, rs.row_tot, b->cap, rs.ctrl, rs.ranges,
+                             rs.tile_view, ks.keys_a, p.heavy_first ? rs.order : nullptr,
+                             p.n_tiles, st);
     if (ev) FE_CUDA(cudaEventRecord(ev[3], st));
     b->sorted = ks.keys_a;
     if (ev) FE_CUDA(cudaEventRecord(ev[4], st));
@@ -1666,9 +1669,9 @@ int fe_render_fwd_noalloc(const fe_render_desc* d, const float* means, const flo
   uint64_t* sorted = ks.keys_a;
   if (!rp.ok || !p.heavy_first) rs.order = nullptr;
   if (rp.ok) {
-    launch_tile_binning_emit(p.va, rp.n_views, rp.max_gy, rs.rects, foot_of(p, rs), p.tile_w,
-                             p.tile_h, rs.row_tot, worst, rs.ctrl, rs.ranges, nullptr, ks.keys_a,
-                             rs.order, p.n_tiles, st);
+    launch_tile_binning_emit(p.va, rp.n_views, rp.max_gy, rp.max_gx, rs.rects, foot_of(p, rs),
+                             p.tile_w, p.tile_h, rs.row_tot, worst, rs.ctrl, rs.ranges, nullptr,
+                             ks.keys_a, rs.order, p.n_tiles, st);
   } else {
     launch_scan(rs.touched, rs.incl, p.n_rec, worst, rs.scan_tmp, rs.ctrl, st);
     launch_emit_keys(p.va, rs.incl, rs.rects, foot_of(p, rs), p.tile_w, p.tile_h, p.n_rec, rs.ctrl,

@@ -729,6 +729,117 @@ __global__ void __launch_bounds__(kRowThreads, 8) tile_emit_kernel_waves(
                  tile_view, keys, order, n_tiles, nseg);
 }
 
+// Tile-major emission for batches of narrow views (at most 32 tiles per row) once the row bases
+// are formed: one warp per (view, tile row), lane x owning tile x of the row, no block barriers.
+// Same outputs as tile_emit_body: each tile's keys in Gaussian-id order from the row's base,
+// every tile's range and view, and the work-class list entries. Lanes take the view's records
+// 32 at a time; a ballot per tile gives the chunk's records covering it and each one's rank.
+constexpr int kWarpRowWarps = 8;
+constexpr int kWarpRowTiles = 32;
+
+// Bit x set when record i of the view reaches tile x of `row` (its footprint's span in the row,
+// or its rectangle's without footprint rows).
+__device__ __forceinline__ uint32_t row_span_mask(const TileRect* __restrict__ vr,
+                                                  const FootRows* __restrict__ vf, int tile_w,
+                                                  int tile_h, int n, int i, int row) {
+  if (i >= n) return 0u;
+  const TileRect r = vr[i];
+  if (!covers_row(r, row)) return 0u;
+  int a = r.x0, b = r.x1;
+  if (vf) foot_row_tiles(vf[i], r, row, tile_w, tile_h, a, b);
+  if (b <= a) return 0u;
+  const uint32_t below_b = b >= 32 ? 0xffffffffu : ((1u << b) - 1u);
+  return below_b & ~((1u << a) - 1u);
+}
+
+__global__ void __launch_bounds__(kWarpRowWarps * 32) tile_emit_warp_kernel(
+    ViewsArg va, const TileRect* __restrict__ rects, const FootRows* __restrict__ foot,
+    int tile_w, int tile_h, const unsigned long long* __restrict__ row_tot, int stride,
+    int64_t capacity, Control* __restrict__ ctrl, uint2* __restrict__ ranges,
+    uint32_t* __restrict__ tile_view, uint64_t* __restrict__ keys, uint32_t* __restrict__ order,
+    int64_t n_tiles) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const unsigned full = 0xffffffffu;
+  const uint32_t lt_mask = (1u << lane) - 1u;
+  const unsigned long long want = ctrl->want_keys, cap = (unsigned long long)capacity;
+  const unsigned long long K = want < cap ? want : cap;
+  if (blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0) {
+    ctrl->num_keys = K;
+    if (want > cap) atomicOr(&ctrl->error, FE_DEVERR_CAPACITY);
+  }
+  const int v = (int)blockIdx.y;
+  const ViewDev& V = view_at(va, v);
+  const int row = (int)blockIdx.x * kWarpRowWarps + warp;
+  if (row >= V.gy) return;  // (uniform over the warp)
+  const int gx = V.gx, n = V.n;
+  if (gx > kWarpRowTiles) {  // the host plans this kernel only for narrower views
+    if (lane == 0) atomicOr(&ctrl->error, FE_DEVERR_CAPACITY);
+    return;
+  }
+  const int64_t tile0 = V.tile_base + (int64_t)row * gx;
+  const TileRect* vr = rects + V.rec_base;
+  const FootRows* vf = foot ? foot + V.rec_base : nullptr;
+  // View base (entry stride - 1) + the row's offset within the view.
+  const unsigned long long row_base =
+      row_tot[(int64_t)v * stride + stride - 1] + row_tot[(int64_t)v * stride + row];
+  uint64_t* row_keys = keys + row_base;
+  const unsigned long long left = K > row_base ? K - row_base : 0ull;
+  const uint32_t lim = left < 0xffffffffull ? (uint32_t)left : 0xffffffffu;
+
+  // Keys of each tile (lane x: tile x), then their exclusive prefix along the row.
+  uint32_t cnt = 0;
+  for (int s0 = 0; s0 < n; s0 += 32) {
+    const uint32_t m = row_span_mask(vr, vf, tile_w, tile_h, n, s0 + lane, row);
+    for (int x = 0; x < gx; ++x) {
+      const uint32_t c = (uint32_t)__popc(__ballot_sync(full, (m >> x) & 1u));
+      if (lane == x) cnt += c;
+    }
+  }
+  uint32_t incl = cnt;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(full, incl, o);
+    if (lane >= o) incl += y;
+  }
+  const uint32_t ex = incl - cnt;
+  uint2 rg = make_uint2(0u, 0u);
+  if (lane < gx) {
+    const unsigned long long lo = min(row_base + ex, K), hi = min(row_base + ex + cnt, K);
+    // every tile of the row: empty tiles (or tiles whose keys were all dropped) get {0,0}
+    rg = hi > lo ? make_uint2((uint32_t)lo, (uint32_t)hi) : make_uint2(0u, 0u);
+    ranges[tile0 + lane] = rg;
+    if (tile_view) tile_view[tile0 + lane] = (uint32_t)v;
+  }
+  if (order) {
+    // Work classes: the lanes of one class share one global atomic for their slots.
+    const int cl = lane < gx ? tile_class(cnt) : -1;
+    const unsigned same = __match_any_sync(full, cl);
+    const int leader = __ffs(same) - 1;
+    uint32_t base = 0;
+    if (lane < gx && lane == leader) base = atomicAdd(&ctrl->tile_class[cl], (uint32_t)__popc(same));
+    base = __shfl_sync(full, base, leader);
+    if (lane < gx)
+      reinterpret_cast<uint4*>(order)[(int64_t)cl * n_tiles + base + (uint32_t)__popc(same & lt_mask)] =
+          make_uint4((uint32_t)(tile0 + lane), rg.x, rg.y, (uint32_t)v);
+  }
+  // Keys: tile x's next slot is lane x's p; a record's rank among the chunk's records covering x
+  // is the ballot's bits below its lane.
+  uint32_t p = ex;
+  for (int s0 = 0; s0 < n; s0 += 32) {
+    const int i = s0 + lane;
+    const uint32_t m = row_span_mask(vr, vf, tile_w, tile_h, n, i, row);
+    for (int x = 0; x < gx; ++x) {
+      const uint32_t bal = __ballot_sync(full, (m >> x) & 1u);
+      const uint32_t px = __shfl_sync(full, p, x);
+      if ((m >> x) & 1u) {
+        const uint32_t k = px + (uint32_t)__popc(bal & lt_mask);
+        if (k < lim) row_keys[k] = ((uint64_t)(tile0 + x) << 32) | (uint32_t)i;
+      }
+      if (lane == x) p += (uint32_t)__popc(bal);
+    }
+  }
+}
+
 inline int grid_for(int64_t work, int threads, int cap) {
   const int64_t b = (work + threads - 1) / threads;
   return (int)(b < 1 ? 1 : (b > cap ? cap : b));
@@ -777,8 +888,8 @@ uint64_t* launch_sort(uint64_t* a, uint64_t* b, int key_bits, const Control* ctr
 }
 
 
-void launch_tile_binning_emit(const ViewsArg& va, int n_views, int max_gy, const TileRect* rects,
-                              const FootRows* foot, int tile_w, int tile_h,
+void launch_tile_binning_emit(const ViewsArg& va, int n_views, int max_gy, int max_gx,
+                              const TileRect* rects, const FootRows* foot, int tile_w, int tile_h,
                               unsigned long long* row_tot, int64_t capacity, Control* ctrl,
                               uint2* ranges, uint32_t* tile_view, uint64_t* keys, uint32_t* order,
                               int64_t n_tiles, cudaStream_t st) {
@@ -790,6 +901,14 @@ void launch_tile_binning_emit(const ViewsArg& va, int n_views, int max_gy, const
     row_offsets_kernel<<<(unsigned)((n_views + kRowWarps - 1) / kRowWarps), kRowThreads, 0, st>>>(
         va, n_views, max_gy, row_tot);
     view_bases_kernel<<<1, kRowThreads, 0, st>>>(n_views, max_gy, row_tot);
+    if (max_gx <= kWarpRowTiles) {
+      // Narrow views: a warp per tile row instead of a block sized for 1024-tile rows.
+      const dim3 grid((unsigned)((max_gy + kWarpRowWarps - 1) / kWarpRowWarps), (unsigned)n_views);
+      tile_emit_warp_kernel<<<grid, kWarpRowWarps * 32, 0, st>>>(
+          va, rects, foot, tile_w, tile_h, row_tot, max_gy + 1, capacity, ctrl, ranges, tile_view,
+          keys, order, n_tiles);
+      return;
+    }
   }
   // Launches of few rows (single views) split each row over up to 8 blocks so that the key
   // writing, the longest part of a row's work, is spread over more SMs.

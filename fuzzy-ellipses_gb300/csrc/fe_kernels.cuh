@@ -56,8 +56,8 @@ uint64_t* launch_sort(uint64_t* a, uint64_t* b, int key_bits, const Control* ctr
 // written beside its range (ViewsArg::tile_view).
 constexpr int kMaxRowTiles = 1024;
 constexpr int kRowBaseViews = 32;  // above this many views the row bases are formed first
-void launch_tile_binning_emit(const ViewsArg& va, int n_views, int max_gy, const TileRect* rects,
-                              const FootRows* foot, int tile_w, int tile_h,
+void launch_tile_binning_emit(const ViewsArg& va, int n_views, int max_gy, int max_gx,
+                              const TileRect* rects, const FootRows* foot, int tile_w, int tile_h,
                               unsigned long long* row_tot, int64_t capacity, Control* ctrl,
                               uint2* ranges, uint32_t* tile_view, uint64_t* keys, uint32_t* order,
                               int64_t n_tiles, cudaStream_t st);

@@ -238,10 +238,13 @@ def test_tile_major_batch_equals_radix_batch(cuda_device, tile, n_views, n_gauss
     assert torch.equal(out[0][0], out[1][0]) and torch.equal(out[0][1], out[1][1])
 
 
-def test_many_view_batch_row_bases_equal_radix_batch(cuda_device):
+@pytest.mark.parametrize("tile", [(16, 16), (8, 8)])
+def test_many_view_batch_row_bases_equal_radix_batch(cuda_device, tile):
     """Past the view count where the tile-major binning first forms every row's key base
     (row_offsets_kernel, view_bases_kernel), a batch of 60 uneven views of 12 scenes renders
-    bit-identically to the radix-sorted batch."""
+    bit-identically to the radix-sorted batch, in index order and heaviest tiles first. These
+    views are at most 32 tiles wide (256 pixels in 8x8 tiles is exactly 32), so the emission is
+    the warp-per-row kernel."""
     items = S.config3(seed=7, n_scenes=12)
     means, prec, logw, scenes, views = [], [], [], [], []
     off = 0
@@ -256,15 +259,16 @@ def test_many_view_batch_row_bases_equal_radix_batch(cuda_device):
         views.append(dict(views[len(views) % 20]))
     m, p, w = [torch.from_numpy(np.concatenate(x)).to(cuda_device) for x in (means, prec, logw)]
     out = []
-    for binning in ("tiles", "radix"):
-        b = fe.Batch(scenes, views, binning=binning)
+    for binning, heavy in (("radix", False), ("tiles", False), ("tiles", True)):
+        b = fe.Batch(scenes, views, tile=tile, binning=binning, heavy_first=heavy)
         assert binning != "tiles" or b.launches_per_forward == 5
         d, a = b.forward(m, p, w)
         st = b.status()
         assert st["device_error"] == 0 and st["num_keys"] == st["want_keys"]
         out.append((d, a, st["num_keys"]))
-    assert out[0][2] == out[1][2]
-    assert torch.equal(out[0][0], out[1][0]) and torch.equal(out[0][1], out[1][1])
+    for o in out[1:]:
+        assert o[2] == out[0][2]
+        assert torch.equal(o[0], out[0][0]) and torch.equal(o[1], out[0][1])
 
 
 def _footprint_scenes():
