@@ -736,6 +736,7 @@ __global__ void __launch_bounds__(kRowThreads, 8) tile_emit_kernel_waves(
 // 32 at a time; a ballot per tile gives the chunk's records covering it and each one's rank.
 constexpr int kWarpRowWarps = 8;
 constexpr int kWarpRowTiles = 32;
+constexpr int kWarpRowCache = 512;  // records whose span masks the key pass reuses
 
 // Bit x set when record i of the view reaches tile x of `row` (its footprint's span in the row,
 // or its rectangle's without footprint rows).
@@ -786,11 +787,16 @@ __global__ void __launch_bounds__(kWarpRowWarps * 32) tile_emit_warp_kernel(
   const unsigned long long left = K > row_base ? K - row_base : 0ull;
   const uint32_t lim = left < 0xffffffffull ? (uint32_t)left : 0xffffffffu;
 
-  // Keys of each tile (lane x: tile x), then their exclusive prefix along the row.
+  // Keys of each tile (lane x: tile x), then their exclusive prefix along the row. The span
+  // masks of the first kWarpRowCache records are kept for the key pass; only tiles that some
+  // record of a chunk reaches are visited.
+  __shared__ uint32_t s_mask[kWarpRowWarps][kWarpRowCache];
   uint32_t cnt = 0;
   for (int s0 = 0; s0 < n; s0 += 32) {
     const uint32_t m = row_span_mask(vr, vf, tile_w, tile_h, n, s0 + lane, row);
-    for (int x = 0; x < gx; ++x) {
+    if (s0 < kWarpRowCache) s_mask[warp][s0 + lane] = m;
+    for (uint32_t u = __reduce_or_sync(full, m); u; u &= u - 1u) {
+      const int x = __ffs(u) - 1;
       const uint32_t c = (uint32_t)__popc(__ballot_sync(full, (m >> x) & 1u));
       if (lane == x) cnt += c;
     }
@@ -827,8 +833,10 @@ __global__ void __launch_bounds__(kWarpRowWarps * 32) tile_emit_warp_kernel(
   uint32_t p = ex;
   for (int s0 = 0; s0 < n; s0 += 32) {
     const int i = s0 + lane;
-    const uint32_t m = row_span_mask(vr, vf, tile_w, tile_h, n, i, row);
-    for (int x = 0; x < gx; ++x) {
+    const uint32_t m = s0 < kWarpRowCache ? s_mask[warp][i]
+                                          : row_span_mask(vr, vf, tile_w, tile_h, n, i, row);
+    for (uint32_t u = __reduce_or_sync(full, m); u; u &= u - 1u) {
+      const int x = __ffs(u) - 1;
       const uint32_t bal = __ballot_sync(full, (m >> x) & 1u);
       const uint32_t px = __shfl_sync(full, p, x);
       if ((m >> x) & 1u) {
