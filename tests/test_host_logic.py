@@ -23,6 +23,26 @@ def test_autotuner_default_and_cache_roundtrip(tmp_path):
     assert t.lookup(sc, views) == autotune.DEFAULT
 
 
+def test_autotuner_keeps_device_and_host_picks_apart(tmp_path):
+    """The host-to-host target is cached under its own key: a device pick does not answer a
+    host lookup and the other way round; both survive a reload from the cache file."""
+    import json
+
+    path = tmp_path / "tune.json"
+    sc, views = [(0, 1000)], [dict(scene=0, height=480, width=640)] * 16
+    key = autotune.bucket(sc, views)
+    path.write_text(json.dumps({
+        key: {"tile": [16, 16], "px": 4, "chunk": 32, "heavy_first": True, "ms": 0.2},
+        key + "_host": {"tile": [32, 8], "px": 2, "chunk": 16, "heavy_first": False, "ms": 0.27}}))
+    t = autotune.Autotuner(path=str(path))
+    dev, host = t.lookup(sc, views), t.lookup(sc, views, target="host")
+    assert (dev["tile"], dev["px"], dev["chunk"], dev["heavy_first"]) == ((16, 16), 4, 32, True)
+    assert (host["tile"], host["px"], host["chunk"]) == ((32, 8), 2, 16)
+    only_dev = autotune.Autotuner(path=str(tmp_path / "missing.json"))
+    only_dev.table[key] = {"tile": [8, 8], "px": 2, "chunk": 8}
+    assert only_dev.lookup(sc, views, target="host") == autotune.DEFAULT
+
+
 def test_footprint_estimate_monotone():
     rng = np.random.default_rng(0)
     sc = S.random_gaussians(100, 0.1, rng)
