@@ -1297,7 +1297,7 @@ static bool host_direct_enabled() {
 // The device address of n floats of host memory at h when the whole range is pinned memory
 // mapped into the current device's address space (its first and last elements resolve to
 // device addresses the same distance apart), else nullptr. Pageable memory gives nullptr.
-static float* mapped_host_floats(float* h, int64_t n) {
+static const float* mapped_host_floats(const float* h, int64_t n) {
   if (n <= 0) return nullptr;
   cudaPointerAttributes a{}, e{};
   if (cudaPointerGetAttributes(&a, h) != cudaSuccess ||
@@ -1308,8 +1308,11 @@ static float* mapped_host_floats(float* h, int64_t n) {
   if (a.type != cudaMemoryTypeHost || e.type != cudaMemoryTypeHost || !a.devicePointer ||
       !e.devicePointer)
     return nullptr;
-  float* d0 = static_cast<float*>(a.devicePointer);
-  return static_cast<float*>(e.devicePointer) == d0 + (n - 1) ? d0 : nullptr;
+  const float* d0 = static_cast<const float*>(a.devicePointer);
+  return static_cast<const float*>(e.devicePointer) == d0 + (n - 1) ? d0 : nullptr;
+}
+static float* mapped_host_floats(float* h, int64_t n) {
+  return const_cast<float*>(mapped_host_floats(static_cast<const float*>(h), n));
 }
 
 static void plan_host_bands(fe_batch* b) {
@@ -1383,6 +1386,13 @@ int fe_batch_fwd_host(fe_batch* b, const float* h_means, const float* h_prec,
   float* dep_map = host_direct_enabled() ? mapped_host_floats(h_depth, b->n_pix) : nullptr;
   float* alp_map = dep_map ? mapped_host_floats(h_alpha, b->n_pix) : nullptr;
   if (dep_map && alp_map) {
+    // Pinned inputs are read by the preprocess through their device mapping (one record per
+    // thread reads its Gaussian's 13 floats), so no copy precedes the binning.
+    const float* m_map = mapped_host_floats(h_means, 3 * n);
+    const float* p_map = m_map ? mapped_host_floats(h_prec, 9 * n) : nullptr;
+    const float* w_map = p_map ? mapped_host_floats(h_logw, n) : nullptr;
+    if (n > 0 && w_map)
+      return batch_forward(b, m_map, p_map, w_map, dep_map, alp_map, nullptr, false, st);
     Carver c{nullptr};
     c.take<float>(3 * n); c.take<float>(9 * n); c.take<float>(n);
     int rc = b->io.reserve(c.off, st);

@@ -260,12 +260,14 @@ int64_t fe_batch_scratch_bytes(const fe_batch *b);
  * or NULL. */
 int fe_batch_fwd(fe_batch *b, const float *d_means, const float *d_prec, const float *d_logw,
                  float *d_depth, float *d_alpha, float *d_stats, fe_stream_t stream);
-/* fe_batch_fwd from HOST memory to HOST memory: h_means (n,3), h_prec (n,3,3), h_logw (n) are
- * copied in on `stream`. When h_depth and h_alpha are pinned host memory mapped into the
+/* fe_batch_fwd from HOST memory to HOST memory: h_means (n,3), h_prec (n,3,3), h_logw (n) and
+ * the outputs h_depth, h_alpha. When h_depth and h_alpha are pinned host memory mapped into the
  * device's address space (cudaHostAlloc / cudaHostRegister; every pinned allocation on a
  * unified-addressing system), the blend stores the images through that mapping as it renders,
  * in one launch on `stream`, so they cross the host link while later tiles render and no copy
- * follows the last tile (environment FE_HOST_DIRECT=0 turns this off). Otherwise the blend runs
+ * follows the last tile (environment FE_HOST_DIRECT=0 turns this off); pinned inputs are then
+ * read by the preprocess through their mapping too, else copied in on `stream`. Otherwise the
+ * Gaussians are copied in on `stream` and the blend runs
  * in bands of whole tile rows (alternating between `stream` and a second stream of the batch, so
  * one band's tail overlaps the next band's start) and each band's depth and alpha rows are
  * copied back on a copy stream of the batch as soon as the band is done, so only the last

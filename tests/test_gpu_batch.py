@@ -131,7 +131,8 @@ def _host_forward_matches(b, m, p, w, pinned=True):
     depth, alpha = b.forward(m, p, w)
     torch.cuda.synchronize()
     if pinned:
-        hd, ha = b.forward_host(m.cpu(), p.cpu(), w.cpu())
+        # pinned inputs too: the preprocess reads them through their device mapping
+        hd, ha = b.forward_host(m.cpu().pin_memory(), p.cpu().pin_memory(), w.cpu().pin_memory())
         assert hd.is_pinned() and ha.is_pinned()
     else:
         hd = torch.full((b.n_pixels,), -7.0)
