@@ -681,10 +681,12 @@ def main():
         "e2e": {"value": e2e_value, "unit": "Mevals/s", "h2d_bytes_per_step": h2d_batch,
                 "d2h_bytes_per_step": out_b.numel() * 4,
                 "path": "fe_batch_fwd_host C-ABI call (ctypes) over the 16 cameras: pinned "
-                        "host Gaussians in, depth and alpha out to pinned host buffers, which "
-                        "the blend stores into through their device mapping as it renders (one "
-                        "launch, tiles in index order, no copy after the last tile); poses part "
-                        "of the batch plan; wall clock per call including the final sync",
+                        "host Gaussians in (read by the preprocess through their device "
+                        "mapping), depth and alpha out to pinned host buffers, which the blend "
+                        "stores into through their device mapping as it renders (one launch, "
+                        "tiles in index order, no copy before the binning or after the last "
+                        "tile); poses part of the batch plan; wall clock per call including the "
+                        "final sync",
                 "ms_per_step": 1e3 * e2e_s,
                 "autotuned": {"tile": f"{tuned_h['tile'][0]}x{tuned_h['tile'][1]}",
                               "px": tuned_h["px"], "chunk": tuned_h["chunk"],
