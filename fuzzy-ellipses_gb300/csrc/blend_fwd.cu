@@ -81,7 +81,8 @@ constexpr float kNoLogit = -1e30f;
 // the device's address space, where whole vectors keep the link's write rate.
 template <int PX>
 __device__ __forceinline__ void store_pixels(float* dst, const float (&x)[PX], int room) {
-  const bool whole = room >= PX && (reinterpret_cast<uintptr_t>(dst) & (sizeof(float) * PX - 1)) == 0;
+  const bool whole =
+      room >= PX && (reinterpret_cast<uintptr_t>(dst) & (sizeof(float) * PX - 1)) == 0;
   if (PX == 4 && whole) {
     *reinterpret_cast<float4*>(dst) = make_float4(x[0], x[1], x[2 % PX], x[3 % PX]);
   } else if (PX == 2 && whole) {
