@@ -822,11 +822,14 @@ __global__ void __launch_bounds__(kWarpRowWarps * 32) tile_emit_warp_kernel(
     const unsigned same = __match_any_sync(full, cl);
     const int leader = __ffs(same) - 1;
     uint32_t base = 0;
-    if (lane < gx && lane == leader) base = atomicAdd(&ctrl->tile_class[cl], (uint32_t)__popc(same));
+    if (lane < gx && lane == leader)
+      base = atomicAdd(&ctrl->tile_class[cl], (uint32_t)__popc(same));
     base = __shfl_sync(full, base, leader);
-    if (lane < gx)
-      reinterpret_cast<uint4*>(order)[(int64_t)cl * n_tiles + base + (uint32_t)__popc(same & lt_mask)] =
+    if (lane < gx) {
+      const uint32_t rank = (uint32_t)__popc(same & lt_mask);
+      reinterpret_cast<uint4*>(order)[(int64_t)cl * n_tiles + base + rank] =
           make_uint4((uint32_t)(tile0 + lane), rg.x, rg.y, (uint32_t)v);
+    }
   }
   // Keys: tile x's next slot is lane x's p; a record's rank among the chunk's records covering x
   // is the ballot's bits below its lane.
